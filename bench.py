@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 quasi-dynamic cycle hot path.
+
+Workload (N=1 line): Green's-function assembly, mid size -- a rough
+strike-slip fault 80 km x 30 km (self-affine height field, Hurst 0.8,
+rms/length 1e-3, seed 0), 200 x 50 rectangles -> N = 20,000 triangles.  One
+step = one full dense assembly of the (3N x 2N) FP64 traction operator (the
+reference's six N x N matrices, 6 N^2 GF entries) plus its FP32 copy.
+``value`` = GF entries/s with the mesh resident on the device; ``e2e`` = the
+same through the host-buffer C-ABI call (mesh in, FP64 operator out to pinned
+host memory).  The same run also measures plain FP64 and FP32-operator RK45
+stepping on that operator (RK stages/s, 7 right-hand-side evaluations per
+attempted step) and reports it under ``stepping``.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the C
+restatement in oracle/, or the reference's own TDstressFS_C built from source
+into oracle/_ref/ when present) on a bounded sample of the same workload.
+Multi-GPU: replicas only (each rank assembles its own operator; no collective
+on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "RK stages/s batched+mixed vs plain FP64, same GPU, ≤1e-5 slip err; GF entries/s"
+MU = 32038120320.0
+LAM = 32038120320.0
+RHO = MU / 3464.0 ** 2
+
+
+def workload(quick=False):
+    from pyquake3d_gb300 import mesh
+    if quick:
+        L, W, nx, nz = 20.0, 10.0, 50, 20      # N = 2,000
+    else:
+        L, W, nx, nz = 80.0, 30.0, 200, 50     # N = 20,000
+    nodes, tris = mesh.rough_fault(L, W, nx, nz, hurst=0.8, ratio=1e-3, seed=0)
+    name = "gf_assembly_rough_%dx%dkm_N%d" % (L, W, tris.shape[0])
+    return name, L, W, nodes, tris
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp64_peak_tflops(torch, dev):
+    """FP64 rate measured here: torch.matmul float64 4096^3 (cuBLAS DGEMM), best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        a @ b
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+# FP64 operations of one (receiver, source) pair of the assembly kernel
+# (both unit slips): counted from pyquake3d_gb300/csrc/gf_device.cuh, see
+# profiles/gf_flops.md.  Divisions and square roots count as one operation.
+GF_FLOP_PER_PAIR = None
+
+
+def gf_flops_per_pair():
+    p = os.path.join(HERE, "profiles", "gf_flops.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)["flops_per_pair"]
+    return None
+
+
+def cpu_gf_sample(nodes, tris, seconds=12.0, kind=None):
+    """Time the host CPU on a bounded sample (source columns) of the assembly."""
+    import oracle
+    N = tris.shape[0]
+    cores = os.cpu_count() or 1
+    ref_so = os.path.join(HERE, "oracle", "_ref", "libTDstressFS_ref.so")
+    use_ref = (kind != "port") and os.path.exists(ref_so)
+    if use_ref:
+        fn, kind = _ref_assemble(ref_so, cores, nodes, tris), "reference"
+    else:
+        fn, kind = (lambda c0, c1: oracle.assemble_dense(nodes, tris, MU, LAM, cols=(c0, c1), nthreads=cores)), "port"
+    # calibrate on a small slice, then size the sample to ~`seconds`
+    c1 = max(cores, 16)
+    t0 = time.perf_counter()
+    fn(0, c1)
+    dt = time.perf_counter() - t0
+    ncols = int(min(N, max(c1, c1 * seconds / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    fn(0, ncols)
+    dt = time.perf_counter() - t0
+    entries = 6.0 * N * ncols
+    return {"value": entries / dt, "unit": "GF entries/s", "cores": cores, "kind": kind,
+            "sample": "%d of %d source columns x all %d receivers (%.3g entries, %.1f s)" % (ncols, N, N, entries, dt)}
+
+
+def _ref_assemble(path, cores, nodes, tris):
+    """Reference TDstressFS_C (built from its source) driven column by column
+    from a thread pool (ctypes releases the GIL), strike and dip unit slip,
+    then the traction projection -- the work of src/QDsim_gpu.py:1745-1785."""
+    import concurrent.futures as cf
+    from pyquake3d_gb300 import mesh
+    lib = ctypes.CDLL(path)
+    D = ctypes.POINTER(ctypes.c_double)
+    lib.TDstressFS_C.argtypes = [D, D, D, ctypes.c_size_t, D, D, D] + [ctypes.c_double] * 5 + [ctypes.c_bool, D, D]
+    lib.TDstressFS_C.restype = None
+    fr, xg = mesh.element_frames(nodes, tris)
+    X, Y, Z = (np.ascontiguousarray(xg[:, k]) for k in range(3))
+    e1, e2, n = fr[:, 0:3], fr[:, 3:6], fr[:, 6:9]
+    N = tris.shape[0]
+    p = lambda a: a.ctypes.data_as(D)
+
+    def column(j):
+        P = [np.ascontiguousarray(nodes[tris[j, k] - 1]) for k in range(3)]
+        out = []
+        for Ss, Ds in ((1.0, 0.0), (0.0, 1.0)):
+            s = np.empty((N, 6))
+            e = np.empty((N, 6))
+            lib.TDstressFS_C(p(X), p(Y), p(Z), N, p(P[0]), p(P[1]), p(P[2]), Ss, Ds, 0.0, MU, LAM, False, p(s), p(e))
+            t = np.stack([s[:, 0] * n[:, 0] + s[:, 3] * n[:, 1] + s[:, 4] * n[:, 2],
+                          s[:, 3] * n[:, 0] + s[:, 1] * n[:, 1] + s[:, 5] * n[:, 2],
+                          s[:, 4] * n[:, 0] + s[:, 5] * n[:, 1] + s[:, 2] * n[:, 2]], axis=1)
+            out.append(np.stack([np.sum(t * e1, 1), np.sum(t * e2, 1), np.sum(t * n, 1)]))
+        return out
+
+    def run(c0, c1):
+        with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+            list(ex.map(column, range(c0, c1)))
+    return run
+
+
+def bench_reference(args):
+    name, L, W, nodes, tris = workload(args.quick)
+    N = tris.shape[0]
+    samples = []
+    cb = None
+    for _ in range(args.warmup):
+        pass
+    for _ in range(max(1, args.steps)):
+        cb = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
+        samples.append(cb["value"])
+    val = statistics.median(samples)
+    cb["value"] = val
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GF entries/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 6.0 * N * N / val * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "N": N, "entries_per_step": 6 * N * N, "halfspace": False},
+            "cpu_baseline": cb, "e2e": {"value": val, "unit": "GF entries/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def bench_ours(args):
+    import torch
+    from pyquake3d_gb300 import _lib, gf, mesh
+    from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    L_ = _lib.load()
+    name, Lkm, Wkm, nodes, tris = workload(args.quick)
+    N = tris.shape[0]
+    nodes_t, tris_t = gf.mesh_to_device(nodes, tris, dev)
+    K64 = torch.empty((3 * N, 2 * N), dtype=torch.float64, device=dev)
+    K32 = torch.empty((3 * N, 2 * N), dtype=torch.float32, device=dev)
+    ws = torch.empty(L_.pq3d_gf_workspace_bytes(N), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def one():
+        gf.assemble_dense(nodes_t, tris_t, MU, LAM, out64=K64, out32=K32, workspace=ws)
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for k in range(args.steps):
+            starts[k].record(stream)
+            one()
+            ends[k].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    total = t0.elapsed_time(t1) / 1e3
+    per_launch = [s.elapsed_time(e) / 1e3 for s, e in zip(starts, ends)]
+    if dist:
+        t = torch.tensor([total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+        if args.steps and dist:
+            dist.barrier()
+    entries = 6.0 * N * N * args.steps * world
+    value = entries / total
+
+    out = {}
+    if rank == 0:
+        peaks, peak_src = measured_peaks()
+        fp64 = fp64_peak_tflops(torch, dev)
+        fpp = gf_flops_per_pair()
+        avg = sum(per_launch) / len(per_launch)
+        roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": fp64,
+                "peak_source": "measured here: cuBLAS DGEMM (torch.matmul float64 4096^3); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "traffic": None, "launch_s": avg}
+        if fpp:
+            ach = fpp * N * N / avg / 1e12
+            roof.update({"achieved": ach, "frac": ach / fp64, "flops_per_pair": fpp})
+        else:
+            roof.update({"achieved": None, "frac": None})
+        tr = os.path.join(HERE, "profiles", "gf_assembly_traffic.json")
+        if os.path.exists(tr):
+            with open(tr) as f:
+                t = json.load(f)
+            roof["traffic"] = t["bytes_per_pair"] * N * N
+            roof["traffic_note"] = t.get("note")
+        out["roofline"] = roof
+        out["clocks"] = clk.summary()
+        # -- end to end: host mesh in, FP64 operator out to pinned host memory
+        host64 = torch.empty((3 * N, 2 * N), dtype=torch.float64, pin_memory=True)
+        gf.assemble_dense_host(nodes, tris, MU, LAM, out64=host64)
+        e2e_steps = max(1, min(args.steps, 3))
+        t_e = time.perf_counter()
+        for _ in range(e2e_steps):
+            gf.assemble_dense_host(nodes, tris, MU, LAM, out64=host64)
+        t_e = time.perf_counter() - t_e
+        out["e2e"] = {"value": 6.0 * N * N * e2e_steps / t_e, "unit": "GF entries/s",
+                      "h2d_bytes_per_step": int(nodes.nbytes + tris.astype(np.int64).nbytes),
+                      "d2h_bytes_per_step": int(host64.numel() * 8), "steps": e2e_steps,
+                      "path": "pq3d_assemble_dense_host (C-ABI), 2 streams, D2H overlapped with assembly"}
+        del host64
+        # -- stepping on the assembled operator
+        out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks)
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
+    line = {"metric": METRIC, "value": value, "unit": "GF entries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "N": N, "entries_per_step": 6 * N * N,
+                       "operator_bytes_per_step": int(K64.numel() * 12), "halfspace": False,
+                       "l2": "output operator (%.1f GB FP64 + FP32 per step) streams through L2; inputs are the "
+                             "mesh only" % (K64.numel() * 12 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "gpu_launches": 3 * args.steps}
+    line.update(out)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks):
+    """Plain FP64 and FP32-operator stepping on the assembled operator."""
+    from pyquake3d_gb300 import mesh
+    from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
+    N = tris.shape[0]
+    _, xg = mesh.element_frames(nodes, tris)
+    tab = mesh.friction_table(xg, Lkm * 1e3, Wkm * 1e3, seed=0)
+    res = {"workload": "plain RK45 stepping on the same mesh (N=%d), %d accepted steps timed" % (N, args.rk_steps)}
+    for label, K in (("fp64", K64), ("fp32_operator", K32)):
+        sim = DenseDeviceSim(K, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+        sim.step(3)
+        c0 = sim.read_ctrl()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        sim.launch(args.rk_steps)
+        e.record()
+        e.synchronize()
+        dt = s.elapsed_time(e) / 1e3
+        c1 = sim.read_ctrl()
+        att = c1.attempts - c0.attempts
+        acc = c1.steps_done - c0.steps_done
+        bytes_step = K.numel() * K.element_size()
+        res[label] = {"rk_stages_per_s": 7.0 * att / dt, "accepted_steps_per_s": acc / dt,
+                      "attempted": int(att), "accepted": int(acc), "ms_per_step": dt / max(acc, 1) * 1e3,
+                      "status": int(c1.status),
+                      "matvec_roofline": {"bound": "hbm", "unit": "GB/s",
+                                          "achieved": bytes_step * acc / dt / 1e9, "peak": peaks["hbm_gbs"],
+                                          "frac": bytes_step * acc / dt / 1e9 / peaks["hbm_gbs"],
+                                          "note": "operator bytes per accepted step / step time (whole step)"}}
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="N=2,000 case (profiling)")
+    ap.add_argument("--rk-steps", type=int, default=200)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,108 @@
+"""ctypes binding of libpq3d.so (the C ABI declared in include/pq3d.h).
+
+The library is built in-tree by ``pyquake3d_gb300.build``.  There is no CPU
+fallback: if the library is missing or CUDA is unavailable, the calls that
+need it raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libpq3d.so")
+HEADER = os.path.join(os.path.dirname(_PKG), "include", "pq3d.h")
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_i64_p = ctypes.POINTER(ctypes.c_int64)
+c_void_p = ctypes.c_void_p
+c_i64 = ctypes.c_int64
+c_int = ctypes.c_int
+c_dbl = ctypes.c_double
+c_size = ctypes.c_size_t
+c_bool = ctypes.c_bool
+
+PQ3D_OK = 0
+PQ3D_ERR_ARG = 1
+PQ3D_ERR_CUDA = 2
+PQ3D_ERR_TIMEOUT = 3
+PQ3D_ERR_STEP = 4
+PQ3D_ERR_UNSUPPORTED = 5
+
+
+class PQ3DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("pq3d error %d: %s" % (code, msg))
+        self.code = code
+
+
+class DenseSim(ctypes.Structure):
+    """Mirror of pq3d_dense_sim."""
+    _fields_ = [("N", c_i64)] + \
+        [(n, c_void_p) for n in ("Tno", "Tt1o", "Tt2o", "state",
+                                 "slipv1", "slipv2", "slipv", "rake", "slip1", "slip2", "slip", "Tt", "fric",
+                                 "a", "b", "dc", "f0", "shear_loading", "normal_loading", "rake0",
+                                 "rates", "vprime", "cand", "K64", "K32", "ctrl")] + \
+        [("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", c_int)]
+
+
+class StepCtrl(ctypes.Structure):
+    """Mirror of pq3d_step_ctrl (104 bytes)."""
+    _fields_ = [("dttry", c_dbl), ("time", c_dbl), ("maxv", c_dbl), ("status", ctypes.c_int32),
+                ("steps_done", ctypes.c_int32), ("attempts", c_i64), ("err_slot", ctypes.c_uint64 * 6),
+                ("maxv_bits", ctypes.c_uint64), ("bar_count", ctypes.c_uint32), ("bar_gen", ctypes.c_uint32)]
+
+
+_SIGS = {
+    "pq3d_last_error": (ctypes.c_char_p, []),
+    "pq3d_version": (c_int, []),
+    "TDstressFS_C": (None, [c_double_p, c_double_p, c_double_p, c_size, c_double_p, c_double_p, c_double_p,
+                            c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_bool, c_double_p, c_double_p]),
+    "TDstressEachSourceAtReceiver_C": (None, [c_dbl, c_dbl, c_dbl, c_double_p, c_double_p, c_double_p, c_size,
+                                              c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_bool, c_double_p, c_double_p]),
+    "TDstressFS_C1": (None, [c_double_p, c_double_p, c_double_p, c_size, c_double_p, c_double_p, c_double_p,
+                             c_dbl, c_dbl, c_dbl, c_dbl, c_dbl] + [c_double_p] * 12),
+    "pq3d_gf_workspace_bytes": (c_size, [c_i64]),
+    "pq3d_assemble_dense": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl, c_dbl, c_int,
+                                    c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
+    "pq3d_assemble_dense_host": (c_int, [c_void_p, c_i64, c_void_p, c_i64, c_dbl, c_dbl, c_int, c_void_p, c_void_p]),
+    "pq3d_dense_matvec_f64": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
+    "pq3d_dense_matvec_f32": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
+    "pq3d_dense_step": (c_int, [ctypes.POINTER(DenseSim), c_int, c_void_p, c_void_p, c_void_p]),
+}
+
+_lib = None
+
+
+def header_functions():
+    """Names of the functions declared in include/pq3d.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", txt, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while", "defined")))
+
+
+def load(build_if_missing: bool = True):
+    """Load libpq3d.so (building it first if it is absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError("libpq3d.so is not built (run python -m pyquake3d_gb300.build)")
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != PQ3D_OK:
+        raise PQ3DError(rc, load().pq3d_last_error().decode())

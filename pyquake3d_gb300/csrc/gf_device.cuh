@@ -1,0 +1,353 @@
+// Device math of the triangular-dislocation Green's function (Nikkhoo &
+// Walter 2015, full space), written for one (receiver, source) pair per
+// thread.
+//
+// Reference behaviour reproduced (file:line in PyQuake3D):
+//   angular-dislocation strain   src/TDstressFS_C.cpp:51-121
+//   configuration test           src/TDstressFS_C.cpp:125-166
+//   per-side rotation            src/TDstressFS_C.cpp:185-256
+//   full-space driver            src/TDstressFS_C.cpp:274-521
+//   traction projection          src/QDsim_gpu.py:1400-1417
+//   receiver frames              src/readmsh.py:75-134
+//
+// Formulation differences from the reference (same mathematics):
+//   * each angular dislocation needs 1/r, 1/(r-z) and 1/W (W = zeta - r and
+//     r - zeta = -W), so one square root and two reciprocals replace the ~30
+//     divisions of the reference expression;
+//   * the strain is linear in the Burgers vector, so the by- and bz-parts of
+//     each angular dislocation are formed once and combined for unit strike
+//     and unit dip slip (the reference evaluates the whole pair twice);
+//   * rotation to the receiver frame, Hooke's law and the traction projection
+//     are one contraction: with the receiver axes rotated into the source
+//     system, t_c = 2 mu e_c^T E n + lambda tr(E) delta_{c,n} (tr and the
+//     frame's orthonormality are rotation invariant).
+//   * receivers on a side line in the triangle plane (mode 0) give zero, as
+//     the C++ does; horizontal sources use e_Y*n_z as strike (published
+//     algorithm; the reference C++ returns NaN there).
+#pragma once
+
+#include <math.h>
+
+namespace pq3d {
+namespace gf {
+
+constexpr double kPi = 3.141592653589793;
+
+// Per-source record (29 values, stored with stride kSrcStride).
+enum SrcField {
+    F_P2X, F_P2Y, F_P2Z,          // origin (vertex 2)
+    F_NX, F_NY, F_NZ,             // triangle normal
+    F_SX, F_SY, F_SZ,             // strike axis
+    F_DX, F_DY, F_DZ,             // dip axis
+    F_P1Y, F_P1Z, F_P3Y, F_P3Z,   // vertices 1, 3 in the triangle system (y, z)
+    F_DEN,                        // barycentric denominator of the mode test
+    F_E13Y, F_E13Z, F_E12Y, F_E12Z, F_E23Y, F_E23Z,   // unit side vectors (y, z)
+    F_CA, F_SA, F_CB, F_SB, F_CC, F_SC,               // cos, sin of (angle - pi) per vertex
+    F_COUNT
+};
+constexpr int kSrcStride = 32;
+constexpr int kRecvStride = 12;   // x, y, z, e1[3], e2[3], n[3]
+
+__host__ __device__ inline void unit3(double v[3])
+{
+    const double l = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= l; v[1] /= l; v[2] /= l;
+}
+
+// Source setup (src/TDstressFS_C.cpp:291-396).  f[i * fstride] receives field i.
+__host__ __device__ inline void setup_source(const double P1[3], const double P2[3], const double P3[3],
+                                             double *f, int fstride)
+{
+    double n[3] = {(P2[1] - P1[1]) * (P3[2] - P1[2]) - (P2[2] - P1[2]) * (P3[1] - P1[1]),
+                   (P2[2] - P1[2]) * (P3[0] - P1[0]) - (P2[0] - P1[0]) * (P3[2] - P1[2]),
+                   (P2[0] - P1[0]) * (P3[1] - P1[1]) - (P2[1] - P1[1]) * (P3[0] - P1[0])};
+    unit3(n);
+    double s[3] = {-n[1], n[0], 0.0};             // e_Z x n
+    double ls = sqrt(s[0] * s[0] + s[1] * s[1]);
+    if (ls == 0.0) { s[0] = 0.0; s[1] = n[2]; ls = fabs(n[2]); }
+    s[0] /= ls; s[1] /= ls;
+    const double d[3] = {n[1] * s[2] - n[2] * s[1], n[2] * s[0] - n[0] * s[2], n[0] * s[1] - n[1] * s[0]};
+    const double q1[3] = {P1[0] - P2[0], P1[1] - P2[1], P1[2] - P2[2]};
+    const double q3[3] = {P3[0] - P2[0], P3[1] - P2[1], P3[2] - P2[2]};
+    double p1[3] = {n[0] * q1[0] + n[1] * q1[1] + n[2] * q1[2],
+                    s[0] * q1[0] + s[1] * q1[1] + s[2] * q1[2],
+                    d[0] * q1[0] + d[1] * q1[1] + d[2] * q1[2]};
+    double p3[3] = {n[0] * q3[0] + n[1] * q3[1] + n[2] * q3[2],
+                    s[0] * q3[0] + s[1] * q3[1] + s[2] * q3[2],
+                    d[0] * q3[0] + d[1] * q3[1] + d[2] * q3[2]};
+    double e12[3] = {-p1[0], -p1[1], -p1[2]};
+    double e13[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
+    double e23[3] = {p3[0], p3[1], p3[2]};
+    unit3(e12); unit3(e13); unit3(e23);
+    const double A = acos(e12[0] * e13[0] + e12[1] * e13[1] + e12[2] * e13[2]);
+    const double B = acos(-e12[0] * e23[0] - e12[1] * e23[1] - e12[2] * e23[2]);
+    const double C = acos(e23[0] * e13[0] + e23[1] * e13[1] + e23[2] * e13[2]);
+    const double Am = -kPi + A, Bm = -kPi + B, Cm = -kPi + C;
+    const double vals[F_COUNT] = {
+        P2[0], P2[1], P2[2], n[0], n[1], n[2], s[0], s[1], s[2], d[0], d[1], d[2],
+        p1[1], p1[2], p3[1], p3[2],
+        -p3[2] * (p1[1] - p3[1]) + p3[1] * (p1[2] - p3[2]),
+        e13[1], e13[2], e12[1], e12[2], e23[1], e23[2],
+        cos(Am), sin(Am), cos(Bm), sin(Bm), cos(Cm), sin(Cm)};
+    for (int i = 0; i < F_COUNT; ++i) f[i * fstride] = vals[i];
+}
+
+// Receiver record (src/readmsh.py:75-134, node-order flag False).
+__host__ __device__ inline void setup_receiver(const double a[3], const double b[3], const double c[3], double *r)
+{
+    for (int k = 0; k < 3; ++k) r[k] = ((a[k] + b[k]) + c[k]) / 3.0;
+    const double ba[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const double ca[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    double n[3] = {ba[1] * ca[2] - ba[2] * ca[1], ba[2] * ca[0] - ba[0] * ca[2], ba[0] * ca[1] - ba[1] * ca[0]};
+    unit3(n);
+    double e1[3];
+    if (fabs(n[2]) < 1) {
+        e1[0] = n[1]; e1[1] = -n[0]; e1[2] = 0.0;
+        const double l = sqrt(e1[0] * e1[0] + e1[1] * e1[1]);
+        e1[0] /= l; e1[1] /= l;
+    } else {
+        e1[0] = 1.0; e1[1] = 0.0; e1[2] = 0.0;
+    }
+    const double e2[3] = {n[1] * e1[2] - n[2] * e1[1], n[2] * e1[0] - n[0] * e1[2], n[0] * e1[1] - n[1] * e1[0]};
+    r[3] = e1[0]; r[4] = e1[1]; r[5] = e1[2];
+    r[6] = e2[0]; r[7] = e2[1]; r[8] = e2[2];
+    r[9] = n[0];  r[10] = n[1]; r[11] = n[2];
+}
+
+// Configuration test: +1, -1, or 0 (side line in the plane).
+__device__ __forceinline__ int tri_mode(double x, double y, double z, double p1y, double p1z,
+                                        double p3y, double p3z, double den)
+{
+    const double a = ((y - p3y) * (0.0 - p3z) - (0.0 - p3y) * (z - p3z)) / den;
+    const double b = ((p1y - p3y) * (z - p3z) - (y - p3y) * (p1z - p3z)) / den;
+    const double c = 1.0 - a - b;
+    int m = 1;
+    if (a <= 0 && b > c && c > a) m = -1;
+    else if (b <= 0 && c > a && a > b) m = -1;
+    else if (c <= 0 && a > b && b > c) m = -1;
+    else if (a == 0 && b >= 0 && c >= 0) m = 0;
+    else if (a >= 0 && b == 0 && c >= 0) m = 0;
+    else if (a >= 0 && b >= 0 && c == 0) m = 0;
+    if (m == 0 && x != 0) m = 1;
+    return m;
+}
+
+// Shared geometric terms of one angular dislocation at (x, y, z) of its own
+// frame, opening angle with cos/sin (ca, sa).
+struct AdGeom {
+    double x, y, z, ca, sa;
+    double eta, ycz, x2, y2, z2;
+    double ir, ir3, iW2;
+    double i_Wr, i_W2r2, i_Wr3, i_rz, i_r2z2, i_r3z, i_W2r;
+    double C, S, gx, gy, gz, fx, fy, fz;
+};
+
+__device__ __forceinline__ void ad_geom(double x, double y, double z, double ca, double sa, double nu, AdGeom &g)
+{
+    g.x = x; g.y = y; g.z = z; g.ca = ca; g.sa = sa;
+    g.eta = y * ca - z * sa;
+    const double zeta = y * sa + z * ca;
+    g.ycz = y * ca + z * sa;
+    g.x2 = x * x; g.y2 = y * y; g.z2 = z * z;
+    const double r2 = g.x2 + g.y2 + g.z2;
+    const double r = sqrt(r2);
+    const double ir = 1.0 / r;
+    const double irz = 1.0 / (r - z);
+    const double iW = 1.0 / (zeta - r);
+    const double ir2 = ir * ir;
+    g.ir = ir;
+    g.ir3 = ir2 * ir;
+    g.iW2 = iW * iW;
+    g.i_Wr = iW * ir;
+    g.i_W2r2 = g.i_Wr * g.i_Wr;
+    g.i_Wr3 = iW * g.ir3;
+    g.i_rz = ir * irz;
+    g.i_r2z2 = g.i_rz * g.i_rz;
+    g.i_r3z = g.ir3 * irz;
+    g.i_W2r = g.iW2 * ir;
+    g.C = (r * ca - z) * g.i_Wr;
+    g.S = (r * sa - y) * g.i_Wr;
+    const double q = 1.0 / (4.0 * kPi);
+    const double i_rzeta = -iW;   // 1/(r - zeta)
+    g.gx = q * (g.eta * ir * i_rzeta - y * g.i_rz);
+    g.gy = q * (x * g.i_rz - ca * x * ir * i_rzeta);
+    g.gz = q * (sa * x * ir * i_rzeta);
+    const double p2 = 2.0 * nu + 1.0;
+    g.fx = p2 * g.i_Wr + g.x2 * g.i_W2r2 - g.x2 * g.i_Wr3;
+    g.fy = g.i_Wr + g.S * g.S - g.y2 * g.i_Wr3;
+    g.fz = g.i_Wr + g.C * g.C - g.z2 * g.i_Wr3;
+}
+
+// Strain of unit by (Ey) and unit bz (Ez) Burgers components.
+__device__ __forceinline__ void ad_parts_yz(const AdGeom &g, double nu, double k, double Ey[6], double Ez[6])
+{
+    const double x = g.x, y = g.y, z = g.z, ca = g.ca, sa = g.sa;
+    const double p2 = 2.0 * nu + 1.0;
+    const double xk = x * k, sak = sa * k, xsak = xk * sa;
+    const double yz = y * z;
+    Ey[0] = -xk * (g.fx * ca + p2 * g.i_rz - g.x2 * g.i_r2z2 - g.x2 * g.i_r3z);
+    Ey[1] = g.gy - xk * (g.i_rz - g.y2 * g.i_r2z2 - g.y2 * g.i_r3z + g.fy * ca);
+    Ey[2] = -xk * (g.fz * ca + z * g.ir3);
+    Ey[3] = 0.5 * g.gx + k * (g.x2 * y * g.i_r2z2 - nu * y * g.i_rz + g.x2 * y * g.i_r3z + nu * ca * g.S
+                              + g.x2 * y * ca * g.i_Wr3 + g.x2 * ca * g.S * g.i_Wr);
+    Ey[4] = k * (-g.x2 * g.ir3 + nu * g.ir + nu * ca * g.C + g.x2 * z * ca * g.i_Wr3 + g.x2 * ca * g.C * g.i_Wr);
+    Ey[5] = 0.5 * g.gz - xk * (y * g.ir3 + sa * ca * ca * g.iW2 - ca * g.ycz * g.i_W2r + yz * ca * g.i_W2r2
+                               - yz * ca * g.i_Wr3);
+    Ez[0] = xsak * g.fx;
+    Ez[1] = xsak * g.fy;
+    Ez[2] = g.gz + xsak * g.fz;
+    Ez[3] = -sak * (nu * g.S + g.x2 * g.S * g.i_Wr + g.x2 * y * g.i_Wr3);
+    Ez[4] = 0.5 * g.gx - sak * (nu * g.C + g.x2 * g.C * g.i_Wr + g.x2 * z * g.i_Wr3);
+    Ez[5] = 0.5 * g.gy - xsak * (yz * g.i_Wr3 - sa * ca * g.iW2 + g.ycz * g.i_W2r - yz * g.i_W2r2);
+}
+
+// Strain of a unit bx (tensile) Burgers component.
+__device__ __forceinline__ void ad_part_x(const AdGeom &g, double nu, double k, double Ex[6])
+{
+    const double x = g.x, y = g.y, z = g.z, ca = g.ca, sa = g.sa, eta = g.eta;
+    const double p2 = 2.0 * nu + 1.0;
+    const double yz = y * z;
+    Ex[0] = g.gx + k * (eta * g.i_Wr + eta * g.x2 * g.i_W2r2 - eta * g.x2 * g.i_Wr3 + y * g.i_rz
+                        - g.x2 * y * g.i_r2z2 - g.x2 * y * g.i_r3z);
+    Ex[1] = k * (g.fy * eta + p2 * y * g.i_rz - g.y2 * y * g.i_r2z2 - g.y2 * y * g.i_r3z - 2.0 * nu * ca * g.S);
+    Ex[2] = k * (eta * g.i_Wr + eta * g.C * g.C - eta * g.z2 * g.i_Wr3 + yz * g.ir3 + 2.0 * nu * sa * g.C);
+    Ex[3] = 0.5 * g.gy - k * (x * g.y2 * g.i_r2z2 - nu * x * g.i_rz + x * g.y2 * g.i_r3z - nu * x * ca * g.i_Wr
+                              + eta * x * g.S * g.i_Wr + eta * x * y * g.i_Wr3);
+    Ex[4] = 0.5 * g.gz - k * (-x * y * g.ir3 + nu * x * sa * g.i_Wr + eta * x * g.C * g.i_Wr + eta * x * z * g.i_Wr3);
+    Ex[5] = k * (g.y2 * g.ir3 - nu * g.ir - nu * ca * g.C + nu * sa * g.S + eta * sa * ca * g.iW2
+                 - eta * g.ycz * g.i_W2r + eta * yz * g.i_W2r2 - eta * yz * g.i_Wr3);
+}
+
+// acc += B^T T' B for the rotation B = [[1,0,0],[0,sz,-sy],[0,sy,sz]] about x
+// (the back-rotation of src/TDstressFS_C.cpp:240-255).
+__device__ __forceinline__ void add_rot_x(double acc[6], const double t[6], double sy, double sz)
+{
+    const double yy = sy * sy, zz = sz * sz, yz = sy * sz;
+    acc[0] += t[0];
+    acc[1] += zz * t[1] + 2.0 * yz * t[5] + yy * t[2];
+    acc[2] += yy * t[1] - 2.0 * yz * t[5] + zz * t[2];
+    acc[3] += sz * t[3] + sy * t[4];
+    acc[4] += -sy * t[3] + sz * t[4];
+    acc[5] += -yz * t[1] + (zz - yy) * t[5] + yz * t[2];
+}
+
+// Source fields through an accessor: F(i) returns field i.
+template <class Src>
+__device__ __forceinline__ void tdcs_point(const Src &F, double X, double Y, double Z, double &x, double &y, double &z)
+{
+    const double dx = X - F(F_P2X), dy = Y - F(F_P2Y), dz = Z - F(F_P2Z);
+    x = F(F_NX) * dx + F(F_NY) * dy + F(F_NZ) * dz;
+    y = F(F_SX) * dx + F(F_SY) * dy + F(F_SZ) * dz;
+    z = F(F_DX) * dx + F(F_DY) * dy + F(F_DZ) * dz;
+}
+
+// TDCS strain (triangle system) of unit strike (Es) and unit dip (Ed) slip.
+// Returns false for mode 0 (strain zero).
+template <class Src>
+__device__ __forceinline__ bool tdcs_strain_sd(const Src &F, double x, double y, double z, double nu, double k,
+                                               double Es[6], double Ed[6])
+{
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { Es[i] = 0.0; Ed[i] = 0.0; }
+    const int m = tri_mode(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
+    if (m == 0) return false;
+    const double sg = (m == 1) ? 1.0 : -1.0;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        double vy, vz, sy, sz, ca, sa;
+        if (v == 0) { vy = F(F_P1Y); vz = F(F_P1Z); sy = -sg * F(F_E13Y); sz = -sg * F(F_E13Z); ca = F(F_CA); sa = F(F_SA); }
+        else if (v == 1) { vy = 0.0; vz = 0.0; sy = sg * F(F_E12Y); sz = sg * F(F_E12Z); ca = F(F_CB); sa = F(F_SB); }
+        else { vy = F(F_P3Y); vz = F(F_P3Z); sy = sg * F(F_E23Y); sz = sg * F(F_E23Z); ca = F(F_CC); sa = F(F_SC); }
+        const double ty = y - vy, tz = z - vz;
+        AdGeom g;
+        ad_geom(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
+        double Ey[6], Ez[6];
+        ad_parts_yz(g, nu, k, Ey, Ez);
+        double ts[6], td[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            ts[i] = sz * Ey[i] + sy * Ez[i];    // strike: (by1, bz1) = (sz, sy)
+            td[i] = -sy * Ey[i] + sz * Ez[i];   // dip:    (by1, bz1) = (-sy, sz)
+        }
+        add_rot_x(Es, ts, sy, sz);
+        add_rot_x(Ed, td, sy, sz);
+    }
+    return true;
+}
+
+// General Burgers vector (bx = Ts, by = Ss, bz = Ds) strain in the triangle system.
+template <class Src>
+__device__ __forceinline__ void tdcs_strain_general(const Src &F, double x, double y, double z, double bx, double by,
+                                                    double bz, double nu, double k, double E[6])
+{
+#pragma unroll
+    for (int i = 0; i < 6; ++i) E[i] = 0.0;
+    const int m = tri_mode(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
+    if (m == 0) return;
+    const double sg = (m == 1) ? 1.0 : -1.0;
+    for (int v = 0; v < 3; ++v) {
+        double vy, vz, sy, sz, ca, sa;
+        if (v == 0) { vy = F(F_P1Y); vz = F(F_P1Z); sy = -sg * F(F_E13Y); sz = -sg * F(F_E13Z); ca = F(F_CA); sa = F(F_SA); }
+        else if (v == 1) { vy = 0.0; vz = 0.0; sy = sg * F(F_E12Y); sz = sg * F(F_E12Z); ca = F(F_CB); sa = F(F_SB); }
+        else { vy = F(F_P3Y); vz = F(F_P3Z); sy = sg * F(F_E23Y); sz = sg * F(F_E23Z); ca = F(F_CC); sa = F(F_SC); }
+        const double ty = y - vy, tz = z - vz;
+        AdGeom g;
+        ad_geom(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
+        double Ey[6], Ez[6], Ex[6];
+        ad_parts_yz(g, nu, k, Ey, Ez);
+        const double by1 = sz * by - sy * bz, bz1 = sy * by + sz * bz;
+        double t[6];
+        if (bx != 0.0) {
+            ad_part_x(g, nu, k, Ex);
+            for (int i = 0; i < 6; ++i) t[i] = bx * Ex[i] + by1 * Ey[i] + bz1 * Ez[i];
+        } else {
+            for (int i = 0; i < 6; ++i) t[i] = by1 * Ey[i] + bz1 * Ez[i];
+        }
+        add_rot_x(E, t, sy, sz);
+    }
+}
+
+// T_EFCS = A^T T A with A rows (n, s, d) of the source system.
+template <class Src>
+__device__ __forceinline__ void tdcs_to_efcs(const Src &F, const double t[6], double e[6])
+{
+    const double A[3][3] = {{F(F_NX), F(F_NY), F(F_NZ)}, {F(F_SX), F(F_SY), F(F_SZ)}, {F(F_DX), F(F_DY), F(F_DZ)}};
+    const double T[3][3] = {{t[0], t[3], t[4]}, {t[3], t[1], t[5]}, {t[4], t[5], t[2]}};
+    double M[3][3];   // M = T A
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[i][j] = T[i][0] * A[0][j] + T[i][1] * A[1][j] + T[i][2] * A[2][j];
+    e[0] = A[0][0] * M[0][0] + A[1][0] * M[1][0] + A[2][0] * M[2][0];
+    e[1] = A[0][1] * M[0][1] + A[1][1] * M[1][1] + A[2][1] * M[2][1];
+    e[2] = A[0][2] * M[0][2] + A[1][2] * M[1][2] + A[2][2] * M[2][2];
+    e[3] = A[0][0] * M[0][1] + A[1][0] * M[1][1] + A[2][0] * M[2][1];
+    e[4] = A[0][0] * M[0][2] + A[1][0] * M[1][2] + A[2][0] * M[2][2];
+    e[5] = A[0][1] * M[0][2] + A[1][1] * M[1][2] + A[2][1] * M[2][2];
+}
+
+__device__ __forceinline__ void hooke(const double e[6], double mu, double lam, double s[6])
+{
+    const double tr = e[0] + e[1] + e[2];
+    s[0] = 2.0 * mu * e[0] + lam * tr;
+    s[1] = 2.0 * mu * e[1] + lam * tr;
+    s[2] = 2.0 * mu * e[2] + lam * tr;
+    s[3] = 2.0 * mu * e[3];
+    s[4] = 2.0 * mu * e[4];
+    s[5] = 2.0 * mu * e[5];
+}
+
+// Tractions (along e1, e2, n of the receiver) of a TDCS strain E, given the
+// receiver axes already rotated into the source system (ue1, ue2, un).
+__device__ __forceinline__ void tractions_tdcs(const double E[6], const double ue1[3], const double ue2[3],
+                                               const double un[3], double two_mu, double lam, double out[3])
+{
+    const double u0 = E[0] * un[0] + E[3] * un[1] + E[4] * un[2];
+    const double u1 = E[3] * un[0] + E[1] * un[1] + E[5] * un[2];
+    const double u2 = E[4] * un[0] + E[5] * un[1] + E[2] * un[2];
+    const double tr = E[0] + E[1] + E[2];
+    out[0] = two_mu * (ue1[0] * u0 + ue1[1] * u1 + ue1[2] * u2);
+    out[1] = two_mu * (ue2[0] * u0 + ue2[1] * u1 + ue2[2] * u2);
+    out[2] = two_mu * (un[0] * u0 + un[1] * u1 + un[2] * u2) + lam * tr;
+}
+
+}  // namespace gf
+}  // namespace pq3d

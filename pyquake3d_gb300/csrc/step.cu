@@ -1,0 +1,427 @@
+// Dense quasi-dynamic stepping on the GPU (plain FP64 path, or the FP32
+// operator copy).
+//
+// Reference behaviour (src/QDsim_gpu.py):
+//   traction product K.(V - Vpl), once per accepted step        948-957
+//   right-hand side (aging law, radiation damping)             830-891
+//   Dormand-Prince 5(4) attempt, max-relative error norm      1128-1262
+//   accept / reject and dt control                              959-985
+//   closed-form slip rate, rake, slip integration              994-1027
+//
+// GPU design: one cooperative persistent kernel advances `nsteps` accepted
+// steps.  Per step: (1) every warp streams the three operator rows of one
+// receiver (16-byte loads) against the interleaved slip-rate deficit v';
+// (2) every thread runs the 7 right-hand-side evaluations of its cells in
+// registers (the traction rates are frozen over the step, so the stages are
+// cell-local), block-max + one atomicMax per block give the two error norms,
+// one grid barrier, and every thread takes the same accept/reject decision;
+// (3) the state update writes v' for the next step's product.  The host only
+// reads the control block after the launch.  Grid barriers are bounded.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace pq3d {
+namespace step {
+
+// Dormand-Prince tableau (src/QDsim_gpu.py:1129-1159)
+constexpr double B21 = .2;
+constexpr double B31 = 3. / 40, B32 = 9. / 40.;
+constexpr double B41 = 44. / 45., B42 = -56. / 15, B43 = 32. / 9;
+constexpr double B51 = 19372. / 6561., B52 = -25360 / 2187., B53 = 64448. / 6561., B54 = -212. / 729.;
+constexpr double B61 = 9017. / 3168., B62 = -355. / 33., B63 = -46732. / 5247., B64 = 49. / 176.,
+                 B65 = -5103. / 18656.;
+constexpr double B71 = 35. / 384., B73 = 500. / 1113., B74 = 125. / 192., B75 = -2187. / 6784., B76 = 11. / 84.;
+constexpr double B81 = 5179. / 57600., B83 = 7571. / 16695., B84 = 393. / 640., B85 = -92097. / 339200.,
+                 B86 = 187. / 2100., B87 = 1. / 40.;
+constexpr double kRelTol = 1e-4;
+
+// ---------------------------------------------------------------------------
+// traction product: rows 3i..3i+2 of K times v' (interleaved strike/dip)
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One warp: out[3i+c] for c = 0..2.  K rows have N double2 (strike, dip).
+__device__ __forceinline__ void rows3_f64(const double2 *__restrict__ K, const double2 *__restrict__ v, int64_t N,
+                                          int64_t i, int lane, double acc[3])
+{
+    const double2 *r0 = K + (3 * i) * N, *r1 = r0 + N, *r2 = r1 + N;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    int64_t j = lane;
+    for (; j + 32 < N; j += 64) {
+        const double2 x0 = __ldg(v + j), x1 = __ldg(v + j + 32);
+        const double2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
+        const double2 k01 = __ldcs(r0 + j + 32), k11 = __ldcs(r1 + j + 32), k21 = __ldcs(r2 + j + 32);
+        a0 = fma(k00.x, x0.x, a0); a0 = fma(k00.y, x0.y, a0);
+        a1 = fma(k10.x, x0.x, a1); a1 = fma(k10.y, x0.y, a1);
+        a2 = fma(k20.x, x0.x, a2); a2 = fma(k20.y, x0.y, a2);
+        b0 = fma(k01.x, x1.x, b0); b0 = fma(k01.y, x1.y, b0);
+        b1 = fma(k11.x, x1.x, b1); b1 = fma(k11.y, x1.y, b1);
+        b2 = fma(k21.x, x1.x, b2); b2 = fma(k21.y, x1.y, b2);
+    }
+    for (; j < N; j += 32) {
+        const double2 x0 = __ldg(v + j);
+        const double2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
+        a0 = fma(k00.x, x0.x, a0); a0 = fma(k00.y, x0.y, a0);
+        a1 = fma(k10.x, x0.x, a1); a1 = fma(k10.y, x0.y, a1);
+        a2 = fma(k20.x, x0.x, a2); a2 = fma(k20.y, x0.y, a2);
+    }
+    acc[0] = warp_sum(a0 + b0);
+    acc[1] = warp_sum(a1 + b1);
+    acc[2] = warp_sum(a2 + b2);
+}
+
+// FP32 operator: rows of N float2, FP32 products and per-lane FP32 sums,
+// cross-lane sum in FP64.
+__device__ __forceinline__ void rows3_f32(const float2 *__restrict__ K, const double2 *__restrict__ v, int64_t N,
+                                          int64_t i, int lane, double acc[3])
+{
+    const float2 *r0 = K + (3 * i) * N, *r1 = r0 + N, *r2 = r1 + N;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
+    int64_t j = lane;
+    for (; j + 32 < N; j += 64) {
+        const double2 xd0 = __ldg(v + j), xd1 = __ldg(v + j + 32);
+        const float2 x0 = make_float2((float)xd0.x, (float)xd0.y), x1 = make_float2((float)xd1.x, (float)xd1.y);
+        const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
+        const float2 k01 = __ldcs(r0 + j + 32), k11 = __ldcs(r1 + j + 32), k21 = __ldcs(r2 + j + 32);
+        a0 = fmaf(k00.x, x0.x, a0); a0 = fmaf(k00.y, x0.y, a0);
+        a1 = fmaf(k10.x, x0.x, a1); a1 = fmaf(k10.y, x0.y, a1);
+        a2 = fmaf(k20.x, x0.x, a2); a2 = fmaf(k20.y, x0.y, a2);
+        b0 = fmaf(k01.x, x1.x, b0); b0 = fmaf(k01.y, x1.y, b0);
+        b1 = fmaf(k11.x, x1.x, b1); b1 = fmaf(k11.y, x1.y, b1);
+        b2 = fmaf(k21.x, x1.x, b2); b2 = fmaf(k21.y, x1.y, b2);
+    }
+    for (; j < N; j += 32) {
+        const double2 xd0 = __ldg(v + j);
+        const float2 x0 = make_float2((float)xd0.x, (float)xd0.y);
+        const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
+        a0 = fmaf(k00.x, x0.x, a0); a0 = fmaf(k00.y, x0.y, a0);
+        a1 = fmaf(k10.x, x0.x, a1); a1 = fmaf(k10.y, x0.y, a1);
+        a2 = fmaf(k20.x, x0.x, a2); a2 = fmaf(k20.y, x0.y, a2);
+    }
+    acc[0] = warp_sum((double)a0 + (double)b0);
+    acc[1] = warp_sum((double)a1 + (double)b1);
+    acc[2] = warp_sum((double)a2 + (double)b2);
+}
+
+template <bool kF32>
+__global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K, const double2 *__restrict__ v,
+                                                     int64_t N, double *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < N; i += nwarps) {
+        double acc[3];
+        if (kF32) rows3_f32((const float2 *)K, v, N, i, lane, acc);
+        else rows3_f64((const double2 *)K, v, N, i, lane, acc);
+        if (lane == 0) { out[3 * i] = acc[0]; out[3 * i + 1] = acc[1]; out[3 * i + 2] = acc[2]; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// right-hand side of one cell (src/QDsim_gpu.py:830-891), pore pressure 0
+
+struct Cell {
+    double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
+};
+
+__device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
+
+__device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
+                                    double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+{
+    const double Tn = Tno * 1e6, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
+    const double es = exp(clip700(-state / c.a));
+    const double aTn = c.a * Tn;
+    const double x1 = clip700(T1 / aTn), x2 = clip700(T2 / aTn);
+    const double ep1 = exp(x1), em1 = exp(-x1), ep2 = exp(x2), em2 = exp(-x2);
+    const double ch1 = (ep1 + em1) / 2, sh1 = (ep1 - em1) / 2;
+    const double ch2 = (ep2 + em2) / 2, sh2 = (ep2 - em2) / 2;
+    const double aTn2 = c.a * (Tn * Tn);
+    const double dV1dtau = 2 * V0 / aTn * es * ch1;
+    const double dV2dtau = 2 * V0 / aTn * es * ch2;
+    const double dV1dsigma = -2 * V0 * T1 / aTn2 * es * ch1;
+    const double dV2dsigma = -2 * V0 * T2 / aTn2 * es * ch2;
+    const double dV1dstate = -2 * V0 / c.a * es * sh1;
+    const double dV2dstate = -2 * V0 / c.a * es * sh2;
+    dstate = c.b / c.dc * (V0 * exp(clip700((c.f0 - state) / c.b)) - c.slipv);
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * c.dsig + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * c.dsig + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    dsig = c.dsig / 1e6;
+    dtau1 = t1 / 1e6;
+    dtau2 = t2 / 1e6;
+}
+
+// One Dormand-Prince attempt of one cell; y = (Tno, Tt1o, Tt2o, state).
+// Writes the 5th-order solution to yo and returns the two relative errors.
+__device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
+                                           double yo[4], double &e1, double &e2)
+{
+    double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
+        u7;
+    const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
+    rhs(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
+    rhs(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
+    rhs(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
+        st + h * (B31 * s1 + B32 * s2), s3, n3, t3, u3);
+    rhs(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
+        Tt2o + h * (B41 * u1 + B42 * u2 + B43 * u3), st + h * (B41 * s1 + B42 * s2 + B43 * s3), s4, n4, t4, u4);
+    rhs(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
+        Tt1o + h * (B51 * t1 + B52 * t2 + B53 * t3 + B54 * t4), Tt2o + h * (B51 * u1 + B52 * u2 + B53 * u3 + B54 * u4),
+        st + h * (B51 * s1 + B52 * s2 + B53 * s3 + B54 * s4), s5, n5, t5, u5);
+    rhs(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
+        Tt1o + h * (B61 * t1 + B62 * t2 + B63 * t3 + B64 * t4 + B65 * t5),
+        Tt2o + h * (B61 * u1 + B62 * u2 + B63 * u3 + B64 * u4 + B65 * u5),
+        st + h * (B61 * s1 + B62 * s2 + B63 * s3 + B64 * s4 + B65 * s5), s6, n6, t6, u6);
+    yo[0] = Tno + h * (B71 * n1 + B73 * n3 + B74 * n4 + B75 * n5 + B76 * n6);
+    yo[1] = Tt1o + h * (B71 * t1 + B73 * t3 + B74 * t4 + B75 * t5 + B76 * t6);
+    yo[2] = Tt2o + h * (B71 * u1 + B73 * u3 + B74 * u4 + B75 * u5 + B76 * u6);
+    yo[3] = st + h * (B71 * s1 + B73 * s3 + B74 * s4 + B75 * s5 + B76 * s6);
+    rhs(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
+    const double Tn8 = Tno + h * (B81 * n1 + B83 * n3 + B84 * n4 + B85 * n5 + B86 * n6 + B87 * n7);
+    const double T18 = Tt1o + h * (B81 * t1 + B83 * t3 + B84 * t4 + B85 * t5 + B86 * t6 + B87 * t7);
+    const double T28 = Tt2o + h * (B81 * u1 + B83 * u3 + B84 * u4 + B85 * u5 + B86 * u6 + B87 * u7);
+    const double st8 = st + h * (B81 * s1 + B83 * s3 + B84 * s4 + B85 * s5 + B86 * s6 + B87 * s7);
+    e1 = fabs(fabs(st8 - yo[3]) / st8);
+    const double ea = fabs(fabs(T18 - yo[1]) / T18);
+    const double eb = fabs(fabs(T28 - yo[2]) / T28);
+    const double ec = fabs(fabs(Tn8 - yo[0]) / Tn8);
+    // max that propagates NaN, like numpy's max
+    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
+}
+
+// max over non-negative doubles (and NaN, which wins) through their bit patterns
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(fabs(x)); }
+
+__device__ __forceinline__ double block_max(double v, double *red)
+{
+    // NaN-propagating max across the block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (isnan(v) || isnan(u)) ? NAN : fmax(v, u);
+    }
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double m = 0.0;
+    const int nw = blockDim.x >> 5;
+    for (int q = 0; q < nw; ++q) m = (isnan(m) || isnan(red[q])) ? NAN : fmax(m, red[q]);
+    return m;
+}
+
+__device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b : a; }
+
+template <bool kF32>
+__global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist)
+{
+    __shared__ double red[8];
+    pq3d_step_ctrl *C = S.ctrl;
+    const int64_t N = S.N;
+    const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+    const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = gtid >> 5, nwarps = gsz >> 5;
+    const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+    unsigned *bc = &C->bar_count, *bg = &C->bar_gen;
+    const unsigned nb = gridDim.x;
+    double dttry = C->dttry, time = C->time;
+    int64_t attempt = 0;
+    double2 *vp = (double2 *)S.vprime;
+
+    // v' from the current slip rate (src/QDsim_gpu.py:948-949)
+    for (int64_t i = gtid; i < N; i += gsz)
+        vp[i] = make_double2(S.slipv1[i] - S.Vpl * cos(S.rake0[i]), S.slipv2[i] - S.Vpl * sin(S.rake0[i]));
+    if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
+
+    for (int step = 0; step < nsteps; ++step) {
+        // (1) traction rates
+        for (int64_t i = warp; i < N; i += nwarps) {
+            double acc[3];
+            if (kF32) rows3_f32((const float2 *)S.K32, vp, N, i, lane, acc);
+            else rows3_f64((const double2 *)S.K64, vp, N, i, lane, acc);
+            if (lane == 0) {
+                S.rates[3 * i] = acc[0];
+                S.rates[3 * i + 1] = acc[1];
+                S.rates[3 * i + 2] = S.fix_Tn ? S.normal_loading[i] : acc[2] + S.normal_loading[i];
+            }
+        }
+        if (lead) C->maxv_bits = 0ull;
+        if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
+
+        // (2) attempts until one is accepted
+        double h = dttry, dtnext = 0.0;
+        int nrjct = 0;
+        for (;;) {
+            const int slot = (int)(attempt % 3);
+            double m1 = 0.0, m2 = 0.0;
+            for (int64_t i = gtid; i < N; i += gsz) {
+                Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
+                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2]};
+                const double y[4] = {S.Tno[i], S.Tt1o[i], S.Tt2o[i], S.state[i]};
+                double yo[4], e1, e2;
+                dp_attempt(c, S.V0, S.eta, h, y, yo, e1, e2);
+                reinterpret_cast<double4_16a *>(S.cand)[i] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
+                m1 = (isnan(m1) || isnan(e1)) ? NAN : fmax(m1, e1);
+                m2 = (isnan(m2) || isnan(e2)) ? NAN : fmax(m2, e2);
+            }
+            m1 = block_max(m1, red);
+            m2 = block_max(m2, red);
+            if (threadIdx.x == 0) {
+                atomicMax((unsigned long long *)&C->err_slot[2 * slot], dbits(m1));
+                atomicMax((unsigned long long *)&C->err_slot[2 * slot + 1], dbits(m2));
+            }
+            if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
+            const double err1 = __longlong_as_double((long long)*((volatile unsigned long long *)&C->err_slot[2 * slot])) + 1e-10;
+            const double err2 = __longlong_as_double((long long)*((volatile unsigned long long *)&C->err_slot[2 * slot + 1])) + 1e-10;
+            if (lead) {
+                const int z = (int)((attempt + 2) % 3);
+                C->err_slot[2 * z] = 0ull;
+                C->err_slot[2 * z + 1] = 0ull;
+                C->attempts += 1;
+            }
+            ++attempt;
+            const double c1 = err1 / kRelTol, c2 = err2 / kRelTol;
+            const double hn1 = h * 0.9 * pow(kRelTol / err1, 0.2);
+            const double hn2 = h * 0.9 * pow(kRelTol / err2, 0.2);
+            if (fmax(c1, c2) < 1.0 && !(isnan(c1) || isnan(c2))) {
+                dtnext = pymin(1.5 * h, pymin(hn1, hn2));
+                break;
+            }
+            ++nrjct;
+            h = pymax(0.5 * h, pymin(hn1, hn2));
+            if (h < 1.e-15 || nrjct > 20) {
+                if (lead) { C->status = PQ3D_ERR_STEP; C->dttry = h; C->time = time; }
+                return;
+            }
+        }
+
+        // (3) state update (src/QDsim_gpu.py:994-1027)
+        double vmax = 0.0;
+        for (int64_t i = gtid; i < N; i += gsz) {
+            const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[i];
+            const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[i];
+            S.Tno[i] = Tno; S.Tt1o[i] = T1; S.Tt2o[i] = T2; S.state[i] = st;
+            S.Tt[i] = sqrt(T1 * T1 + T2 * T2);
+            const double e = (2.0 * S.V0) * exp(-st / a);
+            const double v1 = e * sinh(T1 / Tno / a);
+            const double v2 = e * sinh(T2 / Tno / a);
+            double v = sqrt(v1 * v1 + v2 * v2);
+            S.slipv1[i] = v1; S.slipv2[i] = v2;
+            S.rake[i] = atan2(v2, v1);
+            if (v < 1e-30) v = 1e-30;
+            S.slipv[i] = v;
+            vmax = (isnan(vmax) || isnan(v)) ? NAN : fmax(vmax, v);
+            const double s1 = S.slip1[i] + v1 * h, s2 = S.slip2[i] + v2 * h;
+            S.slip1[i] = s1; S.slip2[i] = s2;
+            S.slip[i] = sqrt(s1 * s1 + s2 * s2);
+            S.fric[i] = S.Tt[i] / Tno;
+            vp[i] = make_double2(v1 - S.Vpl * cos(S.rake0[i]), v2 - S.Vpl * sin(S.rake0[i]));
+        }
+        vmax = block_max(vmax, red);
+        if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, dbits(vmax));
+        time = time + h;
+        dttry = dtnext;
+        if (lead) {
+            if (h_hist) h_hist[step] = h;
+            if (t_hist) t_hist[step] = time;
+            C->steps_done += 1;
+        }
+        if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
+    }
+    if (lead) {
+        C->dttry = dttry;
+        C->time = time;
+        C->maxv = __longlong_as_double((long long)C->maxv_bits);
+    }
+}
+
+struct LaunchCfg {
+    int device = -1;
+    int grid64 = 0, grid32 = 0;
+};
+static thread_local LaunchCfg g_cfg;
+
+static int coop_grid(bool f32, int *grid)
+{
+    int dev;
+    PQ3D_CUDA_TRY(cudaGetDevice(&dev));
+    if (g_cfg.device != dev) {
+        int sms = 0, coop = 0, b64 = 0, b32 = 0;
+        PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) return set_error(PQ3D_ERR_UNSUPPORTED, "device has no cooperative launch");
+        PQ3D_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b64, dense_step_kernel<false>, 256, 0));
+        PQ3D_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b32, dense_step_kernel<true>, 256, 0));
+        if (b64 < 1 || b32 < 1) return set_error(PQ3D_ERR_UNSUPPORTED, "stepper kernel does not fit on an SM");
+        g_cfg.device = dev;
+        g_cfg.grid64 = sms * b64;
+        g_cfg.grid32 = sms * b32;
+    }
+    *grid = f32 ? g_cfg.grid32 : g_cfg.grid64;
+    return PQ3D_OK;
+}
+
+}  // namespace step
+}  // namespace pq3d
+
+using namespace pq3d;
+using namespace pq3d::step;
+
+static int matvec(const void *K, int64_t N, const double *v, double *out, void *stream, bool f32)
+{
+    clear_error();
+    PQ3D_REQUIRE(N > 0 && K && v && out, "pq3d_dense_matvec: bad arguments");
+    PQ3D_REQUIRE(aligned16(v) && (f32 ? ((uintptr_t)K & 7u) == 0 : aligned16(K)),
+                 "pq3d_dense_matvec: K and v must be aligned (16 bytes for FP64, 8 for FP32)");
+    const int threads = 256;
+    const int64_t warps = N;
+    const unsigned blocks = (unsigned)((warps * 32 + threads - 1) / threads);
+    if (f32) matvec_kernel<true><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, (const double2 *)v, N, out);
+    else matvec_kernel<false><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, (const double2 *)v, N, out);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}
+
+extern "C" int pq3d_dense_matvec_f64(const double *K64, int64_t N, const double *v, double *out, void *stream)
+{
+    return matvec(K64, N, v, out, stream, false);
+}
+
+extern "C" int pq3d_dense_matvec_f32(const float *K32, int64_t N, const double *v, double *out, void *stream)
+{
+    return matvec(K32, N, v, out, stream, true);
+}
+
+extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist, void *stream)
+{
+    clear_error();
+    PQ3D_REQUIRE(sim && sim->N > 0 && nsteps >= 0 && sim->ctrl, "pq3d_dense_step: bad arguments");
+    PQ3D_REQUIRE((sim->K64 != nullptr) != (sim->K32 != nullptr), "pq3d_dense_step: exactly one of K64/K32");
+    PQ3D_REQUIRE(aligned16(sim->vprime) && aligned16(sim->cand) && aligned16(sim->K64 ? (const void *)sim->K64
+                                                                                      : (const void *)sim->K32),
+                 "pq3d_dense_step: vprime, cand and K must be 16-byte aligned");
+    if (nsteps == 0) return PQ3D_OK;
+    const bool f32 = sim->K32 != nullptr;
+    int grid = 0;
+    int rc = coop_grid(f32, &grid);
+    if (rc) return rc;
+    // clear the reduction slots and the barrier counter of the control block
+    cudaStream_t st = (cudaStream_t)stream;
+    PQ3D_CUDA_TRY(cudaMemsetAsync(&sim->ctrl->err_slot[0], 0, sizeof(uint64_t) * 7 + sizeof(uint32_t), st));
+    pq3d_dense_sim S = *sim;
+    void *args[] = {(void *)&S, (void *)&nsteps, (void *)&h_hist, (void *)&t_hist};
+    if (f32)
+        PQ3D_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)dense_step_kernel<true>, grid, 256, args, 0, st));
+    else
+        PQ3D_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)dense_step_kernel<false>, grid, 256, args, 0, st));
+    return PQ3D_OK;
+}

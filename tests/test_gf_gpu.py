@@ -1,0 +1,138 @@
+"""GPU parity of the Green's-function kernels against the reference's own
+outputs (golden vectors) and the CPU oracle.  Tolerance: normwise relative
+error <= 1e-10 for FP64 (per receiver / per operator column block) and
+<= 1e-6 for the FP32 copy."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pyquake3d_gb300 import _lib, gf, mesh
+from tests.util import normwise_rel
+
+pytestmark = pytest.mark.gpu
+MU = 32038120320.0
+D = ctypes.POINTER(ctypes.c_double)
+
+
+def _p(a):
+    return a.ctypes.data_as(D)
+
+
+def call_tdstress(L, R, P, Ss, Ds, Ts, half=False):
+    R = np.ascontiguousarray(R)
+    x, y, z = (np.ascontiguousarray(R[:, k]) for k in range(3))
+    n = R.shape[0]
+    s = np.zeros((n, 6))
+    e = np.zeros((n, 6))
+    P1, P2, P3 = (np.ascontiguousarray(p) for p in P)
+    L.TDstressFS_C(_p(x), _p(y), _p(z), n, _p(P1), _p(P2), _p(P3), Ss, Ds, Ts, MU, MU, half, _p(s), _p(e))
+    return s, e
+
+
+def test_tdstressfs_c_matches_reference_golden(cuda, golden):
+    L = _lib.load()
+    g = golden("gf_kat.npz")
+    n = 0
+    for i in range(int(g["n_cases"])):
+        Ss, Ds, Ts, half = g[f"c{i}_b"]
+        if half:
+            continue
+        s, e = call_tdstress(L, g[f"c{i}_R"], g[f"c{i}_P"], Ss, Ds, Ts)
+        assert normwise_rel(g[f"c{i}_stress"], s) < 1e-10, i
+        assert normwise_rel(g[f"c{i}_strain"], e) < 1e-10, i
+        zero = np.all(g[f"c{i}_stress"] == 0.0, axis=1)
+        assert np.all(s[zero] == 0.0), i   # configuration-0 receivers stay zero
+        n += 1
+    assert n >= 20
+
+
+def test_each_source_matches_reference_golden(cuda, golden):
+    L = _lib.load()
+    g = golden("gf_kat.npz")
+    P1, P2, P3, r = g["each_P1"], g["each_P2"], g["each_P3"], g["each_recv"]
+    ns = P1.shape[0]
+    s = np.zeros((ns, 6))
+    e = np.zeros((ns, 6))
+    L.TDstressEachSourceAtReceiver_C(r[0], r[1], r[2], _p(np.ascontiguousarray(P1)), _p(np.ascontiguousarray(P2)),
+                                     _p(np.ascontiguousarray(P3)), ns, 0.0, 1.0, 0.0, MU, MU, False, _p(s), _p(e))
+    assert normwise_rel(g["each_h0_stress"], s) < 1e-10
+    assert normwise_rel(g["each_h0_strain"], e) < 1e-10
+
+
+def test_legacy_twelve_array_variant(cuda, golden):
+    L = _lib.load()
+    g = golden("gf_kat.npz")
+    R, P = g["c0_R"], g["c0_P"]
+    Ss, Ds, Ts, _ = g["c0_b"]
+    n = R.shape[0]
+    outs = [np.zeros(n) for _ in range(12)]
+    x, y, z = (np.ascontiguousarray(R[:, k]) for k in range(3))
+    L.TDstressFS_C1(_p(x), _p(y), _p(z), n, _p(np.ascontiguousarray(P[0])), _p(np.ascontiguousarray(P[1])),
+                    _p(np.ascontiguousarray(P[2])), Ss, Ds, Ts, MU, MU, *[_p(o) for o in outs])
+    s = np.stack(outs[:6], axis=1)
+    assert normwise_rel(g["c0_stress"], s) < 1e-10
+
+
+@pytest.mark.parametrize("which", ["planar", "rough"])
+def test_dense_assembly_matches_reference_python(cuda, golden, which):
+    d = golden("dense_small.npz")
+    K64, K32 = gf.assemble_dense(d[which + "_nodes"], d[which + "_tris"], float(d["mu"]), float(d["lam"]))
+    ops = gf.split_ops(K64)
+    ops32 = gf.split_ops(K32)
+    for name in gf.OPS:
+        ref = d[which + "_" + name]
+        scale = max(np.abs(ref).max(), 1.0)
+        assert np.abs(ops[name].cpu().numpy() - ref).max() / scale < 1e-10, name
+        assert np.abs(ops32[name].cpu().numpy() - ref).max() / scale < 1e-6, name
+
+
+def test_dense_assembly_matches_oracle_rough_n800(cuda):
+    nodes, tris = mesh.rough_fault(20.0, 10.0, 20, 20, seed=7, ratio=5e-3)
+    K64, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False)
+    ref = oracle.assemble_dense(nodes, tris, MU, MU, nthreads=8)
+    got = gf.split_ops(K64)
+    for k, name in enumerate(oracle.OPS):
+        # normwise per receiver row
+        assert normwise_rel(ref[k], got[name].cpu().numpy(), axis=1) < 1e-10, name
+
+
+def test_row_blocks_equal_full_assembly_and_are_deterministic(cuda):
+    nodes, tris = mesh.rough_fault(10.0, 5.0, 11, 7, seed=2)
+    N = tris.shape[0]
+    K, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False)
+    K2, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False)
+    assert torch.equal(K, K2)
+    parts = [gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, rows=(r0, min(N, r0 + 37)))[0]
+             for r0 in range(0, N, 37)]
+    assert torch.equal(torch.cat(parts), K)
+
+
+def test_host_buffer_assembly_matches_device(cuda):
+    nodes, tris = mesh.rough_fault(10.0, 5.0, 16, 9, seed=4)
+    K, K32 = gf.assemble_dense(nodes, tris, MU, MU)
+    Kh, K32h = gf.assemble_dense_host(nodes, tris, MU, MU, fp32_copy=True)
+    assert torch.equal(Kh, K.cpu())
+    assert torch.equal(K32h, K32.cpu())
+
+
+def test_horizontal_source_is_finite(cuda):
+    """Horizontal triangles use e_Y * n_z as strike (published algorithm);
+    the reference C++ returns NaN there.  Check against the oracle."""
+    P = [np.array([0.0, 0.0, -3000.0]), np.array([1000.0, 0.0, -3000.0]), np.array([0.0, 1000.0, -3000.0])]
+    R = np.array([[300.0, 300.0, -2500.0], [2000.0, -500.0, -3500.0]])
+    s, _ = call_tdstress(_lib.load(), R, P, 1.0, 0.0, 0.0)
+    so, _ = oracle.tdstress(R[:, 0], R[:, 1], R[:, 2], *P, 1.0, 0.0, 0.0, MU, MU)
+    assert np.all(np.isfinite(s))
+    assert normwise_rel(so, s) < 1e-10
+
+
+def test_halfspace_request_fails_loudly(cuda):
+    L = _lib.load()
+    R = np.array([[0.0, 100.0, -1000.0]])
+    P = [np.array([0.0, 0.0, -500.0]), np.array([100.0, 0.0, -500.0]), np.array([0.0, 0.0, -600.0])]
+    s, _ = call_tdstress(L, R, P, 1.0, 0.0, 0.0, half=True)
+    assert np.all(np.isnan(s))
+    assert b"half-space" in L.pq3d_last_error()

@@ -1,0 +1,103 @@
+"""The CPU oracle against the golden vectors recorded from the reference
+(tests/golden/make_golden.py): the C restatement of the triangular-dislocation
+kernel against the reference C++ TDstressFS_C, the oracle dense operators
+against the reference Python assembly, and the NumPy stepping against the
+reference CPU trajectory."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.stepping import DenseStepper, StepFailure
+from tests.util import normwise_rel
+
+MU = 32038120320.0
+
+
+def gf_cases(g):
+    for i in range(int(g["n_cases"])):
+        P = g[f"c{i}_P"]
+        R = g[f"c{i}_R"]
+        Ss, Ds, Ts, half = g[f"c{i}_b"]
+        yield i, P, R, Ss, Ds, Ts, bool(half), g[f"c{i}_stress"], g[f"c{i}_strain"]
+
+
+def test_oracle_fullspace_matches_reference_cpp(golden):
+    g = golden("gf_kat.npz")
+    n = 0
+    for i, P, R, Ss, Ds, Ts, half, S, E in gf_cases(g):
+        if half:
+            continue
+        s, e = oracle.tdstress(R[:, 0], R[:, 1], R[:, 2], P[0], P[1], P[2], Ss, Ds, Ts, MU, MU, False)
+        assert normwise_rel(S, s) < 1e-10, i
+        assert normwise_rel(E, e) < 1e-10, i
+        n += 1
+    assert n >= 20
+
+
+def test_oracle_mode0_receivers_are_zero(golden):
+    """Receivers on a side line in the triangle plane keep zero strain (the
+    reference C++ behaviour)."""
+    g = golden("gf_kat.npz")
+    seen = 0
+    for i, P, R, Ss, Ds, Ts, half, S, E in gf_cases(g):
+        zero = np.all(S == 0.0, axis=1)
+        if zero.any() and not half:
+            s, _ = oracle.tdstress(R[:, 0], R[:, 1], R[:, 2], P[0], P[1], P[2], Ss, Ds, Ts, MU, MU, False)
+            assert np.all(s[zero] == 0.0)
+            seen += 1
+    assert seen > 0
+
+
+def test_oracle_each_source(golden):
+    g = golden("gf_kat.npz")
+    r = g["each_recv"]
+    s, e = oracle.tdstress_each_source(r[0], r[1], r[2], g["each_P1"], g["each_P2"], g["each_P3"],
+                                       0.0, 1.0, 0.0, MU, MU, False)
+    assert normwise_rel(g["each_h0_stress"], s) < 1e-10
+    assert normwise_rel(g["each_h0_strain"], e) < 1e-10
+
+
+@pytest.mark.parametrize("mesh", ["planar", "rough"])
+def test_oracle_dense_matches_reference_python(golden, mesh):
+    d = golden("dense_small.npz")
+    K = oracle.assemble_dense(d[mesh + "_nodes"], d[mesh + "_tris"], float(d["mu"]), float(d["lam"]), nthreads=2)
+    for k, name in enumerate(oracle.OPS):
+        ref = d[mesh + "_" + name]
+        scale = max(np.abs(ref).max(), 1.0)
+        assert np.abs(K[k] - ref).max() / scale < 1e-10, name
+
+
+def test_oracle_frames_match_reference(golden):
+    from pyquake3d_gb300 import mesh
+    d = golden("dense_small.npz")
+    for m in ("planar", "rough"):
+        fr, xg = mesh.element_frames(d[m + "_nodes"], d[m + "_tris"])
+        assert np.abs(fr - d[m + "_eleVec"]).max() < 1e-14
+        assert np.abs(xg - d[m + "_xg"]).max() < 1e-9
+
+
+def test_oracle_stepping_matches_reference_trajectory(golden):
+    g = golden("traj_small.npz")
+    d = golden("dense_small.npz")
+    K = {k: d["planar_" + k] for k in oracle.OPS}
+    st = DenseStepper(K, g["table"], mu=float(g["mu"]), density=float(g["rho"]))
+    dt = 1e-3
+    for i in range(400):
+        h, dt, _ = st.simu_forward(dt)
+        assert h == pytest.approx(g["h"][i], rel=1e-12)
+        if (i + 1) in (1, 10, 100, 200, 400):
+            for k in ("slip1", "slipv1", "state", "Tt1o", "Tno"):
+                assert normwise_rel(g[f"s{i + 1}_{k}"], getattr(st, k)) < 1e-12, (i, k)
+
+
+def test_oracle_step_failure_raises():
+    """A state that makes every attempt NaN ends in StepFailure, where the
+    reference calls sys.exit (src/QDsim_gpu.py:983-985)."""
+    N = 4
+    K = {k: np.zeros((N, N)) for k in oracle.OPS}
+    tab = np.zeros((N, 10))
+    tab[:, 1] = 0.01; tab[:, 2] = 0.015; tab[:, 3] = 0.1; tab[:, 4] = 0.6; tab[:, 6] = 25.0; tab[:, 7] = 1e-9
+    st = DenseStepper(K, tab, mu=MU, density=2670.0)
+    st.state[:] = np.nan
+    with pytest.raises(StepFailure):
+        st.simu_forward(1e-3)
