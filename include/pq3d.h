@@ -148,12 +148,16 @@ typedef struct pq3d_step_ctrl {
 
 /* Advance `nsteps` accepted steps on the device.  h_hist/t_hist (device,
  * nsteps doubles each, may be NULL) receive the accepted dt and the time after
- * each step.  One cooperative persistent kernel does, per accepted step, the
+ * each step.  h_force (device, nsteps doubles, normally NULL) replays a
+ * prescribed step sequence: step s takes h_force[s] in one attempt, whatever
+ * its error (used to compare arithmetic precisions on identical steps; the
+ * reference has no such mode).  One cooperative persistent kernel does, per accepted step, the
  * traction product, the retry loop of Dormand-Prince attempts with the
  * max-relative error norm, and the state update (src/QDsim_gpu.py:942-1027,
  * 1128-1262).  Asynchronous on `stream`: the return value reports the launch;
  * the outcome of the steps is ctrl->status (read it after the stream). */
-int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist, void *stream);
+int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist,
+                    const double *h_force, void *stream);
 
 #ifdef __cplusplus
 }

@@ -170,14 +170,18 @@ class DenseStepper:
         self.AdotV2 = np.dot(K['A2s'], v1) + np.dot(K['A2d'], v2)
 
     # src/QDsim_gpu.py:1029-1122
-    def simu_forward(self, dttry):
-        """One accepted step; returns (h, dtnext, attempts)."""
+    def simu_forward(self, dttry, force=False):
+        """One accepted step; returns (h, dtnext, attempts).
+
+        ``force=True`` takes the step with h = dttry whatever its error (replay
+        of a prescribed step sequence, used to compare arithmetic precisions on
+        identical steps; not a reference feature)."""
         nrjct = 0
         h = dttry
         self.traction_rates()
         while True:
             Tno_y, Tt1o_y, Tt2o_y, state_y, c1, c2, hn1, hn2 = self.rk_attempt(h)
-            if max(c1, c2) < 1.0 and not (np.isnan(c1) or np.isnan(c2)):
+            if force or (max(c1, c2) < 1.0 and not (np.isnan(c1) or np.isnan(c2))):
                 dtnext = min(hn1, hn2)
                 dtnext = min(1.5 * h, dtnext)
                 break
@@ -202,10 +206,16 @@ class DenseStepper:
         return h, dtnext, nrjct + 1
 
     def run(self, nsteps, dt0=1e-3):
-        """The reference main loop (src/main_gpu.py:112-118): dttry = dtnext."""
+        """The reference main loop (src/main_gpu.py:112-118): dttry = dtnext.
+        Returns rows (h, time, attempts)."""
         dttry = dt0
         hist = []
         for _ in range(nsteps):
             h, dttry, att = self.simu_forward(dttry)
             hist.append((h, self.time, att))
         return np.array(hist)
+
+    def replay(self, hs):
+        """Take the given step sizes, one attempt each, no step control."""
+        for h in hs:
+            self.simu_forward(float(h), force=True)

@@ -137,21 +137,27 @@ class DenseDeviceSim:
         b = self.ctrl_t.cpu().numpy().tobytes()
         return _lib.StepCtrl.from_buffer_copy(b)
 
-    def launch(self, nsteps, h_hist=None, t_hist=None, stream=None):
+    def launch(self, nsteps, h_hist=None, t_hist=None, h_force=None, stream=None):
         """Queue nsteps accepted steps (asynchronous)."""
         L = _lib.load()
         st = torch.cuda.current_stream(self.device).cuda_stream if stream is None else stream
         rc = L.pq3d_dense_step(ctypes.byref(self.S), int(nsteps),
                                h_hist.data_ptr() if h_hist is not None else None,
-                               t_hist.data_ptr() if t_hist is not None else None, st)
+                               t_hist.data_ptr() if t_hist is not None else None,
+                               h_force.data_ptr() if h_force is not None else None, st)
         _lib.check(rc)
 
-    def step(self, nsteps=1):
-        """nsteps accepted steps; returns (h[n], t[n], ctrl) on the host."""
+    def step(self, nsteps=1, h_force=None):
+        """nsteps accepted steps; returns (h[n], t[n], ctrl) on the host.
+        ``h_force`` (sequence of nsteps step sizes) replays a step sequence."""
         dev = self.device
         h = torch.empty(nsteps, dtype=torch.float64, device=dev)
         t = torch.empty(nsteps, dtype=torch.float64, device=dev)
-        self.launch(nsteps, h, t)
+        hf = None
+        if h_force is not None:
+            hf = torch.as_tensor(np.asarray(h_force, dtype=np.float64)[:nsteps], device=dev).contiguous()
+            assert hf.numel() == nsteps
+        self.launch(nsteps, h, t, hf)
         c = self.read_ctrl()
         if c.status == _lib.PQ3D_ERR_STEP:
             raise StepError("error: dt is too small (after %d accepted steps)" % c.steps_done)

@@ -70,7 +70,7 @@ _SIGS = {
     "pq3d_assemble_dense_host": (c_int, [c_void_p, c_i64, c_void_p, c_i64, c_dbl, c_dbl, c_int, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f64": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f32": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
-    "pq3d_dense_step": (c_int, [ctypes.POINTER(DenseSim), c_int, c_void_p, c_void_p, c_void_p]),
+    "pq3d_dense_step": (c_int, [ctypes.POINTER(DenseSim), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

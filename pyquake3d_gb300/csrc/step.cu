@@ -221,7 +221,8 @@ __device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b
 __device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b : a; }
 
 template <bool kF32>
-__global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist)
+__global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist,
+                                                         const double *h_force)
 {
     __shared__ double red[8];
     pq3d_step_ctrl *C = S.ctrl;
@@ -258,7 +259,7 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
         if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
 
         // (2) attempts until one is accepted
-        double h = dttry, dtnext = 0.0;
+        double h = h_force ? h_force[step] : dttry, dtnext = 0.0;
         int nrjct = 0;
         for (;;) {
             const int slot = (int)(attempt % 3);
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             const double c1 = err1 / kRelTol, c2 = err2 / kRelTol;
             const double hn1 = h * 0.9 * pow(kRelTol / err1, 0.2);
             const double hn2 = h * 0.9 * pow(kRelTol / err2, 0.2);
-            if (fmax(c1, c2) < 1.0 && !(isnan(c1) || isnan(c2))) {
+            if (h_force || (fmax(c1, c2) < 1.0 && !(isnan(c1) || isnan(c2)))) {
                 dtnext = pymin(1.5 * h, pymin(hn1, hn2));
                 break;
             }
@@ -401,7 +402,8 @@ extern "C" int pq3d_dense_matvec_f32(const float *K32, int64_t N, const double *
     return matvec(K32, N, v, out, stream, true);
 }
 
-extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist, void *stream)
+extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist,
+                               const double *h_force, void *stream)
 {
     clear_error();
     PQ3D_REQUIRE(sim && sim->N > 0 && nsteps >= 0 && sim->ctrl, "pq3d_dense_step: bad arguments");
@@ -418,7 +420,7 @@ extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_
     cudaStream_t st = (cudaStream_t)stream;
     PQ3D_CUDA_TRY(cudaMemsetAsync(&sim->ctrl->err_slot[0], 0, sizeof(uint64_t) * 7 + sizeof(uint32_t), st));
     pq3d_dense_sim S = *sim;
-    void *args[] = {(void *)&S, (void *)&nsteps, (void *)&h_hist, (void *)&t_hist};
+    void *args[] = {(void *)&S, (void *)&nsteps, (void *)&h_hist, (void *)&t_hist, (void *)&h_force};
     if (f32)
         PQ3D_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)dense_step_kernel<true>, grid, 256, args, 0, st));
     else

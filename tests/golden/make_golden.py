@@ -264,7 +264,7 @@ def main():
             h, dttry = sim.simu_forward(dttry)
             hs.append(h)
             ts.append(sim.time)
-            if (i + 1) in (1, 10, 100, 200, 400):
+            if (i + 1) in (1, 10, 30, 60, 100, 200, 400):
                 for k in ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2", "slip", "rake"):
                     ckpt[f"s{i + 1}_{k}"] = np.array(getattr(sim, k))
         traj["h"], traj["t"] = np.array(hs), np.array(ts)

