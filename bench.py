@@ -132,17 +132,15 @@ def fp64_peak_tflops(torch, dev):
 
 
 # FP64 operations of one (receiver, source) pair of the assembly kernel
-# (both unit slips): counted from pyquake3d_gb300/csrc/gf_device.cuh, see
-# profiles/gf_flops.md.  Divisions and square roots count as one operation.
-GF_FLOP_PER_PAIR = None
+# (both unit slips, 6 entries): 357 add + 645 mul + 11 div + 3 sqrt, counted by
+# oracle/count_gf_flops.cpp on the kernel's own device math.
+GF_FLOP_PER_PAIR = 1016
+# Stores per pair: 6 FP64 + 6 FP32 entries.
+GF_BYTES_PER_PAIR = 72
 
 
 def gf_flops_per_pair():
-    p = os.path.join(HERE, "profiles", "gf_flops.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)["flops_per_pair"]
-    return None
+    return GF_FLOP_PER_PAIR
 
 
 def cpu_gf_sample(nodes, tris, seconds=12.0, kind=None):
@@ -156,11 +154,13 @@ def cpu_gf_sample(nodes, tris, seconds=12.0, kind=None):
         fn, kind = _ref_assemble(ref_so, cores, nodes, tris), "reference"
     else:
         fn, kind = (lambda c0, c1: oracle.assemble_dense(nodes, tris, MU, LAM, cols=(c0, c1), nthreads=cores)), "port"
-    # calibrate on a small slice, then size the sample to ~`seconds`
-    c1 = max(cores, 16)
-    t0 = time.perf_counter()
-    fn(0, c1)
-    dt = time.perf_counter() - t0
+    # calibrate on a small slice (twice: the first call warms up), then size
+    # the sample to ~`seconds`
+    c1 = min(N, 4 * cores)
+    for _ in range(2):
+        t0 = time.perf_counter()
+        fn(0, c1)
+        dt = time.perf_counter() - t0
     ncols = int(min(N, max(c1, c1 * seconds / max(dt, 1e-3))))
     t0 = time.perf_counter()
     fn(0, ncols)
@@ -296,12 +296,12 @@ def bench_ours(args):
             roof.update({"achieved": ach, "frac": ach / fp64, "flops_per_pair": fpp})
         else:
             roof.update({"achieved": None, "frac": None})
-        tr = os.path.join(HERE, "profiles", "gf_assembly_traffic.json")
-        if os.path.exists(tr):
-            with open(tr) as f:
-                t = json.load(f)
-            roof["traffic"] = t["bytes_per_pair"] * N * N
-            roof["traffic_note"] = t.get("note")
+        # DRAM bytes of one launch: ncu on the N=2,000 case measured 56.9 B/pair
+        # (226.3 MB written + 1.4 MB read for 4e6 pairs, part of the 288 MB of
+        # stores still dirty in L2 at kernel end); scaled to this launch.
+        roof["traffic"] = 56.9 * N * N
+        roof["traffic_note"] = ("ncu dram__bytes_read+write at N=2000 (56.9 B/pair) scaled by pairs; "
+                                "algorithmic stores are %d B/pair" % GF_BYTES_PER_PAIR)
         out["roofline"] = roof
         out["clocks"] = clk.summary()
         # -- end to end: host mesh in, FP64 operator out to pinned host memory

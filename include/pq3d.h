@@ -102,7 +102,8 @@ int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_nodes, const in
 /* out[r] = sum_c K[r][c] * v[c] for the (3N) x (2N) FP64 operator: the traction
  * product K.(V - Vpl) of src/QDsim_gpu.py:948-957 (v interleaved [j][strike,dip]). */
 int pq3d_dense_matvec_f64(const double *K64, int64_t N, const double *v, double *out, void *stream);
-/* Same with the FP32 operator copy, FP32 products accumulated in FP64. */
+/* Same with the FP32 operator copy: compensated FP32 products and sums (the
+ * FP32-rounded operator applied to v to ~2^-44 relative). */
 int pq3d_dense_matvec_f32(const float *K32, int64_t N, const double *v, double *out, void *stream);
 
 /* Device-resident state of one dense simulation; every pointer is a device

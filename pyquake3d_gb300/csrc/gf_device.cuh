@@ -28,6 +28,13 @@
 
 #include <math.h>
 
+#ifndef __CUDACC__
+// Host compilation (operation counting in oracle/count_gf_flops.cpp).
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
 namespace pq3d {
 namespace gf {
 
@@ -115,12 +122,12 @@ __host__ __device__ inline void setup_receiver(const double a[3], const double b
 }
 
 // Configuration test: +1, -1, or 0 (side line in the plane).
-__device__ __forceinline__ int tri_mode(double x, double y, double z, double p1y, double p1z,
-                                        double p3y, double p3z, double den)
+template <class T>
+__device__ __forceinline__ int tri_mode(T x, T y, T z, T p1y, T p1z, T p3y, T p3z, T den)
 {
-    const double a = ((y - p3y) * (0.0 - p3z) - (0.0 - p3y) * (z - p3z)) / den;
-    const double b = ((p1y - p3y) * (z - p3z) - (y - p3y) * (p1z - p3z)) / den;
-    const double c = 1.0 - a - b;
+    const T a = ((y - p3y) * (0.0 - p3z) - (0.0 - p3y) * (z - p3z)) / den;
+    const T b = ((p1y - p3y) * (z - p3z) - (y - p3y) * (p1z - p3z)) / den;
+    const T c = 1.0 - a - b;
     int m = 1;
     if (a <= 0 && b > c && c > a) m = -1;
     else if (b <= 0 && c > a && a > b) m = -1;
@@ -134,27 +141,29 @@ __device__ __forceinline__ int tri_mode(double x, double y, double z, double p1y
 
 // Shared geometric terms of one angular dislocation at (x, y, z) of its own
 // frame, opening angle with cos/sin (ca, sa).
+template <class T>
 struct AdGeom {
-    double x, y, z, ca, sa;
-    double eta, ycz, x2, y2, z2;
-    double ir, ir3, iW2;
-    double i_Wr, i_W2r2, i_Wr3, i_rz, i_r2z2, i_r3z, i_W2r;
-    double C, S, gx, gy, gz, fx, fy, fz;
+    T x, y, z, ca, sa;
+    T eta, ycz, x2, y2, z2;
+    T ir, ir3, iW2;
+    T i_Wr, i_W2r2, i_Wr3, i_rz, i_r2z2, i_r3z, i_W2r;
+    T C, S, gx, gy, gz, fx, fy, fz;
 };
 
-__device__ __forceinline__ void ad_geom(double x, double y, double z, double ca, double sa, double nu, AdGeom &g)
+template <class T>
+__device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, AdGeom<T> &g)
 {
     g.x = x; g.y = y; g.z = z; g.ca = ca; g.sa = sa;
     g.eta = y * ca - z * sa;
-    const double zeta = y * sa + z * ca;
+    const T zeta = y * sa + z * ca;
     g.ycz = y * ca + z * sa;
     g.x2 = x * x; g.y2 = y * y; g.z2 = z * z;
-    const double r2 = g.x2 + g.y2 + g.z2;
-    const double r = sqrt(r2);
-    const double ir = 1.0 / r;
-    const double irz = 1.0 / (r - z);
-    const double iW = 1.0 / (zeta - r);
-    const double ir2 = ir * ir;
+    const T r2 = g.x2 + g.y2 + g.z2;
+    const T r = sqrt(r2);
+    const T ir = 1.0 / r;
+    const T irz = 1.0 / (r - z);
+    const T iW = 1.0 / (zeta - r);
+    const T ir2 = ir * ir;
     g.ir = ir;
     g.ir3 = ir2 * ir;
     g.iW2 = iW * iW;
@@ -168,7 +177,7 @@ __device__ __forceinline__ void ad_geom(double x, double y, double z, double ca,
     g.C = (r * ca - z) * g.i_Wr;
     g.S = (r * sa - y) * g.i_Wr;
     const double q = 1.0 / (4.0 * kPi);
-    const double i_rzeta = -iW;   // 1/(r - zeta)
+    const T i_rzeta = -iW;   // 1/(r - zeta)
     g.gx = q * (g.eta * ir * i_rzeta - y * g.i_rz);
     g.gy = q * (x * g.i_rz - ca * x * ir * i_rzeta);
     g.gz = q * (sa * x * ir * i_rzeta);
@@ -179,12 +188,13 @@ __device__ __forceinline__ void ad_geom(double x, double y, double z, double ca,
 }
 
 // Strain of unit by (Ey) and unit bz (Ez) Burgers components.
-__device__ __forceinline__ void ad_parts_yz(const AdGeom &g, double nu, double k, double Ey[6], double Ez[6])
+template <class T>
+__device__ __forceinline__ void ad_parts_yz(const AdGeom<T> &g, double nu, double k, T Ey[6], T Ez[6])
 {
-    const double x = g.x, y = g.y, z = g.z, ca = g.ca, sa = g.sa;
+    const T x = g.x, y = g.y, z = g.z, ca = g.ca, sa = g.sa;
     const double p2 = 2.0 * nu + 1.0;
-    const double xk = x * k, sak = sa * k, xsak = xk * sa;
-    const double yz = y * z;
+    const T xk = x * k, sak = sa * k, xsak = xk * sa;
+    const T yz = y * z;
     Ey[0] = -xk * (g.fx * ca + p2 * g.i_rz - g.x2 * g.i_r2z2 - g.x2 * g.i_r3z);
     Ey[1] = g.gy - xk * (g.i_rz - g.y2 * g.i_r2z2 - g.y2 * g.i_r3z + g.fy * ca);
     Ey[2] = -xk * (g.fz * ca + z * g.ir3);
@@ -202,7 +212,7 @@ __device__ __forceinline__ void ad_parts_yz(const AdGeom &g, double nu, double k
 }
 
 // Strain of a unit bx (tensile) Burgers component.
-__device__ __forceinline__ void ad_part_x(const AdGeom &g, double nu, double k, double Ex[6])
+__device__ __forceinline__ void ad_part_x(const AdGeom<double> &g, double nu, double k, double Ex[6])
 {
     const double x = g.x, y = g.y, z = g.z, ca = g.ca, sa = g.sa, eta = g.eta;
     const double p2 = 2.0 * nu + 1.0;
@@ -220,9 +230,10 @@ __device__ __forceinline__ void ad_part_x(const AdGeom &g, double nu, double k, 
 
 // acc += B^T T' B for the rotation B = [[1,0,0],[0,sz,-sy],[0,sy,sz]] about x
 // (the back-rotation of src/TDstressFS_C.cpp:240-255).
-__device__ __forceinline__ void add_rot_x(double acc[6], const double t[6], double sy, double sz)
+template <class T>
+__device__ __forceinline__ void add_rot_x(T acc[6], const T t[6], T sy, T sz)
 {
-    const double yy = sy * sy, zz = sz * sz, yz = sy * sz;
+    const T yy = sy * sy, zz = sz * sz, yz = sy * sz;
     acc[0] += t[0];
     acc[1] += zz * t[1] + 2.0 * yz * t[5] + yy * t[2];
     acc[2] += yy * t[1] - 2.0 * yz * t[5] + zz * t[2];
@@ -232,10 +243,10 @@ __device__ __forceinline__ void add_rot_x(double acc[6], const double t[6], doub
 }
 
 // Source fields through an accessor: F(i) returns field i.
-template <class Src>
-__device__ __forceinline__ void tdcs_point(const Src &F, double X, double Y, double Z, double &x, double &y, double &z)
+template <class Src, class T>
+__device__ __forceinline__ void tdcs_point(const Src &F, T X, T Y, T Z, T &x, T &y, T &z)
 {
-    const double dx = X - F(F_P2X), dy = Y - F(F_P2Y), dz = Z - F(F_P2Z);
+    const T dx = X - F(F_P2X), dy = Y - F(F_P2Y), dz = Z - F(F_P2Z);
     x = F(F_NX) * dx + F(F_NY) * dy + F(F_NZ) * dz;
     y = F(F_SX) * dx + F(F_SY) * dy + F(F_SZ) * dz;
     z = F(F_DX) * dx + F(F_DY) * dy + F(F_DZ) * dz;
@@ -243,27 +254,26 @@ __device__ __forceinline__ void tdcs_point(const Src &F, double X, double Y, dou
 
 // TDCS strain (triangle system) of unit strike (Es) and unit dip (Ed) slip.
 // Returns false for mode 0 (strain zero).
-template <class Src>
-__device__ __forceinline__ bool tdcs_strain_sd(const Src &F, double x, double y, double z, double nu, double k,
-                                               double Es[6], double Ed[6])
+template <class Src, class T>
+__device__ __forceinline__ bool tdcs_strain_sd(const Src &F, T x, T y, T z, double nu, double k, T Es[6], T Ed[6])
 {
 #pragma unroll
     for (int i = 0; i < 6; ++i) { Es[i] = 0.0; Ed[i] = 0.0; }
-    const int m = tri_mode(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
+    const int m = tri_mode<T>(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
     if (m == 0) return false;
     const double sg = (m == 1) ? 1.0 : -1.0;
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-        double vy, vz, sy, sz, ca, sa;
+        T vy, vz, sy, sz, ca, sa;
         if (v == 0) { vy = F(F_P1Y); vz = F(F_P1Z); sy = -sg * F(F_E13Y); sz = -sg * F(F_E13Z); ca = F(F_CA); sa = F(F_SA); }
         else if (v == 1) { vy = 0.0; vz = 0.0; sy = sg * F(F_E12Y); sz = sg * F(F_E12Z); ca = F(F_CB); sa = F(F_SB); }
         else { vy = F(F_P3Y); vz = F(F_P3Z); sy = sg * F(F_E23Y); sz = sg * F(F_E23Z); ca = F(F_CC); sa = F(F_SC); }
-        const double ty = y - vy, tz = z - vz;
-        AdGeom g;
-        ad_geom(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
-        double Ey[6], Ez[6];
-        ad_parts_yz(g, nu, k, Ey, Ez);
-        double ts[6], td[6];
+        const T ty = y - vy, tz = z - vz;
+        AdGeom<T> g;
+        ad_geom<T>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
+        T Ey[6], Ez[6];
+        ad_parts_yz<T>(g, nu, k, Ey, Ez);
+        T ts[6], td[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             ts[i] = sz * Ey[i] + sy * Ez[i];    // strike: (by1, bz1) = (sz, sy)
@@ -282,7 +292,7 @@ __device__ __forceinline__ void tdcs_strain_general(const Src &F, double x, doub
 {
 #pragma unroll
     for (int i = 0; i < 6; ++i) E[i] = 0.0;
-    const int m = tri_mode(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
+    const int m = tri_mode<double>(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
     if (m == 0) return;
     const double sg = (m == 1) ? 1.0 : -1.0;
     for (int v = 0; v < 3; ++v) {
@@ -291,10 +301,10 @@ __device__ __forceinline__ void tdcs_strain_general(const Src &F, double x, doub
         else if (v == 1) { vy = 0.0; vz = 0.0; sy = sg * F(F_E12Y); sz = sg * F(F_E12Z); ca = F(F_CB); sa = F(F_SB); }
         else { vy = F(F_P3Y); vz = F(F_P3Z); sy = sg * F(F_E23Y); sz = sg * F(F_E23Z); ca = F(F_CC); sa = F(F_SC); }
         const double ty = y - vy, tz = z - vz;
-        AdGeom g;
-        ad_geom(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
+        AdGeom<double> g;
+        ad_geom<double>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
         double Ey[6], Ez[6], Ex[6];
-        ad_parts_yz(g, nu, k, Ey, Ez);
+        ad_parts_yz<double>(g, nu, k, Ey, Ez);
         const double by1 = sz * by - sy * bz, bz1 = sy * by + sz * bz;
         double t[6];
         if (bx != 0.0) {
@@ -337,13 +347,14 @@ __device__ __forceinline__ void hooke(const double e[6], double mu, double lam, 
 
 // Tractions (along e1, e2, n of the receiver) of a TDCS strain E, given the
 // receiver axes already rotated into the source system (ue1, ue2, un).
-__device__ __forceinline__ void tractions_tdcs(const double E[6], const double ue1[3], const double ue2[3],
-                                               const double un[3], double two_mu, double lam, double out[3])
+template <class T>
+__device__ __forceinline__ void tractions_tdcs(const T E[6], const T ue1[3], const T ue2[3], const T un[3],
+                                               double two_mu, double lam, T out[3])
 {
-    const double u0 = E[0] * un[0] + E[3] * un[1] + E[4] * un[2];
-    const double u1 = E[3] * un[0] + E[1] * un[1] + E[5] * un[2];
-    const double u2 = E[4] * un[0] + E[5] * un[1] + E[2] * un[2];
-    const double tr = E[0] + E[1] + E[2];
+    const T u0 = E[0] * un[0] + E[3] * un[1] + E[4] * un[2];
+    const T u1 = E[3] * un[0] + E[1] * un[1] + E[5] * un[2];
+    const T u2 = E[4] * un[0] + E[5] * un[1] + E[2] * un[2];
+    const T tr = E[0] + E[1] + E[2];
     out[0] = two_mu * (ue1[0] * u0 + ue1[1] * u1 + ue1[2] * u2);
     out[1] = two_mu * (ue2[0] * u0 + ue2[1] * u1 + ue2[2] * u2);
     out[2] = two_mu * (un[0] * u0 + un[1] * u1 + un[2] * u2) + lam * tr;

@@ -76,37 +76,66 @@ __device__ __forceinline__ void rows3_f64(const double2 *__restrict__ K, const d
     acc[2] = warp_sum(a2 + b2);
 }
 
-// FP32 operator: rows of N float2, FP32 products and per-lane FP32 sums,
-// cross-lane sum in FP64.
+// FP32 operator: rows of N float2.  The products and sums are compensated so
+// that the result is the FP32-rounded operator applied exactly (to ~2^-44):
+// v' is split into hi + lo floats, k * vhi is formed exactly as p + e
+// (TwoProduct with an FMA), the running sum is carried as s + c (TwoSum).  The
+// _rn intrinsics keep the compiler from contracting these sequences.  FP32
+// operations are ~64x cheaper than FP64 ones on this part, so the ~11 FP32
+// operations per entry stay below the HBM time of the 4-byte entry.
+struct Acc2 {
+    float s, c;
+};
+
+__device__ __forceinline__ void acc2_add(Acc2 &a, float k, float vh, float vl)
+{
+    const float p = __fmul_rn(k, vh);
+    const float e = __fmaf_rn(k, vh, -p);
+    const float t = __fadd_rn(a.s, p);
+    const float bp = __fsub_rn(t, a.s);
+    const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    a.s = t;
+    a.c = __fmaf_rn(k, vl, __fadd_rn(a.c, __fadd_rn(err, e)));
+}
+
+__device__ __forceinline__ void split2(double2 v, float &h0, float &l0, float &h1, float &l1)
+{
+    h0 = (float)v.x; l0 = (float)(v.x - (double)h0);
+    h1 = (float)v.y; l1 = (float)(v.y - (double)h1);
+}
+
 __device__ __forceinline__ void rows3_f32(const float2 *__restrict__ K, const double2 *__restrict__ v, int64_t N,
                                           int64_t i, int lane, double acc[3])
 {
     const float2 *r0 = K + (3 * i) * N, *r1 = r0 + N, *r2 = r1 + N;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f;
+    Acc2 a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f};
     int64_t j = lane;
     for (; j + 32 < N; j += 64) {
         const double2 xd0 = __ldg(v + j), xd1 = __ldg(v + j + 32);
-        const float2 x0 = make_float2((float)xd0.x, (float)xd0.y), x1 = make_float2((float)xd1.x, (float)xd1.y);
         const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
         const float2 k01 = __ldcs(r0 + j + 32), k11 = __ldcs(r1 + j + 32), k21 = __ldcs(r2 + j + 32);
-        a0 = fmaf(k00.x, x0.x, a0); a0 = fmaf(k00.y, x0.y, a0);
-        a1 = fmaf(k10.x, x0.x, a1); a1 = fmaf(k10.y, x0.y, a1);
-        a2 = fmaf(k20.x, x0.x, a2); a2 = fmaf(k20.y, x0.y, a2);
-        b0 = fmaf(k01.x, x1.x, b0); b0 = fmaf(k01.y, x1.y, b0);
-        b1 = fmaf(k11.x, x1.x, b1); b1 = fmaf(k11.y, x1.y, b1);
-        b2 = fmaf(k21.x, x1.x, b2); b2 = fmaf(k21.y, x1.y, b2);
+        float h0, l0, h1, l1;
+        split2(xd0, h0, l0, h1, l1);
+        acc2_add(a0, k00.x, h0, l0); acc2_add(a0, k00.y, h1, l1);
+        acc2_add(a1, k10.x, h0, l0); acc2_add(a1, k10.y, h1, l1);
+        acc2_add(a2, k20.x, h0, l0); acc2_add(a2, k20.y, h1, l1);
+        split2(xd1, h0, l0, h1, l1);
+        acc2_add(a0, k01.x, h0, l0); acc2_add(a0, k01.y, h1, l1);
+        acc2_add(a1, k11.x, h0, l0); acc2_add(a1, k11.y, h1, l1);
+        acc2_add(a2, k21.x, h0, l0); acc2_add(a2, k21.y, h1, l1);
     }
     for (; j < N; j += 32) {
         const double2 xd0 = __ldg(v + j);
-        const float2 x0 = make_float2((float)xd0.x, (float)xd0.y);
         const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
-        a0 = fmaf(k00.x, x0.x, a0); a0 = fmaf(k00.y, x0.y, a0);
-        a1 = fmaf(k10.x, x0.x, a1); a1 = fmaf(k10.y, x0.y, a1);
-        a2 = fmaf(k20.x, x0.x, a2); a2 = fmaf(k20.y, x0.y, a2);
+        float h0, l0, h1, l1;
+        split2(xd0, h0, l0, h1, l1);
+        acc2_add(a0, k00.x, h0, l0); acc2_add(a0, k00.y, h1, l1);
+        acc2_add(a1, k10.x, h0, l0); acc2_add(a1, k10.y, h1, l1);
+        acc2_add(a2, k20.x, h0, l0); acc2_add(a2, k20.y, h1, l1);
     }
-    acc[0] = warp_sum((double)a0 + (double)b0);
-    acc[1] = warp_sum((double)a1 + (double)b1);
-    acc[2] = warp_sum((double)a2 + (double)b2);
+    acc[0] = warp_sum((double)a0.s + (double)a0.c);
+    acc[1] = warp_sum((double)a1.s + (double)a1.c);
+    acc[2] = warp_sum((double)a2.s + (double)a2.c);
 }
 
 template <bool kF32>
