@@ -160,6 +160,82 @@ typedef struct pq3d_step_ctrl {
 int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist,
                     const double *h_force, void *stream);
 
+/* ---------------- device: batched ensemble (B runs, one mesh) ---------------- */
+
+/* Per-run control block (device memory, one per run). */
+typedef struct pq3d_run_ctrl {
+    double h;              /* trial dt of the next attempt (dttry, then dtnext) */
+    double time;           /* simulated time (s) */
+    double t_end;          /* the run retires once time >= t_end */
+    double h_last;         /* dt of the last accepted step */
+    int64_t attempts;      /* attempted steps (7 right-hand-side evaluations each) */
+    int64_t steps;         /* accepted steps */
+    int64_t max_steps;     /* the run retires after this many accepted steps */
+    uint64_t err1_bits;    /* max-error reduction of the current attempt (double bits) */
+    uint64_t err2_bits;
+    int32_t status;        /* PQ3D_OK or PQ3D_ERR_STEP */
+    int32_t active;        /* 1 while the run steps */
+    int32_t nrjct;         /* rejected attempts of the current step */
+    int32_t accepted;      /* 1 if the last attempt was accepted */
+} pq3d_run_ctrl;
+
+/* Traction-product operand precision of the batched stepper. */
+#define PQ3D_BATCH_FP64 0      /* FP64 operator, FP64 FMA (CUDA cores) */
+#define PQ3D_BATCH_FP32 1      /* FP32 operator, FP32 FMA (CUDA cores), FP64 across chunks */
+#define PQ3D_BATCH_BF16X6 2    /* FP32 operator split on the fly into 3 BF16 pieces, v' into 3 BF16
+                                  pieces, the 6 leading cross products on tcgen05 tensor cores,
+                                  FP32 accumulation in tensor memory, FP64 across K slices */
+
+/* Device state of B simulations sharing one mesh.  Arrays are run-major
+ * [B][N] FP64 unless stated.  Same fields and units as pq3d_dense_sim. */
+typedef struct pq3d_batch_sim {
+    int64_t N;
+    int32_t B;
+    int32_t precision;     /* PQ3D_BATCH_* */
+    double *Tno, *Tt1o, *Tt2o, *state, *slipv1, *slipv2, *slipv, *slip1, *slip2;
+    const double *a, *b, *dc, *f0, *shear_loading, *normal_loading, *cos_rake0, *sin_rake0;
+    double *rates;         /* [nsplit][B][3N] partial traction rates, summed in FP64 by the stepper */
+    int32_t nsplit;        /* K-slices of the operator product (>= 1) */
+    int32_t pad0;
+    double *cand;          /* [B][N][4] candidate state */
+    void *vop;             /* operator-product right-hand side of all runs, padded to Bp = B rounded up
+                              to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], or for
+                              BF16X6 the packed pieces (pq3d_batch_rhs_bytes, zero-initialised) */
+    const void *K;         /* operator: FP64 (3N)x(2N) for FP64, FP32 (3N)x(2N) for FP32, the
+                              packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6 */
+    pq3d_run_ctrl *ctrl;   /* [B] */
+    double V0, Vpl, eta;
+    int32_t fix_Tn;
+    int32_t pad1;
+} pq3d_batch_sim;
+
+/* Packed operator of the tensor-core product: the FP64 operator split into
+ * three BF16 pieces, stored as [3N/128 tiles][2N/32 blocks][3][128 x 32]
+ * shared-memory images (8-row x 16-byte core matrices).  Bytes, and the packing
+ * kernel (run once after assembly). */
+size_t pq3d_batch_operator_bytes(int64_t N);
+int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpacked, void *stream);
+/* Bytes of the packed right-hand side for B runs (BF16X6). */
+size_t pq3d_batch_rhs_bytes(int64_t N, int B);
+/* The tensor-core product alone: out[(s*Bp + n)*3N + m] (s < nsplit K slices,
+ * Bp = B rounded up to 16) from the packed operator and right-hand side. */
+int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, double *out,
+                           void *workspace, size_t workspace_bytes, void *stream);
+
+/* Device workspace bytes of one batched iteration (GEMM split-K partials live in
+ * sim->rates; this is what the tensor-core product needs besides). */
+size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim);
+
+/* Prepare the operator right-hand side from the current slip rates (run once
+ * before the first iteration and after any host-side change of the state). */
+int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream);
+
+/* One batched iteration on `stream`, graph-capturable: the operator product
+ * for all runs, one Dormand-Prince attempt per active run with its own dt,
+ * the per-run accept/reject decision and the state update of the accepted runs
+ * (masked acceptance; rejected runs retry with their smaller dt next time). */
+int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

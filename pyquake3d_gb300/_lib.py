@@ -48,6 +48,30 @@ class DenseSim(ctypes.Structure):
         [("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", c_int)]
 
 
+class RunCtrl(ctypes.Structure):
+    """Mirror of pq3d_run_ctrl (88 bytes)."""
+    _fields_ = [("h", c_dbl), ("time", c_dbl), ("t_end", c_dbl), ("h_last", c_dbl), ("attempts", c_i64),
+                ("steps", c_i64), ("max_steps", c_i64), ("err1_bits", ctypes.c_uint64), ("err2_bits", ctypes.c_uint64),
+                ("status", ctypes.c_int32), ("active", ctypes.c_int32), ("nrjct", ctypes.c_int32),
+                ("accepted", ctypes.c_int32)]
+
+
+class BatchSim(ctypes.Structure):
+    """Mirror of pq3d_batch_sim."""
+    _fields_ = [("N", c_i64), ("B", ctypes.c_int32), ("precision", ctypes.c_int32)] + \
+        [(n, c_void_p) for n in ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2",
+                                 "a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0",
+                                 "rates")] + \
+        [("nsplit", ctypes.c_int32), ("pad0", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
+         ("ctrl", c_void_p), ("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", ctypes.c_int32),
+         ("pad1", ctypes.c_int32)]
+
+
+PQ3D_BATCH_FP64 = 0
+PQ3D_BATCH_FP32 = 1
+PQ3D_BATCH_BF16X6 = 2
+
+
 class StepCtrl(ctypes.Structure):
     """Mirror of pq3d_step_ctrl (104 bytes)."""
     _fields_ = [("dttry", c_dbl), ("time", c_dbl), ("maxv", c_dbl), ("status", ctypes.c_int32),
@@ -71,6 +95,13 @@ _SIGS = {
     "pq3d_dense_matvec_f64": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f32": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_step": (c_int, [ctypes.POINTER(DenseSim), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pq3d_batch_operator_bytes": (c_size, [c_i64]),
+    "pq3d_batch_pack_operator": (c_int, [c_void_p, c_i64, c_void_p, c_void_p]),
+    "pq3d_batch_rhs_bytes": (c_size, [c_i64, c_int]),
+    "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size, c_void_p]),
+    "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
+    "pq3d_batch_prepare": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
+    "pq3d_batch_iterate": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
 }
 
 _lib = None

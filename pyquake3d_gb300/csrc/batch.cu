@@ -1,0 +1,353 @@
+// Batched ensemble stepping: B simulations that share one mesh (one traction
+// operator) and differ in friction, stress and nucleation, stepped together.
+//
+// One iteration (graph-capturable, no host synchronisation):
+//   1. operator product for all runs at once:  rates[.][r] = K . v'_r
+//      (a GEMM (3N x 2N) x (2N x B) instead of B matrix-vector products)
+//   2. attempt: one Dormand-Prince 5(4) attempt per (run, cell) with the run's
+//      own dt, per-run max error norms by one atomicMax per block
+//   3. decide: per run accept/reject and the next dt (src/QDsim_gpu.py:959-985)
+//   4. update: accepted runs advance (slip rate, slip, v'); rejected runs keep
+//      their state and retry with the smaller dt at the next iteration
+//      ("masked stage acceptance": every run keeps its own step sequence).
+// Semantics per run are those of the single-simulation stepper (step.cu) and
+// the reference CPU path (src/QDsim_gpu.py:1029-1122).
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "gemm_tc.cuh"
+#include "rk_device.cuh"
+
+namespace pq3d {
+namespace batch {
+
+using namespace ::pq3d::rk;
+
+
+// padded run count of the operator right-hand side and of the rate partials
+__host__ __device__ inline int padded_runs(int B) { return (B + 15) / 16 * 16; }
+
+// ---------------------------------------------------------------------------
+// operator right-hand side v'_r = V_r - Vpl (cos, sin)(rake0), interleaved
+
+__device__ __forceinline__ void vprime(const pq3d_batch_sim &S, int64_t idx, double &v1, double &v2)
+{
+    v1 = S.slipv1[idx] - S.Vpl * S.cos_rake0[idx];
+    v2 = S.slipv2[idx] - S.Vpl * S.sin_rake0[idx];
+}
+
+// 3-piece BF16 split of an FP64 value: x ~= p0 + p1 + p2 (24 significant bits).
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
+{
+    p0 = __double2bfloat16(x);
+    const double r1 = x - (double)__bfloat162float(p0);
+    p1 = __double2bfloat16(r1);
+    const double r2 = r1 - (double)__bfloat162float(p1);
+    p2 = __double2bfloat16(r2);
+}
+
+__device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_t i, double v1, double v2)
+{
+    const int64_t N = S.N;
+    const int Bp = padded_runs(S.B);
+    const int64_t o = (int64_t)r * 2 * N + 2 * i;
+    (void)Bp;
+    if (S.precision == PQ3D_BATCH_FP64) {
+        reinterpret_cast<double2 *>((double *)S.vop + o)[0] = make_double2(v1, v2);
+    } else if (S.precision == PQ3D_BATCH_FP32) {
+        reinterpret_cast<float2 *>((float *)S.vop + o)[0] = make_float2((float)v1, (float)v2);
+    } else {
+        // packed images [k block][piece][Bp x 32] (see gemm_tc.cuh)
+        const int64_t k = 2 * i;
+        const int64_t img = (int64_t)Bp * tc::kBlockK;
+        __nv_bfloat16 *P = (__nv_bfloat16 *)S.vop + (k / tc::kBlockK) * tc::kPieces * img +
+                           tc::image_offset(r, (int)(k % tc::kBlockK));
+        __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+        split3(v1, a0, a1, a2);
+        split3(v2, b0, b1, b2);
+        __nv_bfloat162 q;
+        q.x = a0; q.y = b0; reinterpret_cast<__nv_bfloat162 *>(P)[0] = q;
+        q.x = a1; q.y = b1; reinterpret_cast<__nv_bfloat162 *>(P + img)[0] = q;
+        q.x = a2; q.y = b2; reinterpret_cast<__nv_bfloat162 *>(P + 2 * img)[0] = q;
+    }
+}
+
+__global__ void prepare_kernel(pq3d_batch_sim S)
+{
+    const int r = blockIdx.y;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    double v1 = 0.0, v2 = 0.0;
+    if (r < S.B) vprime(S, (int64_t)r * S.N + i, v1, v2);   // padding runs stay zero
+    write_vop(S, r, i, v1, v2);
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-core operator products (FP64 and FP32 arms)
+
+// FP64: one warp per (run, receiver): rows 3i..3i+2 against v'_r.
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const double2 *__restrict__ K, const double2 *__restrict__ V,
+                                                       int64_t N, int B, double *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (w >= N * B) return;
+    const int r = (int)(w / N);
+    const int64_t i = w - (int64_t)r * N;
+    const double2 *v = V + (int64_t)r * N;
+    const double2 *r0 = K + 3 * i * N, *r1 = r0 + N, *r2 = r1 + N;
+    double a0 = 0, a1 = 0, a2 = 0;
+    for (int64_t j = lane; j < N; j += 32) {
+        const double2 x = v[j], k0 = r0[j], k1 = r1[j], k2 = r2[j];
+        a0 = fma(k0.x, x.x, fma(k0.y, x.y, a0));
+        a1 = fma(k1.x, x.x, fma(k1.y, x.y, a1));
+        a2 = fma(k2.x, x.x, fma(k2.y, x.y, a2));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) {
+        double *o = out + (int64_t)r * 3 * N + 3 * i;
+        o[0] = a0; o[1] = a1; o[2] = a2;
+    }
+}
+
+// FP32: CTA tile 128 rows x 64 runs, K chunks of 32 through shared memory,
+// FP32 FMAs with the partial sums moved to FP64 every 256 columns.
+constexpr int kF32Rows = 128, kF32Runs = 64, kF32K = 32;
+
+__global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__ K, const float *__restrict__ V,
+                                                       int64_t N, int Bp, double *__restrict__ out)
+{
+    __shared__ float As[kF32K][kF32Rows + 4];
+    __shared__ float Vs[kF32K][kF32Runs + 4];
+    const int t = threadIdx.x;
+    const int tr = t & 31, tn = t >> 5;       // rows tr*4..+3, runs tn*8..+7
+    const int64_t M = 3 * N, Kd = 2 * N;
+    const int64_t m0 = (int64_t)blockIdx.x * kF32Rows;
+    const int n0 = blockIdx.y * kF32Runs;
+    float acc[4][8];
+    double acc64[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) { acc[a][b] = 0.f; acc64[a][b] = 0.0; }
+    int chunk = 0;
+    for (int64_t k0 = 0; k0 < Kd; k0 += kF32K, ++chunk) {
+        // K tile: 128 x 32 floats, 16 per thread (row-major, contiguous along k)
+        for (int q = t; q < kF32Rows * kF32K; q += 256) {
+            const int mm = q / kF32K, kk = q % kF32K;
+            const int64_t m = m0 + mm, k = k0 + kk;
+            As[kk][mm] = (m < M && k < Kd) ? K[m * Kd + k] : 0.f;
+        }
+        for (int q = t; q < kF32Runs * kF32K; q += 256) {
+            const int nn = q / kF32K, kk = q % kF32K;
+            const int n = n0 + nn;
+            const int64_t k = k0 + kk;
+            Vs[kk][nn] = (n < Bp && k < Kd) ? V[(int64_t)n * Kd + k] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < kF32K; ++kk) {
+            float a[4], b[8];
+#pragma unroll
+            for (int x = 0; x < 4; ++x) a[x] = As[kk][tr * 4 + x];
+#pragma unroll
+            for (int y = 0; y < 8; ++y) b[y] = Vs[kk][tn * 8 + y];
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 8; ++y) acc[x][y] = fmaf(a[x], b[y], acc[x][y]);
+        }
+        __syncthreads();
+        if ((chunk & 7) == 7) {
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 8; ++y) { acc64[x][y] += (double)acc[x][y]; acc[x][y] = 0.f; }
+        }
+    }
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+        const int64_t m = m0 + tr * 4 + x;
+        if (m >= M) continue;
+#pragma unroll
+        for (int y = 0; y < 8; ++y) {
+            const int n = n0 + tn * 8 + y;
+            if (n < Bp) out[(int64_t)n * M + m] = acc64[x][y] + (double)acc[x][y];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// attempt / decide / update
+
+__global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
+{
+    __shared__ double red[8];
+    __shared__ int act;
+    __shared__ double hs;
+    const int r = blockIdx.y;
+    pq3d_run_ctrl *C = S.ctrl + r;
+    if (threadIdx.x == 0) { act = C->active; hs = C->h; }
+    __syncthreads();
+    if (!act) return;
+    const int64_t N = S.N;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double m1 = 0.0, m2 = 0.0;
+    if (i < N) {
+        const int64_t idx = (int64_t)r * N + i;
+        const int Bp = padded_runs(S.B);
+        double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+        for (int s = 0; s < S.nsplit; ++s) {
+            const double *p = S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
+            q0 += p[0]; q1 += p[1]; q2 += p[2];
+        }
+        const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
+        Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig};
+        const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
+        double yo[4], e1, e2;
+        dp_attempt(c, S.V0, S.eta, hs, y, yo, e1, e2);
+        reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
+        m1 = e1;
+        m2 = e2;
+    }
+    m1 = block_max(m1, red);
+    m2 = block_max(m2, red);
+    if (threadIdx.x == 0) {
+        atomicMax((unsigned long long *)&C->err1_bits, dbits(m1));
+        atomicMax((unsigned long long *)&C->err2_bits, dbits(m2));
+    }
+}
+
+__global__ void decide_kernel(pq3d_run_ctrl *ctrl, int B)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B) return;
+    pq3d_run_ctrl *C = ctrl + r;
+    if (!C->active) { C->accepted = 0; return; }
+    const double err1 = __longlong_as_double((long long)C->err1_bits) + 1e-10;
+    const double err2 = __longlong_as_double((long long)C->err2_bits) + 1e-10;
+    C->err1_bits = 0ull;
+    C->err2_bits = 0ull;
+    const double h = C->h;
+    C->attempts += 1;
+    const double c1 = err1 / kRelTol, c2 = err2 / kRelTol;
+    const double hn1 = h * 0.9 * pow(kRelTol / err1, 0.2);
+    const double hn2 = h * 0.9 * pow(kRelTol / err2, 0.2);
+    if (fmax(c1, c2) < 1.0 && !(isnan(c1) || isnan(c2))) {
+        C->accepted = 1;
+        C->h_last = h;
+        C->time = C->time + h;
+        C->steps += 1;
+        C->nrjct = 0;
+        C->h = pymin(1.5 * h, pymin(hn1, hn2));
+        if (C->steps >= C->max_steps || C->time >= C->t_end) C->active = 0;
+    } else {
+        C->accepted = 0;
+        C->nrjct += 1;
+        const double hn = pymax(0.5 * h, pymin(hn1, hn2));
+        C->h = hn;
+        if (hn < 1.e-15 || C->nrjct > 20) {
+            C->status = PQ3D_ERR_STEP;
+            C->active = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
+{
+    __shared__ int acc;
+    __shared__ double hs;
+    const int r = blockIdx.y;
+    const pq3d_run_ctrl *C = S.ctrl + r;
+    if (threadIdx.x == 0) { acc = C->accepted; hs = C->h_last; }
+    __syncthreads();
+    if (!acc) return;
+    const int64_t N = S.N;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int64_t idx = (int64_t)r * N + i;
+    const double h = hs;
+    const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
+    const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[idx];
+    S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
+    const double e = (2.0 * S.V0) * exp(-st / a);
+    const double v1 = e * sinh(T1 / Tno / a);
+    const double v2 = e * sinh(T2 / Tno / a);
+    double v = sqrt(v1 * v1 + v2 * v2);
+    if (v < 1e-30) v = 1e-30;
+    S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
+    S.slip1[idx] += v1 * h;
+    S.slip2[idx] += v2 * h;
+    write_vop(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
+}
+
+static int check_sim(const pq3d_batch_sim *S)
+{
+    PQ3D_REQUIRE(S && S->N > 0 && S->B > 0 && S->B <= 1024 && S->ctrl && S->K && S->vop && S->rates && S->cand,
+                 "pq3d_batch: bad simulation structure");
+    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_BF16X6, "pq3d_batch: bad precision");
+    PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
+    PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
+    if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
+    return PQ3D_OK;
+}
+
+}  // namespace batch
+}  // namespace pq3d
+
+using namespace pq3d;
+using namespace pq3d::batch;
+
+extern "C" size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim)
+{
+    if (!sim || sim->precision != PQ3D_BATCH_BF16X6) return 0;
+    return pq3d::tc::gemm_bf16x6_workspace_bytes(sim->N, padded_runs(sim->B), sim->nsplit);
+}
+
+extern "C" int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream)
+{
+    clear_error();
+    int rc = check_sim(sim);
+    if (rc) return rc;
+    const int Bp = padded_runs(sim->B);
+    dim3 grid((unsigned)((sim->N + 255) / 256), (unsigned)Bp);
+    prepare_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*sim);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}
+
+extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream)
+{
+    clear_error();
+    int rc = check_sim(sim);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const pq3d_batch_sim &S = *sim;
+    const int Bp = padded_runs(S.B);
+    // 1. operator product
+    if (S.precision == PQ3D_BATCH_FP64) {
+        const int64_t warps = S.N * Bp;
+        gemm_f64_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
+            (const double2 *)S.K, (const double2 *)S.vop, S.N, Bp, S.rates);
+    } else if (S.precision == PQ3D_BATCH_FP32) {
+        dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
+        gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Bp, S.rates);
+    } else {
+        rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.rates, workspace,
+                                   workspace_bytes, st);
+        if (rc) return rc;
+    }
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    // 2-4. attempt, decide, update
+    dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
+    attempt_kernel<<<grid, 256, 0, st>>>(S);
+    decide_kernel<<<(S.B + 127) / 128, 128, 0, st>>>(S.ctrl, S.B);
+    update_kernel<<<grid, 256, 0, st>>>(S);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}

@@ -1,0 +1,326 @@
+// Batched traction product on the 5th-generation tensor cores (tcgen05).
+//
+//   out[s][n][m] = sum_{k in slice s} K[m][k] * V[n][k]
+//   K: (3N) x (2N) traction operator, V: B slip-rate deficits (one per run).
+//
+// Precision ("BF16x6"): the FP64 operator and the FP64 right-hand side are
+// split into three BF16 pieces each (x = x0 + x1 + x2, 24 significant bits);
+// the six cross products x_i * y_j with i + j <= 2 are accumulated in FP32 in
+// tensor memory.  Their sum carries the operands to ~2^-24 (the FP32 operator
+// copy's own rounding), while two-piece "BF16x3" carries them to ~2^-16.
+// Slices of the reduction (split-K) are added in FP64 by the consumer.
+//
+// Data path (one CTA = one 128-row tile of K x one K slice, all runs):
+//   * the operator pieces are packed once, after assembly, into ready-made
+//     shared-memory images: for every (tile, 32-column block) three 128 x 32
+//     BF16 images of 8-row x 16-byte core matrices (K-major, no swizzle); the
+//     right-hand side pieces are written in the same image layout by the
+//     stepper.  One pipeline stage is therefore two contiguous 1-D bulk
+//     copies (cp.async.bulk, completion on an mbarrier), no tensor map.
+//   * warp 0 lane 0 produces stages, warp 1 lane 0 issues 12 tcgen05.mma
+//     (M=128, N=B, K=16; 6 products x 2 K-steps) per stage and frees the stage
+//     with tcgen05.commit; all 4 warps drain the FP32 accumulator from tensor
+//     memory (tcgen05.ld 32x32b) and store FP64.
+//   * every mbarrier wait is bounded; a wait that gives up records an error
+//     word in the workspace, the kernel still waits (bounded) for its own
+//     tensor-core work, frees its tensor memory and returns.
+// No cluster, no multicast: each CTA reads its own tiles.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "gemm_tc.cuh"
+
+namespace pq3d {
+namespace tc {
+
+constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr uint32_t kImageA = kTileM * kBlockK * 2;   // bytes of one A piece image (8 KB)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for the phase of parity `parity` to complete
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (it > 32) __nanosleep(128);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major, no swizzle: start address, leading
+// byte offset (between core matrices along K), stride byte offset (between
+// 8-row groups), descriptor version 1 at bits 46-47.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+__host__ __device__ inline uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t tmem_cols(int Bp)
+{
+    uint32_t c = 32;
+    while ((int)c < Bp) c <<= 1;
+    return c;
+}
+
+// The 6 leading cross products of the 3-piece splits: (piece of K, piece of V).
+__constant__ int kPairA[6] = {0, 0, 1, 0, 1, 2};
+__constant__ int kPairB[6] = {0, 1, 0, 2, 1, 0};
+
+__global__ void __launch_bounds__(128, 1)
+gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bp, int nsplit,
+                   double *__restrict__ out, int *__restrict__ err, int stages)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mt = blockIdx.x;
+    const int slice = blockIdx.y;
+    const int64_t KB = (2 * N + kBlockK - 1) / kBlockK;
+    const int64_t kb0 = KB * slice / nsplit, kb1 = KB * (slice + 1) / nsplit;
+    const int nkb = (int)(kb1 - kb0);
+    const uint32_t a_bytes = kPieces * kImageA;
+    const uint32_t b_img = (uint32_t)Bp * kBlockK * 2;
+    const uint32_t b_bytes = kPieces * b_img;
+    const uint32_t stage_bytes = a_bytes + b_bytes;
+    uint8_t *bars = smem + (size_t)stages * stage_bytes;
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * stages, done = full0 + 16 * stages;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 16 * stages + 8);
+    const uint32_t ncols = tmem_cols(Bp);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *(volatile uint32_t *)tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // producer: two bulk copies per stage
+        for (int it = 0; it < nkb; ++it) {
+            const int st = it % stages, use = it / stages;
+            if (!mbar_wait(empty0 + 8 * st, (use & 1) ^ 1)) { atomicExch(err, 1); break; }
+            const uint32_t sa = smem_u32(smem + (size_t)st * stage_bytes);
+            const int64_t kb = kb0 + it;
+            mbar_expect_tx(full0 + 8 * st, stage_bytes);
+            bulk_g2s(sa, Kp + (size_t)(mt * KB + kb) * a_bytes, a_bytes, full0 + 8 * st);
+            bulk_g2s(sa + a_bytes, Vp + (size_t)kb * b_bytes, b_bytes, full0 + 8 * st);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // tensor-core issuer
+        const uint32_t idesc = idesc_bf16(kTileM, Bp);
+        for (int it = 0; it < nkb; ++it) {
+            const int st = it % stages, use = it / stages;
+            if (!mbar_wait(full0 + 8 * st, use & 1)) { atomicExch(err, 2); break; }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + (size_t)st * stage_bytes);
+            const uint32_t sb = sa + a_bytes;
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+#pragma unroll
+                for (int p = 0; p < 6; ++p) {
+                    const uint64_t ad = smem_desc(sa + kPairA[p] * kImageA + ks * 256, 128, 512);
+                    const uint64_t bd = smem_desc(sb + kPairB[p] * b_img + ks * 256, 128, 512);
+                    mma_bf16(tmem, ad, bd, idesc, (it > 0 || ks > 0 || p > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(empty0 + 8 * st);
+        }
+        mma_commit(done);
+    }
+    __syncwarp();
+
+    // epilogue: TMEM lane = tile row, column = run
+    const bool got = __all_sync(0xffffffffu, mbar_wait(done, 0) ? 1 : 0);
+    tc_fence_after();
+    const int64_t M = 3 * N;
+    const int64_t m = mt * kTileM + 32 * warp + lane;
+    if (got) {
+        for (int c0 = 0; c0 < Bp; c0 += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, r);
+            if (m < M) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    out[((int64_t)slice * Bp + c0 + j) * M + m] = (double)__uint_as_float(r[j]);
+            }
+        }
+    } else if (lane == 0) {
+        atomicExch(err, 3);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
+// FP64 operator -> three BF16 pieces in the tile-image layout.
+__global__ void pack_operator_kernel(const double *__restrict__ K64, int64_t N, __nv_bfloat16 *__restrict__ out)
+{
+    const int64_t mt = blockIdx.y, kb = blockIdx.x;
+    const int64_t KB = gridDim.x;
+    const int64_t M = 3 * N, Kd = 2 * N;
+    __nv_bfloat16 *base = out + (size_t)(mt * KB + kb) * kPieces * kTileM * kBlockK;
+    for (int e = threadIdx.x; e < kTileM * kBlockK; e += blockDim.x) {
+        const int row = e / kBlockK, col = e % kBlockK;
+        const int64_t m = mt * kTileM + row, k = kb * kBlockK + col;
+        const double x = (m < M && k < Kd) ? K64[m * Kd + k] : 0.0;
+        const __nv_bfloat16 p0 = __double2bfloat16(x);
+        const double r1 = x - (double)__bfloat162float(p0);
+        const __nv_bfloat16 p1 = __double2bfloat16(r1);
+        const __nv_bfloat16 p2 = __double2bfloat16(r1 - (double)__bfloat162float(p1));
+        const int o = image_offset(row, col);
+        base[o] = p0;
+        base[kTileM * kBlockK + o] = p1;
+        base[2 * kTileM * kBlockK + o] = p2;
+    }
+}
+
+size_t gemm_bf16x6_workspace_bytes(int64_t, int, int) { return 256; }
+
+struct Cfg {
+    int device = -1;
+    int max_smem = 0;
+};
+static thread_local Cfg g_cfg;
+
+int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, double *out, void *workspace,
+                size_t workspace_bytes, cudaStream_t stream)
+{
+    PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x6: null pointer");
+    PQ3D_REQUIRE(workspace_bytes >= 256 && aligned16(workspace), "gemm_bf16x6: workspace must be >= 256 bytes");
+    PQ3D_REQUIRE(Bp >= 16 && Bp <= 256 && Bp % 16 == 0, "gemm_bf16x6: padded run count must be 16..256, multiple of 16");
+    PQ3D_REQUIRE(aligned16(Kpacked) && aligned16(Vpacked), "gemm_bf16x6: operands must be 16-byte aligned");
+    const int64_t KB = k_blocks(N);
+    PQ3D_REQUIRE(nsplit >= 1 && nsplit <= KB, "gemm_bf16x6: nsplit must be in [1, %lld]", (long long)KB);
+    int dev;
+    PQ3D_CUDA_TRY(cudaGetDevice(&dev));
+    if (g_cfg.device != dev) {
+        int maxs = 0;
+        PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        PQ3D_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16x6_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
+        g_cfg.device = dev;
+        g_cfg.max_smem = maxs;
+    }
+    const size_t stage_bytes = (size_t)kPieces * (kImageA + (size_t)Bp * kBlockK * 2);
+    int stages = (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16));
+    if (stages > 6) stages = 6;
+    PQ3D_REQUIRE(stages >= 2, "gemm_bf16x6: not enough shared memory for B=%d", Bp);
+    const size_t smem = (size_t)stages * stage_bytes + 16 * (size_t)stages + 16;
+    dim3 grid((unsigned)m_tiles(N), (unsigned)nsplit);
+    gemm_bf16x6_kernel<<<grid, 128, smem, stream>>>((const uint8_t *)Kpacked, (const uint8_t *)Vpacked, N, Bp, nsplit,
+                                                     out, (int *)workspace, stages);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}
+
+}  // namespace tc
+}  // namespace pq3d
+
+using namespace pq3d;
+
+extern "C" size_t pq3d_batch_operator_bytes(int64_t N) { return N > 0 ? tc::packed_operator_bytes(N) : 0; }
+
+extern "C" size_t pq3d_batch_rhs_bytes(int64_t N, int B)
+{
+    const int Bp = (B + 15) / 16 * 16;
+    return N > 0 && B > 0 ? tc::packed_rhs_bytes(N, Bp) : 0;
+}
+
+extern "C" int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpacked, void *stream)
+{
+    clear_error();
+    PQ3D_REQUIRE(K64 && Kpacked && N > 0, "pq3d_batch_pack_operator: bad arguments");
+    PQ3D_REQUIRE(aligned16(Kpacked), "pq3d_batch_pack_operator: output must be 16-byte aligned");
+    dim3 grid((unsigned)tc::k_blocks(N), (unsigned)tc::m_tiles(N));
+    tc::pack_operator_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(K64, N, (__nv_bfloat16 *)Kpacked);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}
+
+extern "C" int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit,
+                                      double *out, void *workspace, size_t workspace_bytes, void *stream)
+{
+    clear_error();
+    return tc::gemm_bf16x6(Kpacked, Vpacked, N, (B + 15) / 16 * 16, nsplit, out, workspace, workspace_bytes,
+                           (cudaStream_t)stream);
+}

@@ -20,21 +20,12 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "rk_device.cuh"
 
 namespace pq3d {
 namespace step {
 
-// Dormand-Prince tableau (src/QDsim_gpu.py:1129-1159)
-constexpr double B21 = .2;
-constexpr double B31 = 3. / 40, B32 = 9. / 40.;
-constexpr double B41 = 44. / 45., B42 = -56. / 15, B43 = 32. / 9;
-constexpr double B51 = 19372. / 6561., B52 = -25360 / 2187., B53 = 64448. / 6561., B54 = -212. / 729.;
-constexpr double B61 = 9017. / 3168., B62 = -355. / 33., B63 = -46732. / 5247., B64 = 49. / 176.,
-                 B65 = -5103. / 18656.;
-constexpr double B71 = 35. / 384., B73 = 500. / 1113., B74 = 125. / 192., B75 = -2187. / 6784., B76 = 11. / 84.;
-constexpr double B81 = 5179. / 57600., B83 = 7571. / 16695., B84 = 393. / 640., B85 = -92097. / 339200.,
-                 B86 = 187. / 2100., B87 = 1. / 40.;
-constexpr double kRelTol = 1e-4;
+using namespace ::pq3d::rk;
 
 // ---------------------------------------------------------------------------
 // traction product: rows 3i..3i+2 of K times v' (interleaved strike/dip)
@@ -152,102 +143,6 @@ __global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K,
         if (lane == 0) { out[3 * i] = acc[0]; out[3 * i + 1] = acc[1]; out[3 * i + 2] = acc[2]; }
     }
 }
-
-// ---------------------------------------------------------------------------
-// right-hand side of one cell (src/QDsim_gpu.py:830-891), pore pressure 0
-
-struct Cell {
-    double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
-};
-
-__device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
-
-__device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
-                                    double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
-{
-    const double Tn = Tno * 1e6, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
-    const double es = exp(clip700(-state / c.a));
-    const double aTn = c.a * Tn;
-    const double x1 = clip700(T1 / aTn), x2 = clip700(T2 / aTn);
-    const double ep1 = exp(x1), em1 = exp(-x1), ep2 = exp(x2), em2 = exp(-x2);
-    const double ch1 = (ep1 + em1) / 2, sh1 = (ep1 - em1) / 2;
-    const double ch2 = (ep2 + em2) / 2, sh2 = (ep2 - em2) / 2;
-    const double aTn2 = c.a * (Tn * Tn);
-    const double dV1dtau = 2 * V0 / aTn * es * ch1;
-    const double dV2dtau = 2 * V0 / aTn * es * ch2;
-    const double dV1dsigma = -2 * V0 * T1 / aTn2 * es * ch1;
-    const double dV2dsigma = -2 * V0 * T2 / aTn2 * es * ch2;
-    const double dV1dstate = -2 * V0 / c.a * es * sh1;
-    const double dV2dstate = -2 * V0 / c.a * es * sh2;
-    dstate = c.b / c.dc * (V0 * exp(clip700((c.f0 - state) / c.b)) - c.slipv);
-    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * c.dsig + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
-    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * c.dsig + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
-    dsig = c.dsig / 1e6;
-    dtau1 = t1 / 1e6;
-    dtau2 = t2 / 1e6;
-}
-
-// One Dormand-Prince attempt of one cell; y = (Tno, Tt1o, Tt2o, state).
-// Writes the 5th-order solution to yo and returns the two relative errors.
-__device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
-                                           double yo[4], double &e1, double &e2)
-{
-    double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
-        u7;
-    const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
-    rhs(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
-    rhs(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
-    rhs(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
-        st + h * (B31 * s1 + B32 * s2), s3, n3, t3, u3);
-    rhs(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
-        Tt2o + h * (B41 * u1 + B42 * u2 + B43 * u3), st + h * (B41 * s1 + B42 * s2 + B43 * s3), s4, n4, t4, u4);
-    rhs(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
-        Tt1o + h * (B51 * t1 + B52 * t2 + B53 * t3 + B54 * t4), Tt2o + h * (B51 * u1 + B52 * u2 + B53 * u3 + B54 * u4),
-        st + h * (B51 * s1 + B52 * s2 + B53 * s3 + B54 * s4), s5, n5, t5, u5);
-    rhs(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
-        Tt1o + h * (B61 * t1 + B62 * t2 + B63 * t3 + B64 * t4 + B65 * t5),
-        Tt2o + h * (B61 * u1 + B62 * u2 + B63 * u3 + B64 * u4 + B65 * u5),
-        st + h * (B61 * s1 + B62 * s2 + B63 * s3 + B64 * s4 + B65 * s5), s6, n6, t6, u6);
-    yo[0] = Tno + h * (B71 * n1 + B73 * n3 + B74 * n4 + B75 * n5 + B76 * n6);
-    yo[1] = Tt1o + h * (B71 * t1 + B73 * t3 + B74 * t4 + B75 * t5 + B76 * t6);
-    yo[2] = Tt2o + h * (B71 * u1 + B73 * u3 + B74 * u4 + B75 * u5 + B76 * u6);
-    yo[3] = st + h * (B71 * s1 + B73 * s3 + B74 * s4 + B75 * s5 + B76 * s6);
-    rhs(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
-    const double Tn8 = Tno + h * (B81 * n1 + B83 * n3 + B84 * n4 + B85 * n5 + B86 * n6 + B87 * n7);
-    const double T18 = Tt1o + h * (B81 * t1 + B83 * t3 + B84 * t4 + B85 * t5 + B86 * t6 + B87 * t7);
-    const double T28 = Tt2o + h * (B81 * u1 + B83 * u3 + B84 * u4 + B85 * u5 + B86 * u6 + B87 * u7);
-    const double st8 = st + h * (B81 * s1 + B83 * s3 + B84 * s4 + B85 * s5 + B86 * s6 + B87 * s7);
-    e1 = fabs(fabs(st8 - yo[3]) / st8);
-    const double ea = fabs(fabs(T18 - yo[1]) / T18);
-    const double eb = fabs(fabs(T28 - yo[2]) / T28);
-    const double ec = fabs(fabs(Tn8 - yo[0]) / Tn8);
-    // max that propagates NaN, like numpy's max
-    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
-}
-
-// max over non-negative doubles (and NaN, which wins) through their bit patterns
-__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(fabs(x)); }
-
-__device__ __forceinline__ double block_max(double v, double *red)
-{
-    // NaN-propagating max across the block
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (isnan(v) || isnan(u)) ? NAN : fmax(v, u);
-    }
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double m = 0.0;
-    const int nw = blockDim.x >> 5;
-    for (int q = 0; q < nw; ++q) m = (isnan(m) || isnan(red[q])) ? NAN : fmax(m, red[q]);
-    return m;
-}
-
-__device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b : a; }
 
 template <bool kF32>
 __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist,

@@ -1,0 +1,154 @@
+"""Batched ensemble: B simulations that share one mesh, stepped together.
+
+Each run has its own friction, stress and nucleation (its own per-cell table)
+and its own adaptive dt; one device iteration does the traction product for
+all runs as one (3N x 2N) x (2N x B) product, one Dormand-Prince attempt per
+run, the per-run accept/reject decision and the update of the accepted runs
+(rejected runs retry with their smaller dt).  Iterations are captured into a
+CUDA graph and replayed without host synchronisation.
+
+Precisions of the traction product (``precision=``):
+  "fp64"   FP64 operator on CUDA cores (reference arithmetic, slow on GB300)
+  "fp32"   FP32 operator copy on CUDA cores ("plain FP32")
+  "bf16x6" the operator and v' each split into three BF16 pieces, the six
+           leading cross products on the tcgen05 tensor cores with FP32
+           accumulation in tensor memory; K slices added in FP64
+Time, slip, the state and the RK error norm stay FP64 in every mode.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .QDsim_gpu import initial_state
+
+PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6}
+STATE = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2")
+PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0")
+
+
+def padded_runs(B: int) -> int:
+    return (B + 15) // 16 * 16
+
+
+class PackedOperator:
+    """The tensor-core operand: FP64 operator split into 3 BF16 pieces, packed
+    as shared-memory tile images (built once per mesh)."""
+
+    def __init__(self, K64: torch.Tensor):
+        L = _lib.load()
+        assert K64.dtype == torch.float64 and K64.is_contiguous()
+        self.N = K64.shape[1] // 2
+        self.device = K64.device
+        self.data = torch.empty(L.pq3d_batch_operator_bytes(self.N), dtype=torch.uint8, device=self.device)
+        _lib.check(L.pq3d_batch_pack_operator(K64.data_ptr(), self.N, self.data.data_ptr(),
+                                              torch.cuda.current_stream(self.device).cuda_stream))
+
+
+class Ensemble:
+    """Device state and launch structure of B runs on one mesh.
+
+    K: the (3N, 2N) operator -- FP64 for "fp64", FP32 for "fp32", a
+    :class:`PackedOperator` for "bf16x6".  tables: (B, N, 10) per-cell tables
+    (``read_parameter`` layout)."""
+
+    def __init__(self, K, tables, *, mu, Cs, V0=1e-6, Vpl=1e-9, precision="bf16x6", nsplit=None, dttry=1e-3,
+                 max_steps=2 ** 62, t_end=float("inf"), fix_Tn=False):
+        L = _lib.load()
+        self.precision = precision
+        prec = PRECISIONS[precision]
+        tables = np.asarray(tables, dtype=np.float64)
+        B, N = tables.shape[0], tables.shape[1]
+        self.B, self.N, self.Bp = B, N, padded_runs(B)
+        dev = K.device if not isinstance(K, PackedOperator) else K.device
+        self.device = dev
+        if precision == "bf16x6":
+            assert isinstance(K, PackedOperator) and K.N == N
+            kop = K.data
+            if nsplit is None:
+                nsplit = 2
+        else:
+            assert isinstance(K, torch.Tensor) and K.shape == (3 * N, 2 * N) and K.is_contiguous()
+            assert K.dtype == (torch.float64 if precision == "fp64" else torch.float32)
+            kop = K
+            nsplit = 1
+        self.K = kop
+        self.nsplit = int(nsplit)
+        inits = [initial_state(t, V0, Vpl) for t in tables]
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.t = {}
+        for k in STATE + ("a", "b", "dc", "f0", "shear_loading", "normal_loading"):
+            self.t[k] = torch.as_tensor(np.stack([s[k] for s in inits]), **f64).contiguous()
+        self.t["cos_rake0"] = torch.cos(torch.as_tensor(np.stack([s["rake0"] for s in inits]), **f64)).contiguous()
+        self.t["sin_rake0"] = torch.sin(torch.as_tensor(np.stack([s["rake0"] for s in inits]), **f64)).contiguous()
+        self.t["rates"] = torch.zeros(self.nsplit * self.Bp * 3 * N, **f64)
+        self.t["cand"] = torch.zeros(B * N * 4, **f64)
+        if precision == "fp64":
+            self.vop = torch.zeros(self.Bp * 2 * N, **f64)
+        elif precision == "fp32":
+            self.vop = torch.zeros(self.Bp * 2 * N, dtype=torch.float32, device=dev)
+        else:
+            self.vop = torch.zeros(L.pq3d_batch_rhs_bytes(N, B), dtype=torch.uint8, device=dev)
+        self.ctrl_t = torch.zeros(B * ctypes.sizeof(_lib.RunCtrl), dtype=torch.uint8, device=dev)
+        S = _lib.BatchSim()
+        S.N, S.B, S.precision, S.nsplit = N, B, prec, self.nsplit
+        for k in STATE + PARAMS + ("rates", "cand"):
+            setattr(S, k, self.t[k].data_ptr())
+        S.vop, S.K, S.ctrl = self.vop.data_ptr(), self.K.data_ptr(), self.ctrl_t.data_ptr()
+        S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
+        self.S = S
+        self.ws = torch.zeros(max(256, L.pq3d_batch_workspace_bytes(ctypes.byref(S))), dtype=torch.uint8, device=dev)
+        self.set_ctrl(dttry=dttry, max_steps=max_steps, t_end=t_end)
+        self.prepare()
+        self.graph = None
+
+    # -- control -----------------------------------------------------------
+    def set_ctrl(self, dttry=1e-3, max_steps=2 ** 62, t_end=float("inf"), active=None):
+        arr = (_lib.RunCtrl * self.B)()
+        for r in range(self.B):
+            c = arr[r]
+            c.h, c.time, c.t_end = float(dttry), 0.0, float(t_end)
+            c.max_steps = int(max_steps)
+            c.active = 1 if active is None else int(bool(active[r]))
+        host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
+        self.ctrl_t.copy_(host)
+
+    def read_ctrl(self):
+        b = self.ctrl_t.cpu().numpy().tobytes()
+        return list((_lib.RunCtrl * self.B).from_buffer_copy(b))
+
+    def prepare(self):
+        L = _lib.load()
+        _lib.check(L.pq3d_batch_prepare(ctypes.byref(self.S), torch.cuda.current_stream(self.device).cuda_stream))
+
+    # -- stepping ----------------------------------------------------------
+    def iterate(self, n=1):
+        """Queue n iterations (asynchronous)."""
+        L = _lib.load()
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        for _ in range(n):
+            _lib.check(L.pq3d_batch_iterate(ctypes.byref(self.S), self.ws.data_ptr(), self.ws.numel(), st))
+
+    def capture(self, n_iter):
+        """Capture n_iter iterations into a CUDA graph (after one warm-up
+        iteration has configured the kernels)."""
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.iterate(n_iter)
+        self.graph = g
+        self.graph_iters = n_iter
+        return g
+
+    def replay(self, times=1):
+        for _ in range(times):
+            self.graph.replay()
+
+    def error_word(self):
+        return int(self.ws[:4].view(torch.int32).item())
+
+    def stages(self):
+        """Right-hand-side evaluations so far: 7 per attempted step, all runs."""
+        return 7 * sum(c.attempts for c in self.read_ctrl())

@@ -27,3 +27,34 @@ def test_reference_ctypes_signatures_bind():
 
 def test_error_text_starts_empty():
     assert _lib.load().pq3d_last_error() == b""
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors have the sizes and field offsets of include/pq3d.h."""
+    import os
+    import subprocess
+    src = tmp_path / "probe.c"
+    fields = {"pq3d_batch_sim": ("BatchSim", ["N", "B", "precision", "Tno", "rates", "nsplit", "cand", "vop", "K",
+                                              "ctrl", "V0", "eta", "fix_Tn"]),
+              "pq3d_dense_sim": ("DenseSim", ["N", "Tno", "fric", "a", "rake0", "rates", "cand", "K64", "K32", "ctrl",
+                                              "V0", "eta", "fix_Tn"]),
+              "pq3d_run_ctrl": ("RunCtrl", ["h", "time", "attempts", "max_steps", "err2_bits", "status", "accepted"]),
+              "pq3d_step_ctrl": ("StepCtrl", ["dttry", "status", "attempts", "err_slot", "maxv_bits", "bar_gen"])}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "pq3d.h"', "int main(void){"]
+    for cname, (_, fl) in fields.items():
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        for f in fl:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+    lines.append("return 0;}")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.check_call(["gcc", "-I", os.path.dirname(_lib.HEADER), "-o", str(exe), str(src)])
+    vals = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    k = 0
+    for cname, (pyname, fl) in fields.items():
+        cls = getattr(_lib, pyname)
+        assert ctypes.sizeof(cls) == vals[k], cname
+        k += 1
+        for f in fl:
+            assert getattr(cls, f).offset == vals[k], (cname, f)
+            k += 1
