@@ -319,6 +319,8 @@ def bench_ours(args):
         del host64
         # -- stepping on the assembled operator
         out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks)
+        if not args.no_batch:
+            out["batched"] = bench_batched(torch, dev, args, peaks)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
     line = {"metric": METRIC, "value": value, "unit": "GF entries/s", "n_gpus": world, "steps": args.steps,
@@ -370,6 +372,96 @@ def bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks):
     return res
 
 
+def bench_batched(torch, dev, args, peaks):
+    """Config: batched ensemble, B runs on one planar N=10,000 mesh (100 x 50 km,
+    1 km squares), per-run friction draws (seed 0), BF16x6 tensor-core traction
+    product vs the plain FP64 single-simulation stepper on the same mesh."""
+    import ctypes
+    from pyquake3d_gb300 import _lib, gf, mesh
+    from pyquake3d_gb300.ensemble import Ensemble, PackedOperator
+    from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
+    L_ = _lib.load()
+    Lkm, Wkm, nx, nz = (100.0, 50.0, 100, 50) if not args.quick else (40.0, 20.0, 40, 20)
+    B = args.batch
+    nodes, tris = mesh.planar_fault(Lkm, Wkm, nx, nz)
+    N = tris.shape[0]
+    _, xg = mesh.element_frames(nodes, tris)
+    tabs = mesh.ensemble_tables(xg, Lkm * 1e3, Wkm * 1e3, B=B, seed=0, v_nuc=1e-3)
+    K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
+    P = PackedOperator(K64)
+    res = {"workload": "batched ensemble: planar %dx%d km, N=%d, B=%d runs, per-run a-b, Dc, sigma_n, nucleation "
+                       "patch from seed 0; RK stages = 7 x attempted steps, all runs" % (Lkm, Wkm, N, B)}
+    out = {}
+    for prec, K in (("bf16x6", P), ("fp32", K32)):
+        ens = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, nsplit=args.nsplit)
+        ens.iterate(2)
+        torch.cuda.synchronize()
+        ens.capture(args.graph_iters)
+        ens.replay(1)
+        torch.cuda.synchronize()
+        st0 = ens.stages()
+        reps = max(1, args.batch_iters // args.graph_iters)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(dev.index or 0) as clk:
+            s.record()
+            ens.replay(reps)
+            e.record()
+            e.synchronize()
+        dt = s.elapsed_time(e) / 1e3
+        st1 = ens.stages()
+        c = ens.read_ctrl()
+        out[prec] = {"rk_stages_per_s": (st1 - st0) / dt, "iterations": reps * args.graph_iters,
+                     "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
+                     "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
+                     "clocks": clk.summary(), "error_word": ens.error_word() if prec == "bf16x6" else 0}
+        if prec == "bf16x6":
+            # the tensor-core product alone, CUDA events over repeated launches
+            st = torch.cuda.current_stream(dev).cuda_stream
+            for _ in range(3):
+                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                                          ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
+            nl = 20
+            s.record()
+            for _ in range(nl):
+                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                                          ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
+            e.record()
+            e.synchronize()
+            tg = s.elapsed_time(e) / 1e3 / nl
+            Bp = ens.Bp
+            op_bytes = P.data.numel()
+            flops = 6 * 2.0 * (3 * N) * (2 * N) * Bp
+            out[prec]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit,
+                                 "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": op_bytes / tg / 1e9,
+                                              "peak": peaks["hbm_gbs"], "frac": op_bytes / tg / 1e9 / peaks["hbm_gbs"],
+                                              "algorithmic_bytes": op_bytes,
+                                              "note": "packed BF16x3-piece operator streamed once per product"},
+                                 "tensor": {"achieved_tflops": flops / tg / 1e12, "peak_tflops": peaks["bf16_tflops"],
+                                            "frac": flops / tg / 1e12 / peaks["bf16_tflops"],
+                                            "flops": flops, "note": "6 BF16 products x 2 x 3N x 2N x Bp"}}
+        del ens
+    # plain FP64 single simulation on the same mesh (run 0's parameters)
+    sim = DenseDeviceSim(K64, initial_state(tabs[0], 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+    sim.step(3)
+    c0 = sim.read_ctrl()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    sim.launch(args.rk_steps)
+    e.record()
+    e.synchronize()
+    dt = s.elapsed_time(e) / 1e3
+    c1 = sim.read_ctrl()
+    plain = 7.0 * (c1.attempts - c0.attempts) / dt
+    out["plain_fp64_single"] = {"rk_stages_per_s": plain, "accepted_steps": int(c1.steps_done - c0.steps_done),
+                                "ms_per_step": dt / max(1, c1.steps_done - c0.steps_done) * 1e3}
+    out["ratio_bf16x6_vs_plain_fp64"] = out["bf16x6"]["rk_stages_per_s"] / plain
+    out["ratio_fp32_vs_plain_fp64"] = out["fp32"]["rk_stages_per_s"] / plain
+    res.update(out)
+    del K64, K32, P
+    torch.cuda.empty_cache()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,6 +472,11 @@ def main():
     ap.add_argument("--rk-steps", type=int, default=200)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--nsplit", type=int, default=None)
+    ap.add_argument("--graph-iters", type=int, default=25)
+    ap.add_argument("--batch-iters", type=int, default=300)
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

@@ -103,8 +103,10 @@ int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_nodes, const in
  * product K.(V - Vpl) of src/QDsim_gpu.py:948-957 (v interleaved [j][strike,dip]). */
 int pq3d_dense_matvec_f64(const double *K64, int64_t N, const double *v, double *out, void *stream);
 /* Same with the FP32 operator copy: compensated FP32 products and sums (the
- * FP32-rounded operator applied to v to ~2^-44 relative). */
-int pq3d_dense_matvec_f32(const float *K32, int64_t N, const double *v, double *out, void *stream);
+ * FP32-rounded operator applied to v to ~2^-44 relative).  v is given split
+ * into FP32 pieces, vsplit[j] = (hi_strike, hi_dip, lo_strike, lo_dip) with
+ * v ~= hi + lo (16-byte aligned, N x 4 floats). */
+int pq3d_dense_matvec_f32(const float *K32, int64_t N, const float *vsplit, double *out, void *stream);
 
 /* Device-resident state of one dense simulation; every pointer is a device
  * array of N doubles unless stated.  Field meaning follows the reference
@@ -119,7 +121,8 @@ typedef struct pq3d_dense_sim {
     const double *a, *b, *dc, *f0, *shear_loading, *normal_loading, *rake0;
     /* traction rates out[3N] = K.(V-Vpl): [3i+0]=AdotV1, [3i+1]=AdotV2, [3i+2]=Bs.v1+Bd.v2 */
     double *rates;
-    /* scratch: vprime[2N], cand[4N] */
+    /* scratch: vprime[2N] (FP64 operator: v' as [N] double2; FP32 operator: its
+     * hi/lo split as [N] float4), cand[4N] */
     double *vprime, *cand;
     /* FP64 operator (3N)x(2N) or FP32 operator (exactly one non-NULL) */
     const double *K64;

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__
 // ---------------------------------------------------------------------------
 // attempt / decide / update
 
+template <bool kMixed>
 __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
 {
     __shared__ double red[8];
@@ -207,10 +208,12 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
             q0 += p[0]; q1 += p[1]; q2 += p[2];
         }
         const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
-        Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig};
+        const double a = S.a[idx], b = S.b[idx], dc = S.dc[idx];
+        Cell c{a, b, dc, S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig, 0.0, 0.0, 0.0};
+        if (kMixed) { c.inv_a = 1.0 / a; c.inv_b = 1.0 / b; c.bdc = b / dc; }
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
         double yo[4], e1, e2;
-        dp_attempt(c, S.V0, S.eta, hs, y, yo, e1, e2);
+        dp_attempt<kMixed>(c, S.V0, S.eta, hs, y, yo, e1, e2);
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
         m1 = e1;
         m2 = e2;
@@ -345,7 +348,9 @@ extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, si
     PQ3D_CUDA_TRY(cudaGetLastError());
     // 2-4. attempt, decide, update
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
-    attempt_kernel<<<grid, 256, 0, st>>>(S);
+    // FP64 arm: the reference right-hand side; mixed arms: rhs_mixed
+    if (S.precision == PQ3D_BATCH_FP64) attempt_kernel<false><<<grid, 256, 0, st>>>(S);
+    else attempt_kernel<true><<<grid, 256, 0, st>>>(S);
     decide_kernel<<<(S.B + 127) / 128, 128, 0, st>>>(S.ctrl, S.B);
     update_kernel<<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());

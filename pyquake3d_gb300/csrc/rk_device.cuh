@@ -27,6 +27,7 @@ constexpr double kRelTol = 1e-4;
 
 struct Cell {
     double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
+    double inv_a, inv_b, bdc;   // 1/a, 1/b, b/dc (used by the mixed-precision right-hand side)
 };
 
 __device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
@@ -56,24 +57,76 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     dtau2 = t2 / 1e6;
 }
 
+// e^x for the mixed-precision right-hand side: x = (n + f) / log2(e) with n
+// integer and |f| <= 1/2 (Cody-Waite range reduction); 2^f from the FP32
+// exp2f, 2^n exact.  Relative error ~2.5e-7 (that of exp2f), 6 FP64
+// operations instead of the ~20 of an FP64 exp.  The argument is clipped to
+// +-700 like the reference's safe_exp.
+__device__ __forceinline__ double fexp(double x)
+{
+    x = fmin(fmax(x, -700.0), 700.0);
+    const double t = x * 1.4426950408889634;
+    const double n = rint(t);
+    const float f = (float)(t - n);
+    const double scale = __longlong_as_double((long long)((int)n + 1023) << 52);
+    return (double)exp2f(f) * scale;
+}
+
+// Mixed-precision right-hand side (batched mixed modes).  Same equations as
+// rhs(); the factors e^{-psi/a} cosh(x), e^{-psi/a} sinh(x) are formed as
+// (e^{x - psi/a} +- e^{-x - psi/a}) / 2 with fexp, and the divisions share
+// one reciprocal per stage.  The state and its increments stay FP64.
+__device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
+                                          double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+{
+    const double Tn = Tno * 1e6, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
+    const double inv_aTn = 1.0 / (c.a * Tn);
+    const double x1 = clip700(T1 * inv_aTn), x2 = clip700(T2 * inv_aTn);
+    const double sp = clip700(-state * c.inv_a);
+    const double e1p = fexp(sp + x1), e1m = fexp(sp - x1), e2p = fexp(sp + x2), e2m = fexp(sp - x2);
+    const double twoV0 = 2.0 * V0;
+    const double dV1dtau = twoV0 * inv_aTn * (0.5 * (e1p + e1m));
+    const double dV2dtau = twoV0 * inv_aTn * (0.5 * (e2p + e2m));
+    const double inv_Tn = c.a * inv_aTn;
+    const double dV1dsigma = -dV1dtau * T1 * inv_Tn;
+    const double dV2dsigma = -dV2dtau * T2 * inv_Tn;
+    const double dV1dstate = -twoV0 * c.inv_a * (0.5 * (e1p - e1m));
+    const double dV2dstate = -twoV0 * c.inv_a * (0.5 * (e2p - e2m));
+    dstate = c.bdc * (V0 * fexp((c.f0 - state) * c.inv_b) - c.slipv);
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * c.dsig + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * c.dsig + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    dsig = c.dsig * 1e-6;
+    dtau1 = t1 * 1e-6;
+    dtau2 = t2 * 1e-6;
+}
+
+template <bool kMixed>
+__device__ __forceinline__ void rhs_sel(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
+                                        double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+{
+    if (kMixed) rhs_mixed(c, V0, eta, Tno, Tt1o, Tt2o, state, dstate, dsig, dtau1, dtau2);
+    else rhs(c, V0, eta, Tno, Tt1o, Tt2o, state, dstate, dsig, dtau1, dtau2);
+}
+
 // One Dormand-Prince attempt of one cell; y = (Tno, Tt1o, Tt2o, state).
 // Writes the 5th-order solution to yo and returns the two relative errors.
+template <bool kMixed = false>
 __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
                                            double yo[4], double &e1, double &e2)
 {
     double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
         u7;
     const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
-    rhs(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
-    rhs(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
-    rhs(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
+    rhs_sel<kMixed>(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
+    rhs_sel<kMixed>(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
+    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
         st + h * (B31 * s1 + B32 * s2), s3, n3, t3, u3);
-    rhs(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
+    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
         Tt2o + h * (B41 * u1 + B42 * u2 + B43 * u3), st + h * (B41 * s1 + B42 * s2 + B43 * s3), s4, n4, t4, u4);
-    rhs(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
+    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
         Tt1o + h * (B51 * t1 + B52 * t2 + B53 * t3 + B54 * t4), Tt2o + h * (B51 * u1 + B52 * u2 + B53 * u3 + B54 * u4),
         st + h * (B51 * s1 + B52 * s2 + B53 * s3 + B54 * s4), s5, n5, t5, u5);
-    rhs(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
+    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
         Tt1o + h * (B61 * t1 + B62 * t2 + B63 * t3 + B64 * t4 + B65 * t5),
         Tt2o + h * (B61 * u1 + B62 * u2 + B63 * u3 + B64 * u4 + B65 * u5),
         st + h * (B61 * s1 + B62 * s2 + B63 * s3 + B64 * s4 + B65 * s5), s6, n6, t6, u6);
@@ -81,7 +134,7 @@ __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta,
     yo[1] = Tt1o + h * (B71 * t1 + B73 * t3 + B74 * t4 + B75 * t5 + B76 * t6);
     yo[2] = Tt2o + h * (B71 * u1 + B73 * u3 + B74 * u4 + B75 * u5 + B76 * u6);
     yo[3] = st + h * (B71 * s1 + B73 * s3 + B74 * s4 + B75 * s5 + B76 * s6);
-    rhs(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
+    rhs_sel<kMixed>(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
     const double Tn8 = Tno + h * (B81 * n1 + B83 * n3 + B84 * n4 + B85 * n5 + B86 * n6 + B87 * n7);
     const double T18 = Tt1o + h * (B81 * t1 + B83 * t3 + B84 * t4 + B85 * t5 + B86 * t6 + B87 * t7);
     const double T28 = Tt2o + h * (B81 * u1 + B83 * u3 + B84 * u4 + B85 * u5 + B86 * u6 + B87 * u7);

@@ -89,40 +89,36 @@ __device__ __forceinline__ void acc2_add(Acc2 &a, float k, float vh, float vl)
     a.c = __fmaf_rn(k, vl, __fadd_rn(a.c, __fadd_rn(err, e)));
 }
 
-__device__ __forceinline__ void split2(double2 v, float &h0, float &l0, float &h1, float &l1)
+// v' of one cell split into FP32 pieces: (hi1, hi2, lo1, lo2), v ~= hi + lo.
+__device__ __forceinline__ float4 split_v(double v1, double v2)
 {
-    h0 = (float)v.x; l0 = (float)(v.x - (double)h0);
-    h1 = (float)v.y; l1 = (float)(v.y - (double)h1);
+    const float h1 = (float)v1, h2 = (float)v2;
+    return make_float4(h1, h2, (float)(v1 - (double)h1), (float)(v2 - (double)h2));
 }
 
-__device__ __forceinline__ void rows3_f32(const float2 *__restrict__ K, const double2 *__restrict__ v, int64_t N,
+__device__ __forceinline__ void rows3_f32(const float2 *__restrict__ K, const float4 *__restrict__ v, int64_t N,
                                           int64_t i, int lane, double acc[3])
 {
     const float2 *r0 = K + (3 * i) * N, *r1 = r0 + N, *r2 = r1 + N;
     Acc2 a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f};
     int64_t j = lane;
     for (; j + 32 < N; j += 64) {
-        const double2 xd0 = __ldg(v + j), xd1 = __ldg(v + j + 32);
+        const float4 x0 = __ldg(v + j), x1 = __ldg(v + j + 32);
         const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
         const float2 k01 = __ldcs(r0 + j + 32), k11 = __ldcs(r1 + j + 32), k21 = __ldcs(r2 + j + 32);
-        float h0, l0, h1, l1;
-        split2(xd0, h0, l0, h1, l1);
-        acc2_add(a0, k00.x, h0, l0); acc2_add(a0, k00.y, h1, l1);
-        acc2_add(a1, k10.x, h0, l0); acc2_add(a1, k10.y, h1, l1);
-        acc2_add(a2, k20.x, h0, l0); acc2_add(a2, k20.y, h1, l1);
-        split2(xd1, h0, l0, h1, l1);
-        acc2_add(a0, k01.x, h0, l0); acc2_add(a0, k01.y, h1, l1);
-        acc2_add(a1, k11.x, h0, l0); acc2_add(a1, k11.y, h1, l1);
-        acc2_add(a2, k21.x, h0, l0); acc2_add(a2, k21.y, h1, l1);
+        acc2_add(a0, k00.x, x0.x, x0.z); acc2_add(a0, k00.y, x0.y, x0.w);
+        acc2_add(a1, k10.x, x0.x, x0.z); acc2_add(a1, k10.y, x0.y, x0.w);
+        acc2_add(a2, k20.x, x0.x, x0.z); acc2_add(a2, k20.y, x0.y, x0.w);
+        acc2_add(a0, k01.x, x1.x, x1.z); acc2_add(a0, k01.y, x1.y, x1.w);
+        acc2_add(a1, k11.x, x1.x, x1.z); acc2_add(a1, k11.y, x1.y, x1.w);
+        acc2_add(a2, k21.x, x1.x, x1.z); acc2_add(a2, k21.y, x1.y, x1.w);
     }
     for (; j < N; j += 32) {
-        const double2 xd0 = __ldg(v + j);
+        const float4 x0 = __ldg(v + j);
         const float2 k00 = __ldcs(r0 + j), k10 = __ldcs(r1 + j), k20 = __ldcs(r2 + j);
-        float h0, l0, h1, l1;
-        split2(xd0, h0, l0, h1, l1);
-        acc2_add(a0, k00.x, h0, l0); acc2_add(a0, k00.y, h1, l1);
-        acc2_add(a1, k10.x, h0, l0); acc2_add(a1, k10.y, h1, l1);
-        acc2_add(a2, k20.x, h0, l0); acc2_add(a2, k20.y, h1, l1);
+        acc2_add(a0, k00.x, x0.x, x0.z); acc2_add(a0, k00.y, x0.y, x0.w);
+        acc2_add(a1, k10.x, x0.x, x0.z); acc2_add(a1, k10.y, x0.y, x0.w);
+        acc2_add(a2, k20.x, x0.x, x0.z); acc2_add(a2, k20.y, x0.y, x0.w);
     }
     acc[0] = warp_sum((double)a0.s + (double)a0.c);
     acc[1] = warp_sum((double)a1.s + (double)a1.c);
@@ -130,7 +126,7 @@ __device__ __forceinline__ void rows3_f32(const float2 *__restrict__ K, const do
 }
 
 template <bool kF32>
-__global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K, const double2 *__restrict__ v,
+__global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K, const void *__restrict__ v,
                                                      int64_t N, double *__restrict__ out)
 {
     const int lane = threadIdx.x & 31;
@@ -138,8 +134,8 @@ __global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K,
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t i = warp; i < N; i += nwarps) {
         double acc[3];
-        if (kF32) rows3_f32((const float2 *)K, v, N, i, lane, acc);
-        else rows3_f64((const double2 *)K, v, N, i, lane, acc);
+        if (kF32) rows3_f32((const float2 *)K, (const float4 *)v, N, i, lane, acc);
+        else rows3_f64((const double2 *)K, (const double2 *)v, N, i, lane, acc);
         if (lane == 0) { out[3 * i] = acc[0]; out[3 * i + 1] = acc[1]; out[3 * i + 2] = acc[2]; }
     }
 }
@@ -160,18 +156,23 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
     const unsigned nb = gridDim.x;
     double dttry = C->dttry, time = C->time;
     int64_t attempt = 0;
+    // v' (FP64 operator: double2 per cell; FP32 operator: its hi/lo FP32 split)
     double2 *vp = (double2 *)S.vprime;
+    float4 *vs = (float4 *)S.vprime;
 
     // v' from the current slip rate (src/QDsim_gpu.py:948-949)
-    for (int64_t i = gtid; i < N; i += gsz)
-        vp[i] = make_double2(S.slipv1[i] - S.Vpl * cos(S.rake0[i]), S.slipv2[i] - S.Vpl * sin(S.rake0[i]));
+    for (int64_t i = gtid; i < N; i += gsz) {
+        const double v1 = S.slipv1[i] - S.Vpl * cos(S.rake0[i]), v2 = S.slipv2[i] - S.Vpl * sin(S.rake0[i]);
+        if (kF32) vs[i] = split_v(v1, v2);
+        else vp[i] = make_double2(v1, v2);
+    }
     if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
 
     for (int step = 0; step < nsteps; ++step) {
         // (1) traction rates
         for (int64_t i = warp; i < N; i += nwarps) {
             double acc[3];
-            if (kF32) rows3_f32((const float2 *)S.K32, vp, N, i, lane, acc);
+            if (kF32) rows3_f32((const float2 *)S.K32, vs, N, i, lane, acc);
             else rows3_f64((const double2 *)S.K64, vp, N, i, lane, acc);
             if (lane == 0) {
                 S.rates[3 * i] = acc[0];
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             double m1 = 0.0, m2 = 0.0;
             for (int64_t i = gtid; i < N; i += gsz) {
                 Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
-                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2]};
+                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2], 0.0, 0.0, 0.0};
                 const double y[4] = {S.Tno[i], S.Tt1o[i], S.Tt2o[i], S.state[i]};
                 double yo[4], e1, e2;
                 dp_attempt(c, S.V0, S.eta, h, y, yo, e1, e2);
@@ -249,7 +250,9 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             S.slip1[i] = s1; S.slip2[i] = s2;
             S.slip[i] = sqrt(s1 * s1 + s2 * s2);
             S.fric[i] = S.Tt[i] / Tno;
-            vp[i] = make_double2(v1 - S.Vpl * cos(S.rake0[i]), v2 - S.Vpl * sin(S.rake0[i]));
+            const double w1 = v1 - S.Vpl * cos(S.rake0[i]), w2 = v2 - S.Vpl * sin(S.rake0[i]);
+            if (kF32) vs[i] = split_v(w1, w2);
+            else vp[i] = make_double2(w1, w2);
         }
         vmax = block_max(vmax, red);
         if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, dbits(vmax));
@@ -301,7 +304,7 @@ static int coop_grid(bool f32, int *grid)
 using namespace pq3d;
 using namespace pq3d::step;
 
-static int matvec(const void *K, int64_t N, const double *v, double *out, void *stream, bool f32)
+static int matvec(const void *K, int64_t N, const void *v, double *out, void *stream, bool f32)
 {
     clear_error();
     PQ3D_REQUIRE(N > 0 && K && v && out, "pq3d_dense_matvec: bad arguments");
@@ -310,8 +313,8 @@ static int matvec(const void *K, int64_t N, const double *v, double *out, void *
     const int threads = 256;
     const int64_t warps = N;
     const unsigned blocks = (unsigned)((warps * 32 + threads - 1) / threads);
-    if (f32) matvec_kernel<true><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, (const double2 *)v, N, out);
-    else matvec_kernel<false><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, (const double2 *)v, N, out);
+    if (f32) matvec_kernel<true><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, v, N, out);
+    else matvec_kernel<false><<<blocks, threads, 0, (cudaStream_t)stream>>>(K, v, N, out);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }
@@ -321,9 +324,9 @@ extern "C" int pq3d_dense_matvec_f64(const double *K64, int64_t N, const double 
     return matvec(K64, N, v, out, stream, false);
 }
 
-extern "C" int pq3d_dense_matvec_f32(const float *K32, int64_t N, const double *v, double *out, void *stream)
+extern "C" int pq3d_dense_matvec_f32(const float *K32, int64_t N, const float *vsplit, double *out, void *stream)
 {
-    return matvec(K32, N, v, out, stream, true);
+    return matvec(K32, N, vsplit, out, stream, true);
 }
 
 extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist,

@@ -30,7 +30,11 @@ def test_matvec_f64_f32_match_numpy(cuda):
         ref = K @ v
         assert np.abs(out.cpu().numpy() - ref).max() <= 1e-13 * np.abs(K).sum(axis=1).max() * np.abs(v).max()
         K32 = Kt.float().contiguous()
-        _lib.check(L.pq3d_dense_matvec_f32(K32.data_ptr(), N, vt.data_ptr(), out.data_ptr(), st))
+        vv = vt.view(N, 2)
+        hi = vv.float()
+        lo = (vv - hi.double()).float()
+        vs = torch.cat([hi, lo], dim=1).contiguous()
+        _lib.check(L.pq3d_dense_matvec_f32(K32.data_ptr(), N, vs.data_ptr(), out.data_ptr(), st))
         assert np.abs(out.cpu().numpy() - ref).max() <= 1e-5 * np.abs(K).sum(axis=1).max() * np.abs(v).max()
 
 
