@@ -88,6 +88,23 @@ int pq3d_assemble_dense(const double *nodes, const int64_t *tris, int64_t N,
                         double *K64, float *K32, void *workspace, size_t workspace_bytes,
                         void *stream);
 
+/* Variant of pq3d_assemble_dense that allocates nothing and takes no
+ * workspace -- no counterpart in the reference.  For callers that cannot call
+ * cudaMalloc: a host application whose device memory is handed out by its own
+ * pool allocator (for example a framework that reserves the device memory up
+ * front and forbids side allocations), or a loop that cannot afford the
+ * implicit device synchronisation and the failure modes of cudaMalloc/cudaFree
+ * between its launches.  The source and receiver tables live in a fixed
+ * 11.5 MB __device__ array inside this library, so N is limited to 32768
+ * elements (larger N returns PQ3D_ERR_ARG).  The first call on a device looks
+ * up the array's device address with that device current (cudaGetSymbolAddress)
+ * and caches it; make that first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (other streams, other host
+ * threads) race on it, so serialise them.  The caller still provides nodes,
+ * tris, K64 and K32 as in pq3d_assemble_dense. */
+int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *tris, int64_t N, int64_t row0, int64_t row1,
+                                double mu, double lambda_, int halfspace, double *K64, float *K32, void *stream);
+
 /* Host-buffer variant for callers that keep the mesh and the operator in host
  * memory (the reference keeps A1s..Bd as NumPy arrays): copies the mesh in,
  * assembles in row blocks on two streams and copies each block back while the

@@ -91,6 +91,8 @@ _SIGS = {
     "pq3d_gf_workspace_bytes": (c_size, [c_i64]),
     "pq3d_assemble_dense": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl, c_dbl, c_int,
                                     c_void_p, c_void_p, c_void_p, c_size, c_void_p]),
+    "pq3d_assemble_dense_noalloc": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl, c_dbl, c_int,
+                                            c_void_p, c_void_p, c_void_p]),
     "pq3d_assemble_dense_host": (c_int, [c_void_p, c_i64, c_void_p, c_i64, c_dbl, c_dbl, c_int, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f64": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f32": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),

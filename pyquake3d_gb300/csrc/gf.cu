@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -270,6 +271,36 @@ static int assemble_rows(const double *nodes, const int64_t *tris, int64_t N, in
     return PQ3D_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed scratch for pq3d_assemble_dense_noalloc: the source and receiver
+// tables of one call (kSrcStride + kRecvStride doubles per element) for up to
+// kNoAllocMaxN elements, 11.5 MB held by every GPU that loads this library.
+constexpr int64_t kNoAllocMaxN = 32768;
+static __device__ __align__(256) double g_noalloc_scratch[(size_t)(kSrcStride + kRecvStride) * kNoAllocMaxN];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[256];   // device address of g_noalloc_scratch, per device ordinal
+
+// Device address of the fixed scratch on the current device, looked up once
+// per device (with that device current) and cached.
+static int noalloc_scratch(double **out)
+{
+    int dev = 0;
+    PQ3D_CUDA_TRY(cudaGetDevice(&dev));
+    PQ3D_REQUIRE(dev >= 0 && dev < 256, "pq3d_assemble_dense_noalloc: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(PQ3D_ERR_CUDA, "pq3d_assemble_dense_noalloc: cudaGetSymbolAddress failed: %s",
+                             cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = (double *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return PQ3D_OK;
+}
+
 }  // namespace gf
 }  // namespace pq3d
 
@@ -415,4 +446,27 @@ done:
     cudaFree(d_tris);
     cudaFree(d_ws);
     return rc;
+}
+
+extern "C" int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *tris, int64_t N, int64_t row0,
+                                           int64_t row1, double mu, double lambda_, int halfspace, double *K64,
+                                           float *K32, void *stream)
+{
+    clear_error();
+    PQ3D_REQUIRE(N > 0 && row0 >= 0 && row1 <= N && row0 <= row1, "pq3d_assemble_dense_noalloc: bad sizes");
+    PQ3D_REQUIRE(N <= kNoAllocMaxN, "pq3d_assemble_dense_noalloc: N = %lld exceeds the fixed scratch limit of %lld "
+                 "elements (use pq3d_assemble_dense with a caller-provided workspace)", (long long)N,
+                 (long long)kNoAllocMaxN);
+    PQ3D_REQUIRE(nodes && tris && K64, "pq3d_assemble_dense_noalloc: null pointer");
+    PQ3D_REQUIRE(aligned16(K64) && (!K32 || ((uintptr_t)K32 & 7u) == 0),
+                 "pq3d_assemble_dense_noalloc: K64 must be 16-byte aligned, K32 8-byte aligned");
+    if (halfspace) return set_error(PQ3D_ERR_UNSUPPORTED, "pq3d_assemble_dense_noalloc: half-space not available");
+    double *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    if (row0 == row1) return PQ3D_OK;
+    // every table entry the assembly reads is rewritten by this call's set-up
+    // kernels, so nothing has to be cleared between calls
+    return assemble_rows(nodes, tris, N, row0, row1, mu, lambda_, K64, K32, scratch, scratch + (size_t)kSrcStride * N,
+                         true, (cudaStream_t)stream);
 }
