@@ -321,6 +321,8 @@ def bench_ours(args):
         out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks)
         if not args.no_batch:
             out["batched"] = bench_batched(torch, dev, args, peaks)
+        if not args.no_hmat:
+            out["hmatrix"] = bench_hmatrix(torch, dev, args, peaks)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
     line = {"metric": METRIC, "value": value, "unit": "GF entries/s", "n_gpus": world, "steps": args.steps,
@@ -462,6 +464,83 @@ def bench_batched(torch, dev, args, peaks):
     return res
 
 
+def bench_hmatrix(torch, dev, args, peaks):
+    """Config: H-matrix path.  Rough fault 200 x 40 km, 500 x 100 cells ->
+    N = 100,000; cluster leaf 64, block leaf 64, eta = 2, ACA tolerance 1e-4,
+    FP32 factors.  RK45 stepping with the H-matrix product for a bounded
+    number of stages; product error against dense FP64 rows (assembly kernel)
+    at 1,000 seeded receivers."""
+    from pyquake3d_gb300 import gf, mesh
+    from pyquake3d_gb300.ensemble import Ensemble
+    from pyquake3d_gb300.hmatrix import HMatrix
+    Lkm, Wkm, nx, nz = (200.0, 40.0, 500, 100) if not args.quick else (40.0, 20.0, 80, 40)
+    nodes, tris = mesh.rough_fault(Lkm, Wkm, nx, nz, hurst=0.8, ratio=1e-3, seed=0)
+    N = tris.shape[0]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, eta=2.0, tol=1e-4, device=dev)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    res = {"workload": "H-matrix: rough %dx%d km, N=%d, leaf 64, eta 2, ACA tol 1e-4, FP32 factors" % (Lkm, Wkm, N),
+           "build_s": t_build, "stats": H.stats}
+    # product timing (B = 1)
+    v = torch.randn(1, 2 * N, dtype=torch.float64, device=dev)
+    ws = torch.empty(H.workspace_bytes(1), dtype=torch.uint8, device=dev)
+    out = torch.empty(1, 3 * N, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        H.apply(v, out, ws)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(10):
+        H.apply(v, out, ws)
+    e.record()
+    e.synchronize()
+    ta = s.elapsed_time(e) / 10 / 1e3
+    res["apply_ms"] = ta * 1e3
+    res["apply_roofline"] = {"bound": "hbm", "unit": "GB/s", "achieved": H.stats["bytes"] / ta / 1e9,
+                             "peak": peaks["hbm_gbs"], "frac": H.stats["bytes"] / ta / 1e9 / peaks["hbm_gbs"],
+                             "algorithmic_bytes": H.stats["bytes"], "note": "dense blocks + U + V (FP32) once"}
+    # error against dense FP64 rows at 1000 seeded receivers
+    rng = np.random.default_rng(0)
+    recv = np.sort(rng.choice(N, size=min(1000, N), replace=False))
+    vv = v[0]
+    y = out[0]
+    num = den = 0.0
+    nodes_t, tris_t = gf.mesh_to_device(nodes, tris, dev)
+    row = torch.empty((3, 2 * N), dtype=torch.float64, device=dev)
+    wsg = torch.empty(L_ws_bytes(N), dtype=torch.uint8, device=dev)
+    for i in recv:
+        gf.assemble_dense(nodes_t, tris_t, MU, LAM, fp32_copy=False, rows=(int(i), int(i) + 1), out64=row, workspace=wsg)
+        ref = row @ vv
+        num += float(torch.sum((ref - y[3 * i:3 * i + 3]) ** 2))
+        den += float(torch.sum(ref ** 2))
+    res["error_vs_dense_rows"] = {"rel_l2": (num / den) ** 0.5, "receivers": int(len(recv)), "seed": 0}
+    # stepping with the H-matrix product
+    _, xg = mesh.element_frames(nodes, tris)
+    tab = mesh.friction_table(xg, Lkm * 1e3, Wkm * 1e3, seed=0, v_nuc=1e-3)
+    ens = Ensemble(H, tab[None], mu=MU, Cs=3464.0, precision="hmat")
+    ens.iterate(2)
+    torch.cuda.synchronize()
+    st0 = ens.stages()
+    iters = max(1, args.hmat_stages // 7)
+    s.record()
+    ens.iterate(iters)
+    e.record()
+    e.synchronize()
+    dt = s.elapsed_time(e) / 1e3
+    st1 = ens.stages()
+    res["stepping"] = {"rk_stages_per_s": (st1 - st0) / dt, "stages": int(st1 - st0), "seconds": dt,
+                       "status": int(ens.read_ctrl()[0].status)}
+    del H, ens
+    torch.cuda.empty_cache()
+    return res
+
+
+def L_ws_bytes(N):
+    from pyquake3d_gb300 import _lib
+    return _lib.load().pq3d_gf_workspace_bytes(N)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -473,6 +552,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-hmat", action="store_true")
+    ap.add_argument("--hmat-stages", type=int, default=500)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--nsplit", type=int, default=None)
     ap.add_argument("--graph-iters", type=int, default=25)

@@ -205,6 +205,7 @@ typedef struct pq3d_run_ctrl {
 #define PQ3D_BATCH_BF16X6 2    /* FP32 operator split on the fly into 3 BF16 pieces, v' into 3 BF16
                                   pieces, the 6 leading cross products on tcgen05 tensor cores,
                                   FP32 accumulation in tensor memory, FP64 across K slices */
+#define PQ3D_BATCH_HMAT 3      /* H-matrix product (pq3d_hmat_apply); K points to a host pq3d_hmat */
 
 /* Device state of B simulations sharing one mesh.  Arrays are run-major
  * [B][N] FP64 unless stated.  Same fields and units as pq3d_dense_sim. */
@@ -222,7 +223,8 @@ typedef struct pq3d_batch_sim {
                               to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], or for
                               BF16X6 the packed pieces (pq3d_batch_rhs_bytes, zero-initialised) */
     const void *K;         /* operator: FP64 (3N)x(2N) for FP64, FP32 (3N)x(2N) for FP32, the
-                              packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6 */
+                              packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6, a host
+                              pointer to a pq3d_hmat for HMAT (v' then FP64 [Bp][2N]) */
     pq3d_run_ctrl *ctrl;   /* [B] */
     double V0, Vpl, eta;
     int32_t fix_Tn;
@@ -255,6 +257,61 @@ int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream);
  * the per-run accept/reject decision and the state update of the accepted runs
  * (masked acceptance; rejected runs retry with their smaller dt next time). */
 int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------- device: H-matrix ---------------- */
+
+/* Source and receiver tables of a mesh (the set-up step of the assembly) into
+ * `workspace` (pq3d_gf_workspace_bytes(N)): used by the H-matrix kernels. */
+int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, void *workspace, size_t workspace_bytes,
+                  void *stream);
+
+/* H-matrix of the (3N)x(2N) traction operator in a renumbering where every
+ * cluster is a contiguous range (perm[p] = element at position p).  Replaces
+ * the reference's BlockTree (src/Hmatrix.py:277-2196) for the product. */
+typedef struct pq3d_hmat {
+    int64_t N;
+    int32_t nblocks, nleaves;
+    int64_t t_rows;               /* sum of the ranks of the low-rank blocks */
+    const int64_t *perm;          /* [N] */
+    const int64_t *blk;           /* [nblocks][4]: r0, r1, c0, c1 (permuted element ranges) */
+    const int32_t *rank;          /* [nblocks]: rank k >= 0 of a low-rank block, -1 for a dense block */
+    const int64_t *off;           /* [nblocks]: offset (floats) of the block in data */
+    const float *data;            /* dense block (3m x 2n) or U (3m x k) then V (k x 2n), row-major FP32 */
+    const int32_t *lr_ids;        /* low-rank block ids, in order */
+    const int64_t *lr_row0;       /* [count, prefix sums of their ranks (count + 1 values)] */
+    const int64_t *t_off;         /* [nblocks]: first rank row of the block in the product workspace */
+    const int64_t *leaf;          /* [nleaves][2]: permuted ranges of the leaf row clusters */
+    const int64_t *leaf_ptr;      /* [nleaves + 1] */
+    const int32_t *leaf_blocks;   /* blocks whose row range covers each leaf row cluster, fixed order */
+} pq3d_hmat;
+
+/* ACA (partial pivoting, relative Frobenius tolerance `tol`) of the listed
+ * admissible blocks, one CTA per block, rows and columns generated by the GF
+ * kernel from `tables` (pq3d_gf_setup).  Per block b: kcap[b] = rank cap,
+ * UV + uv_off[b] = FP64 scratch for U (kcap x 3m) then V (kcap x 2n),
+ * used + used_off[b] = 3m zeroed bytes.  Outputs rank[b] and status[b]
+ * (0 converged, 1 rank cap reached, 2 non-finite).  Replaces ACA_worker /
+ * ACA_plus_full_traceS/D (src/Hmatrix.py:661-1344). */
+int pq3d_hmat_aca(const double *tables, int64_t N, const int64_t *perm, int nblocks, const int64_t *blk,
+                  const int32_t *kcap, double tol, double mu, double lambda_, double *UV, const int64_t *uv_off,
+                  uint8_t *used, const int64_t *used_off, int32_t *rank, int32_t *status, void *stream);
+/* Dense blocks ids[0..nids) into D + d_off[b] (FP32, 3m x 2n row-major); every
+ * d_off[b] must be even (8-byte aligned block starts). */
+int pq3d_hmat_dense_blocks(const double *tables, int64_t N, const int64_t *perm, const int64_t *blk,
+                           const int32_t *ids, int nids, double mu, double lambda_, float *D, const int64_t *d_off,
+                           void *stream);
+/* FP64 ACA factors of blocks ids[] -> FP32 U (3m x k) and V (k x 2n) at out + out_off[b]. */
+int pq3d_hmat_pack_factors(const double *UV, const int64_t *uv_off, const int64_t *blk, const int32_t *kcap,
+                           const int32_t *rank, const int32_t *ids, int nids, float *out, const int64_t *out_off,
+                           void *stream);
+/* Y[r] = H X[r] for B right-hand sides: X [B][2N] (element order, interleaved
+ * strike/dip), Y [B][3N] (traction components per element).  Deterministic:
+ * each output row adds its blocks in a fixed order with compensated FP32
+ * arithmetic.  Replaces blocks_process_MVM (src/Hmatrix.py:1773-1866), all six
+ * operator types at once. */
+size_t pq3d_hmat_workspace_bytes(const pq3d_hmat *H, int B);
+int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, double *Y, void *workspace, size_t workspace_bytes,
+                    void *stream);
 
 #ifdef __cplusplus
 }

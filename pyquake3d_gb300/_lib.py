@@ -67,9 +67,17 @@ class BatchSim(ctypes.Structure):
          ("pad1", ctypes.c_int32)]
 
 
+class HMat(ctypes.Structure):
+    """Mirror of pq3d_hmat."""
+    _fields_ = [("N", c_i64), ("nblocks", ctypes.c_int32), ("nleaves", ctypes.c_int32), ("t_rows", c_i64)] + \
+        [(n, c_void_p) for n in ("perm", "blk", "rank", "off", "data", "lr_ids", "lr_row0", "t_off", "leaf",
+                                 "leaf_ptr", "leaf_blocks")]
+
+
 PQ3D_BATCH_FP64 = 0
 PQ3D_BATCH_FP32 = 1
 PQ3D_BATCH_BF16X6 = 2
+PQ3D_BATCH_HMAT = 3
 
 
 class StepCtrl(ctypes.Structure):
@@ -102,6 +110,15 @@ _SIGS = {
     "pq3d_batch_rhs_bytes": (c_size, [c_i64, c_int]),
     "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
+    "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_size, c_void_p]),
+    "pq3d_hmat_aca": (c_int, [c_void_p, c_i64, c_void_p, c_int, c_void_p, c_void_p, c_dbl, c_dbl, c_dbl, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pq3d_hmat_dense_blocks": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_int, c_dbl, c_dbl, c_void_p,
+                                       c_void_p, c_void_p]),
+    "pq3d_hmat_pack_factors": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                       c_void_p, c_void_p]),
+    "pq3d_hmat_workspace_bytes": (c_size, [ctypes.POINTER(HMat), c_int]),
+    "pq3d_hmat_apply": (c_int, [ctypes.POINTER(HMat), c_void_p, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "pq3d_batch_prepare": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
     "pq3d_batch_iterate": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
 }

@@ -53,7 +53,7 @@ __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_
     const int Bp = padded_runs(S.B);
     const int64_t o = (int64_t)r * 2 * N + 2 * i;
     (void)Bp;
-    if (S.precision == PQ3D_BATCH_FP64) {
+    if (S.precision == PQ3D_BATCH_FP64 || S.precision == PQ3D_BATCH_HMAT) {
         reinterpret_cast<double2 *>((double *)S.vop + o)[0] = make_double2(v1, v2);
     } else if (S.precision == PQ3D_BATCH_FP32) {
         reinterpret_cast<float2 *>((float *)S.vop + o)[0] = make_float2((float)v1, (float)v2);
@@ -293,7 +293,9 @@ static int check_sim(const pq3d_batch_sim *S)
 {
     PQ3D_REQUIRE(S && S->N > 0 && S->B > 0 && S->B <= 1024 && S->ctrl && S->K && S->vop && S->rates && S->cand,
                  "pq3d_batch: bad simulation structure");
-    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_BF16X6, "pq3d_batch: bad precision");
+    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_HMAT, "pq3d_batch: bad precision");
+    if (S->precision == PQ3D_BATCH_HMAT)
+        PQ3D_REQUIRE(((const pq3d_hmat *)S->K)->N == S->N, "pq3d_batch: H-matrix size differs from N");
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
     PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
     if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
@@ -308,6 +310,8 @@ using namespace pq3d::batch;
 
 extern "C" size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim)
 {
+    if (sim && sim->precision == PQ3D_BATCH_HMAT)
+        return pq3d_hmat_workspace_bytes((const pq3d_hmat *)sim->K, padded_runs(sim->B));
     if (!sim || sim->precision != PQ3D_BATCH_BF16X6) return 0;
     return pq3d::tc::gemm_bf16x6_workspace_bytes(sim->N, padded_runs(sim->B), sim->nsplit);
 }
@@ -340,9 +344,13 @@ extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, si
     } else if (S.precision == PQ3D_BATCH_FP32) {
         dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
         gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Bp, S.rates);
-    } else {
+    } else if (S.precision == PQ3D_BATCH_BF16X6) {
         rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.rates, workspace,
                                    workspace_bytes, st);
+        if (rc) return rc;
+    } else {
+        rc = pq3d_hmat_apply((const pq3d_hmat *)S.K, (const double *)S.vop, Bp, S.rates, workspace, workspace_bytes,
+                             stream);
         if (rc) return rc;
     }
     PQ3D_CUDA_TRY(cudaGetLastError());

@@ -84,22 +84,8 @@ assemble_dense_kernel(const double *__restrict__ src, const double *__restrict__
     const SoaSrc F{s_src + t, kTJ};
     const int64_t ld = 2 * N;
     for (int ii = 0; ii < nrec; ++ii) {
-        const double *R = s_rcv + ii * kRecvStride;
-        double x, y, z;
-        tdcs_point(F, R[0], R[1], R[2], x, y, z);
-        double Es[6], Ed[6];
-        tdcs_strain_sd(F, x, y, z, nu, k, Es, Ed);
-        double ue1[3], ue2[3], un[3];   // receiver axes in the source system
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int fa = F_NX + 3 * a;
-            ue1[a] = F(fa) * R[3] + F(fa + 1) * R[4] + F(fa + 2) * R[5];
-            ue2[a] = F(fa) * R[6] + F(fa + 1) * R[7] + F(fa + 2) * R[8];
-            un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
-        }
         double ts[3], td[3];
-        tractions_tdcs(Es, ue1, ue2, un, two_mu, lam, ts);
-        tractions_tdcs(Ed, ue1, ue2, un, two_mu, lam, td);
+        pair_tractions(F, s_rcv + ii * kRecvStride, nu, k, two_mu, lam, ts, td);
         const int64_t r = 3 * (i0 + ii - row0);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -469,4 +455,20 @@ extern "C" int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *t
     // kernels, so nothing has to be cleared between calls
     return assemble_rows(nodes, tris, N, row0, row1, mu, lambda_, K64, K32, scratch, scratch + (size_t)kSrcStride * N,
                          true, (cudaStream_t)stream);
+}
+
+extern "C" int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, void *workspace,
+                             size_t workspace_bytes, void *stream)
+{
+    clear_error();
+    PQ3D_REQUIRE(nodes && tris && workspace && N > 0, "pq3d_gf_setup: bad arguments");
+    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N) && aligned16(workspace), "pq3d_gf_setup: workspace too small");
+    double *src = (double *)workspace;
+    double *recv = src + (size_t)kSrcStride * N;
+    const int th = 128;
+    const unsigned nb = (unsigned)((N + th - 1) / th);
+    setup_sources_kernel<<<nb, th, 0, (cudaStream_t)stream>>>(nodes, tris, N, src);
+    setup_receivers_kernel<<<nb, th, 0, (cudaStream_t)stream>>>(nodes, tris, N, recv);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
 }

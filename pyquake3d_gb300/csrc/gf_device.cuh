@@ -360,5 +360,28 @@ __device__ __forceinline__ void tractions_tdcs(const T E[6], const T ue1[3], con
     out[2] = two_mu * (un[0] * u0 + un[1] * u1 + un[2] * u2) + lam * tr;
 }
 
+// The six tractions of one (receiver, source) pair: receiver record R
+// (centroid, e1, e2, n), source fields F; ts = unit strike slip, td = unit dip
+// slip, components (e1, e2, n).
+template <class Src>
+__device__ __forceinline__ void pair_tractions(const Src &F, const double *R, double nu, double k, double two_mu,
+                                               double lam, double ts[3], double td[3])
+{
+    double x, y, z;
+    tdcs_point(F, R[0], R[1], R[2], x, y, z);
+    double Es[6], Ed[6];
+    tdcs_strain_sd(F, x, y, z, nu, k, Es, Ed);
+    double ue1[3], ue2[3], un[3];   // receiver axes in the source system
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int fa = F_NX + 3 * a;
+        ue1[a] = F(fa) * R[3] + F(fa + 1) * R[4] + F(fa + 2) * R[5];
+        ue2[a] = F(fa) * R[6] + F(fa + 1) * R[7] + F(fa + 2) * R[8];
+        un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
+    }
+    tractions_tdcs(Es, ue1, ue2, un, two_mu, lam, ts);
+    tractions_tdcs(Ed, ue1, ue2, un, two_mu, lam, td);
+}
+
 }  // namespace gf
 }  // namespace pq3d

@@ -13,6 +13,7 @@ Precisions of the traction product (``precision=``):
   "bf16x6" the operator and v' each split into three BF16 pieces, the six
            leading cross products on the tcgen05 tensor cores with FP32
            accumulation in tensor memory; K slices added in FP64
+  "hmat"   an :class:`~pyquake3d_gb300.hmatrix.HMatrix` (large meshes)
 Time, slip, the state and the RK error norm stay FP64 in every mode.
 """
 from __future__ import annotations
@@ -25,7 +26,8 @@ import torch
 from . import _lib
 from .QDsim_gpu import initial_state
 
-PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6}
+PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6,
+              "hmat": _lib.PQ3D_BATCH_HMAT}
 STATE = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2")
 PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0")
 
@@ -73,9 +75,14 @@ class Ensemble:
         tables = np.asarray(tables, dtype=np.float64)
         B, N = tables.shape[0], tables.shape[1]
         self.B, self.N, self.Bp = B, N, padded_runs(B)
-        dev = K.device if not isinstance(K, PackedOperator) else K.device
+        dev = K.device
         self.device = dev
-        if precision == "bf16x6":
+        if precision == "hmat":
+            assert K.N == N
+            kop = None
+            nsplit = 1
+            self.hmat = K
+        elif precision == "bf16x6":
             assert isinstance(K, PackedOperator) and K.N == N
             kop = K.data
             if nsplit is None:
@@ -96,7 +103,7 @@ class Ensemble:
         self.t["sin_rake0"] = torch.sin(torch.as_tensor(np.stack([s["rake0"] for s in inits]), **f64)).contiguous()
         self.t["rates"] = torch.zeros(self.nsplit * self.Bp * 3 * N, **f64)
         self.t["cand"] = torch.zeros(B * N * 4, **f64)
-        if precision == "fp64":
+        if precision in ("fp64", "hmat"):
             self.vop = torch.zeros(self.Bp * 2 * N, **f64)
         elif precision == "fp32":
             self.vop = torch.zeros(self.Bp * 2 * N, dtype=torch.float32, device=dev)
@@ -107,7 +114,8 @@ class Ensemble:
         S.N, S.B, S.precision, S.nsplit = N, B, prec, self.nsplit
         for k in STATE + PARAMS + ("rates", "cand"):
             setattr(S, k, self.t[k].data_ptr())
-        S.vop, S.K, S.ctrl = self.vop.data_ptr(), self.K.data_ptr(), self.ctrl_t.data_ptr()
+        S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
+        S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
         self.S = S
         self.ws = torch.zeros(max(256, L.pq3d_batch_workspace_bytes(ctypes.byref(S))), dtype=torch.uint8, device=dev)

@@ -1,0 +1,298 @@
+"""H-matrix of the traction operator on the GPU.
+
+Partition (host, set-up): the reference's geometric rules
+(src/Hmatrix.py:68-192, 2077-2142): binary cluster tree over the element
+centroids by bisecting the longest bounding-box axis at its midpoint (points
+<= midpoint go left, order kept, a leaf at <= min_size points or when a side
+would be empty); block tree by recursive quad-splitting of (row, column)
+cluster pairs, a leaf block when admissible (min(diam) <= eta * dist, eta = 2)
+or when either side has <= mini_leaf points or no children.  Low-rank blocks:
+both sides > mini_leaf (src/Hmatrix.py:1292-1344); the rest are dense.
+Elements are renumbered in depth-first leaf order, so every cluster is a
+contiguous range and a block is a pair of ranges.
+
+Compression and product (device, csrc/hmat.cu): ACA with partial pivoting on
+the combined (3m x 2n) block (all six operators at once) with a relative
+tolerance, FP32 factors, dense near field in FP32, and a deterministic product
+for B right-hand sides.
+
+Reference-shaped API: ``createHmatrix(xg, nodelst, elelst, eleVec, Para0,
+mini_leaf)`` -> :class:`BlockTree` with ``calc_Hmatrix_ACA(dir,
+save_corefunc)`` and ``blocks_process_MVM(x, blocks, type)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+
+import numpy as np
+import torch
+
+from . import _lib
+from .mesh import element_frames
+
+sys.setrecursionlimit(max(10000, sys.getrecursionlimit()))
+
+
+class _Node:
+    __slots__ = ("start", "end", "left", "right", "lo", "hi")
+
+
+def build_partition(xg, min_size=16, mini_leaf=32, eta=2.0):
+    """Returns (perm, blocks, leaves): perm[p] = element at position p;
+    blocks = int64 array (nb, 5): r0, r1, c0, c1, lowrank (0/1) in depth-first
+    order; leaves = int64 array (nl, 2) of leaf cluster ranges."""
+    xg = np.asarray(xg, dtype=np.float64)
+    perm = []
+    leaves = []
+
+    def tree(idx, pts):
+        node = _Node()
+        node.start = len(perm)
+        node.lo = pts.min(axis=0)
+        node.hi = pts.max(axis=0)
+        node.left = node.right = None
+        split = None
+        if len(idx) > min_size:
+            j = int(np.argmax(node.hi - node.lo))
+            g = (node.lo[j] + node.hi[j]) / 2
+            m1 = pts[:, j] <= g
+            m2 = pts[:, j] > g
+            if m1.any() and m2.any():
+                split = (m1, m2)
+        if split is None:
+            perm.extend(idx.tolist())
+            leaves.append((node.start, len(perm)))
+        else:
+            m1, m2 = split
+            node.left = tree(idx[m1], pts[m1])
+            node.right = tree(idx[m2], pts[m2])
+        node.end = len(perm)
+        return node
+
+    root = tree(np.arange(len(xg)), xg)
+    blocks = []
+
+    def admissible(a, b):
+        d_a = np.sqrt(np.sum((a.hi - a.lo) ** 2))
+        d_b = np.sqrt(np.sum((b.hi - b.lo) ** 2))
+        dist = np.sqrt(np.sum(np.maximum(0, b.lo - a.hi) ** 2 + np.maximum(0, a.lo - b.hi) ** 2))
+        return min(d_a, d_b) <= eta * dist
+
+    def rec(r, c):
+        nr, nc = r.end - r.start, c.end - c.start
+        if admissible(r, c) or nr <= mini_leaf or nc <= mini_leaf or \
+                r.left is None or r.right is None or c.left is None or c.right is None:
+            blocks.append((r.start, r.end, c.start, c.end, int(nr > mini_leaf and nc > mini_leaf)))
+            return
+        rec(r.left, c.left)
+        rec(r.left, c.right)
+        rec(r.right, c.left)
+        rec(r.right, c.right)
+
+    rec(root, root)
+    return np.asarray(perm, dtype=np.int64), np.asarray(blocks, dtype=np.int64), np.asarray(leaves, dtype=np.int64)
+
+
+class HMatrix:
+    """Device H-matrix of the (3N)x(2N) traction operator of a mesh."""
+
+    def __init__(self, nodes, tris, mu, lam, *, min_size=16, mini_leaf=32, eta=2.0, tol=1e-4, kmax=128,
+                 device="cuda", chunk_bytes=8 << 30):
+        L = _lib.load()
+        self.device = torch.device(device)
+        dev = self.device
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        tris = np.ascontiguousarray(tris, dtype=np.int64)
+        N = tris.shape[0]
+        self.N = N
+        _, xg = element_frames(nodes, tris)
+        perm, blocks, leaves = build_partition(xg, min_size, mini_leaf, eta)
+        self.perm_host, self.blocks_host, self.leaves_host = perm, blocks, leaves
+        st = torch.cuda.current_stream(dev).cuda_stream
+        self.nodes_t = torch.as_tensor(nodes, device=dev)
+        self.tris_t = torch.as_tensor(tris, device=dev)
+        self.tables = torch.empty(L.pq3d_gf_workspace_bytes(N), dtype=torch.uint8, device=dev)
+        _lib.check(L.pq3d_gf_setup(self.nodes_t.data_ptr(), self.tris_t.data_ptr(), N, self.tables.data_ptr(),
+                                   self.tables.numel(), st))
+        self.perm = torch.as_tensor(perm, device=dev)
+        nb = blocks.shape[0]
+        blk = np.ascontiguousarray(blocks[:, :4])
+        self.blk = torch.as_tensor(blk, device=dev)
+        m = blocks[:, 1] - blocks[:, 0]
+        n = blocks[:, 3] - blocks[:, 2]
+        lowrank = blocks[:, 4].astype(bool)
+        kcap = np.minimum(kmax, np.minimum(3 * m, 2 * n)).astype(np.int32)
+        kcap[~lowrank] = 0
+        self.kcap = torch.as_tensor(kcap, device=dev)
+        rank = np.full(nb, -1, dtype=np.int32)
+        status = np.zeros(nb, dtype=np.int32)
+        lr = np.nonzero(lowrank)[0]
+        # ACA in chunks of blocks, bounded scratch
+        uv_need = kcap.astype(np.int64) * (3 * m + 2 * n)
+        rank_t = torch.full((nb,), -1, dtype=torch.int32, device=dev)
+        status_t = torch.zeros(nb, dtype=torch.int32, device=dev)
+        factors = {}
+        i = 0
+        self.aca_chunks = 0
+        while i < len(lr):
+            j = i
+            tot = 0
+            while j < len(lr) and (j == i or tot + uv_need[lr[j]] * 8 <= chunk_bytes):
+                tot += uv_need[lr[j]] * 8
+                j += 1
+            ids = lr[i:j]
+            uv_off = np.zeros(nb, dtype=np.int64)
+            used_off = np.zeros(nb, dtype=np.int64)
+            uv_off[ids] = np.concatenate([[0], np.cumsum(uv_need[ids])[:-1]])
+            used_off[ids] = np.concatenate([[0], np.cumsum(3 * m[ids])[:-1]])
+            UV = torch.empty(int(uv_need[ids].sum()), dtype=torch.float64, device=dev)
+            used = torch.zeros(int((3 * m[ids]).sum()), dtype=torch.uint8, device=dev)
+            uv_off_t = torch.as_tensor(uv_off, device=dev)
+            used_off_t = torch.as_tensor(used_off, device=dev)
+            # the kernel indexes blocks by grid position: pass the chunk's sub-arrays
+            sub = torch.as_tensor(ids, device=dev)
+            blk_c = self.blk[sub].contiguous()
+            kcap_c = self.kcap[sub].contiguous()
+            uvo_c = uv_off_t[sub].contiguous()
+            uso_c = used_off_t[sub].contiguous()
+            rk_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
+            stt_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
+            _lib.check(L.pq3d_hmat_aca(self.tables.data_ptr(), N, self.perm.data_ptr(), len(ids), blk_c.data_ptr(),
+                                       kcap_c.data_ptr(), float(tol), float(mu), float(lam), UV.data_ptr(),
+                                       uvo_c.data_ptr(), used.data_ptr(), uso_c.data_ptr(), rk_c.data_ptr(),
+                                       stt_c.data_ptr(), st))
+            rank[ids] = rk_c.cpu().numpy()
+            status[ids] = stt_c.cpu().numpy()
+            factors[(i, j)] = (ids, UV, uvo_c, blk_c, kcap_c, rk_c)
+            self.aca_chunks += 1
+            i = j
+        ok = lowrank & (status == 0)
+        rank[~ok] = -1
+        self.aca_status = status
+        # storage offsets: dense 3m x 2n, low rank k (3m + 2n) floats, each block
+        # padded to a multiple of 4 floats so that every block starts 16-byte
+        # aligned (the dense-block kernel stores float2 pairs)
+        size = np.where(rank >= 0, rank.astype(np.int64) * (3 * m + 2 * n), 6 * m * n)
+        size = (size + 3) // 4 * 4
+        off = np.concatenate([[0], np.cumsum(size)[:-1]]).astype(np.int64)
+        assert np.all(off % 4 == 0)
+        self.data = torch.empty(int(size.sum()), dtype=torch.float32, device=dev)
+        self.off = torch.as_tensor(off, device=dev)
+        self.rank = torch.as_tensor(rank, device=dev)
+        dense_ids = np.nonzero(rank < 0)[0].astype(np.int32)
+        if len(dense_ids):
+            ids_t = torch.as_tensor(dense_ids, device=dev)
+            _lib.check(L.pq3d_hmat_dense_blocks(self.tables.data_ptr(), N, self.perm.data_ptr(), self.blk.data_ptr(),
+                                                ids_t.data_ptr(), len(dense_ids), float(mu), float(lam),
+                                                self.data.data_ptr(), self.off.data_ptr(), st))
+        for (ids, UV, uvo_c, blk_c, kcap_c, rk_c) in factors.values():
+            good = np.nonzero(rank[ids] >= 0)[0].astype(np.int32)   # positions inside the chunk
+            if len(good) == 0:
+                continue
+            pos = torch.as_tensor(good, device=dev)
+            out_off = self.off[torch.as_tensor(ids, device=dev)].contiguous()
+            _lib.check(L.pq3d_hmat_pack_factors(UV.data_ptr(), uvo_c.data_ptr(), blk_c.data_ptr(), kcap_c.data_ptr(),
+                                                rk_c.data_ptr(), pos.data_ptr(), len(good), self.data.data_ptr(),
+                                                out_off.data_ptr(), st))
+        torch.cuda.synchronize(dev)
+        del factors
+        # low-rank bookkeeping and leaf lists
+        lr_ids = np.nonzero(rank >= 0)[0].astype(np.int32)
+        ranks = rank[lr_ids].astype(np.int64)
+        prefix = np.concatenate([[0], np.cumsum(ranks)]).astype(np.int64)
+        t_off = np.zeros(nb, dtype=np.int64)
+        t_off[lr_ids] = prefix[:-1]
+        self.t_rows = int(prefix[-1])
+        self.lr_ids = torch.as_tensor(lr_ids if len(lr_ids) else np.zeros(1, np.int32), device=dev)
+        self.lr_row0 = torch.as_tensor(np.concatenate([[len(lr_ids)], prefix]).astype(np.int64), device=dev)
+        self.t_off = torch.as_tensor(t_off, device=dev)
+        nl = leaves.shape[0]
+        leaf_start = leaves[:, 0]
+        lists = [[] for _ in range(nl)]
+        for b in range(nb):
+            a = np.searchsorted(leaf_start, blocks[b, 0], side="left")
+            z = np.searchsorted(leaf_start, blocks[b, 1], side="left")
+            for q in range(a, z):
+                lists[q].append(b)
+        leaf_ptr = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.int64)
+        self.leaf = torch.as_tensor(np.ascontiguousarray(leaves), device=dev)
+        self.leaf_ptr = torch.as_tensor(leaf_ptr, device=dev)
+        self.leaf_blocks = torch.as_tensor(np.concatenate([np.asarray(x, np.int32) for x in lists]), device=dev)
+        H = _lib.HMat()
+        H.N, H.nblocks, H.nleaves, H.t_rows = N, nb, nl, self.t_rows
+        for k in ("perm", "blk", "rank", "off", "data", "lr_ids", "lr_row0", "t_off", "leaf", "leaf_ptr",
+                  "leaf_blocks"):
+            setattr(H, k, getattr(self, k).data_ptr())
+        self.H = H
+        self.stats = {"N": N, "blocks": int(nb), "lowrank_blocks": int(len(lr_ids)),
+                      "dense_blocks": int(len(dense_ids)), "aca_not_converged": int(np.sum(lowrank & (status != 0))),
+                      "max_rank": int(ranks.max()) if len(ranks) else 0,
+                      "mean_rank": float(ranks.mean()) if len(ranks) else 0.0,
+                      "bytes": int(self.data.numel() * 4), "dense_fp32_bytes": int(6 * N * N * 4),
+                      "leaves": int(nl)}
+
+    def workspace_bytes(self, B):
+        return _lib.load().pq3d_hmat_workspace_bytes(ctypes.byref(self.H), int(B))
+
+    def apply(self, X, out=None, workspace=None):
+        """Y = H X for X of shape (B, 2N) (FP64, element order, interleaved
+        strike/dip); returns Y (B, 3N)."""
+        L = _lib.load()
+        X = X.contiguous()
+        B = X.shape[0]
+        Y = out if out is not None else torch.empty((B, 3 * self.N), dtype=torch.float64, device=self.device)
+        ws = workspace if workspace is not None else torch.empty(self.workspace_bytes(B), dtype=torch.uint8,
+                                                                 device=self.device)
+        _lib.check(L.pq3d_hmat_apply(ctypes.byref(self.H), X.data_ptr(), B, Y.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     torch.cuda.current_stream(self.device).cuda_stream))
+        return Y
+
+    def matvec(self, v):
+        return self.apply(v.reshape(1, -1))[0]
+
+
+OP_INDEX = {"A1s": (0, 0), "A2s": (1, 0), "Bs": (2, 0), "A1d": (0, 1), "A2d": (1, 1), "Bd": (2, 1)}
+
+
+class BlockTree:
+    """Reference-shaped wrapper (src/Hmatrix.py:277): the partition is built
+    by createHmatrix, calc_Hmatrix_ACA compresses on the GPU,
+    blocks_process_MVM applies one of the six operators."""
+
+    def __init__(self, nodelst, elelst, mu, lam, halfspace, mini_leaf, eta=2.0, tol=1e-4, device="cuda"):
+        if halfspace:
+            raise NotImplementedError("half-space Green's functions are not available in this build")
+        self.nodelst, self.elelst = nodelst, elelst
+        self.mu_, self.lambda_, self.mini_leaf, self.eta, self.tol, self.device = mu, lam, mini_leaf, eta, tol, device
+        _, xg = element_frames(np.asarray(nodelst, dtype=np.float64), np.asarray(elelst, dtype=np.int64))
+        self.perm, self.blocks, self.leaves = build_partition(xg, 16, mini_leaf, eta)
+        self.H = None
+        self.blocks_to_process = [tuple(b) for b in self.blocks]
+
+    def calc_Hmatrix_ACA(self, dir=None, save_corefunc=False):
+        self.H = HMatrix(self.nodelst, self.elelst, self.mu_, self.lambda_, min_size=16, mini_leaf=self.mini_leaf,
+                         eta=self.eta, tol=self.tol, device=self.device)
+        return self.blocks_to_process
+
+    def blocks_process_MVM(self, xvector, blocks_to_process=None, type="A1s"):
+        """y = op(type) x on all blocks (one GPU holds every block; the
+        blocks argument is accepted for call compatibility)."""
+        if self.H is None:
+            self.calc_Hmatrix_ACA()
+        c, s = OP_INDEX[type]
+        N = self.H.N
+        X = torch.zeros((1, 2 * N), dtype=torch.float64, device=self.H.device)
+        X[0, s::2] = torch.as_tensor(np.asarray(xvector, dtype=np.float64), device=self.H.device)
+        return self.H.apply(X)[0, c::3].cpu().numpy()
+
+
+def createHmatrix(xg, nodelst, elelst, eleVec, Para0, mini_leaf=32):
+    """src/Hmatrix.py:2147-2196: build the block tree (compression happens in
+    calc_Hmatrix_ACA).  Para0 keys: 'Shear modulus', 'Lame constants',
+    'Half space' (values or strings)."""
+    mu = float(Para0["Shear modulus"])
+    lam = float(Para0["Lame constants"])
+    half = Para0.get("Half space", False)
+    half = half if isinstance(half, bool) else str(half) == "True"
+    return BlockTree(nodelst, elelst, mu, lam, half, mini_leaf)

@@ -234,6 +234,52 @@ def reference_sim(QDsim_gpu, nodes, tris, table, workdir):
     return sim
 
 
+def make_hmatrix_golden(nodes, tris, mini_leaf, seed=0):
+    """Leaf blocks of the reference's H-matrix (src/Hmatrix.py:2147-2196) and
+    its ACA products for one seeded x, from a scratch directory whose
+    src/TDstressFS_C.so is the reference built from source."""
+    import shutil
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        os.mkdir(os.path.join(td, "src"))
+        shutil.copy(os.path.join(REPO, "oracle", "_ref", "libTDstressFS_ref.so"), os.path.join(td, "src", "TDstressFS_C.so"))
+        cwd = os.getcwd()
+        os.chdir(td)
+        try:
+            import Hmatrix
+            import readmsh
+            eleVec, xg = readmsh.get_eleVec(nodes, tris, False)
+            para = {"GPU": False, "Shear modulus": MU, "Lame constants": LAM, "Half space": False,
+                    "Hmatrix_mpi_plot": False, "Using C++ green function": True}
+            tree = Hmatrix.createHmatrix(xg, nodes, tris, eleVec, para, mini_leaf=mini_leaf)
+            np.random.seed(seed)
+            # calc_Hmatrix_ACA collects the leaf blocks itself (src/Hmatrix.py:1603-1616)
+            blocks = tree.calc_Hmatrix_ACA(td, save_corefunc=False)
+            rows = [np.asarray(b.row_cluster, dtype=np.int64) for b in blocks]
+            cols = [np.asarray(b.col_cluster, dtype=np.int64) for b in blocks]
+            out["row_ptr"] = np.cumsum([0] + [len(r) for r in rows])
+            out["col_ptr"] = np.cumsum([0] + [len(c) for c in cols])
+            out["rows"] = np.concatenate(rows)
+            out["cols"] = np.concatenate(cols)
+            x = np.random.default_rng(seed).standard_normal(len(xg))
+            out["x"] = x
+            for typ in ("A1s", "A2s", "Bs", "A1d", "A2d", "Bd"):
+                out["y_" + typ] = tree.blocks_process_MVM(x, blocks, typ)
+            out["aca"] = np.array([bool(getattr(b, "judaca", False)) for b in blocks])
+        finally:
+            os.chdir(cwd)
+    out["nodes"], out["tris"], out["mini_leaf"] = nodes, tris, mini_leaf
+    return out
+
+
+def main_hmatrix_only():
+    import_reference_python()
+    nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
+    hm = make_hmatrix_golden(nodes, tris, mini_leaf=32)
+    np.savez_compressed(os.path.join(HERE, "hmatrix_small.npz"), **hm)
+    print("hmatrix_small.npz: %d leaf blocks, %d ACA" % (len(hm["row_ptr"]) - 1, int(hm["aca"].sum())))
+
+
 def main():
     rng = np.random.default_rng(20251203)
     lib = load_ref_lib()
@@ -284,9 +330,17 @@ def main():
         dense["rough_eleVec"], dense["rough_xg"] = sim.eleVec, sim.xg
     dense["mu"], dense["lam"] = MU, LAM
     np.savez_compressed(os.path.join(HERE, "dense_small.npz"), **dense)
+    # reference H-matrix: rough 24 x 12 km fault, 0.6 km cells -> N = 1600
+    nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
+    hm = make_hmatrix_golden(nodes, tris, mini_leaf=32)
+    np.savez_compressed(os.path.join(HERE, "hmatrix_small.npz"), **hm)
+    print("hmatrix_small.npz: %d leaf blocks, %d ACA" % (len(hm["row_ptr"]) - 1, int(hm["aca"].sum())))
     np.savez_compressed(os.path.join(HERE, "traj_small.npz"), **traj)
     print("dense_small.npz, traj_small.npz written")
 
 
 if __name__ == "__main__":
-    main()
+    if "--hmatrix-only" in sys.argv:
+        main_hmatrix_only()
+    else:
+        main()

@@ -1,0 +1,53 @@
+"""The H-matrix partition (cluster tree + block tree) against the oracle's
+restatement of the reference rules and against the reference's own
+partition recorded in tests/golden/hmatrix_small.npz."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import hmatrix as ohm
+from pyquake3d_gb300 import mesh
+from pyquake3d_gb300.hmatrix import build_partition
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "hmatrix_small.npz")
+
+
+def _as_sets(perm, blocks):
+    """Blocks as sorted index tuples (the renumbering orders a cluster's
+    elements by depth-first leaf order, the reference by original order)."""
+    return [(tuple(sorted(perm[b[0]:b[1]])), tuple(sorted(perm[b[2]:b[3]])), bool(b[4])) for b in blocks]
+
+
+@pytest.mark.parametrize("which,params", [("planar", (16, 32)), ("rough", (16, 32)), ("rough", (64, 64)),
+                                          ("planar", (8, 16))])
+def test_partition_matches_oracle(which, params):
+    if which == "planar":
+        nodes, tris = mesh.planar_fault(30.0, 15.0, 30, 15)
+    else:
+        nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
+    _, xg = mesh.element_frames(nodes, tris)
+    perm, blocks, leaves = build_partition(xg, params[0], params[1])
+    got = _as_sets(perm, blocks)
+    ref = [(tuple(sorted(r)), tuple(sorted(c)), lr) for r, c, lr in ohm.leaf_blocks(xg, params[0], params[1])]
+    assert got == ref
+    # leaves tile [0, N), blocks tile the whole matrix
+    assert leaves[0, 0] == 0 and leaves[-1, 1] == len(xg) and np.all(leaves[1:, 0] == leaves[:-1, 1])
+    area = np.sum((blocks[:, 1] - blocks[:, 0]) * (blocks[:, 3] - blocks[:, 2]))
+    assert area == len(xg) ** 2
+    assert sorted(perm.tolist()) == list(range(len(xg)))
+
+
+def test_oracle_partition_matches_reference_golden():
+    if not os.path.exists(GOLDEN):
+        pytest.fail("missing golden " + GOLDEN)
+    g = np.load(GOLDEN)
+    _, xg = mesh.element_frames(g["nodes"], g["tris"])
+    ref = []
+    for b in range(len(g["row_ptr"]) - 1):
+        ref.append((tuple(g["rows"][g["row_ptr"][b]:g["row_ptr"][b + 1]]),
+                    tuple(g["cols"][g["col_ptr"][b]:g["col_ptr"][b + 1]])))
+    got = [(tuple(r), tuple(c)) for r, c, _ in ohm.leaf_blocks(xg, 16, int(g["mini_leaf"]))]
+    assert got == ref
+    lr = [lowrank for _, _, lowrank in ohm.leaf_blocks(xg, 16, int(g["mini_leaf"]))]
+    assert np.array_equal(np.array(lr), g["aca"])
