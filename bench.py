@@ -323,6 +323,8 @@ def bench_ours(args):
             out["batched"] = bench_batched(torch, dev, args, peaks)
         if not args.no_hmat:
             out["hmatrix"] = bench_hmatrix(torch, dev, args, peaks)
+        if not args.no_serve:
+            out["serving"] = bench_serving(torch, dev, args)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
     line = {"metric": METRIC, "value": value, "unit": "GF entries/s", "n_gpus": world, "steps": args.steps,
@@ -536,6 +538,92 @@ def bench_hmatrix(torch, dev, args, peaks):
     return res
 
 
+SERVE_MESHES = [(2000, 50, 20), (4000, 80, 25), (6000, 100, 30), (8000, 100, 40), (12000, 150, 40),
+                (20000, 200, 50), (30000, 250, 60), (40000, 250, 80)]
+
+
+def bench_serving(torch, dev, args):
+    """Config: serving loop.  8 meshes, N = 2k..40k (0.5 km cells, planar and
+    rough alternating; dense BF16x6 operator for N <= 20k, H-matrix above),
+    requests by a seeded Poisson process (4/s), per-request friction draw and
+    simulated span U(1, 20) years, 16 slots per mesh, HBM budget 150 GB."""
+    from pyquake3d_gb300 import gf, mesh
+    from pyquake3d_gb300.ensemble import Ensemble
+    from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
+    from pyquake3d_gb300.serving import YEAR, Request, Server, poisson_arrivals
+    sizes = SERVE_MESHES if not args.quick else [(n // 8, nx // 4, nz // 2) for n, nx, nz in SERVE_MESHES[:4]]
+    meshes = []
+    for k, (_, nx, nz) in enumerate(sizes):
+        f = mesh.planar_fault if k % 2 == 0 else mesh.rough_fault
+        L, W = nx * 0.5, nz * 0.5
+        nodes, tris = f(L, W, nx, nz)
+        meshes.append({"nodes": nodes, "tris": tris, "L": L * 1e3, "W": W * 1e3})
+    srv = Server(meshes, mu=MU, lam=LAM, cs=3464.0, slots=16, budget_bytes=150e9, graph_iters=8,
+                 max_steps=args.serve_max_steps, device=dev)
+    nreq = args.serve_requests
+    arr = poisson_arrivals(nreq, 4.0, seed=0)
+    rng = np.random.default_rng(0)
+    reqs = []
+    for i in range(nreq):
+        m = int(rng.integers(len(meshes)))
+        _, xg = mesh.element_frames(meshes[m]["nodes"], meshes[m]["tris"])
+        tab = mesh.ensemble_tables(xg, meshes[m]["L"], meshes[m]["W"], B=1, seed=int(rng.integers(1 << 30)),
+                                   v_nuc=1e-3)[0]
+        reqs.append(Request(rid=i, mesh=m, arrival_s=float(arr[i]), table=tab,
+                            span_s=float(rng.uniform(1.0, 20.0)) * YEAR))
+    res = srv.run(reqs, time_limit_s=args.serve_time_limit)
+    res["meshes"] = [{"N": int(sp["tris"].shape[0]), "kind": srv.kind[m], "operator_GB": srv.op_bytes[m] / 1e9,
+                      "build_s": srv.build_s[m]} for m, sp in enumerate(meshes)]
+    # one-at-a-time on the plain path: plain FP64 stepping (dense) or a single
+    # H-matrix run, measured per mesh; each request's duration = its own stage
+    # count / that rate; FIFO one request at a time from its arrival
+    plain = {}
+    for m, sp in enumerate(meshes):
+        tab = reqs[0].table if reqs[0].mesh == m else None
+        _, xg = mesh.element_frames(sp["nodes"], sp["tris"])
+        tab = mesh.ensemble_tables(xg, sp["L"], sp["W"], B=1, seed=1, v_nuc=1e-3)[0]
+        if srv.kind[m] == "dense_bf16x6":
+            K64, _ = gf.assemble_dense(sp["nodes"], sp["tris"], MU, LAM, fp32_copy=False, device=dev)
+            sim = DenseDeviceSim(K64, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+            sim.step(2)
+            c0 = sim.read_ctrl()
+            t0 = time.perf_counter()
+            sim.step(40)
+            dt = time.perf_counter() - t0
+            c1 = sim.read_ctrl()
+            plain[m] = 7.0 * (c1.attempts - c0.attempts) / dt
+            del K64, sim
+            torch.cuda.empty_cache()
+        else:
+            ens = Ensemble(srv.ens[m].hmat, tab[None], mu=MU, Cs=3464.0, precision="hmat")
+            ens.iterate(2)
+            torch.cuda.synchronize()
+            s0 = ens.stages()
+            t0 = time.perf_counter()
+            ens.iterate(60)
+            torch.cuda.synchronize()
+            plain[m] = (ens.stages() - s0) / (time.perf_counter() - t0)
+    t_free = 0.0
+    ttr = []
+    for r in sorted(reqs, key=lambda r: r.arrival_s):
+        if r.done_s is None:
+            continue
+        start = max(r.arrival_s, t_free)
+        t_free = start + 7.0 * r.attempts / plain[r.mesh]
+        ttr.append(t_free - r.arrival_s)
+    res["sequential_plain_estimate"] = {"p50_time_to_result_s": float(np.percentile(ttr, 50)) if ttr else None,
+                                        "p99_time_to_result_s": float(np.percentile(ttr, 99)) if ttr else None,
+                                        "plain_rk_stages_per_s": {str(srv.meshes[m]["tris"].shape[0]): v
+                                                                  for m, v in plain.items()},
+                                        "method": "per-mesh plain rates measured here x each served request's "
+                                                  "own attempt count, FIFO one at a time"}
+    res["workload"] = ("serving: %d requests, Poisson 4/s seed 0, 8 meshes N=%s, 16 slots/mesh, 150 GB budget, "
+                       "span U(1,20) yr, max %d steps/run" % (nreq, [m[0] for m in sizes], args.serve_max_steps))
+    del srv
+    torch.cuda.empty_cache()
+    return res
+
+
 def L_ws_bytes(N):
     from pyquake3d_gb300 import _lib
     return _lib.load().pq3d_gf_workspace_bytes(N)
@@ -553,6 +641,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-hmat", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-max-steps", type=int, default=3000)
+    ap.add_argument("--serve-time-limit", type=float, default=90.0)
     ap.add_argument("--hmat-stages", type=int, default=500)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--nsplit", type=int, default=None)

@@ -349,7 +349,8 @@ extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, si
                                    workspace_bytes, st);
         if (rc) return rc;
     } else {
-        rc = pq3d_hmat_apply((const pq3d_hmat *)S.K, (const double *)S.vop, Bp, S.rates, workspace, workspace_bytes,
+        // the H-matrix product needs no padding runs: the first B rows only
+        rc = pq3d_hmat_apply((const pq3d_hmat *)S.K, (const double *)S.vop, S.B, S.rates, workspace, workspace_bytes,
                              stream);
         if (rc) return rc;
     }

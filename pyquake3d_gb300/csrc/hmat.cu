@@ -16,10 +16,15 @@
 //     (no host round trip per row), the first pivot row is row 0, ties in
 //     argmax go to the smallest index -- deterministic;
 //   * a block that has not converged at its rank cap is stored dense;
-//   * factors and dense blocks are stored in FP32; products use compensated
-//     FP32 arithmetic with the right-hand side split into FP32 hi + lo pieces,
-//     accumulated per output row in a fixed block order (no atomics, the same
-//     result for a run alone or in a batch).
+//   * factors and dense blocks are stored in FP32; products use FP32 FMAs
+//     with the right-hand side split into FP32 hi + lo pieces (2 FMAs per
+//     entry, per-lane FP32 sums, FP64 across lanes), accumulated per output
+//     row in a fixed block order (no atomics, the same result for a run alone
+//     or in a batch).  The ACA tolerance (1e-4) dominates this rounding by
+//     orders of magnitude.
+//   * several right-hand sides run in one launch (one grid row per run); each
+//     run streams the blocks itself (a single-pass multi-run product would
+//     need a GEMM-style tiling of the near field; not done).
 // Index space: elements are renumbered so that every cluster is a contiguous
 // range (perm[p] = element at position p); a block is a pair of ranges.
 #include <math.h>
@@ -235,19 +240,14 @@ __global__ void pack_factors_kernel(const double *__restrict__ UV, const int64_t
 // ---------------------------------------------------------------------------
 // product  Y[r][3e + c] = sum over blocks of the H-matrix rows of element e
 
-struct Acc2 {
+struct Acc2 {   // FP32 partial sum of one lane
     float s, c;
 };
 
 __device__ __forceinline__ void acc2_add(Acc2 &a, float k, float vh, float vl)
 {
-    const float p = __fmul_rn(k, vh);
-    const float e = __fmaf_rn(k, vh, -p);
-    const float t = __fadd_rn(a.s, p);
-    const float bp = __fsub_rn(t, a.s);
-    const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    a.s = t;
-    a.c = __fmaf_rn(k, vl, __fadd_rn(a.c, __fadd_rn(err, e)));
+    a.s = fmaf(k, vh, a.s);
+    a.c = fmaf(k, vl, a.c);
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -257,7 +257,7 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// X (FP64, [Bp][2N], element order) -> Xs ([Bp][2N] pairs of float hi/lo, permuted order)
+// X (FP64, [B][2N], element order) -> Xs ([B][2N] float (hi, lo) pairs, permuted order)
 __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t *__restrict__ perm, int64_t N, int B,
                                      float2 *__restrict__ Xs)
 {
@@ -270,7 +270,9 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
     Xs[(int64_t)r * 2 * N + i] = make_float2(h, (float)(x - (double)h));
 }
 
-// T[t_off[b] + l*B + r] = V_b[l] . x_r[cols of b]; one warp per (block, rank row)
+// T[(t_off[b] + l) * B + r] = V_b[l] . x_r[cols of b]; one warp per (block,
+// rank row).  Runs are the fastest-varying part of the block index, so the B
+// CTAs that read the same factor rows run together and share them in L2.
 __global__ void lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off,
                                  const int64_t *__restrict__ blk, const int32_t *__restrict__ rank,
                                  const int32_t *__restrict__ lr_ids, const int64_t *__restrict__ lr_row0, int nlr_rows,
@@ -278,7 +280,8 @@ __global__ void lowrank_T_kernel(const float *__restrict__ data, const int64_t *
                                  const int64_t *__restrict__ t_off)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int r = (int)(blockIdx.x % (unsigned)B);
+    const int64_t w = ((blockIdx.x / (unsigned)B) * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (w >= nlr_rows) return;
     // locate (block, l): lr_row0 = [count, prefix sums of the ranks of the
     // low-rank blocks (count + 1 values)]; find the last block starting <= w
@@ -295,22 +298,20 @@ __global__ void lowrank_T_kernel(const float *__restrict__ data, const int64_t *
     const int Nc = 2 * (int)(blk[4 * b + 3] - c0);
     const int M = 3 * (int)(blk[4 * b + 1] - blk[4 * b]);
     const float *v = data + off[b] + (int64_t)M * k + (int64_t)l * Nc;
-    for (int r = 0; r < B; ++r) {
-        const float2 *x = Xs + (int64_t)r * 2 * N + 2 * c0;
-        Acc2 a{0.f, 0.f};
-        for (int col = lane; col < Nc; col += 32) {
-            const float2 xv = x[col];
-            acc2_add(a, v[col], xv.x, xv.y);
-        }
-        const double s = warp_sum((double)a.s + (double)a.c);
-        if (lane == 0) T[(t_off[b] + l) * (int64_t)B + r] = s;
+    const float2 *x = Xs + (int64_t)r * 2 * N + 2 * c0;
+    Acc2 a{0.f, 0.f};
+    for (int col = lane; col < Nc; col += 32) {
+        const float2 xv = x[col];
+        acc2_add(a, __ldg(v + col), xv.x, xv.y);
     }
+    const double sum = warp_sum((double)a.s + (double)a.c);
+    if (lane == 0) T[(t_off[b] + l) * (int64_t)B + r] = sum;
 }
 
-// One CTA per leaf row cluster.  The descriptors of the leaf's blocks are
-// staged in shared memory; every warp owns groups of 4 consecutive output rows
-// (of one run) and adds the blocks of the leaf in list order, 4 independent
-// row streams per block.
+// One CTA per (leaf row cluster, run), the run fastest in the block index so
+// that the B CTAs of one leaf read its blocks together (L2 reuse).  The descriptors
+// of the leaf's blocks are staged in shared memory; every warp owns groups of
+// 4 consecutive output rows and adds the blocks of the leaf in list order.
 struct BlkDesc {
     int64_t off, c0, row0;   // storage offset (floats), first column element, first local row of this leaf
     int64_t t0;              // first rank row in T
@@ -318,6 +319,7 @@ struct BlkDesc {
 };
 
 constexpr int kMaxLeafBlocks = 160;
+constexpr int kRowsPerWarp = 4;
 
 __global__ void __launch_bounds__(kThreads)
 leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
@@ -326,13 +328,16 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
                  const double *__restrict__ T, const int64_t *__restrict__ t_off, int64_t N, int B,
                  double *__restrict__ Y)
 {
+    constexpr int R = kRowsPerWarp;
     __shared__ BlkDesc desc[kMaxLeafBlocks];
-    const int L = blockIdx.x;
+    const int L = (int)(blockIdx.x / (unsigned)B), r = (int)(blockIdx.x % (unsigned)B);
     const int64_t p0 = leaf[2 * L], p1 = leaf[2 * L + 1];
     const int rows = 3 * (int)(p1 - p0);
     const int64_t q0 = leaf_ptr[L], q1 = leaf_ptr[L + 1];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = kThreads / 32;
-    const int ngroups = (rows + 3) / 4;
+    const int ngroups = (rows + R - 1) / R;
+    const float2 *xr = Xs + (int64_t)r * 2 * N;
+    double *Yr = Y + (int64_t)r * 3 * N;
     for (int64_t qs = q0; qs < q1; qs += kMaxLeafBlocks) {
         const int nq = (int)min((int64_t)kMaxLeafBlocks, q1 - qs);
         __syncthreads();
@@ -349,22 +354,22 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
             desc[i] = d;
         }
         __syncthreads();
-        for (int gg = w; gg < ngroups * B; gg += nw) {
-            const int r = gg / ngroups, g = gg % ngroups;
-            const int lr0 = 4 * g;
-            const int nr = min(4, rows - lr0);
-            Acc2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (int g = w; g < ngroups; g += nw) {
+            const int lr0 = R * g;
+            const int nr = min(R, rows - lr0);
+            Acc2 a[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) a[i] = Acc2{0.f, 0.f};
             // carry the partial sums of the previous descriptor chunk
             if (qs > q0 && lane == 0) {
                 for (int i = 0; i < nr; ++i) {
                     const int lr = lr0 + i;
-                    const double prev = Y[(int64_t)r * 3 * N + 3 * perm[p0 + lr / 3] + lr % 3];
+                    const double prev = Yr[3 * perm[p0 + lr / 3] + lr % 3];
                     const float h = (float)prev;
                     a[i].s = h;
                     a[i].c = (float)(prev - (double)h);
                 }
             }
-            const float2 *xr = Xs + (int64_t)r * 2 * N;
             for (int q = 0; q < nq; ++q) {
                 const BlkDesc d = desc[q];
                 if (d.k < 0) {
@@ -373,7 +378,7 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
                     for (int col = lane; col < d.Nc; col += 32) {
                         const float2 xv = x[col];
 #pragma unroll
-                        for (int i = 0; i < 4; ++i)
+                        for (int i = 0; i < R; ++i)
                             if (i < nr) acc2_add(a[i], __ldg(base + (int64_t)i * d.Nc + col), xv.x, xv.y);
                     }
                 } else if (d.k > 0) {
@@ -383,17 +388,17 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
                         const double tv = tb[(int64_t)l * B + r];
                         const float th = (float)tv, tl = (float)(tv - (double)th);
 #pragma unroll
-                        for (int i = 0; i < 4; ++i)
+                        for (int i = 0; i < R; ++i)
                             if (i < nr) acc2_add(a[i], __ldg(base + (int64_t)i * d.k + l), th, tl);
                     }
                 }
             }
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < R; ++i) {
                 const double sum = warp_sum((double)a[i].s + (double)a[i].c);
                 if (lane == 0 && i < nr) {
                     const int lr = lr0 + i;
-                    Y[(int64_t)r * 3 * N + 3 * perm[p0 + lr / 3] + lr % 3] = sum;
+                    Yr[3 * perm[p0 + lr / 3] + lr % 3] = sum;
                 }
             }
         }
@@ -470,13 +475,19 @@ extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, doubl
     double *T = (double *)((char *)workspace + (size_t)B * 2 * N * sizeof(float2));
     dim3 g1((unsigned)((2 * N + 255) / 256), (unsigned)B);
     permute_split_kernel<<<g1, 256, 0, st>>>(X, H->perm, N, B, Xs);
+    // all runs in one launch, run fastest in the block index; a run's result
+    // does not depend on B
     if (H->t_rows > 0) {
-        const int64_t threads = H->t_rows * 32;
-        lowrank_T_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-            H->data, H->off, H->blk, H->rank, H->lr_ids, H->lr_row0, (int)H->t_rows, Xs, N, B, T, H->t_off);
+        const int64_t nT = (H->t_rows * 32 + 255) / 256 * B;
+        PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
+        const unsigned gT = (unsigned)nT;
+        lowrank_T_kernel<<<gT, 256, 0, st>>>(H->data, H->off, H->blk, H->rank, H->lr_ids, H->lr_row0, (int)H->t_rows,
+                                             Xs, N, B, T, H->t_off);
     }
-    leaf_rows_kernel<<<H->nleaves, kThreads, 0, st>>>(H->data, H->off, H->blk, H->rank, H->leaf, H->leaf_ptr,
-                                                      H->leaf_blocks, H->perm, Xs, T, H->t_off, N, B, Y);
+    PQ3D_REQUIRE((int64_t)H->nleaves * B < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many leaves x runs");
+    const unsigned gL = (unsigned)(H->nleaves * B);
+    leaf_rows_kernel<<<gL, kThreads, 0, st>>>(H->data, H->off, H->blk, H->rank, H->leaf, H->leaf_ptr, H->leaf_blocks,
+                                              H->perm, Xs, T, H->t_off, N, B, Y);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

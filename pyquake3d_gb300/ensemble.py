@@ -138,6 +138,33 @@ class Ensemble:
         b = self.ctrl_t.cpu().numpy().tobytes()
         return list((_lib.RunCtrl * self.B).from_buffer_copy(b))
 
+    def load_run(self, slot, table, *, dttry=1e-3, t_end=float("inf"), max_steps=2 ** 62, V0=1e-6, Vpl=1e-9):
+        """Put a new run into `slot` (stream-ordered on the current stream):
+        its initial state from the per-cell table, a fresh control record, and
+        the operator right-hand side of every slot recomputed."""
+        init = initial_state(np.asarray(table, dtype=np.float64), V0, Vpl)
+        dev = self.device
+        for k in STATE + ("a", "b", "dc", "f0", "shear_loading", "normal_loading"):
+            self.t[k][slot].copy_(torch.as_tensor(init[k], dtype=torch.float64), non_blocking=False)
+        r0 = torch.as_tensor(init["rake0"], dtype=torch.float64, device=dev)
+        self.t["cos_rake0"][slot].copy_(torch.cos(r0))
+        self.t["sin_rake0"][slot].copy_(torch.sin(r0))
+        c = _lib.RunCtrl()
+        c.h, c.time, c.t_end, c.max_steps, c.active = float(dttry), 0.0, float(t_end), int(max_steps), 1
+        sz = ctypes.sizeof(_lib.RunCtrl)
+        self.ctrl_t[slot * sz:(slot + 1) * sz].copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
+        self.prepare()
+
+    def deactivate(self, slot):
+        c = _lib.RunCtrl()
+        sz = ctypes.sizeof(_lib.RunCtrl)
+        self.ctrl_t[slot * sz:(slot + 1) * sz].copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
+
+    def state_bytes(self):
+        """Device bytes of the per-run state, rates, right-hand side and control."""
+        return sum(t.numel() * t.element_size() for t in self.t.values()) + self.vop.numel() * self.vop.element_size() \
+            + self.ctrl_t.numel() + self.ws.numel()
+
     def prepare(self):
         L = _lib.load()
         _lib.check(L.pq3d_batch_prepare(ctypes.byref(self.S), torch.cuda.current_stream(self.device).cuda_stream))
