@@ -229,6 +229,15 @@ typedef struct pq3d_batch_sim {
     double V0, Vpl, eta;
     int32_t fix_Tn;
     int32_t pad1;
+    /* Receiver-row shard (FP64 and FP32 only): this process steps cells
+     * [cell0, cell0 + N) of an N_total-cell mesh.  The per-cell arrays, cand
+     * and rates hold the shard's N cells; K holds the shard's 3N rows of the
+     * (3 N_total) x (2 N_total) operator; vop holds v' of ALL N_total cells
+     * ([Bp][2 N_total]), of which the shard writes its own slice and the
+     * caller exchanges the rest (allgather) after each iteration.  N_total = 0
+     * means an unsharded simulation (N_total = N, cell0 = 0). */
+    int64_t N_total;
+    int64_t cell0;
 } pq3d_batch_sim;
 
 /* Packed operator of the tensor-core product: the FP64 operator split into
@@ -257,6 +266,16 @@ int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream);
  * the per-run accept/reject decision and the state update of the accepted runs
  * (masked acceptance; rejected runs retry with their smaller dt next time). */
 int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream);
+
+/* The same iteration in two halves, for row-sharded simulations: _begin does
+ * the operator product and the attempt and leaves each run's max error norms
+ * of this shard in ctrl[r].err1_bits / err2_bits (FP64 bit patterns, order-
+ * preserving as signed 64-bit integers); the caller reduces them with MAX over
+ * the shards and writes the result back; _end decides and updates.  The
+ * decision only reads the control record, so every shard takes the same one.
+ * pq3d_batch_iterate = _begin + _end. */
+int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream);
+int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream);
 
 /* ---------------- device: H-matrix ---------------- */
 

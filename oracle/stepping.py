@@ -120,7 +120,9 @@ class DenseStepper:
         return dstatedt, self.dsigmadt / 1e6, dtau1dt / 1e6, dtau2dt / 1e6
 
     # src/QDsim_gpu.py:1266-1397
-    def rk_attempt(self, h):
+    def rk_attempt_raw(self, h):
+        """The seven stages; returns the 5th-order candidate and the two raw
+        error maxima (before the 1e-10 floor) over this object's cells."""
         d = self.derivative
         Tno, Tt1o, Tt2o, state = self.Tno, self.Tt1o, self.Tt2o, self.state
         s1, n1, t1, u1 = d(Tno, Tt1o, Tt2o, state)
@@ -146,16 +148,26 @@ class DenseStepper:
         Tt1o_8 = Tt1o + h * (B81 * t1 + B83 * t3 + B84 * t4 + B85 * t5 + B86 * t6 + B87 * t7)
         Tt2o_8 = Tt2o + h * (B81 * u1 + B83 * u3 + B84 * u4 + B85 * u5 + B86 * u6 + B87 * u7)
         state_8 = state + h * (B81 * s1 + B83 * s3 + B84 * s4 + B85 * s5 + B86 * s6 + B87 * s7)
-        err1 = np.max(np.abs(np.abs(state_8 - state_y) / state_8)) + 1e-10
+        m1 = np.max(np.abs(np.abs(state_8 - state_y) / state_8))
         e2a = np.max(np.abs(np.abs(Tt1o_8 - Tt1o_y) / Tt1o_8))
         e2b = np.max(np.abs(np.abs(Tt2o_8 - Tt2o_y) / Tt2o_8))
         e2c = np.max(np.abs(np.abs(Tno_8 - Tno_y) / Tno_8))
-        err2 = max(e2a, e2b, e2c) + 1e-10
+        return Tno_y, Tt1o_y, Tt2o_y, state_y, m1, max(e2a, e2b, e2c)
+
+    @staticmethod
+    def step_control(h, m1, m2):
+        """(c1, c2, hn1, hn2) from the raw error maxima."""
+        err1 = m1 + 1e-10
+        err2 = m2 + 1e-10
         c1 = err1 / REL_TOL
         c2 = err2 / REL_TOL
         hn1 = h * 0.9 * (REL_TOL / err1) ** 0.2
         hn2 = h * 0.9 * (REL_TOL / err2) ** 0.2
-        return Tno_y, Tt1o_y, Tt2o_y, state_y, c1, c2, hn1, hn2
+        return c1, c2, hn1, hn2
+
+    def rk_attempt(self, h):
+        Tno_y, Tt1o_y, Tt2o_y, state_y, m1, m2 = self.rk_attempt_raw(h)
+        return (Tno_y, Tt1o_y, Tt2o_y, state_y) + self.step_control(h, m1, m2)
 
     def traction_rates(self):
         """K.(V - Vpl) once per accepted step (src/QDsim_gpu.py:1033-1042)."""
@@ -190,6 +202,11 @@ class DenseStepper:
             h = max(0.5 * h, dtnext)
             if h < 1.e-15 or nrjct > 20:
                 raise StepFailure("dt is too small")
+        self.accept(h, Tno_y, Tt1o_y, Tt2o_y, state_y)
+        return h, dtnext, nrjct + 1
+
+    def accept(self, h, Tno_y, Tt1o_y, Tt2o_y, state_y):
+        """State update of an accepted step (src/QDsim_gpu.py:1077-1113)."""
         self.time = self.time + h
         self.Tno, self.Tt1o, self.Tt2o, self.state = Tno_y, Tt1o_y, Tt2o_y, state_y
         self.Tt = np.sqrt(self.Tt1o * self.Tt1o + self.Tt2o * self.Tt2o)
@@ -203,7 +220,6 @@ class DenseStepper:
         self.slip2 = self.slip2 + self.slipv2 * h
         self.slip = np.sqrt(self.slip1 * self.slip1 + self.slip2 * self.slip2)
         self.fric = self.Tt / (self.Tno - self.P * 1e-6)
-        return h, dtnext, nrjct + 1
 
     def run(self, nsteps, dt0=1e-3):
         """The reference main loop (src/main_gpu.py:112-118): dttry = dtnext.

@@ -64,7 +64,7 @@ class BatchSim(ctypes.Structure):
                                  "rates")] + \
         [("nsplit", ctypes.c_int32), ("pad0", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
          ("ctrl", c_void_p), ("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", ctypes.c_int32),
-         ("pad1", ctypes.c_int32)]
+         ("pad1", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64)]
 
 
 class HMat(ctypes.Structure):
@@ -121,6 +121,8 @@ _SIGS = {
     "pq3d_hmat_apply": (c_int, [ctypes.POINTER(HMat), c_void_p, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "pq3d_batch_prepare": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
     "pq3d_batch_iterate": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
+    "pq3d_batch_iterate_begin": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
+    "pq3d_batch_iterate_end": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
 }
 
 _lib = None

@@ -28,6 +28,9 @@ using namespace ::pq3d::rk;
 // padded run count of the operator right-hand side and of the rate partials
 __host__ __device__ inline int padded_runs(int B) { return (B + 15) / 16 * 16; }
 
+// cells of the whole mesh (a row shard holds N of them, from cell0)
+__host__ __device__ inline int64_t total_cells(const pq3d_batch_sim &S) { return S.N_total > 0 ? S.N_total : S.N; }
+
 // ---------------------------------------------------------------------------
 // operator right-hand side v'_r = V_r - Vpl (cos, sin)(rake0), interleaved
 
@@ -47,18 +50,17 @@ __device__ __forceinline__ void split3(double x, __nv_bfloat16 &p0, __nv_bfloat1
     p2 = __double2bfloat16(r2);
 }
 
+// i: local cell of the shard; v' goes to the mesh-wide position cell0 + i
 __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_t i, double v1, double v2)
 {
-    const int64_t N = S.N;
     const int Bp = padded_runs(S.B);
-    const int64_t o = (int64_t)r * 2 * N + 2 * i;
-    (void)Bp;
+    const int64_t o = (int64_t)r * 2 * total_cells(S) + 2 * (S.cell0 + i);
     if (S.precision == PQ3D_BATCH_FP64 || S.precision == PQ3D_BATCH_HMAT) {
         reinterpret_cast<double2 *>((double *)S.vop + o)[0] = make_double2(v1, v2);
     } else if (S.precision == PQ3D_BATCH_FP32) {
         reinterpret_cast<float2 *>((float *)S.vop + o)[0] = make_float2((float)v1, (float)v2);
     } else {
-        // packed images [k block][piece][Bp x 32] (see gemm_tc.cuh)
+        // packed images [k block][piece][Bp x 32] (see gemm_tc.cuh); never sharded
         const int64_t k = 2 * i;
         const int64_t img = (int64_t)Bp * tc::kBlockK;
         __nv_bfloat16 *P = (__nv_bfloat16 *)S.vop + (k / tc::kBlockK) * tc::kPieces * img +
@@ -86,19 +88,20 @@ __global__ void prepare_kernel(pq3d_batch_sim S)
 // ---------------------------------------------------------------------------
 // CUDA-core operator products (FP64 and FP32 arms)
 
-// FP64: one warp per (run, receiver): rows 3i..3i+2 against v'_r.
+// FP64: one warp per (run, receiver): rows 3i..3i+2 (N receivers of the
+// shard) against v'_r (Nt sources of the mesh).
 __global__ void __launch_bounds__(256) gemm_f64_kernel(const double2 *__restrict__ K, const double2 *__restrict__ V,
-                                                       int64_t N, int B, double *__restrict__ out)
+                                                       int64_t N, int64_t Nt, int B, double *__restrict__ out)
 {
     const int lane = threadIdx.x & 31;
     const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (w >= N * B) return;
     const int r = (int)(w / N);
     const int64_t i = w - (int64_t)r * N;
-    const double2 *v = V + (int64_t)r * N;
-    const double2 *r0 = K + 3 * i * N, *r1 = r0 + N, *r2 = r1 + N;
+    const double2 *v = V + (int64_t)r * Nt;
+    const double2 *r0 = K + 3 * i * Nt, *r1 = r0 + Nt, *r2 = r1 + Nt;
     double a0 = 0, a1 = 0, a2 = 0;
-    for (int64_t j = lane; j < N; j += 32) {
+    for (int64_t j = lane; j < Nt; j += 32) {
         const double2 x = v[j], k0 = r0[j], k1 = r1[j], k2 = r2[j];
         a0 = fma(k0.x, x.x, fma(k0.y, x.y, a0));
         a1 = fma(k1.x, x.x, fma(k1.y, x.y, a1));
@@ -116,17 +119,18 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const double2 *__restrict
 }
 
 // FP32: CTA tile 128 rows x 64 runs, K chunks of 32 through shared memory,
-// FP32 FMAs with the partial sums moved to FP64 every 256 columns.
+// FP32 FMAs with the partial sums moved to FP64 every 256 columns.  N
+// receivers of the shard (3N rows), Nt sources of the mesh (2 Nt columns).
 constexpr int kF32Rows = 128, kF32Runs = 64, kF32K = 32;
 
 __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__ K, const float *__restrict__ V,
-                                                       int64_t N, int Bp, double *__restrict__ out)
+                                                       int64_t N, int64_t Nt, int Bp, double *__restrict__ out)
 {
     __shared__ float As[kF32K][kF32Rows + 4];
     __shared__ float Vs[kF32K][kF32Runs + 4];
     const int t = threadIdx.x;
     const int tr = t & 31, tn = t >> 5;       // rows tr*4..+3, runs tn*8..+7
-    const int64_t M = 3 * N, Kd = 2 * N;
+    const int64_t M = 3 * N, Kd = 2 * Nt;
     const int64_t m0 = (int64_t)blockIdx.x * kF32Rows;
     const int n0 = blockIdx.y * kF32Runs;
     float acc[4][8];
@@ -299,6 +303,13 @@ static int check_sim(const pq3d_batch_sim *S)
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
     PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
     if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
+    PQ3D_REQUIRE(S->N_total >= 0 && S->cell0 >= 0, "pq3d_batch: bad shard");
+    if (S->N_total > 0 && (S->N_total != S->N || S->cell0 != 0)) {
+        PQ3D_REQUIRE(S->precision == PQ3D_BATCH_FP64 || S->precision == PQ3D_BATCH_FP32,
+                     "pq3d_batch: row shards need the FP64 or FP32 product");
+        PQ3D_REQUIRE(S->cell0 + S->N <= S->N_total, "pq3d_batch: shard [%lld, %lld) outside the mesh of %lld cells",
+                     (long long)S->cell0, (long long)(S->cell0 + S->N), (long long)S->N_total);
+    }
     return PQ3D_OK;
 }
 
@@ -323,12 +334,13 @@ extern "C" int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream)
     if (rc) return rc;
     const int Bp = padded_runs(sim->B);
     dim3 grid((unsigned)((sim->N + 255) / 256), (unsigned)Bp);
-    prepare_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*sim);
+    prepare_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*sim);   // the shard's own slice of v'
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }
 
-extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream)
+extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes,
+                                        void *stream)
 {
     clear_error();
     int rc = check_sim(sim);
@@ -336,14 +348,15 @@ extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, si
     cudaStream_t st = (cudaStream_t)stream;
     const pq3d_batch_sim &S = *sim;
     const int Bp = padded_runs(S.B);
+    const int64_t Nt = total_cells(S);
     // 1. operator product
     if (S.precision == PQ3D_BATCH_FP64) {
         const int64_t warps = S.N * Bp;
         gemm_f64_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
-            (const double2 *)S.K, (const double2 *)S.vop, S.N, Bp, S.rates);
+            (const double2 *)S.K, (const double2 *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_FP32) {
         dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
-        gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Bp, S.rates);
+        gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
         rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.rates, workspace,
                                    workspace_bytes, st);
@@ -355,13 +368,31 @@ extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, si
         if (rc) return rc;
     }
     PQ3D_CUDA_TRY(cudaGetLastError());
-    // 2-4. attempt, decide, update
+    // 2. attempt (FP64 arm: the reference right-hand side; mixed arms: rhs_mixed)
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
-    // FP64 arm: the reference right-hand side; mixed arms: rhs_mixed
     if (S.precision == PQ3D_BATCH_FP64) attempt_kernel<false><<<grid, 256, 0, st>>>(S);
     else attempt_kernel<true><<<grid, 256, 0, st>>>(S);
+    PQ3D_CUDA_TRY(cudaGetLastError());
+    return PQ3D_OK;
+}
+
+extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
+{
+    clear_error();
+    int rc = check_sim(sim);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const pq3d_batch_sim &S = *sim;
+    // 3-4. decide, update
     decide_kernel<<<(S.B + 127) / 128, 128, 0, st>>>(S.ctrl, S.B);
+    dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
     update_kernel<<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
+}
+
+extern "C" int pq3d_batch_iterate(const pq3d_batch_sim *sim, void *workspace, size_t workspace_bytes, void *stream)
+{
+    const int rc = pq3d_batch_iterate_begin(sim, workspace, workspace_bytes, stream);
+    return rc ? rc : pq3d_batch_iterate_end(sim, stream);
 }

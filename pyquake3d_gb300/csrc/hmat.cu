@@ -18,8 +18,8 @@
 //   * a block that has not converged at its rank cap is stored dense;
 //   * factors and dense blocks are stored in FP32; products use FP32 FMAs
 //     with the right-hand side split into FP32 hi + lo pieces (2 FMAs per
-//     entry, per-lane FP32 sums, FP64 across lanes), accumulated per output
-//     row in a fixed block order (no atomics, the same result for a run alone
+//     entry, FP32 sums over one block segment, FP64 beyond), accumulated per
+//     output row in a fixed order (no atomics, the same result for a run alone
 //     or in a batch).  The ACA tolerance (1e-4) dominates this rounding by
 //     orders of magnitude.
 //   * several right-hand sides run in one launch (one grid row per run); each
@@ -196,8 +196,15 @@ aca_kernel(const double *__restrict__ src, const double *__restrict__ recv, int6
     }
 }
 
-// Dense blocks: block b stored row-major (3m x 2n) FP32 at d_off[b]; d_off[b]
-// must be a multiple of 2 floats (float2 stores; the host pads to 4).
+// Storage of block b at data + off[b] (FP32, column-major so that the lanes
+// of a warp read consecutive rows of one column):
+//   dense:    D[col * M + row]                 (M = 3m rows, Nc = 2n columns)
+//   low rank: U[l * M + row] for l < k, then V[l * Nc + col]   (K_b ~ U V)
+// Rows are receiver x traction component (3p + c), columns source x slip
+// direction (2q + s) in the block's local (renumbered) order.
+
+// Dense blocks, one CTA per block; consecutive threads take consecutive
+// receivers of one source.
 __global__ void __launch_bounds__(kThreads)
 dense_blocks_kernel(const double *__restrict__ src, const double *__restrict__ recv, int64_t N,
                     const int64_t *__restrict__ perm, const int64_t *__restrict__ blk, const int32_t *__restrict__ ids,
@@ -207,17 +214,23 @@ dense_blocks_kernel(const double *__restrict__ src, const double *__restrict__ r
     const int b = ids[blockIdx.x];
     const int64_t r0 = blk[4 * b], r1 = blk[4 * b + 1], c0 = blk[4 * b + 2], c1 = blk[4 * b + 3];
     const int m = (int)(r1 - r0), n = (int)(c1 - c0);
+    const int64_t M = 3 * (int64_t)m;
     float *Db = D + d_off[b];
     for (int64_t e = threadIdx.x; e < (int64_t)m * n; e += kThreads) {
-        const int p = (int)(e / n), q = (int)(e % n);
+        const int q = (int)(e / m), p = (int)(e % m);
         double ts[3], td[3];
         pair_tractions(GSrc{src + perm[c0 + q], N}, recv + kRecvStride * perm[r0 + p], nu, kf, two_mu, lam, ts, td);
-        for (int c = 0; c < 3; ++c)
-            *reinterpret_cast<float2 *>(Db + (int64_t)(3 * p + c) * 2 * n + 2 * q) = make_float2((float)ts[c], (float)td[c]);
+        float *col_s = Db + (int64_t)(2 * q) * M + 3 * p;
+        float *col_d = col_s + M;
+        for (int c = 0; c < 3; ++c) {
+            col_s[c] = (float)ts[c];
+            col_d[c] = (float)td[c];
+        }
     }
 }
 
-// Copy the converged ACA factors to FP32 storage: U_b (3m x k) row-major, V_b (k x 2n).
+// Copy the converged ACA factors (FP64, U as k rows of length M, then V as k
+// rows of length Nc) to FP32 storage in the same order.
 __global__ void pack_factors_kernel(const double *__restrict__ UV, const int64_t *__restrict__ uv_off,
                                     const int64_t *__restrict__ blk, const int32_t *__restrict__ kcap,
                                     const int32_t *__restrict__ rank, const int32_t *__restrict__ ids,
@@ -230,24 +243,25 @@ __global__ void pack_factors_kernel(const double *__restrict__ UV, const int64_t
     const double *V = U + (int64_t)K * M;
     float *Uo = out + out_off[b];
     float *Vo = Uo + (int64_t)M * k;
-    for (int64_t e = threadIdx.x; e < (int64_t)M * k; e += blockDim.x) {
-        const int row = (int)(e / k), l = (int)(e % k);
-        Uo[e] = (float)U[(int64_t)l * M + row];
-    }
+    for (int64_t e = threadIdx.x; e < (int64_t)M * k; e += blockDim.x) Uo[e] = (float)U[e];
     for (int64_t e = threadIdx.x; e < (int64_t)k * Nc; e += blockDim.x) Vo[e] = (float)V[e];
 }
 
 // ---------------------------------------------------------------------------
 // product  Y[r][3e + c] = sum over blocks of the H-matrix rows of element e
+//
+// Arithmetic: FP32 entries times the right-hand side split into FP32 hi + lo
+// (2 FMAs per entry), FP32 partial sums over at most one block segment (or
+// 1024 columns), then FP64.
 
 struct Acc2 {   // FP32 partial sum of one lane
     float s, c;
 };
 
-__device__ __forceinline__ void acc2_add(Acc2 &a, float k, float vh, float vl)
+__device__ __forceinline__ void acc2_add(Acc2 &a, float k, float2 x)
 {
-    a.s = fmaf(k, vh, a.s);
-    a.c = fmaf(k, vl, a.c);
+    a.s = fmaf(k, x.x, a.s);
+    a.c = fmaf(k, x.y, a.c);
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -255,6 +269,12 @@ __device__ __forceinline__ double warp_sum(double v)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+__device__ __forceinline__ float2 split2(double x)
+{
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
 }
 
 // X (FP64, [B][2N], element order) -> Xs ([B][2N] float (hi, lo) pairs, permuted order)
@@ -265,19 +285,18 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
     const int r = blockIdx.y;
     if (i >= 2 * N || r >= B) return;
     const int64_t q = i >> 1;
-    const double x = X[(int64_t)r * 2 * N + 2 * perm[q] + (i & 1)];
-    const float h = (float)x;
-    Xs[(int64_t)r * 2 * N + i] = make_float2(h, (float)(x - (double)h));
+    Xs[(int64_t)r * 2 * N + i] = split2(X[(int64_t)r * 2 * N + 2 * perm[q] + (i & 1)]);
 }
 
-// T[(t_off[b] + l) * B + r] = V_b[l] . x_r[cols of b]; one warp per (block,
-// rank row).  Runs are the fastest-varying part of the block index, so the B
-// CTAs that read the same factor rows run together and share them in L2.
-__global__ void lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off,
-                                 const int64_t *__restrict__ blk, const int32_t *__restrict__ rank,
-                                 const int32_t *__restrict__ lr_ids, const int64_t *__restrict__ lr_row0, int nlr_rows,
-                                 const float2 *__restrict__ Xs, int64_t N, int B, double *__restrict__ T,
-                                 const int64_t *__restrict__ t_off)
+// T[(t_off[b] + l) * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo)
+// pair; one warp per (block, rank row).  Runs are the fastest-varying part of
+// the block index, so the B CTAs that read the same factor rows run together
+// and share them in L2.
+__global__ void __launch_bounds__(256)
+lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
+                 const int32_t *__restrict__ rank, const int32_t *__restrict__ lr_ids,
+                 const int64_t *__restrict__ lr_row0, int nlr_rows, const float2 *__restrict__ Xs, int64_t N, int B,
+                 float2 *__restrict__ T, const int64_t *__restrict__ t_off)
 {
     const int lane = threadIdx.x & 31;
     const int r = (int)(blockIdx.x % (unsigned)B);
@@ -299,108 +318,176 @@ __global__ void lowrank_T_kernel(const float *__restrict__ data, const int64_t *
     const int M = 3 * (int)(blk[4 * b + 1] - blk[4 * b]);
     const float *v = data + off[b] + (int64_t)M * k + (int64_t)l * Nc;
     const float2 *x = Xs + (int64_t)r * 2 * N + 2 * c0;
-    Acc2 a{0.f, 0.f};
-    for (int col = lane; col < Nc; col += 32) {
-        const float2 xv = x[col];
-        acc2_add(a, __ldg(v + col), xv.x, xv.y);
+    double sum = 0.0;
+    for (int c0k = 0; c0k < Nc; c0k += 1024) {
+        const int cend = min(Nc, c0k + 1024);
+        Acc2 a0{0.f, 0.f}, a1{0.f, 0.f};
+        int col = c0k + lane;
+        for (; col + 96 < cend; col += 128) {
+            const float k0 = __ldg(v + col), k1 = __ldg(v + col + 32), k2 = __ldg(v + col + 64),
+                        k3 = __ldg(v + col + 96);
+            const float2 x0 = x[col], x1 = x[col + 32], x2 = x[col + 64], x3 = x[col + 96];
+            acc2_add(a0, k0, x0);
+            acc2_add(a1, k1, x1);
+            acc2_add(a0, k2, x2);
+            acc2_add(a1, k3, x3);
+        }
+        for (; col < cend; col += 32) acc2_add(a0, __ldg(v + col), x[col]);
+        sum += ((double)a0.s + (double)a1.s) + ((double)a0.c + (double)a1.c);
     }
-    const double sum = warp_sum((double)a.s + (double)a.c);
-    if (lane == 0) T[(t_off[b] + l) * (int64_t)B + r] = sum;
+    sum = warp_sum(sum);
+    if (lane == 0) T[(t_off[b] + l) * (int64_t)B + r] = split2(sum);
 }
 
 // One CTA per (leaf row cluster, run), the run fastest in the block index so
-// that the B CTAs of one leaf read its blocks together (L2 reuse).  The descriptors
-// of the leaf's blocks are staged in shared memory; every warp owns groups of
-// 4 consecutive output rows and adds the blocks of the leaf in list order.
+// that the B CTAs of one leaf read its blocks together (L2 reuse).
+//
+// Lane j of every warp owns rows j, j + 32, ... of the leaf (up to kPassRows
+// rows per pass).  The work of the leaf -- the columns of its dense blocks and
+// the rank columns of its low-rank blocks, in list order -- is cut into 8
+// contiguous ranges, one per warp; a warp walks its range column by column
+// (a coalesced 128-byte load per 32 rows, the column's x value broadcast),
+// and the 8 per-warp partial sums of a row are added in warp order through
+// shared memory.  The result does not depend on B or on timing.
 struct BlkDesc {
-    int64_t off, c0, row0;   // storage offset (floats), first column element, first local row of this leaf
-    int64_t t0;              // first rank row in T
-    int32_t Nc, k;           // columns (2n), rank (-1 dense)
+    int64_t off;    // storage offset (floats)
+    int64_t x0;     // dense: first column in Xs (2 c0); low rank: first T row (t_off)
+    int32_t row0;   // first local row of this leaf in the block
+    int32_t M;      // rows of the block (column stride)
+    int32_t w;      // work columns: Nc (dense) or k (low rank)
+    int32_t dense;
 };
 
 constexpr int kMaxLeafBlocks = 160;
-constexpr int kRowsPerWarp = 4;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxR = 6;
+constexpr int kPassRows = 32 * kMaxR;
+
+template <int R>
+__device__ __forceinline__ void leaf_segment(const float *__restrict__ col0, int64_t M, const float2 *__restrict__ xp,
+                                             int64_t xs, int ca, int cb, bool last_ok, double (&acc)[kMaxR])
+{
+    Acc2 a[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) a[i] = Acc2{0.f, 0.f};
+    int c = ca;
+    for (; c + 1 < cb; c += 2) {
+        const float *p0 = col0 + (int64_t)c * M, *p1 = p0 + M;
+        const float2 x0 = xp[(int64_t)c * xs], x1 = xp[(int64_t)(c + 1) * xs];
+        float k0[R], k1[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const bool ok = (i < R - 1) || last_ok;
+            k0[i] = ok ? __ldg(p0 + 32 * i) : 0.f;
+            k1[i] = ok ? __ldg(p1 + 32 * i) : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            acc2_add(a[i], k0[i], x0);
+            acc2_add(a[i], k1[i], x1);
+        }
+    }
+    if (c < cb) {
+        const float *p0 = col0 + (int64_t)c * M;
+        const float2 x0 = xp[(int64_t)c * xs];
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const bool ok = (i < R - 1) || last_ok;
+            acc2_add(a[i], ok ? __ldg(p0 + 32 * i) : 0.f, x0);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] += (double)a[i].s + (double)a[i].c;
+}
+
+template <int R>
+__device__ void leaf_range(const BlkDesc *desc, const int *wpre, int nq, int64_t lo, int64_t hi, int pr0, int prow,
+                           const float *__restrict__ data, const float2 *__restrict__ xr,
+                           const float2 *__restrict__ T, int B, int r, double (&acc)[kMaxR])
+{
+    const int lane = threadIdx.x & 31;
+    const bool last_ok = lane + 32 * (R - 1) < prow;
+    // first descriptor whose range ends after lo
+    int q = 0;
+    while (q < nq && wpre[q + 1] <= lo) ++q;
+    for (; q < nq && wpre[q] < hi; ++q) {
+        const BlkDesc d = desc[q];
+        const int ca = (int)max((int64_t)0, lo - wpre[q]);
+        const int cb = (int)min((int64_t)d.w, hi - wpre[q]);
+        if (ca >= cb) continue;
+        const float *col0 = data + d.off + d.row0 + pr0 + lane;
+        if (d.dense) leaf_segment<R>(col0, d.M, xr + d.x0, 1, ca, cb, last_ok, acc);
+        else leaf_segment<R>(col0, d.M, T + d.x0 * B + r, B, ca, cb, last_ok, acc);
+    }
+}
 
 __global__ void __launch_bounds__(kThreads)
 leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
                  const int32_t *__restrict__ rank, const int64_t *__restrict__ leaf, const int64_t *__restrict__ leaf_ptr,
                  const int32_t *__restrict__ leaf_blocks, const int64_t *__restrict__ perm, const float2 *__restrict__ Xs,
-                 const double *__restrict__ T, const int64_t *__restrict__ t_off, int64_t N, int B,
+                 const float2 *__restrict__ T, const int64_t *__restrict__ t_off, int64_t N, int B,
                  double *__restrict__ Y)
 {
-    constexpr int R = kRowsPerWarp;
     __shared__ BlkDesc desc[kMaxLeafBlocks];
+    __shared__ int wpre[kMaxLeafBlocks + 1];
+    __shared__ double red[kWarps][kPassRows];
     const int L = (int)(blockIdx.x / (unsigned)B), r = (int)(blockIdx.x % (unsigned)B);
     const int64_t p0 = leaf[2 * L], p1 = leaf[2 * L + 1];
     const int rows = 3 * (int)(p1 - p0);
     const int64_t q0 = leaf_ptr[L], q1 = leaf_ptr[L + 1];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = kThreads / 32;
-    const int ngroups = (rows + R - 1) / R;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const float2 *xr = Xs + (int64_t)r * 2 * N;
     double *Yr = Y + (int64_t)r * 3 * N;
-    for (int64_t qs = q0; qs < q1; qs += kMaxLeafBlocks) {
-        const int nq = (int)min((int64_t)kMaxLeafBlocks, q1 - qs);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nq; i += kThreads) {
-            const int bb = leaf_blocks[qs + i];
-            const int64_t r0 = blk[4 * bb], c0 = blk[4 * bb + 2];
-            BlkDesc d;
-            d.off = off[bb];
-            d.c0 = c0;
-            d.row0 = 3 * (p0 - r0);
-            d.t0 = t_off[bb];
-            d.Nc = 2 * (int)(blk[4 * bb + 3] - c0);
-            d.k = rank[bb];
-            desc[i] = d;
+    for (int pr0 = 0; pr0 < rows; pr0 += kPassRows) {
+        const int prow = min(kPassRows, rows - pr0);
+        const int R = (prow + 31) / 32;
+        double acc[kMaxR];
+#pragma unroll
+        for (int i = 0; i < kMaxR; ++i) acc[i] = 0.0;
+        for (int64_t qs = q0; qs < q1; qs += kMaxLeafBlocks) {
+            const int nq = (int)min((int64_t)kMaxLeafBlocks, q1 - qs);
+            __syncthreads();
+            for (int i = threadIdx.x; i < nq; i += kThreads) {
+                const int bb = leaf_blocks[qs + i];
+                const int64_t r0 = blk[4 * bb], c0 = blk[4 * bb + 2];
+                const int k = rank[bb];
+                BlkDesc d;
+                d.off = off[bb];
+                d.row0 = 3 * (int)(p0 - r0);
+                d.M = 3 * (int)(blk[4 * bb + 1] - r0);
+                d.dense = k < 0;
+                d.w = k < 0 ? 2 * (int)(blk[4 * bb + 3] - c0) : k;
+                d.x0 = k < 0 ? 2 * c0 : t_off[bb];
+                desc[i] = d;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int s = 0;
+                for (int i = 0; i < nq; ++i) { wpre[i] = s; s += desc[i].w; }
+                wpre[nq] = s;
+            }
+            __syncthreads();
+            const int64_t W = wpre[nq];
+            const int64_t lo = W * wid / kWarps, hi = W * (wid + 1) / kWarps;
+            switch (R) {
+                case 1: leaf_range<1>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+                case 2: leaf_range<2>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+                case 3: leaf_range<3>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+                case 4: leaf_range<4>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+                case 5: leaf_range<5>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+                default: leaf_range<6>(desc, wpre, nq, lo, hi, pr0, prow, data, xr, T, B, r, acc); break;
+            }
         }
         __syncthreads();
-        for (int g = w; g < ngroups; g += nw) {
-            const int lr0 = R * g;
-            const int nr = min(R, rows - lr0);
-            Acc2 a[R];
 #pragma unroll
-            for (int i = 0; i < R; ++i) a[i] = Acc2{0.f, 0.f};
-            // carry the partial sums of the previous descriptor chunk
-            if (qs > q0 && lane == 0) {
-                for (int i = 0; i < nr; ++i) {
-                    const int lr = lr0 + i;
-                    const double prev = Yr[3 * perm[p0 + lr / 3] + lr % 3];
-                    const float h = (float)prev;
-                    a[i].s = h;
-                    a[i].c = (float)(prev - (double)h);
-                }
-            }
-            for (int q = 0; q < nq; ++q) {
-                const BlkDesc d = desc[q];
-                if (d.k < 0) {
-                    const float *base = data + d.off + (d.row0 + lr0) * d.Nc;
-                    const float2 *x = xr + 2 * d.c0;
-                    for (int col = lane; col < d.Nc; col += 32) {
-                        const float2 xv = x[col];
+        for (int i = 0; i < kMaxR; ++i) red[wid][lane + 32 * i] = acc[i];
+        __syncthreads();
+        for (int lr = threadIdx.x; lr < prow; lr += kThreads) {
+            double s = 0.0;
 #pragma unroll
-                        for (int i = 0; i < R; ++i)
-                            if (i < nr) acc2_add(a[i], __ldg(base + (int64_t)i * d.Nc + col), xv.x, xv.y);
-                    }
-                } else if (d.k > 0) {
-                    const float *base = data + d.off + (d.row0 + lr0) * d.k;
-                    const double *tb = T + d.t0 * (int64_t)B;
-                    for (int l = lane; l < d.k; l += 32) {
-                        const double tv = tb[(int64_t)l * B + r];
-                        const float th = (float)tv, tl = (float)(tv - (double)th);
-#pragma unroll
-                        for (int i = 0; i < R; ++i)
-                            if (i < nr) acc2_add(a[i], __ldg(base + (int64_t)i * d.k + l), th, tl);
-                    }
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < R; ++i) {
-                const double sum = warp_sum((double)a[i].s + (double)a[i].c);
-                if (lane == 0 && i < nr) {
-                    const int lr = lr0 + i;
-                    Yr[3 * perm[p0 + lr / 3] + lr % 3] = sum;
-                }
-            }
+            for (int w = 0; w < kWarps; ++w) s += red[w][lr];
+            const int row = pr0 + lr;
+            Yr[3 * perm[p0 + row / 3] + row % 3] = s;
         }
     }
 }
@@ -440,7 +527,7 @@ extern "C" int pq3d_hmat_dense_blocks(const double *tables, int64_t N, const int
 {
     clear_error();
     PQ3D_REQUIRE(tables && perm && blk && ids && D && d_off && N > 0, "pq3d_hmat_dense_blocks: bad arguments");
-    PQ3D_REQUIRE(((uintptr_t)D & 7u) == 0, "pq3d_hmat_dense_blocks: D must be 8-byte aligned");
+    PQ3D_REQUIRE(((uintptr_t)D & 3u) == 0, "pq3d_hmat_dense_blocks: D must be 4-byte aligned");
     if (nids <= 0) return PQ3D_OK;
     const double nu = poisson_(mu, lambda_);
     const double kf = 1.0 / (8.0 * kPi * (1.0 - nu));
@@ -467,12 +554,12 @@ extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, doubl
     clear_error();
     PQ3D_REQUIRE(H && X && Y && workspace && B >= 1, "pq3d_hmat_apply: bad arguments");
     const int64_t N = H->N;
-    const size_t need = (size_t)B * 2 * N * sizeof(float2) + (size_t)H->t_rows * B * sizeof(double);
+    const size_t need = (size_t)B * 2 * N * sizeof(float2) + (size_t)H->t_rows * B * sizeof(float2);
     PQ3D_REQUIRE(workspace_bytes >= need && aligned16(workspace), "pq3d_hmat_apply: workspace too small (%zu < %zu)",
                  workspace_bytes, need);
     cudaStream_t st = (cudaStream_t)stream;
     float2 *Xs = (float2 *)workspace;
-    double *T = (double *)((char *)workspace + (size_t)B * 2 * N * sizeof(float2));
+    float2 *T = (float2 *)((char *)workspace + (size_t)B * 2 * N * sizeof(float2));
     dim3 g1((unsigned)((2 * N + 255) / 256), (unsigned)B);
     permute_split_kernel<<<g1, 256, 0, st>>>(X, H->perm, N, B, Xs);
     // all runs in one launch, run fastest in the block index; a run's result
@@ -495,5 +582,5 @@ extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, doubl
 extern "C" size_t pq3d_hmat_workspace_bytes(const pq3d_hmat *H, int B)
 {
     if (!H || B < 1) return 0;
-    return (size_t)B * 2 * H->N * sizeof(float2) + (size_t)H->t_rows * B * sizeof(double);
+    return (size_t)B * 2 * H->N * sizeof(float2) + (size_t)H->t_rows * B * sizeof(float2);
 }

@@ -65,16 +65,24 @@ class Ensemble:
 
     K: the (3N, 2N) operator -- FP64 for "fp64", FP32 for "fp32", a
     :class:`PackedOperator` for "bf16x6".  tables: (B, N, 10) per-cell tables
-    (``read_parameter`` layout)."""
+    (``read_parameter`` layout).
+
+    shard=(cell0, N_total): this object steps cells [cell0, cell0 + N) of an
+    N_total-cell mesh ("fp64" / "fp32"); K is then the shard's (3N, 2 N_total)
+    row block and :mod:`pyquake3d_gb300.shards` drives the iterations."""
 
     def __init__(self, K, tables, *, mu, Cs, V0=1e-6, Vpl=1e-9, precision="bf16x6", nsplit=None, dttry=1e-3,
-                 max_steps=2 ** 62, t_end=float("inf"), fix_Tn=False):
+                 max_steps=2 ** 62, t_end=float("inf"), fix_Tn=False, shard=None):
         L = _lib.load()
         self.precision = precision
         prec = PRECISIONS[precision]
         tables = np.asarray(tables, dtype=np.float64)
         B, N = tables.shape[0], tables.shape[1]
         self.B, self.N, self.Bp = B, N, padded_runs(B)
+        self.cell0, self.N_total = (0, N) if shard is None else (int(shard[0]), int(shard[1]))
+        if shard is not None and precision not in ("fp64", "fp32"):
+            raise ValueError("row shards need the fp64 or fp32 product")
+        Nt = self.N_total
         dev = K.device
         self.device = dev
         if precision == "hmat":
@@ -88,7 +96,7 @@ class Ensemble:
             if nsplit is None:
                 nsplit = auto_nsplit(N, dev)
         else:
-            assert isinstance(K, torch.Tensor) and K.shape == (3 * N, 2 * N) and K.is_contiguous()
+            assert isinstance(K, torch.Tensor) and K.shape == (3 * N, 2 * Nt) and K.is_contiguous()
             assert K.dtype == (torch.float64 if precision == "fp64" else torch.float32)
             kop = K
             nsplit = 1
@@ -104,9 +112,9 @@ class Ensemble:
         self.t["rates"] = torch.zeros(self.nsplit * self.Bp * 3 * N, **f64)
         self.t["cand"] = torch.zeros(B * N * 4, **f64)
         if precision in ("fp64", "hmat"):
-            self.vop = torch.zeros(self.Bp * 2 * N, **f64)
+            self.vop = torch.zeros(self.Bp * 2 * Nt, **f64)
         elif precision == "fp32":
-            self.vop = torch.zeros(self.Bp * 2 * N, dtype=torch.float32, device=dev)
+            self.vop = torch.zeros(self.Bp * 2 * Nt, dtype=torch.float32, device=dev)
         else:
             self.vop = torch.zeros(L.pq3d_batch_rhs_bytes(N, B), dtype=torch.uint8, device=dev)
         self.ctrl_t = torch.zeros(B * ctypes.sizeof(_lib.RunCtrl), dtype=torch.uint8, device=dev)
@@ -117,6 +125,8 @@ class Ensemble:
         S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
+        if shard is not None:
+            S.N_total, S.cell0 = Nt, self.cell0
         self.S = S
         self.ws = torch.zeros(max(256, L.pq3d_batch_workspace_bytes(ctypes.byref(S))), dtype=torch.uint8, device=dev)
         self.set_ctrl(dttry=dttry, max_steps=max_steps, t_end=t_end)
@@ -190,6 +200,34 @@ class Ensemble:
     def replay(self, times=1):
         for _ in range(times):
             self.graph.replay()
+
+    # -- row-shard phases (driven by pyquake3d_gb300.shards) ----------------
+    def begin(self):
+        """Operator product of this shard's rows and one attempt (the runs'
+        error norms of this shard are left in the control records)."""
+        L = _lib.load()
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _lib.check(L.pq3d_batch_iterate_begin(ctypes.byref(self.S), self.ws.data_ptr(), self.ws.numel(), st))
+
+    def end(self):
+        """Accept/reject decision and update of this shard's cells."""
+        L = _lib.load()
+        _lib.check(L.pq3d_batch_iterate_end(ctypes.byref(self.S), torch.cuda.current_stream(self.device).cuda_stream))
+
+    _ERR = _lib.RunCtrl.err1_bits.offset // 8
+
+    def error_words(self):
+        """(B, 2) int64: the FP64 bit patterns of the runs' error norms (err1,
+        err2); MAX over shards of these words is MAX of the norms."""
+        return self.ctrl_t.view(torch.int64).view(self.B, -1)[:, self._ERR:self._ERR + 2].clone()
+
+    def set_error_words(self, w):
+        self.ctrl_t.view(torch.int64).view(self.B, -1)[:, self._ERR:self._ERR + 2].copy_(w)
+
+    def vprime(self):
+        """(Bp, 2 N_total) view of v' of all cells (this shard writes columns
+        [2 cell0, 2 (cell0 + N)))."""
+        return self.vop.view(self.Bp, 2 * self.N_total)
 
     def error_word(self):
         return int(self.ws[:4].view(torch.int32).item())

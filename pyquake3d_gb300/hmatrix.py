@@ -170,9 +170,9 @@ class HMatrix:
         ok = lowrank & (status == 0)
         rank[~ok] = -1
         self.aca_status = status
-        # storage offsets: dense 3m x 2n, low rank k (3m + 2n) floats, each block
-        # padded to a multiple of 4 floats so that every block starts 16-byte
-        # aligned (the dense-block kernel stores float2 pairs)
+        # storage offsets: dense 3m x 2n (column-major), low rank k (3m + 2n)
+        # floats (U column-major, then V row-major), each block padded to a
+        # multiple of 4 floats so that every block starts 16-byte aligned
         size = np.where(rank >= 0, rank.astype(np.int64) * (3 * m + 2 * n), 6 * m * n)
         size = (size + 3) // 4 * 4
         off = np.concatenate([[0], np.cumsum(size)[:-1]]).astype(np.int64)

@@ -1,0 +1,62 @@
+"""Receiver-row shards of the batched stepper on one GPU (the in-process
+exchange; the collectives over torch.distributed are covered by the gloo
+tests): three shards give the same bits as the unsharded ensemble, for the
+FP64 and the FP32 product, on the golden mesh and on a 2,000-cell mesh."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pyquake3d_gb300 import gf, mesh
+from pyquake3d_gb300.ensemble import Ensemble
+from pyquake3d_gb300.shards import InProcessExchange, iterate_sharded, make_shards
+from tests.test_batch_gpu import CS, _tables
+
+pytestmark = pytest.mark.gpu
+MU = 32038120320.0
+
+
+def _check(K, tabs, precision, world, iters):
+    whole = Ensemble(K, tabs, mu=MU, Cs=CS, precision=precision)
+    whole.iterate(iters)
+    shards = make_shards(K, tabs, world, mu=MU, Cs=CS, precision=precision)
+    iterate_sharded(shards, InProcessExchange(), iters)
+    torch.cuda.synchronize()
+    cw = whole.read_ctrl()
+    for s in shards:
+        cs = s.read_ctrl()
+        for r in range(tabs.shape[0]):
+            assert (cs[r].steps, cs[r].attempts, cs[r].time, cs[r].h) == \
+                   (cw[r].steps, cw[r].attempts, cw[r].time, cw[r].h), r
+    assert cw[0].steps > 10
+    for k in ("slip1", "slip2", "Tt1o", "state", "slipv"):
+        got = torch.cat([s.t[k] for s in shards], dim=1)
+        assert torch.equal(got, whole.t[k]), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_shards_bitwise_golden(cuda, golden, precision):
+    d = golden("dense_small.npz")
+    g = golden("traj_small.npz")
+    K = torch.as_tensor(gf.join_ops({k: d["planar_" + k] for k in oracle.OPS}), device=cuda).contiguous()
+    if precision == "fp32":
+        K = K.float().contiguous()
+    _check(K, _tables(g, 3), precision, 3, 150)
+
+
+def test_shards_bitwise_n2000(cuda):
+    nodes, tris = mesh.planar_fault(40.0, 25.0, 40, 25)
+    N = tris.shape[0]
+    K, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
+    _, xg = mesh.element_frames(nodes, tris)
+    tabs = mesh.ensemble_tables(xg, 40e3, 25e3, 2, seed=1, v_nuc=1e-3)
+    assert tabs.shape == (2, N, 10)
+    _check(K, tabs, "fp64", 4, 80)
+
+
+def test_shard_rejects_tensor_core_product(cuda, golden):
+    d = golden("dense_small.npz")
+    K = torch.as_tensor(gf.join_ops({k: d["planar_" + k] for k in oracle.OPS}), device=cuda).contiguous()
+    tabs = _tables(golden("traj_small.npz"), 1)
+    with pytest.raises(ValueError):
+        Ensemble(K[:96].contiguous(), tabs[:, :32], mu=MU, Cs=CS, precision="bf16x6", shard=(0, 64))
