@@ -297,7 +297,7 @@ typedef struct pq3d_hmat {
     const int64_t *off;           /* [nblocks]: offset (floats) of the block in data */
     const float *data;            /* dense block (3m x 2n) or U (3m x k) then V (k x 2n), row-major FP32 */
     const int32_t *lr_ids;        /* low-rank block ids, in order */
-    const int64_t *lr_row0;       /* [count, prefix sums of their ranks (count + 1 values)] */
+    const int32_t *t_blk;         /* [t_rows] block of each rank row (low-rank blocks in lr_ids order) */
     const int64_t *t_off;         /* [nblocks]: first rank row of the block in the product workspace */
     const int64_t *leaf;          /* [nleaves][2]: permuted ranges of the leaf row clusters */
     const int64_t *leaf_ptr;      /* [nleaves + 1] */

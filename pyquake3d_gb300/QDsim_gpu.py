@@ -19,7 +19,8 @@ exits (dt < 1e-15 or > 20 rejected attempts, src/QDsim_gpu.py:983-985) this
 raises :class:`StepError`.
 
 Supported inputs: per-cell parameter files (``InputHetoparamter: True``,
-layout of src/QDsim_gpu.py:714-770), full-space, no dilatancy.  Other
+layout of src/QDsim_gpu.py:714-770), full- or half-space (``Half space``),
+no dilatancy.  Other
 parameter-file options raise ``NotImplementedError`` rather than silently
 computing something else.
 """
@@ -194,8 +195,6 @@ class QDsim:
             raise NotImplementedError("only per-cell parameter files (InputHetoparamter: True) are supported")
         if self.Ifdila:
             raise NotImplementedError("pore-pressure dilatancy coupling is not supported")
-        if self.halfspace_jud:
-            raise NotImplementedError("half-space Green's functions are not available in this build")
         self.device = torch.device(device) if device is not None else torch.device("cuda")
         self.operator_dtype = operator_dtype
         self.read_parameter(P["Inputparamter file"])
@@ -220,7 +219,8 @@ class QDsim:
             K64 = torch.as_tensor(gf.join_ops(ops), device=self.device)
             K32 = K64.float()
         else:
-            K64, K32 = gf.assemble_dense(self.nodelst, self.elelst, self.mu, self.lambda_, device=self.device)
+            K64, K32 = gf.assemble_dense(self.nodelst, self.elelst, self.mu, self.lambda_,
+                                         halfspace=self.halfspace_jud, device=self.device)
             if d is not None and self.Para0.get("save Corefunc", "False") == "True":
                 os.makedirs(d, exist_ok=True)
                 for k, v in gf.split_ops(K64).items():

@@ -9,6 +9,9 @@
 //   points_one_source / point_many_sources
 //                                     the two host-pointer entry points of the
 //                                     reference TDstressFS_C.so
+//   half-space (jud_halfspace / halfspace != 0): per-source image record and
+//   free-surface side table (setup_hs), the pair evaluated by
+//   pair_tractions_hs / point_strain_hs (hs_device.cuh)
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -19,6 +22,7 @@
 
 #include "common.cuh"
 #include "gf_device.cuh"
+#include "hs_device.cuh"
 
 namespace pq3d {
 namespace gf {
@@ -35,6 +39,7 @@ struct ValSrc {   // fields held in a small array
 };
 
 struct SrcVal { double f[kSrcStride]; };
+struct FscVal { double f[kFscStride]; };
 
 __global__ void setup_sources_kernel(const double *__restrict__ nodes, const int64_t *__restrict__ tris, int64_t N,
                                      double *__restrict__ src)
@@ -58,6 +63,22 @@ __global__ void setup_receivers_kernel(const double *__restrict__ nodes, const i
     const double *C = nodes + 3 * (tris[3 * i + 2] - 1);
     double a[3] = {A[0], A[1], A[2]}, b[3] = {B[0], B[1], B[2]}, c[3] = {C[0], C[1], C[2]};
     setup_receiver(a, b, c, recv + kRecvStride * i);
+}
+
+// Half-space records of source j: the mirrored triangle's source record
+// (img, stride N) and the free-surface side table (fsc, stride N).
+__global__ void setup_hs_kernel(const double *__restrict__ nodes, const int64_t *__restrict__ tris, int64_t N,
+                                double *__restrict__ img, double *__restrict__ fsc)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const double *P1 = nodes + 3 * (tris[3 * j] - 1);
+    const double *P2 = nodes + 3 * (tris[3 * j + 1] - 1);
+    const double *P3 = nodes + 3 * (tris[3 * j + 2] - 1);
+    double a[3] = {P1[0], P1[1], P1[2]}, b[3] = {P2[0], P2[1], P2[2]}, c[3] = {P3[0], P3[1], P3[2]};
+    double am[3] = {a[0], a[1], -a[2]}, bm[3] = {b[0], b[1], -b[2]}, cm[3] = {c[0], c[1], -c[2]};
+    setup_source(am, bm, cm, img + j, (int)N);
+    setup_fsc(a, b, c, fsc + j, (int)N);
 }
 
 constexpr int kTJ = 128;   // sources per block (one per thread)
@@ -94,6 +115,80 @@ assemble_dense_kernel(const double *__restrict__ src, const double *__restrict__
                 *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2((float)ts[c], (float)td[c]);
         }
     }
+}
+
+// Half-space variant: main record in shared memory, image record and side
+// table read from their structure-of-arrays tables (coalesced over sources).
+template <bool kWrite32>
+__global__ void __launch_bounds__(kTJ)
+assemble_dense_hs_kernel(const double *__restrict__ src, const double *__restrict__ recv,
+                         const double *__restrict__ img, const double *__restrict__ fsc, int64_t N, int64_t row0,
+                         int64_t row1, double nu, double k, double two_mu, double lam, double *__restrict__ K64,
+                         float *__restrict__ K32)
+{
+    __shared__ double s_src[F_COUNT * kTJ];
+    __shared__ double s_rcv[kTI * kRecvStride];
+    const int t = threadIdx.x;
+    const int64_t j0 = (int64_t)blockIdx.x * kTJ;
+    const int64_t i0 = row0 + (int64_t)blockIdx.y * kTI;
+    const int64_t j = j0 + t;
+    for (int f = 0; f < F_COUNT; ++f) s_src[f * kTJ + t] = (j < N) ? src[f * N + j] : 0.0;
+    const int nrec = (int)((row1 - i0) < kTI ? (row1 - i0) : kTI);
+    for (int q = t; q < nrec * kRecvStride; q += kTJ) s_rcv[q] = recv[i0 * kRecvStride + q];
+    __syncthreads();
+    if (j >= N) return;
+    const SoaSrc F{s_src + t, kTJ};
+    const SoaSrc Fi{img + j, (int)N};
+    const SoaSrc G{fsc + j, (int)N};
+    const int64_t ld = 2 * N;
+    for (int ii = 0; ii < nrec; ++ii) {
+        double ts[3], td[3];
+        pair_tractions_hs(F, Fi, G, s_rcv + ii * kRecvStride, nu, k, two_mu, lam, ts, td);
+        const int64_t r = 3 * (i0 + ii - row0);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            *reinterpret_cast<double2 *>(K64 + (r + c) * ld + 2 * j) = make_double2(ts[c], td[c]);
+            if (kWrite32)
+                *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2((float)ts[c], (float)td[c]);
+        }
+    }
+}
+
+__global__ void points_one_source_hs_kernel(SrcVal s, SrcVal si, FscVal g, const double *__restrict__ X,
+                                            const double *__restrict__ Y, const double *__restrict__ Z, int64_t n,
+                                            double bx, double by, double bz, double mu, double lam, double nu,
+                                            double k, double *__restrict__ stress, double *__restrict__ strain)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ValSrc F{s.f}, Fi{si.f}, G{g.f};
+    double e[6], sg[6];
+    point_strain_hs(F, Fi, G, X[i], Y[i], Z[i], bx, by, bz, nu, k, e);
+    hooke(e, mu, lam, sg);
+    for (int c = 0; c < 6; ++c) { stress[6 * i + c] = sg[c]; strain[6 * i + c] = e[c]; }
+}
+
+__global__ void point_many_sources_hs_kernel(double X, double Y, double Z, const double *__restrict__ P1,
+                                             const double *__restrict__ P2, const double *__restrict__ P3,
+                                             int64_t ns, double bx, double by, double bz, double mu, double lam,
+                                             double nu, double k, double *__restrict__ stress,
+                                             double *__restrict__ strain)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= ns) return;
+    double f[kSrcStride], fi[kSrcStride], g[kFscStride];
+    double a[3] = {P1[3 * j], P1[3 * j + 1], P1[3 * j + 2]};
+    double b[3] = {P2[3 * j], P2[3 * j + 1], P2[3 * j + 2]};
+    double c[3] = {P3[3 * j], P3[3 * j + 1], P3[3 * j + 2]};
+    double am[3] = {a[0], a[1], -a[2]}, bm[3] = {b[0], b[1], -b[2]}, cm[3] = {c[0], c[1], -c[2]};
+    setup_source(a, b, c, f, 1);
+    setup_source(am, bm, cm, fi, 1);
+    setup_fsc(a, b, c, g, 1);
+    const ValSrc F{f}, Fi{fi}, G{g};
+    double e[6], sg[6];
+    point_strain_hs(F, Fi, G, X, Y, Z, bx, by, bz, nu, k, e);
+    hooke(e, mu, lam, sg);
+    for (int q = 0; q < 6; ++q) { stress[6 * j + q] = sg[q]; strain[6 * j + q] = e[q]; }
 }
 
 __global__ void points_one_source_kernel(SrcVal s, const double *__restrict__ X, const double *__restrict__ Y,
@@ -173,6 +268,16 @@ static void nan_fill(double *p, size_t n)
     for (size_t i = 0; i < n; ++i) p[i] = NAN;
 }
 
+// The reference prints this and carries on (src/TDstressFS_C.cpp:1949-1953).
+static void warn_halfspace_z(const double *X, const double *Y, const double *Z, size_t n, const double *P1,
+                             const double *P2, const double *P3)
+{
+    (void)X; (void)Y;
+    bool bad = (P1 && P1[2] > 0.0) || (P2 && P2[2] > 0.0) || (P3 && P3[2] > 0.0);
+    for (size_t i = 0; i < n && !bad; ++i) bad = Z[i] > 0.0;
+    if (bad) fprintf(stdout, "Half-space solution: Z coordinates must be negative!\n");
+}
+
 static int points_one_source(const double *X, const double *Y, const double *Z, size_t n, const double *P1,
                              const double *P2, const double *P3, double Ss, double Ds, double Ts, double mu,
                              double lam, bool half, double *stress, double *strain)
@@ -180,8 +285,7 @@ static int points_one_source(const double *X, const double *Y, const double *Z, 
     clear_error();
     if (n == 0) return PQ3D_OK;
     PQ3D_REQUIRE(X && Y && Z && P1 && P2 && P3 && stress && strain, "TDstressFS_C: null pointer");
-    if (half)
-        return set_error(PQ3D_ERR_UNSUPPORTED, "TDstressFS_C: half-space solution is not available in this build");
+    if (half) warn_halfspace_z(X, Y, Z, n, P1, P2, P3);
     HostCtx *c;
     int rc = host_ctx(15 * n, &c);
     if (rc) return rc;
@@ -194,8 +298,18 @@ static int points_one_source(const double *X, const double *Y, const double *Z, 
     setup_source(a, b, cc, s.f, 1);
     const double nu = poisson(mu, lam);
     const int threads = 128;
-    points_one_source_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, c->stream>>>(
-        s, dX, dY, dZ, (int64_t)n, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
+    if (half) {
+        SrcVal si;
+        FscVal g;
+        double am[3] = {a[0], a[1], -a[2]}, bm[3] = {b[0], b[1], -b[2]}, cm[3] = {cc[0], cc[1], -cc[2]};
+        setup_source(am, bm, cm, si.f, 1);
+        setup_fsc(a, b, cc, g.f, 1);
+        points_one_source_hs_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, c->stream>>>(
+            s, si, g, dX, dY, dZ, (int64_t)n, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
+    } else {
+        points_one_source_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, c->stream>>>(
+            s, dX, dY, dZ, (int64_t)n, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
+    }
     PQ3D_CUDA_TRY(cudaGetLastError());
     PQ3D_CUDA_TRY(cudaMemcpyAsync(stress, dS, 6 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PQ3D_CUDA_TRY(cudaMemcpyAsync(strain, dE, 6 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -210,9 +324,7 @@ static int point_many_sources(double x, double y, double z, const double *P1, co
     clear_error();
     if (ns == 0) return PQ3D_OK;
     PQ3D_REQUIRE(P1 && P2 && P3 && stress && strain, "TDstressEachSourceAtReceiver_C: null pointer");
-    if (half)
-        return set_error(PQ3D_ERR_UNSUPPORTED,
-                         "TDstressEachSourceAtReceiver_C: half-space solution is not available in this build");
+    if (half) warn_halfspace_z(&x, &y, &z, 1, nullptr, nullptr, nullptr);
     HostCtx *c;
     int rc = host_ctx(21 * ns, &c);
     if (rc) return rc;
@@ -222,8 +334,12 @@ static int point_many_sources(double x, double y, double z, const double *P1, co
     PQ3D_CUDA_TRY(cudaMemcpyAsync(d3, P3, 3 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     const double nu = poisson(mu, lam);
     const int threads = 128;
-    point_many_sources_kernel<<<(unsigned)((ns + threads - 1) / threads), threads, 0, c->stream>>>(
-        x, y, z, d1, d2, d3, (int64_t)ns, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
+    if (half)
+        point_many_sources_hs_kernel<<<(unsigned)((ns + threads - 1) / threads), threads, 0, c->stream>>>(
+            x, y, z, d1, d2, d3, (int64_t)ns, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
+    else
+        point_many_sources_kernel<<<(unsigned)((ns + threads - 1) / threads), threads, 0, c->stream>>>(
+            x, y, z, d1, d2, d3, (int64_t)ns, Ts, Ss, Ds, mu, lam, nu, kfac(nu), dS, dE);
     PQ3D_CUDA_TRY(cudaGetLastError());
     PQ3D_CUDA_TRY(cudaMemcpyAsync(stress, dS, 6 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PQ3D_CUDA_TRY(cudaMemcpyAsync(strain, dE, 6 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -231,23 +347,36 @@ static int point_many_sources(double x, double y, double z, const double *P1, co
     return PQ3D_OK;
 }
 
-// Workspace: source table [kSrcStride][N] then receiver table [N][kRecvStride].
-static size_t ws_bytes(int64_t N) { return (size_t)N * (kSrcStride + kRecvStride) * sizeof(double); }
+// Workspace: source table [kSrcStride][N], receiver table [N][kRecvStride],
+// then (half-space) image table [kImgStride][N] and side table [kFscStride][N].
+static size_t ws_bytes(int64_t N, bool half)
+{
+    return (size_t)N * (kSrcStride + kRecvStride + (half ? kImgStride + kFscStride : 0)) * sizeof(double);
+}
 
 static int assemble_rows(const double *nodes, const int64_t *tris, int64_t N, int64_t row0, int64_t row1, double mu,
                          double lam, double *K64, float *K32, double *src, double *recv, bool do_setup,
-                         cudaStream_t st)
+                         cudaStream_t st, bool half = false)
 {
+    double *img = recv + (size_t)kRecvStride * N, *fsc = img + (size_t)kImgStride * N;
     if (do_setup) {
         const int th = 128;
         const unsigned nb = (unsigned)((N + th - 1) / th);
         setup_sources_kernel<<<nb, th, 0, st>>>(nodes, tris, N, src);
         setup_receivers_kernel<<<nb, th, 0, st>>>(nodes, tris, N, recv);
+        if (half) setup_hs_kernel<<<nb, th, 0, st>>>(nodes, tris, N, img, fsc);
         PQ3D_CUDA_TRY(cudaGetLastError());
     }
     const double nu = poisson(mu, lam);
     dim3 grid((unsigned)((N + kTJ - 1) / kTJ), (unsigned)((row1 - row0 + kTI - 1) / kTI));
-    if (K32)
+    if (half) {
+        if (K32)
+            assemble_dense_hs_kernel<true><<<grid, kTJ, 0, st>>>(src, recv, img, fsc, N, row0, row1, nu, kfac(nu),
+                                                                2.0 * mu, lam, K64, K32);
+        else
+            assemble_dense_hs_kernel<false><<<grid, kTJ, 0, st>>>(src, recv, img, fsc, N, row0, row1, nu, kfac(nu),
+                                                                 2.0 * mu, lam, K64, K32);
+    } else if (K32)
         assemble_dense_kernel<true><<<grid, kTJ, 0, st>>>(src, recv, N, row0, row1, nu, kfac(nu), 2.0 * mu, lam,
                                                          K64, K32);
     else
@@ -340,7 +469,8 @@ extern "C" void TDstressFS_C1(const double *X, const double *Y, const double *Z,
         }
 }
 
-extern "C" size_t pq3d_gf_workspace_bytes(int64_t N) { return N > 0 ? ws_bytes(N) : 0; }
+// the size that serves both full- and half-space assemblies
+extern "C" size_t pq3d_gf_workspace_bytes(int64_t N) { return N > 0 ? ws_bytes(N, true) : 0; }
 
 extern "C" int pq3d_assemble_dense(const double *nodes, const int64_t *tris, int64_t N, int64_t row0, int64_t row1,
                                    double mu, double lambda_, int halfspace, double *K64, float *K32, void *workspace,
@@ -351,13 +481,13 @@ extern "C" int pq3d_assemble_dense(const double *nodes, const int64_t *tris, int
     PQ3D_REQUIRE(nodes && tris && K64 && workspace, "pq3d_assemble_dense: null pointer");
     PQ3D_REQUIRE(aligned16(K64) && (!K32 || ((uintptr_t)K32 & 7u) == 0) && aligned16(workspace),
                  "pq3d_assemble_dense: K64/workspace must be 16-byte aligned, K32 8-byte aligned");
-    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N), "pq3d_assemble_dense: workspace too small (%zu < %zu)",
-                 workspace_bytes, ws_bytes(N));
-    if (halfspace) return set_error(PQ3D_ERR_UNSUPPORTED, "pq3d_assemble_dense: half-space not available");
+    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N, halfspace != 0), "pq3d_assemble_dense: workspace too small (%zu < %zu)",
+                 workspace_bytes, ws_bytes(N, halfspace != 0));
     if (row0 == row1) return PQ3D_OK;
     double *src = (double *)workspace;
     double *recv = src + (size_t)kSrcStride * N;
-    return assemble_rows(nodes, tris, N, row0, row1, mu, lambda_, K64, K32, src, recv, true, (cudaStream_t)stream);
+    return assemble_rows(nodes, tris, N, row0, row1, mu, lambda_, K64, K32, src, recv, true, (cudaStream_t)stream,
+                         halfspace != 0);
 }
 
 extern "C" int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_nodes, const int64_t *tris_host,
@@ -366,7 +496,7 @@ extern "C" int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_node
 {
     clear_error();
     PQ3D_REQUIRE(N > 0 && n_nodes > 0 && nodes_host && tris_host && K64_host, "pq3d_assemble_dense_host: bad args");
-    if (halfspace) return set_error(PQ3D_ERR_UNSUPPORTED, "pq3d_assemble_dense_host: half-space not available");
+    const bool half = halfspace != 0;
     const size_t ld = 2 * (size_t)N;
     // rows per block: about 256 MB of FP64 output per block
     int64_t rb = std::max<int64_t>(kTI, ((int64_t)(256u << 20) / (int64_t)(3 * ld * sizeof(double))) / kTI * kTI);
@@ -387,7 +517,7 @@ extern "C" int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_node
     } while (0)
     PQ3D_H_TRY(cudaMalloc(&d_nodes, 3 * n_nodes * sizeof(double)));
     PQ3D_H_TRY(cudaMalloc(&d_tris, 3 * N * sizeof(int64_t)));
-    PQ3D_H_TRY(cudaMalloc(&d_ws, ws_bytes(N)));
+    PQ3D_H_TRY(cudaMalloc(&d_ws, ws_bytes(N, half)));
     for (int b = 0; b < 2; ++b) {
         PQ3D_H_TRY(cudaMalloc(&d_K64[b], 3 * rb * ld * sizeof(double)));
         if (K32_host) PQ3D_H_TRY(cudaMalloc(&d_K32[b], 3 * rb * ld * sizeof(float)));
@@ -402,6 +532,10 @@ extern "C" int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_node
         const unsigned nb = (unsigned)((N + th - 1) / th);
         setup_sources_kernel<<<nb, th, 0, st[0]>>>(d_nodes, d_tris, N, src);
         setup_receivers_kernel<<<nb, th, 0, st[0]>>>(d_nodes, d_tris, N, recv);
+        if (half) {
+            double *img = recv + (size_t)kRecvStride * N;
+            setup_hs_kernel<<<nb, th, 0, st[0]>>>(d_nodes, d_tris, N, img, img + (size_t)kImgStride * N);
+        }
         PQ3D_H_TRY(cudaGetLastError());
         PQ3D_H_TRY(cudaEventRecord(setup_done, st[0]));
         PQ3D_H_TRY(cudaStreamWaitEvent(st[1], setup_done, 0));
@@ -409,7 +543,8 @@ extern "C" int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_node
         for (int64_t r0 = 0; r0 < N; r0 += rb, ++blk) {
             const int b = blk & 1;
             const int64_t r1 = std::min<int64_t>(N, r0 + rb);
-            rc = assemble_rows(d_nodes, d_tris, N, r0, r1, mu, lambda_, d_K64[b], d_K32[b], src, recv, false, st[b]);
+            rc = assemble_rows(d_nodes, d_tris, N, r0, r1, mu, lambda_, d_K64[b], d_K32[b], src, recv, false, st[b],
+                               half);
             if (rc) goto done;
             PQ3D_H_TRY(cudaMemcpyAsync(K64_host + 3 * r0 * ld, d_K64[b], 3 * (r1 - r0) * ld * sizeof(double),
                                        cudaMemcpyDeviceToHost, st[b]));
@@ -446,7 +581,9 @@ extern "C" int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *t
     PQ3D_REQUIRE(nodes && tris && K64, "pq3d_assemble_dense_noalloc: null pointer");
     PQ3D_REQUIRE(aligned16(K64) && (!K32 || ((uintptr_t)K32 & 7u) == 0),
                  "pq3d_assemble_dense_noalloc: K64 must be 16-byte aligned, K32 8-byte aligned");
-    if (halfspace) return set_error(PQ3D_ERR_UNSUPPORTED, "pq3d_assemble_dense_noalloc: half-space not available");
+    if (halfspace)
+        return set_error(PQ3D_ERR_UNSUPPORTED, "pq3d_assemble_dense_noalloc: the fixed scratch holds the full-space "
+                         "tables only; use pq3d_assemble_dense for the half-space");
     double *scratch = nullptr;
     int rc = noalloc_scratch(&scratch);
     if (rc) return rc;
@@ -462,7 +599,7 @@ extern "C" int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N
 {
     clear_error();
     PQ3D_REQUIRE(nodes && tris && workspace && N > 0, "pq3d_gf_setup: bad arguments");
-    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N) && aligned16(workspace), "pq3d_gf_setup: workspace too small");
+    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N, false) && aligned16(workspace), "pq3d_gf_setup: workspace too small");
     double *src = (double *)workspace;
     double *recv = src + (size_t)kSrcStride * N;
     const int th = 128;

@@ -289,29 +289,22 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
 }
 
 // T[(t_off[b] + l) * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo)
-// pair; one warp per (block, rank row).  Runs are the fastest-varying part of
-// the block index, so the B CTAs that read the same factor rows run together
-// and share them in L2.
+// pair; one warp per (rank row, run), t_blk[w] = the block of rank row w.
+// Runs are the fastest-varying part of the block index, so the B CTAs that
+// read the same factor rows run together and share them in L2.
 __global__ void __launch_bounds__(256)
 lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
-                 const int32_t *__restrict__ rank, const int32_t *__restrict__ lr_ids,
-                 const int64_t *__restrict__ lr_row0, int nlr_rows, const float2 *__restrict__ Xs, int64_t N, int B,
-                 float2 *__restrict__ T, const int64_t *__restrict__ t_off)
+                 const int32_t *__restrict__ rank, const int32_t *__restrict__ t_blk, int64_t t_rows,
+                 const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T,
+                 const int64_t *__restrict__ t_off)
 {
     const int lane = threadIdx.x & 31;
     const int r = (int)(blockIdx.x % (unsigned)B);
     const int64_t w = ((blockIdx.x / (unsigned)B) * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (w >= nlr_rows) return;
-    // locate (block, l): lr_row0 = [count, prefix sums of the ranks of the
-    // low-rank blocks (count + 1 values)]; find the last block starting <= w
-    const int nlr = (int)lr_row0[0];
-    int lo = 0, hi = nlr;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (lr_row0[1 + mid] <= w) lo = mid; else hi = mid;
-    }
-    const int b = lr_ids[lo];
-    const int l = (int)(w - lr_row0[1 + lo]);
+    if (w >= t_rows) return;
+    const int b = t_blk[w];
+    const int64_t t0 = t_off[b];
+    const int l = (int)(w - t0);
     const int k = rank[b];
     const int64_t c0 = blk[4 * b + 2];
     const int Nc = 2 * (int)(blk[4 * b + 3] - c0);
@@ -336,7 +329,7 @@ lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
         sum += ((double)a0.s + (double)a1.s) + ((double)a0.c + (double)a1.c);
     }
     sum = warp_sum(sum);
-    if (lane == 0) T[(t_off[b] + l) * (int64_t)B + r] = split2(sum);
+    if (lane == 0) T[(t0 + l) * (int64_t)B + r] = split2(sum);
 }
 
 // One CTA per (leaf row cluster, run), the run fastest in the block index so
@@ -367,27 +360,30 @@ template <int R>
 __device__ __forceinline__ void leaf_segment(const float *__restrict__ col0, int64_t M, const float2 *__restrict__ xp,
                                              int64_t xs, int ca, int cb, bool last_ok, double (&acc)[kMaxR])
 {
+    constexpr int U = 4;   // columns in flight per warp
     Acc2 a[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) a[i] = Acc2{0.f, 0.f};
     int c = ca;
-    for (; c + 1 < cb; c += 2) {
-        const float *p0 = col0 + (int64_t)c * M, *p1 = p0 + M;
-        const float2 x0 = xp[(int64_t)c * xs], x1 = xp[(int64_t)(c + 1) * xs];
-        float k0[R], k1[R];
+    for (; c + U <= cb; c += U) {
+        float k[U][R];
+        float2 x[U];
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-            const bool ok = (i < R - 1) || last_ok;
-            k0[i] = ok ? __ldg(p0 + 32 * i) : 0.f;
-            k1[i] = ok ? __ldg(p1 + 32 * i) : 0.f;
+        for (int u = 0; u < U; ++u) {
+            const float *p = col0 + (int64_t)(c + u) * M;
+            x[u] = xp[(int64_t)(c + u) * xs];
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const bool ok = (i < R - 1) || last_ok;
+                k[u][i] = ok ? __ldg(p + 32 * i) : 0.f;
+            }
         }
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-            acc2_add(a[i], k0[i], x0);
-            acc2_add(a[i], k1[i], x1);
-        }
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int i = 0; i < R; ++i) acc2_add(a[i], k[u][i], x[u]);
     }
-    if (c < cb) {
+    for (; c < cb; ++c) {
         const float *p0 = col0 + (int64_t)c * M;
         const float2 x0 = xp[(int64_t)c * xs];
 #pragma unroll
@@ -401,7 +397,7 @@ __device__ __forceinline__ void leaf_segment(const float *__restrict__ col0, int
 }
 
 template <int R>
-__device__ void leaf_range(const BlkDesc *desc, const int *wpre, int nq, int64_t lo, int64_t hi, int pr0, int prow,
+__device__ __forceinline__ void leaf_range(const BlkDesc *desc, const int *wpre, int nq, int64_t lo, int64_t hi, int pr0, int prow,
                            const float *__restrict__ data, const float2 *__restrict__ xr,
                            const float2 *__restrict__ T, int B, int r, double (&acc)[kMaxR])
 {
@@ -421,7 +417,7 @@ __device__ void leaf_range(const BlkDesc *desc, const int *wpre, int nq, int64_t
     }
 }
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
 leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
                  const int32_t *__restrict__ rank, const int64_t *__restrict__ leaf, const int64_t *__restrict__ leaf_ptr,
                  const int32_t *__restrict__ leaf_blocks, const int64_t *__restrict__ perm, const float2 *__restrict__ Xs,
@@ -567,9 +563,8 @@ extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, doubl
     if (H->t_rows > 0) {
         const int64_t nT = (H->t_rows * 32 + 255) / 256 * B;
         PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
-        const unsigned gT = (unsigned)nT;
-        lowrank_T_kernel<<<gT, 256, 0, st>>>(H->data, H->off, H->blk, H->rank, H->lr_ids, H->lr_row0, (int)H->t_rows,
-                                             Xs, N, B, T, H->t_off);
+        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, H->off, H->blk, H->rank, H->t_blk, H->t_rows, Xs, N,
+                                                       B, T, H->t_off);
     }
     PQ3D_REQUIRE((int64_t)H->nleaves * B < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many leaves x runs");
     const unsigned gL = (unsigned)(H->nleaves * B);

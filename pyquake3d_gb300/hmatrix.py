@@ -205,8 +205,9 @@ class HMatrix:
         t_off[lr_ids] = prefix[:-1]
         self.t_rows = int(prefix[-1])
         self.lr_ids = torch.as_tensor(lr_ids if len(lr_ids) else np.zeros(1, np.int32), device=dev)
-        self.lr_row0 = torch.as_tensor(np.concatenate([[len(lr_ids)], prefix]).astype(np.int64), device=dev)
         self.t_off = torch.as_tensor(t_off, device=dev)
+        t_blk = np.repeat(lr_ids, ranks) if len(lr_ids) else np.zeros(1, np.int32)
+        self.t_blk = torch.as_tensor(np.ascontiguousarray(t_blk, dtype=np.int32), device=dev)
         nl = leaves.shape[0]
         leaf_start = leaves[:, 0]
         lists = [[] for _ in range(nl)]
@@ -221,7 +222,7 @@ class HMatrix:
         self.leaf_blocks = torch.as_tensor(np.concatenate([np.asarray(x, np.int32) for x in lists]), device=dev)
         H = _lib.HMat()
         H.N, H.nblocks, H.nleaves, H.t_rows = N, nb, nl, self.t_rows
-        for k in ("perm", "blk", "rank", "off", "data", "lr_ids", "lr_row0", "t_off", "leaf", "leaf_ptr",
+        for k in ("perm", "blk", "rank", "off", "data", "lr_ids", "t_blk", "t_off", "leaf", "leaf_ptr",
                   "leaf_blocks"):
             setattr(H, k, getattr(self, k).data_ptr())
         self.H = H

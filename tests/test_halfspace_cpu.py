@@ -1,0 +1,134 @@
+"""Half-space Green's function on the CPU: the oracle against the
+reference's half-space golden vectors, the device math (host build of
+pyquake3d_gb300/csrc/hs_device.cuh) against the oracle, and both FP64
+evaluations against a 40-digit one where the formula is ill-conditioned."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.util import normwise_rel
+
+MU = 32038120320.0
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _cases(g):
+    for i in range(int(g["n_cases"])):
+        Ss, Ds, Ts, half = g[f"c{i}_b"]
+        if half:
+            yield i, g[f"c{i}_P"], g[f"c{i}_R"], Ss, Ds, Ts, g[f"c{i}_stress"], g[f"c{i}_strain"]
+
+
+def _surface_sources(g):
+    Pz = np.stack([g["each_P1"][:, 2], g["each_P2"][:, 2], g["each_P3"][:, 2]], axis=1)
+    return (Pz == 0.0).any(axis=1)
+
+
+def test_oracle_halfspace_matches_reference_cpp(golden):
+    g = golden("gf_kat.npz")
+    n = 0
+    for i, P, R, Ss, Ds, Ts, S, E in _cases(g):
+        s, e = oracle.tdstress(R[:, 0], R[:, 1], R[:, 2], P[0], P[1], P[2], Ss, Ds, Ts, MU, MU, True)
+        assert normwise_rel(S, s) < 1e-10, i
+        assert normwise_rel(E, e) < 1e-10, i
+        n += 1
+    assert n >= 9
+
+
+def test_oracle_halfspace_each_source(golden):
+    g = golden("gf_kat.npz")
+    r = g["each_recv"]
+    s, e = oracle.tdstress_each_source(r[0], r[1], r[2], g["each_P1"], g["each_P2"], g["each_P3"],
+                                       0.0, 1.0, 0.0, MU, MU, True)
+    surf = _surface_sources(g)
+    for j in range(e.shape[0]):
+        assert normwise_rel(g["each_h1_strain"][j], e[j]) < (2e-8 if surf[j] else 1e-10), j
+
+
+def test_ill_conditioned_source_against_40_digits(golden):
+    """A source with vertices on the free surface: the reference C++ and
+    the oracle are both FP64 evaluations of a formula with heavy cancellation
+    there; both stay within 1e-8 (of the pair's total strain) of a 40-digit
+    evaluation, which is what the 2e-8 bar above allows for."""
+    pytest.importorskip("mpmath")
+    from tests.hs_highprec import fsc_strain
+    g = golden("gf_kat.npz")
+    r = g["each_recv"]
+    _, e_all = oracle.tdstress_each_source(r[0], r[1], r[2], g["each_P1"], g["each_P2"], g["each_P3"],
+                                           0.0, 1.0, 0.0, MU, MU, True)
+    dis = [normwise_rel(g["each_h1_strain"][q], e_all[q]) for q in range(e_all.shape[0])]
+    j = int(np.argmax(dis))          # where the two FP64 evaluations disagree most
+    assert _surface_sources(g)[j] and dis[j] > 1e-9
+    P = [g["each_P1"][j], g["each_P2"][j], g["each_P3"][j]]
+    exact = fsc_strain(*P, 0.0, 1.0, 0.0, r)
+    X, Y, Z = r[:1].copy(), r[1:2].copy(), r[2:3].copy()
+    _, e_fs = oracle.tdstress(X, Y, Z, *P, 0.0, 1.0, 0.0, MU, MU, False)
+    Q = [np.array([p[0], p[1], -p[2]]) for p in P]
+    _, e_im = oracle.tdstress(X, Y, Z, *Q, 0.0, 1.0, 0.0, MU, MU, False)
+    _, e_hs = oracle.tdstress(X, Y, Z, *P, 0.0, 1.0, 0.0, MU, MU, True)
+    ref_total = g["each_h1_strain"][j]
+    scale = np.linalg.norm(ref_total)
+    fsc_oracle = e_hs[0] - e_fs[0] - e_im[0]
+    fsc_ref = ref_total - e_fs[0] - e_im[0]
+    assert np.linalg.norm(fsc_oracle - exact) / scale < 1e-8
+    assert np.linalg.norm(fsc_ref - exact) / scale < 1e-8
+
+
+@pytest.fixture(scope="module")
+def host_check(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.fail("no C++ compiler for the host build of the device math")
+    exe = str(tmp_path_factory.mktemp("hs") / "hs_host_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "hs_host_check.cpp")], check=True)
+    return exe
+
+
+def test_device_math_matches_oracle(host_check):
+    """Strain for a general Burgers vector and the six unit-slip tractions
+    from the device code (compiled for the host) against the oracle:
+    400 seeded pairs, including sources with vertices on the surface, surface
+    triangles and receivers on the surface; errors scaled by the larger of
+    the half- and full-space strain (surface triangles with surface receivers
+    cancel to ~1e-19)."""
+    rng = np.random.default_rng(1)
+    cases = []
+    for t in range(400):
+        P = rng.normal(size=(3, 3)) * 2000 + np.array([0, 0, -5000.0])
+        P[:, 2] = -np.abs(P[:, 2])
+        if t % 10 == 0:
+            P[:2, 2] = 0.0
+        if t % 25 == 0:
+            P[:, 2] = 0.0
+        X = np.array([rng.uniform(-8000, 8000), rng.uniform(-8000, 8000), -rng.uniform(0, 10000)])
+        if t % 7 == 0:
+            X[2] = 0.0
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        e1 = np.cross([0, 0, 1.0], n)
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(n, e1)
+        cases.append((P, X, rng.normal(size=3), e1, e2, n))
+    inp = "%d\n" % len(cases) + "\n".join(
+        " ".join("%.17g" % v for v in np.concatenate([P.ravel(), X, b, e1, e2, n])) for P, X, b, e1, e2, n in cases)
+    out = subprocess.run([host_check], input=inp, capture_output=True, text=True, check=True).stdout
+    res = np.array([[float(v) for v in line.split()] for line in out.strip().split("\n")])
+    for i, (P, X, b, e1, e2, n) in enumerate(cases):
+        x = (X[:1], X[1:2], X[2:3])
+        _, e = oracle.tdstress(*x, P[0], P[1], P[2], b[0], b[1], b[2], MU, MU, True)
+        _, e0 = oracle.tdstress(*x, P[0], P[1], P[2], b[0], b[1], b[2], MU, MU, False)
+        scale = max(np.linalg.norm(e[0]), np.linalg.norm(e0[0]))
+        assert np.linalg.norm(res[i, :6] - e[0]) / scale < 1e-10, i
+        tt, t0 = [], []
+        for Ss, Ds in ((1.0, 0.0), (0.0, 1.0)):
+            for half, acc in ((True, tt), (False, t0)):
+                s, _ = oracle.tdstress(*x, P[0], P[1], P[2], Ss, Ds, 0.0, MU, MU, half)
+                S = np.array([[s[0, 0], s[0, 3], s[0, 4]], [s[0, 3], s[0, 1], s[0, 5]], [s[0, 4], s[0, 5], s[0, 2]]])
+                t = S @ n
+                acc.extend([t @ e1, t @ e2, t @ n])
+        scale = max(np.linalg.norm(tt), np.linalg.norm(t0))
+        assert np.linalg.norm(res[i, 6:] - np.array(tt)) / scale < 1e-10, i
