@@ -323,6 +323,7 @@ def bench_ours(args):
             out["batched"] = bench_batched(torch, dev, args, peaks)
         if not args.no_hmat:
             out["hmatrix"] = bench_hmatrix(torch, dev, args, peaks)
+        out["halfspace"] = bench_halfspace(torch, dev, args)
         if not args.no_serve:
             out["serving"] = bench_serving(torch, dev, args)
         if not args.no_cpu:
@@ -534,6 +535,37 @@ def bench_hmatrix(torch, dev, args, peaks):
     res["stepping"] = {"rk_stages_per_s": (st1 - st0) / dt, "stages": int(st1 - st0), "seconds": dt,
                        "status": int(ens.read_ctrl()[0].status)}
     del H, ens
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_halfspace(torch, dev, args):
+    """Half-space GF assembly (image dislocation + free-surface correction):
+    rough fault 40 x 20 km reaching the free surface, 50 x 25 cells ->
+    N = 2,500 (1 km cells), FP64 operator + FP32 copy, against the full-space
+    assembly of the same mesh."""
+    from pyquake3d_gb300 import gf, mesh
+    nodes, tris = mesh.rough_fault(40.0, 20.0, 50, 25, hurst=0.8, ratio=1e-3, seed=0)
+    N = tris.shape[0]
+    nodes_t, tris_t = gf.mesh_to_device(nodes, tris, dev)
+    K64 = torch.empty((3 * N, 2 * N), dtype=torch.float64, device=dev)
+    K32 = torch.empty((3 * N, 2 * N), dtype=torch.float32, device=dev)
+    ws = torch.empty(L_ws_bytes(N), dtype=torch.uint8, device=dev)
+    res = {"workload": "half-space GF assembly: rough 40x20 km to the surface, N=%d" % N}
+    for half in (False, True):
+        for _ in range(2):
+            gf.assemble_dense(nodes_t, tris_t, MU, LAM, halfspace=half, out64=K64, out32=K32, workspace=ws)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        s.record()
+        for _ in range(reps):
+            gf.assemble_dense(nodes_t, tris_t, MU, LAM, halfspace=half, out64=K64, out32=K32, workspace=ws)
+        e.record()
+        e.synchronize()
+        t = s.elapsed_time(e) / reps / 1e3
+        res["halfspace" if half else "fullspace"] = {"s": t, "pairs_per_s": N * N / t, "entries_per_s": 6 * N * N / t}
+    res["cost_ratio"] = res["halfspace"]["s"] / res["fullspace"]["s"]
+    del K64, K32
     torch.cuda.empty_cache()
     return res
 

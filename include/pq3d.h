@@ -280,9 +280,10 @@ int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream);
 /* ---------------- device: H-matrix ---------------- */
 
 /* Source and receiver tables of a mesh (the set-up step of the assembly) into
- * `workspace` (pq3d_gf_workspace_bytes(N)): used by the H-matrix kernels. */
-int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, void *workspace, size_t workspace_bytes,
-                  void *stream);
+ * `workspace` (pq3d_gf_workspace_bytes(N)), and with halfspace != 0 the image
+ * and free-surface tables: used by the H-matrix kernels. */
+int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, int halfspace, void *workspace,
+                  size_t workspace_bytes, void *stream);
 
 /* H-matrix of the (3N)x(2N) traction operator in a renumbering where every
  * cluster is a contiguous range (perm[p] = element at position p).  Replaces
@@ -295,7 +296,8 @@ typedef struct pq3d_hmat {
     const int64_t *blk;           /* [nblocks][4]: r0, r1, c0, c1 (permuted element ranges) */
     const int32_t *rank;          /* [nblocks]: rank k >= 0 of a low-rank block, -1 for a dense block */
     const int64_t *off;           /* [nblocks]: offset (floats) of the block in data */
-    const float *data;            /* dense block (3m x 2n) or U (3m x k) then V (k x 2n), row-major FP32 */
+    const float *data;            /* FP32: dense block (3m x 2n, column-major) or U (3m x k, column-major)
+                                     then V (k x 2n, row-major) */
     const int32_t *lr_ids;        /* low-rank block ids, in order */
     const int32_t *t_blk;         /* [t_rows] block of each rank row (low-rank blocks in lr_ids order) */
     const int64_t *t_off;         /* [nblocks]: first rank row of the block in the product workspace */
@@ -312,14 +314,15 @@ typedef struct pq3d_hmat {
  * (0 converged, 1 rank cap reached, 2 non-finite).  Replaces ACA_worker /
  * ACA_plus_full_traceS/D (src/Hmatrix.py:661-1344). */
 int pq3d_hmat_aca(const double *tables, int64_t N, const int64_t *perm, int nblocks, const int64_t *blk,
-                  const int32_t *kcap, double tol, double mu, double lambda_, double *UV, const int64_t *uv_off,
-                  uint8_t *used, const int64_t *used_off, int32_t *rank, int32_t *status, void *stream);
-/* Dense blocks ids[0..nids) into D + d_off[b] (FP32, 3m x 2n row-major); every
- * d_off[b] must be even (8-byte aligned block starts). */
+                  const int32_t *kcap, double tol, double mu, double lambda_, int halfspace, double *UV,
+                  const int64_t *uv_off, uint8_t *used, const int64_t *used_off, int32_t *rank, int32_t *status,
+                  void *stream);
+/* Dense blocks ids[0..nids) into D + d_off[b] (FP32, column-major: element
+ * (row, col) at col * 3m + row). */
 int pq3d_hmat_dense_blocks(const double *tables, int64_t N, const int64_t *perm, const int64_t *blk,
-                           const int32_t *ids, int nids, double mu, double lambda_, float *D, const int64_t *d_off,
-                           void *stream);
-/* FP64 ACA factors of blocks ids[] -> FP32 U (3m x k) and V (k x 2n) at out + out_off[b]. */
+                           const int32_t *ids, int nids, double mu, double lambda_, int halfspace, float *D,
+                           const int64_t *d_off, void *stream);
+/* FP64 ACA factors of blocks ids[] -> FP32 U (column-major, 3m x k) and V (k x 2n) at out + out_off[b]. */
 int pq3d_hmat_pack_factors(const double *UV, const int64_t *uv_off, const int64_t *blk, const int32_t *kcap,
                            const int32_t *rank, const int32_t *ids, int nids, float *out, const int64_t *out_off,
                            void *stream);

@@ -257,3 +257,19 @@ class QDsim:
         for k in STATE_FIELDS:
             setattr(self, k, self.dev.t[k].cpu().numpy())
         return h, dtnext
+
+    def ouputVTK(self, fname):
+        """Snapshot as legacy VTK (the reference's method name, fields and
+        layout, src/QDsim_gpu.py:1927-2073): the device state is staged into
+        one pinned host buffer by a single copy, then written."""
+        import torch
+        from .mesh import write_vtk
+        if hasattr(self, "dev"):
+            keys = STATE_FIELDS + ("a", "b", "dc")
+            staged = torch.stack([self.dev.t[k] for k in keys])
+            host = torch.empty(staged.shape, dtype=staged.dtype, pin_memory=True)
+            host.copy_(staged)
+            fields = {k: host[i].numpy() for i, k in enumerate(keys)}
+        else:
+            fields = {k: np.asarray(getattr(self, k)) for k in STATE_FIELDS + ("a", "b", "dc")}
+        write_vtk(fname, self.nodelst, self.elelst, fields)

@@ -110,11 +110,11 @@ _SIGS = {
     "pq3d_batch_rhs_bytes": (c_size, [c_i64, c_int]),
     "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size, c_void_p]),
     "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
-    "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_size, c_void_p]),
-    "pq3d_hmat_aca": (c_int, [c_void_p, c_i64, c_void_p, c_int, c_void_p, c_void_p, c_dbl, c_dbl, c_dbl, c_void_p,
-                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
-    "pq3d_hmat_dense_blocks": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_int, c_dbl, c_dbl, c_void_p,
-                                       c_void_p, c_void_p]),
+    "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_void_p, c_size, c_void_p]),
+    "pq3d_hmat_aca": (c_int, [c_void_p, c_i64, c_void_p, c_int, c_void_p, c_void_p, c_dbl, c_dbl, c_dbl, c_int,
+                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pq3d_hmat_dense_blocks": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_int, c_dbl, c_dbl, c_int,
+                                       c_void_p, c_void_p, c_void_p]),
     "pq3d_hmat_pack_factors": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                        c_void_p, c_void_p]),
     "pq3d_hmat_workspace_bytes": (c_size, [ctypes.POINTER(HMat), c_int]),

@@ -594,18 +594,23 @@ extern "C" int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *t
                          true, (cudaStream_t)stream);
 }
 
-extern "C" int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, void *workspace,
+extern "C" int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, int halfspace, void *workspace,
                              size_t workspace_bytes, void *stream)
 {
     clear_error();
     PQ3D_REQUIRE(nodes && tris && workspace && N > 0, "pq3d_gf_setup: bad arguments");
-    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N, false) && aligned16(workspace), "pq3d_gf_setup: workspace too small");
+    PQ3D_REQUIRE(workspace_bytes >= ws_bytes(N, halfspace != 0) && aligned16(workspace),
+                 "pq3d_gf_setup: workspace too small");
     double *src = (double *)workspace;
     double *recv = src + (size_t)kSrcStride * N;
     const int th = 128;
     const unsigned nb = (unsigned)((N + th - 1) / th);
     setup_sources_kernel<<<nb, th, 0, (cudaStream_t)stream>>>(nodes, tris, N, src);
     setup_receivers_kernel<<<nb, th, 0, (cudaStream_t)stream>>>(nodes, tris, N, recv);
+    if (halfspace) {
+        double *img = recv + (size_t)kRecvStride * N;
+        setup_hs_kernel<<<nb, th, 0, (cudaStream_t)stream>>>(nodes, tris, N, img, img + (size_t)kImgStride * N);
+    }
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

@@ -31,6 +31,7 @@
 
 #include "common.cuh"
 #include "gf_device.cuh"
+#include "hs_device.cuh"
 
 namespace pq3d {
 namespace hm {
@@ -44,6 +45,22 @@ struct GSrc {   // source fields from the global structure-of-arrays table
 };
 
 constexpr int kThreads = 256;
+
+// The six tractions of pair (receiver record R, source element j): full
+// space, or half space (image record and free-surface side table).
+template <bool kHalf>
+struct PairGen {
+    const double *src, *img, *fsc;
+    int64_t N;
+    double nu, kf, two_mu, lam;
+    __device__ __forceinline__ void operator()(int64_t j, const double *R, double ts[3], double td[3]) const
+    {
+        if (kHalf)
+            pair_tractions_hs(GSrc{src + j, N}, GSrc{img + j, N}, GSrc{fsc + j, N}, R, nu, kf, two_mu, lam, ts, td);
+        else
+            pair_tractions(GSrc{src + j, N}, R, nu, kf, two_mu, lam, ts, td);
+    }
+};
 
 __device__ __forceinline__ void block_argmax(double v, int idx, double *sv, int *si, double &best, int &bidx)
 {
@@ -78,10 +95,11 @@ __device__ __forceinline__ double block_sum(double v, double *sv)
 }
 
 // One CTA per admissible block.  U: kcap x M (row l = u_l), V: kcap x Nc.
+template <bool kHalf>
 __global__ void __launch_bounds__(kThreads)
-aca_kernel(const double *__restrict__ src, const double *__restrict__ recv, int64_t N, const int64_t *__restrict__ perm,
-           const int64_t *__restrict__ blk, const int32_t *__restrict__ kcap, double tol, double nu, double kf,
-           double two_mu, double lam, double *__restrict__ UV, const int64_t *__restrict__ uv_off,
+aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *__restrict__ perm,
+           const int64_t *__restrict__ blk, const int32_t *__restrict__ kcap, double tol,
+           double *__restrict__ UV, const int64_t *__restrict__ uv_off,
            uint8_t *__restrict__ used_ws, const int64_t *__restrict__ used_off, int32_t *__restrict__ rank_out,
            int32_t *__restrict__ status_out)
 {
@@ -106,9 +124,8 @@ aca_kernel(const double *__restrict__ src, const double *__restrict__ recv, int6
         const double *R = recv + kRecvStride * perm[r0 + pr];
         double *v = V + (int64_t)k * Nc;
         for (int q = t; q < n; q += kThreads) {
-            const int64_t j = perm[c0 + q];
             double ts[3], td[3];
-            pair_tractions(GSrc{src + j, N}, R, nu, kf, two_mu, lam, ts, td);
+            gen(perm[c0 + q], R, ts, td);
             v[2 * q] = ts[cr];
             v[2 * q + 1] = td[cr];
         }
@@ -142,11 +159,11 @@ aca_kernel(const double *__restrict__ src, const double *__restrict__ recv, int6
         const double pivot = v[jstar];
         // residual column jstar (source q, slip s) over all rows, scaled by the pivot
         const int qc = jstar / 2, sc = jstar % 2;
-        const double *Fb = src + perm[c0 + qc];
+        const int64_t jb = perm[c0 + qc];
         double *u = U + (int64_t)k * M;
         for (int p = t; p < m; p += kThreads) {
             double ts[3], td[3];
-            pair_tractions(GSrc{Fb, N}, recv + kRecvStride * perm[r0 + p], nu, kf, two_mu, lam, ts, td);
+            gen(jb, recv + kRecvStride * perm[r0 + p], ts, td);
             const double *tt = sc ? td : ts;
             u[3 * p] = tt[0];
             u[3 * p + 1] = tt[1];
@@ -205,10 +222,10 @@ aca_kernel(const double *__restrict__ src, const double *__restrict__ recv, int6
 
 // Dense blocks, one CTA per block; consecutive threads take consecutive
 // receivers of one source.
+template <bool kHalf>
 __global__ void __launch_bounds__(kThreads)
-dense_blocks_kernel(const double *__restrict__ src, const double *__restrict__ recv, int64_t N,
-                    const int64_t *__restrict__ perm, const int64_t *__restrict__ blk, const int32_t *__restrict__ ids,
-                    double nu, double kf, double two_mu, double lam, float *__restrict__ D,
+dense_blocks_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *__restrict__ perm,
+                    const int64_t *__restrict__ blk, const int32_t *__restrict__ ids, float *__restrict__ D,
                     const int64_t *__restrict__ d_off)
 {
     const int b = ids[blockIdx.x];
@@ -219,7 +236,7 @@ dense_blocks_kernel(const double *__restrict__ src, const double *__restrict__ r
     for (int64_t e = threadIdx.x; e < (int64_t)m * n; e += kThreads) {
         const int q = (int)(e / m), p = (int)(e % m);
         double ts[3], td[3];
-        pair_tractions(GSrc{src + perm[c0 + q], N}, recv + kRecvStride * perm[r0 + p], nu, kf, two_mu, lam, ts, td);
+        gen(perm[c0 + q], recv + kRecvStride * perm[r0 + p], ts, td);
         float *col_s = Db + (int64_t)(2 * q) * M + 3 * p;
         float *col_d = col_s + M;
         for (int c = 0; c < 3; ++c) {
@@ -252,7 +269,8 @@ __global__ void pack_factors_kernel(const double *__restrict__ UV, const int64_t
 //
 // Arithmetic: FP32 entries times the right-hand side split into FP32 hi + lo
 // (2 FMAs per entry), FP32 partial sums over at most one block segment (or
-// 1024 columns), then FP64.
+// 1024 columns), then float-float (FF) sums; FP64 only for the final sum of a
+// row's per-warp partials.
 
 struct Acc2 {   // FP32 partial sum of one lane
     float s, c;
@@ -268,6 +286,36 @@ __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Float-float (unevaluated sum hi + lo) accumulation with FP32 operations
+// only (Knuth's TwoSum), for the reductions of the low-rank product: GB300's
+// FP64 rate is 1/64 of FP32, and an FP64 reduction per rank row made that
+// kernel FP64-bound.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    const float l = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+    const float h = __fadd_rn(s, l);
+    return FF{h, __fsub_rn(l, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ FF warp_sum_ff(FF v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        FF w;
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v = ff_add(v, w);
+    }
     return v;
 }
 
@@ -311,7 +359,7 @@ lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
     const int M = 3 * (int)(blk[4 * b + 1] - blk[4 * b]);
     const float *v = data + off[b] + (int64_t)M * k + (int64_t)l * Nc;
     const float2 *x = Xs + (int64_t)r * 2 * N + 2 * c0;
-    double sum = 0.0;
+    FF sum{0.f, 0.f};
     for (int c0k = 0; c0k < Nc; c0k += 1024) {
         const int cend = min(Nc, c0k + 1024);
         Acc2 a0{0.f, 0.f}, a1{0.f, 0.f};
@@ -326,10 +374,13 @@ lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
             acc2_add(a1, k3, x3);
         }
         for (; col < cend; col += 32) acc2_add(a0, __ldg(v + col), x[col]);
-        sum += ((double)a0.s + (double)a1.s) + ((double)a0.c + (double)a1.c);
+        // the hi and lo parts of the FP32 partial sums of this chunk
+        sum = ff_add(sum, FF{a0.s, 0.f});
+        sum = ff_add(sum, FF{a1.s, 0.f});
+        sum = ff_add(sum, FF{__fadd_rn(a0.c, a1.c), 0.f});
     }
-    sum = warp_sum(sum);
-    if (lane == 0) T[(t0 + l) * (int64_t)B + r] = split2(sum);
+    sum = warp_sum_ff(sum);
+    if (lane == 0) T[(t0 + l) * (int64_t)B + r] = make_float2(sum.hi, sum.lo);
 }
 
 // One CTA per (leaf row cluster, run), the run fastest in the block index so
@@ -358,7 +409,7 @@ constexpr int kPassRows = 32 * kMaxR;
 
 template <int R>
 __device__ __forceinline__ void leaf_segment(const float *__restrict__ col0, int64_t M, const float2 *__restrict__ xp,
-                                             int64_t xs, int ca, int cb, bool last_ok, double (&acc)[kMaxR])
+                                             int64_t xs, int ca, int cb, bool last_ok, FF (&acc)[kMaxR])
 {
     constexpr int U = 4;   // columns in flight per warp
     Acc2 a[R];
@@ -393,13 +444,16 @@ __device__ __forceinline__ void leaf_segment(const float *__restrict__ col0, int
         }
     }
 #pragma unroll
-    for (int i = 0; i < R; ++i) acc[i] += (double)a[i].s + (double)a[i].c;
+    for (int i = 0; i < R; ++i) {
+        acc[i] = ff_add(acc[i], FF{a[i].s, 0.f});
+        acc[i] = ff_add(acc[i], FF{a[i].c, 0.f});
+    }
 }
 
 template <int R>
 __device__ __forceinline__ void leaf_range(const BlkDesc *desc, const int *wpre, int nq, int64_t lo, int64_t hi, int pr0, int prow,
                            const float *__restrict__ data, const float2 *__restrict__ xr,
-                           const float2 *__restrict__ T, int B, int r, double (&acc)[kMaxR])
+                           const float2 *__restrict__ T, int B, int r, FF (&acc)[kMaxR])
 {
     const int lane = threadIdx.x & 31;
     const bool last_ok = lane + 32 * (R - 1) < prow;
@@ -437,9 +491,9 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
     for (int pr0 = 0; pr0 < rows; pr0 += kPassRows) {
         const int prow = min(kPassRows, rows - pr0);
         const int R = (prow + 31) / 32;
-        double acc[kMaxR];
+        FF acc[kMaxR];
 #pragma unroll
-        for (int i = 0; i < kMaxR; ++i) acc[i] = 0.0;
+        for (int i = 0; i < kMaxR; ++i) acc[i] = FF{0.f, 0.f};
         for (int64_t qs = q0; qs < q1; qs += kMaxLeafBlocks) {
             const int nq = (int)min((int64_t)kMaxLeafBlocks, q1 - qs);
             __syncthreads();
@@ -476,7 +530,7 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
         }
         __syncthreads();
 #pragma unroll
-        for (int i = 0; i < kMaxR; ++i) red[wid][lane + 32 * i] = acc[i];
+        for (int i = 0; i < kMaxR; ++i) red[wid][lane + 32 * i] = (double)acc[i].hi + (double)acc[i].lo;
         __syncthreads();
         for (int lr = threadIdx.x; lr < prow; lr += kThreads) {
             double s = 0.0;
@@ -496,11 +550,19 @@ using namespace pq3d::hm;
 
 static inline double poisson_(double mu, double lam) { return 1.0 / (1.0 + lam / mu) / 2.0; }
 
-extern "C" int pq3d_gf_setup(const double *nodes, const int64_t *tris, int64_t N, void *workspace,
-                             size_t workspace_bytes, void *stream);
+// Table layout written by pq3d_gf_setup: source [kSrcStride][N], receiver
+// [N][kRecvStride], image [kImgStride][N], side table [kFscStride][N].
+template <bool kHalf>
+static PairGen<kHalf> make_gen(const double *tables, int64_t N, double mu, double lambda_)
+{
+    const double nu = poisson_(mu, lambda_);
+    const double *img = tables + (size_t)(kSrcStride + kRecvStride) * N;
+    return PairGen<kHalf>{tables, img, img + (size_t)kImgStride * N, N, nu, 1.0 / (8.0 * kPi * (1.0 - nu)),
+                          2.0 * mu, lambda_};
+}
 
 extern "C" int pq3d_hmat_aca(const double *tables, int64_t N, const int64_t *perm, int nblocks, const int64_t *blk,
-                             const int32_t *kcap, double tol, double mu, double lambda_, double *UV,
+                             const int32_t *kcap, double tol, double mu, double lambda_, int halfspace, double *UV,
                              const int64_t *uv_off, uint8_t *used, const int64_t *used_off, int32_t *rank,
                              int32_t *status, void *stream)
 {
@@ -508,27 +570,34 @@ extern "C" int pq3d_hmat_aca(const double *tables, int64_t N, const int64_t *per
     PQ3D_REQUIRE(tables && perm && blk && kcap && UV && uv_off && used && used_off && rank && status && N > 0,
                  "pq3d_hmat_aca: bad arguments");
     if (nblocks <= 0) return PQ3D_OK;
-    const double nu = poisson_(mu, lambda_);
-    const double kf = 1.0 / (8.0 * kPi * (1.0 - nu));
-    aca_kernel<<<nblocks, kThreads, 0, (cudaStream_t)stream>>>(tables, tables + (size_t)kSrcStride * N, N, perm, blk,
-                                                               kcap, tol, nu, kf, 2.0 * mu, lambda_, UV, uv_off, used,
-                                                               used_off, rank, status);
+    const double *recv = tables + (size_t)kSrcStride * N;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (halfspace)
+        aca_kernel<true><<<nblocks, kThreads, 0, st>>>(make_gen<true>(tables, N, mu, lambda_), recv, perm, blk, kcap,
+                                                       tol, UV, uv_off, used, used_off, rank, status);
+    else
+        aca_kernel<false><<<nblocks, kThreads, 0, st>>>(make_gen<false>(tables, N, mu, lambda_), recv, perm, blk,
+                                                        kcap, tol, UV, uv_off, used, used_off, rank, status);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }
 
 extern "C" int pq3d_hmat_dense_blocks(const double *tables, int64_t N, const int64_t *perm, const int64_t *blk,
-                                      const int32_t *ids, int nids, double mu, double lambda_, float *D,
-                                      const int64_t *d_off, void *stream)
+                                      const int32_t *ids, int nids, double mu, double lambda_, int halfspace,
+                                      float *D, const int64_t *d_off, void *stream)
 {
     clear_error();
     PQ3D_REQUIRE(tables && perm && blk && ids && D && d_off && N > 0, "pq3d_hmat_dense_blocks: bad arguments");
     PQ3D_REQUIRE(((uintptr_t)D & 3u) == 0, "pq3d_hmat_dense_blocks: D must be 4-byte aligned");
     if (nids <= 0) return PQ3D_OK;
-    const double nu = poisson_(mu, lambda_);
-    const double kf = 1.0 / (8.0 * kPi * (1.0 - nu));
-    dense_blocks_kernel<<<nids, kThreads, 0, (cudaStream_t)stream>>>(tables, tables + (size_t)kSrcStride * N, N, perm,
-                                                                     blk, ids, nu, kf, 2.0 * mu, lambda_, D, d_off);
+    const double *recv = tables + (size_t)kSrcStride * N;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (halfspace)
+        dense_blocks_kernel<true><<<nids, kThreads, 0, st>>>(make_gen<true>(tables, N, mu, lambda_), recv, perm, blk,
+                                                             ids, D, d_off);
+    else
+        dense_blocks_kernel<false><<<nids, kThreads, 0, st>>>(make_gen<false>(tables, N, mu, lambda_), recv, perm,
+                                                              blk, ids, D, d_off);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

@@ -23,6 +23,8 @@ save_corefunc)`` and ``blocks_process_MVM(x, blocks, type)``.
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 import sys
 
 import numpy as np
@@ -98,7 +100,7 @@ class HMatrix:
     """Device H-matrix of the (3N)x(2N) traction operator of a mesh."""
 
     def __init__(self, nodes, tris, mu, lam, *, min_size=16, mini_leaf=32, eta=2.0, tol=1e-4, kmax=128,
-                 device="cuda", chunk_bytes=8 << 30):
+                 device="cuda", chunk_bytes=8 << 30, halfspace=False):
         L = _lib.load()
         self.device = torch.device(device)
         dev = self.device
@@ -113,7 +115,9 @@ class HMatrix:
         self.nodes_t = torch.as_tensor(nodes, device=dev)
         self.tris_t = torch.as_tensor(tris, device=dev)
         self.tables = torch.empty(L.pq3d_gf_workspace_bytes(N), dtype=torch.uint8, device=dev)
-        _lib.check(L.pq3d_gf_setup(self.nodes_t.data_ptr(), self.tris_t.data_ptr(), N, self.tables.data_ptr(),
+        hs = int(bool(halfspace))
+        self.halfspace = bool(halfspace)
+        _lib.check(L.pq3d_gf_setup(self.nodes_t.data_ptr(), self.tris_t.data_ptr(), N, hs, self.tables.data_ptr(),
                                    self.tables.numel(), st))
         self.perm = torch.as_tensor(perm, device=dev)
         nb = blocks.shape[0]
@@ -159,7 +163,7 @@ class HMatrix:
             rk_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             stt_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             _lib.check(L.pq3d_hmat_aca(self.tables.data_ptr(), N, self.perm.data_ptr(), len(ids), blk_c.data_ptr(),
-                                       kcap_c.data_ptr(), float(tol), float(mu), float(lam), UV.data_ptr(),
+                                       kcap_c.data_ptr(), float(tol), float(mu), float(lam), hs, UV.data_ptr(),
                                        uvo_c.data_ptr(), used.data_ptr(), uso_c.data_ptr(), rk_c.data_ptr(),
                                        stt_c.data_ptr(), st))
             rank[ids] = rk_c.cpu().numpy()
@@ -184,7 +188,7 @@ class HMatrix:
         if len(dense_ids):
             ids_t = torch.as_tensor(dense_ids, device=dev)
             _lib.check(L.pq3d_hmat_dense_blocks(self.tables.data_ptr(), N, self.perm.data_ptr(), self.blk.data_ptr(),
-                                                ids_t.data_ptr(), len(dense_ids), float(mu), float(lam),
+                                                ids_t.data_ptr(), len(dense_ids), float(mu), float(lam), hs,
                                                 self.data.data_ptr(), self.off.data_ptr(), st))
         for (ids, UV, uvo_c, blk_c, kcap_c, rk_c) in factors.values():
             good = np.nonzero(rank[ids] >= 0)[0].astype(np.int32)   # positions inside the chunk
@@ -220,18 +224,44 @@ class HMatrix:
         self.leaf = torch.as_tensor(np.ascontiguousarray(leaves), device=dev)
         self.leaf_ptr = torch.as_tensor(leaf_ptr, device=dev)
         self.leaf_blocks = torch.as_tensor(np.concatenate([np.asarray(x, np.int32) for x in lists]), device=dev)
-        H = _lib.HMat()
-        H.N, H.nblocks, H.nleaves, H.t_rows = N, nb, nl, self.t_rows
-        for k in ("perm", "blk", "rank", "off", "data", "lr_ids", "t_blk", "t_off", "leaf", "leaf_ptr",
-                  "leaf_blocks"):
-            setattr(H, k, getattr(self, k).data_ptr())
-        self.H = H
+        self._make_struct()
         self.stats = {"N": N, "blocks": int(nb), "lowrank_blocks": int(len(lr_ids)),
                       "dense_blocks": int(len(dense_ids)), "aca_not_converged": int(np.sum(lowrank & (status != 0))),
                       "max_rank": int(ranks.max()) if len(ranks) else 0,
                       "mean_rank": float(ranks.mean()) if len(ranks) else 0.0,
                       "bytes": int(self.data.numel() * 4), "dense_fp32_bytes": int(6 * N * N * 4),
                       "leaves": int(nl)}
+
+    _ARRAYS = ("perm", "blk", "rank", "off", "data", "lr_ids", "t_blk", "t_off", "leaf", "leaf_ptr", "leaf_blocks")
+
+    def _make_struct(self):
+        H = _lib.HMat()
+        H.N, H.nblocks, H.nleaves, H.t_rows = self.N, int(self.blk.shape[0]), int(self.leaf.shape[0]), self.t_rows
+        for k in self._ARRAYS:
+            setattr(H, k, getattr(self, k).data_ptr())
+        self.H = H
+
+    def save(self, path):
+        """Write the compressed operator (the device arrays, one .npz): the
+        warm-start cache of a mesh, in place of the reference's pickled block
+        list (src/Hmatrix.py:1552-1555)."""
+        arrs = {k: getattr(self, k).cpu().numpy() for k in self._ARRAYS}
+        np.savez(path, N=self.N, t_rows=self.t_rows, stats=json.dumps(self.stats), halfspace=self.halfspace, **arrs)
+
+    @classmethod
+    def load(cls, path, device="cuda"):
+        """An H-matrix written by :meth:`save` (no ACA, no GF evaluation)."""
+        g = np.load(path)
+        self = cls.__new__(cls)
+        self.device = torch.device(device)
+        self.N = int(g["N"])
+        self.t_rows = int(g["t_rows"])
+        self.stats = json.loads(str(g["stats"]))
+        self.halfspace = bool(g["halfspace"]) if "halfspace" in g else False
+        for k in cls._ARRAYS:
+            setattr(self, k, torch.as_tensor(g[k], device=self.device))
+        self._make_struct()
+        return self
 
     def workspace_bytes(self, B):
         return _lib.load().pq3d_hmat_workspace_bytes(ctypes.byref(self.H), int(B))
@@ -262,8 +292,7 @@ class BlockTree:
     blocks_process_MVM applies one of the six operators."""
 
     def __init__(self, nodelst, elelst, mu, lam, halfspace, mini_leaf, eta=2.0, tol=1e-4, device="cuda"):
-        if halfspace:
-            raise NotImplementedError("half-space Green's functions are not available in this build")
+        self.halfspace = bool(halfspace)
         self.nodelst, self.elelst = nodelst, elelst
         self.mu_, self.lambda_, self.mini_leaf, self.eta, self.tol, self.device = mu, lam, mini_leaf, eta, tol, device
         _, xg = element_frames(np.asarray(nodelst, dtype=np.float64), np.asarray(elelst, dtype=np.int64))
@@ -272,8 +301,19 @@ class BlockTree:
         self.blocks_to_process = [tuple(b) for b in self.blocks]
 
     def calc_Hmatrix_ACA(self, dir=None, save_corefunc=False):
-        self.H = HMatrix(self.nodelst, self.elelst, self.mu_, self.lambda_, min_size=16, mini_leaf=self.mini_leaf,
-                         eta=self.eta, tol=self.tol, device=self.device)
+        """Compress on the GPU; with ``dir``, reuse ``dir/hmatrix.npz`` when it
+        exists and write it when ``save_corefunc`` (the reference's cache
+        switch, src/Hmatrix.py:1552-1555)."""
+        cache = os.path.join(dir, "hmatrix.npz") if dir else None
+        if cache and os.path.exists(cache):
+            self.H = HMatrix.load(cache, device=self.device)
+        else:
+            self.H = HMatrix(self.nodelst, self.elelst, self.mu_, self.lambda_, min_size=16,
+                             mini_leaf=self.mini_leaf, eta=self.eta, tol=self.tol, device=self.device,
+                             halfspace=self.halfspace)
+            if cache and save_corefunc:
+                os.makedirs(dir, exist_ok=True)
+                self.H.save(cache)
         return self.blocks_to_process
 
     def blocks_process_MVM(self, xvector, blocks_to_process=None, type="A1s"):

@@ -194,3 +194,78 @@ def write_msh_v2(path: str, nodes: np.ndarray, tris: np.ndarray) -> None:
         for i, t in enumerate(tris):
             f.write("%d 2 2 0 1 %d %d %d\n" % (i + 1, t[0], t[1], t[2]))
         f.write("$EndElements\n")
+
+
+def read_mshV2(fname: str):
+    """gmsh v2 ASCII reader with the reference's semantics
+    (src/readmsh.py:12-68): node coordinates in km -> metres; elements are the
+    lines of the $Elements section with at least 8 fields, their last three
+    integers the (1-based) vertex tags.  Returns (nodes[Nn,3], tris[N,3])."""
+    nodes, tris = [], []
+    section = None
+    with open(fname) as f:
+        for raw in f:
+            line = raw.strip()
+            if line.startswith("$"):
+                section = {"$Nodes": "nodes", "$Elements": "elements"}.get(line)
+                first = True
+                continue
+            if section is None:
+                continue
+            if first:                      # the count line
+                first = False
+                continue
+            parts = line.split()
+            if section == "nodes" and len(parts) >= 4:
+                nodes.append([float(parts[1]), float(parts[2]), float(parts[3])])
+            elif section == "elements" and len(parts) >= 8:
+                tris.append([int(parts[-3]), int(parts[-2]), int(parts[-1])])
+    return np.asarray(nodes, dtype=np.float64) * 1e3, np.asarray(tris, dtype=np.int64)
+
+
+# Cell fields of a snapshot, in the reference's order and names
+# (src/QDsim_gpu.py:1927-2073): (VTK name, state key, scale, format).
+VTK_FIELDS = (
+    ("Normal_[MPa]", "Tno", 1.0, "%f"), ("Pore_pressure[MPa]", "P", 1e-6, "%f"), ("Shear_[MPa]", "Tt", 1.0, "%f"),
+    ("Shear_1[MPa]", "Tt1o", 1.0, "%f"), ("Shear_2[MPa]", "Tt2o", 1.0, "%f"),
+    ("rake[Degree]", "rake", 180.0 / np.pi, "%f"), ("state", "state", 1.0, "%f"),
+    ("Slipv[m/s]", "slipv", 1.0, "%.20f"), ("Slipv1[m/s]", "slipv1", 1.0, "%.20f"),
+    ("Slipv2[m/s]", "slipv2", 1.0, "%.20f"), ("a", "a", 1.0, "%f"), ("b", "b", 1.0, "%f"),
+    ("a-b", "a-b", 1.0, "%f"), ("dc", "dc", 1.0, "%f"), ("fric", "fric", 1.0, "%f"),
+    ("slip", "slip", 1.0, "%.20f"), ("slip1", "slip1", 1.0, "%.20f"), ("slip2", "slip2", 1.0, "%.20f"))
+
+
+def write_vtk(fname: str, nodes: np.ndarray, tris: np.ndarray, fields: dict) -> None:
+    """Legacy ASCII VTK unstructured grid of triangles with the snapshot's
+    cell fields (host arrays; ``fields`` keyed by the state names of
+    VTK_FIELDS, ``a-b`` derived when absent, ``P`` zero when absent)."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    tris = np.asarray(tris, dtype=np.int64)
+    N = tris.shape[0]
+    f = dict(fields)
+    f.setdefault("P", np.zeros(N))
+    if "a-b" not in f:
+        f["a-b"] = np.asarray(f["a"]) - np.asarray(f["b"])
+    with open(fname, "w") as out:
+        out.write("# vtk DataFile Version 3.0\ntest\nASCII\nDATASET  UNSTRUCTURED_GRID\n")
+        out.write("POINTS %d float\n" % nodes.shape[0])
+        np.savetxt(out, nodes, fmt="%f")
+        out.write("CELLS %d %d\n" % (N, 4 * N))
+        np.savetxt(out, np.column_stack([np.full(N, 3), tris - 1]), fmt="%d")
+        out.write("CELL_TYPES %d\n" % N)
+        out.write("5 " * N + "\n")
+        out.write("CELL_DATA %d " % N)
+        for name, key, scale, fmt in VTK_FIELDS:
+            out.write("SCALARS %s float\nLOOKUP_TABLE default\n" % name)
+            vals = np.asarray(f[key], dtype=np.float64) * scale
+            out.write(" ".join(fmt % v for v in vals) + " \n")
+
+
+def read_vtk_cell_data(fname: str) -> dict:
+    """The SCALARS blocks of a file written by :func:`write_vtk` (for checks)."""
+    out = {}
+    lines = open(fname).read().split("\n")
+    for i, line in enumerate(lines):
+        if "SCALARS " in line:        # the first one shares its line with CELL_DATA, as the reference writes it
+            out[line.split("SCALARS ")[1].split()[0]] = np.array([float(v) for v in lines[i + 2].split()])
+    return out

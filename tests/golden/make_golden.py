@@ -196,7 +196,7 @@ Actively shearing zone thickness: 3e-3
 Effective compressibility: 8e-11
 Constant porepressure: 2
 Initial porepressure: 2
-Half space: False
+Half space: {half}
 Fix_Tn:False
 ssv_scale: 1.0
 ssh1_scale: 1.6
@@ -220,10 +220,10 @@ Plate loading rate: 1e-9
 RHO = MU / 3464.0 ** 2  # cs = 3.464 km/s
 
 
-def reference_sim(QDsim_gpu, nodes, tris, table, workdir):
+def reference_sim(QDsim_gpu, nodes, tris, table, workdir, half=False):
     core = os.path.join(workdir, "core")
     with open(os.path.join(workdir, "parameter.txt"), "w") as f:
-        f.write(PARAM_TXT.format(core=core, lam=LAM, mu=MU, rho=RHO))
+        f.write(PARAM_TXT.format(core=core, lam=LAM, mu=MU, rho=RHO, half="True" if half else "False"))
     mesh.write_parameter_file(os.path.join(workdir, "cells.dat"), table)
     cwd = os.getcwd()
     os.chdir(workdir)
@@ -278,6 +278,95 @@ def main_hmatrix_only():
     hm = make_hmatrix_golden(nodes, tris, mini_leaf=32)
     np.savez_compressed(os.path.join(HERE, "hmatrix_small.npz"), **hm)
     print("hmatrix_small.npz: %d leaf blocks, %d ACA" % (len(hm["row_ptr"]) - 1, int(hm["aca"].sum())))
+
+
+def dipping_fault(dip_deg=60.0):
+    """8 x 4 km planar fault dipping dip_deg, 1 km cells, top edge on the free
+    surface -> N = 64."""
+    nodes, tris = mesh.planar_fault(8.0, 4.0, 8, 4)
+    nodes = nodes.copy()
+    nodes[:, 1] = nodes[:, 2] / np.tan(np.radians(dip_deg))
+    return nodes, tris
+
+
+def _hs_reference_ops(lib, nodes, tris, ev, xg):
+    """Dense half-space traction operators from the reference C++
+    TDstressFS_C (jud_halfspace), projected as QDsim_gpu.GetTtstress does."""
+    N = tris.shape[0]
+    X, Y, Z = (np.ascontiguousarray(xg[:, q]) for q in range(3))
+    cpp = {k: np.zeros((N, N)) for k in ("A1s", "A2s", "Bs", "A1d", "A2d", "Bd")}
+    for j in range(N):
+        P = [np.ascontiguousarray(nodes[tris[j, q] - 1]) for q in range(3)]
+        for sl, (Ss, Ds) in (("s", (1.0, 0.0)), ("d", (0.0, 1.0))):
+            st = np.zeros((N, 6))
+            sn = np.zeros((N, 6))
+            lib.TDstressFS_C(_ptr(X), _ptr(Y), _ptr(Z), N, _ptr(P[0]), _ptr(P[1]), _ptr(P[2]), Ss, Ds, 0.0, MU, LAM,
+                             True, _ptr(st), _ptr(sn))
+            S = np.stack([np.stack([st[:, 0], st[:, 3], st[:, 4]], 1), np.stack([st[:, 3], st[:, 1], st[:, 5]], 1),
+                          np.stack([st[:, 4], st[:, 5], st[:, 2]], 1)], 1)
+            t = np.einsum("nij,nj->ni", S, ev[:, 6:9])
+            cpp["A1" + sl][:, j] = np.einsum("ni,ni->n", t, ev[:, 0:3])
+            cpp["A2" + sl][:, j] = np.einsum("ni,ni->n", t, ev[:, 3:6])
+            cpp["B" + sl][:, j] = np.einsum("ni,ni->n", t, ev[:, 6:9])
+    return cpp
+
+
+def main_halfspace_only():
+    """Half-space dense operators: a dipping fault reaching the surface, from
+    the reference's own dense path (QDsim_gpu.get_coreAB_mulproess with
+    "Half space: True", NumPy GF) and from the reference C++ TDstressFS_C
+    (jud_halfspace); and a rough vertical fault reaching the surface (C++),
+    whose near-vertical sides make the formula ill-conditioned."""
+    lib = load_ref_lib()
+    QDsim_gpu = import_reference_python()
+    nodes, tris = dipping_fault()
+    _, xg = mesh.element_frames(nodes, tris)
+    table = mesh.friction_table(xg, 8e3, 4e3, v_nuc=1e-3, seed=0)
+    out = {"nodes": nodes, "tris": tris, "mu": MU, "lam": LAM}
+    with tempfile.TemporaryDirectory() as td:
+        sim = reference_sim(QDsim_gpu, nodes, tris, table, td, half=True)
+        for k in ("A1s", "A2s", "Bs", "A1d", "A2d", "Bd"):
+            out["py_" + k] = getattr(sim, k)
+        ev, xgr = sim.eleVec, sim.xg
+    cpp = _hs_reference_ops(lib, nodes, tris, ev, xgr)
+    for k, v in cpp.items():
+        out["cpp_" + k] = v
+    d = max(np.abs(out["py_" + k] - cpp[k]).max() / np.abs(cpp[k]).max() for k in cpp)
+    # rough vertical fault, 6 x 3 km, 0.75 km cells -> N = 64, top edge at z = 0
+    rn, rt = mesh.rough_fault(6.0, 3.0, 8, 4, seed=3)
+    frames, rxg = mesh.element_frames(rn, rt)
+    for k, v in _hs_reference_ops(lib, rn, rt, frames, rxg).items():
+        out["rough_cpp_" + k] = v
+    out["rough_nodes"], out["rough_tris"] = rn, rt
+    # 40-digit values of the 8 entries where the oracle and the reference C++
+    # disagree most (ill-conditioned pairs): the yardstick for FP64 evaluations
+    import oracle
+    from pyquake3d_gb300.gf import join_ops
+    from tests.hs_highprec import fsc_strain
+    ref = join_ops({k: out["rough_cpp_" + k] for k in oracle.OPS})
+    orc = join_ops(dict(zip(oracle.OPS, oracle.assemble_dense(rn, rt, MU, LAM, halfspace=True))))
+    idx = np.argsort(np.abs(orc - ref).ravel())[-8:]
+    vals = []
+    for flat in idx:
+        r, c = divmod(int(flat), ref.shape[1])
+        i, j, comp, slip = r // 3, c // 2, r % 3, c % 2
+        P = [rn[rt[j, q] - 1] for q in range(3)]
+        x = rxg[i]
+        Ss, Ds = (1.0, 0.0) if slip == 0 else (0.0, 1.0)
+        X = (x[:1].copy(), x[1:2].copy(), x[2:3].copy())
+        _, e_fs = oracle.tdstress(*X, *P, Ss, Ds, 0.0, MU, LAM, False)
+        Q = [np.array([p[0], p[1], -p[2]]) for p in P]
+        _, e_im = oracle.tdstress(*X, *Q, Ss, Ds, 0.0, MU, LAM, False)
+        e = e_fs[0] + e_im[0] + fsc_strain(*P, Ss, Ds, 0.0, x)
+        tr = e[0] + e[1] + e[2]
+        S = 2 * MU * np.array([[e[0], e[3], e[4]], [e[3], e[1], e[5]], [e[4], e[5], e[2]]]) + LAM * tr * np.eye(3)
+        n = frames[i, 6:9]
+        t = S @ n
+        vals.append([t @ frames[i, 0:3], t @ frames[i, 3:6], t @ n][comp])
+    out["rough_true_idx"] = idx.astype(np.int64)
+    out["rough_true_val"] = np.array(vals)
+    np.savez_compressed(os.path.join(HERE, "hs_dense_small.npz"), **out)
+    print("hs_dense_small.npz: N = %d, reference NumPy vs C++ max rel %.2e" % (tris.shape[0], d))
 
 
 def main():
@@ -342,5 +431,7 @@ def main():
 if __name__ == "__main__":
     if "--hmatrix-only" in sys.argv:
         main_hmatrix_only()
+    elif "--halfspace-only" in sys.argv:
+        main_halfspace_only()
     else:
         main()

@@ -169,27 +169,45 @@ def test_halfspace_each_source_matches_reference_golden(cuda, golden):
     assert normwise_rel(g["each_h1_stress"], s) < 2e-8
 
 
-def test_halfspace_dense_assembly_matches_oracle(cuda):
-    """Dense half-space operator of a rough mesh whose top row of elements
-    touches the free surface, against the oracle (complex-step evaluation of
-    the same harmonic function).  Both are FP64 evaluations of a formula that
-    loses up to ~10 digits for sides within ~1e-3 rad of vertical; bar 1e-8
-    normwise, 5e-8 per receiver row (scaled by the full-space row)."""
-    nodes, tris = mesh.rough_fault(6.0, 3.0, 8, 4, seed=3)
-    assert nodes[:, 2].max() == 0.0
-    N = tris.shape[0]
-    K64, K32 = gf.assemble_dense(nodes, tris, MU, MU, halfspace=True, device=cuda)
-    Kfs, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
-    ref = gf.join_ops(dict(zip(oracle.OPS, oracle.assemble_dense(nodes, tris, MU, MU, halfspace=True))))
+def test_halfspace_dense_assembly_matches_reference(cuda, golden):
+    """Dense half-space operator of a 60-degree dipping fault whose top edge
+    lies on the free surface (N = 64) against the reference's own dense path
+    (QDsim_gpu.get_coreAB_mulproess with "Half space: True") and its C++
+    TDstressFS_C: normwise <= 1e-10; the FP32 copy <= 1e-6; the host-buffer
+    entry point gives the same bits."""
+    g = golden("hs_dense_small.npz")
+    nodes, tris = g["nodes"], g["tris"]
+    K64, K32 = gf.assemble_dense(nodes, tris, float(g["mu"]), float(g["lam"]), halfspace=True, device=cuda)
     got = K64.cpu().numpy()
-    fs = Kfs.cpu().numpy()
-    assert normwise_rel(ref, got) < 1e-8
-    for i in range(N):
-        r = slice(3 * i, 3 * i + 3)
-        assert np.linalg.norm(got[r] - ref[r]) / np.linalg.norm(fs[r]) < 5e-8, i
+    for src in ("py_", "cpp_"):
+        ref = gf.join_ops({k: g[src + k] for k in oracle.OPS})
+        assert normwise_rel(ref, got) < 1e-10, src
     assert normwise_rel(got, K32.double().cpu().numpy()) < 1e-6
-    # half-space differs from full-space (the surface matters on this mesh)
-    assert normwise_rel(fs, got) > 1e-3
-    # the host-buffer entry point gives the same bits
-    Kh, _ = gf.assemble_dense_host(nodes, tris, MU, MU, halfspace=True)
+    Kfs, _ = gf.assemble_dense(nodes, tris, float(g["mu"]), float(g["lam"]), fp32_copy=False, device=cuda)
+    assert normwise_rel(Kfs.cpu().numpy(), got) > 1e-3      # the free surface matters here
+    Kh, _ = gf.assemble_dense_host(nodes, tris, float(g["mu"]), float(g["lam"]), halfspace=True)
     assert np.array_equal(Kh.numpy(), got)
+
+
+def test_halfspace_rough_fault_against_reference(cuda, golden):
+    """Rough vertical fault reaching the surface (N = 64): many sides lie
+    within ~3e-4 rad of vertical, where the free-surface formula loses up to
+    ~13 digits in FP64 (the reference C++ itself is up to ~3e-3 of a pair's
+    strain off a 40-digit evaluation there, test_halfspace_cpu.py), so FP64
+    evaluations agree only to that noise: the oracle is 4.9e-8 (Frobenius)
+    from the reference, the GPU (FMA-contracted) 1.7e-7.  Bar 5e-7."""
+    g = golden("hs_dense_small.npz")
+    nodes, tris = g["rough_nodes"], g["rough_tris"]
+    assert nodes[:, 2].max() == 0.0
+    mu, lam = float(g["mu"]), float(g["lam"])
+    K64, _ = gf.assemble_dense(nodes, tris, mu, lam, halfspace=True, fp32_copy=False, device=cuda)
+    got = K64.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    ref = gf.join_ops({k: g["rough_cpp_" + k] for k in oracle.OPS})
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 5e-7
+    # at the 8 worst-conditioned entries (40-digit values in the golden) the
+    # GPU is in total no farther from the exact value than the reference is
+    idx, true = g["rough_true_idx"], g["rough_true_val"]
+    err_gpu = np.abs(got.ravel()[idx] - true).sum()
+    err_ref = np.abs(ref.ravel()[idx] - true).sum()
+    assert err_gpu <= err_ref, (err_gpu, err_ref)

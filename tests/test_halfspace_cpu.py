@@ -49,6 +49,17 @@ def test_oracle_halfspace_each_source(golden):
         assert normwise_rel(g["each_h1_strain"][j], e[j]) < (2e-8 if surf[j] else 1e-10), j
 
 
+def test_oracle_halfspace_dense_matches_reference(golden):
+    """The reference's own dense half-space operators (NumPy dense path and
+    C++) of a dipping fault reaching the surface."""
+    from pyquake3d_gb300.gf import join_ops
+    g = golden("hs_dense_small.npz")
+    got = join_ops(dict(zip(oracle.OPS, oracle.assemble_dense(g["nodes"], g["tris"], float(g["mu"]), float(g["lam"]),
+                                                              halfspace=True))))
+    for src in ("py_", "cpp_"):
+        assert normwise_rel(join_ops({k: g[src + k] for k in oracle.OPS}), got) < 1e-10, src
+
+
 def test_ill_conditioned_source_against_40_digits(golden):
     """A source with vertices on the free surface: the reference C++ and
     the oracle are both FP64 evaluations of a formula with heavy cancellation
@@ -132,3 +143,21 @@ def test_device_math_matches_oracle(host_check):
                 acc.extend([t @ e1, t @ e2, t @ n])
         scale = max(np.linalg.norm(tt), np.linalg.norm(t0))
         assert np.linalg.norm(res[i, 6:] - np.array(tt)) / scale < 1e-10, i
+
+
+def test_rough_fault_oracle_not_less_accurate_than_reference(golden):
+    """On the rough surface-reaching fault the oracle and the reference C++
+    disagree most on ill-conditioned pairs (near-vertical sides).  At those 8
+    entries the golden holds 40-digit values (tests/golden/make_golden.py):
+    the oracle's total distance to them is at most the reference's."""
+    from pyquake3d_gb300.gf import join_ops
+    g = golden("hs_dense_small.npz")
+    nodes, tris = g["rough_nodes"], g["rough_tris"]
+    ref = join_ops({k: g["rough_cpp_" + k] for k in oracle.OPS})
+    orc = join_ops(dict(zip(oracle.OPS, oracle.assemble_dense(nodes, tris, float(g["mu"]), float(g["lam"]),
+                                                              halfspace=True))))
+    idx, true = g["rough_true_idx"], g["rough_true_val"]
+    err_orc = np.abs(orc.ravel()[idx] - true)
+    err_ref = np.abs(ref.ravel()[idx] - true)
+    assert err_ref.max() > 1e-6 * np.abs(true).max()       # genuinely ill-conditioned entries
+    assert err_orc.sum() <= err_ref.sum()

@@ -122,3 +122,54 @@ def test_hmatrix_stepping_matches_dense(cuda, golden):
     alone = Ensemble(H, tabs[1:2], mu=MU, Cs=3464.0, precision="hmat", max_steps=30)
     alone.iterate(120)
     assert torch.equal(alone.t["slip1"][0], ens.t["slip1"][1])
+
+
+def test_hmatrix_save_load_roundtrip(cuda, tmp_path):
+    """The warm-start cache: an H-matrix written by save() and read back by
+    load() gives the same bits, and BlockTree.calc_Hmatrix_ACA(dir,
+    save_corefunc=True) writes and then reuses it."""
+    nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
+    N = tris.shape[0]
+    H = HMatrix(nodes, tris, MU, MU, min_size=32, mini_leaf=32, tol=1e-4, device=cuda)
+    H.save(str(tmp_path / "h.npz"))
+    H2 = HMatrix.load(str(tmp_path / "h.npz"), device=cuda)
+    X = torch.as_tensor(np.random.default_rng(0).standard_normal((2, 2 * N)), device=cuda)
+    assert torch.equal(H.apply(X), H2.apply(X))
+    assert H2.stats == H.stats
+    tree = createHmatrix(None, nodes, tris, None, {"Shear modulus": MU, "Lame constants": MU, "Half space": False},
+                         mini_leaf=32)
+    d = str(tmp_path / "core")
+    tree.calc_Hmatrix_ACA(d, save_corefunc=True)
+    assert os.path.exists(os.path.join(d, "hmatrix.npz"))
+    x = np.random.default_rng(1).standard_normal(N)
+    y1 = tree.blocks_process_MVM(x, None, "A1s")
+    tree2 = createHmatrix(None, nodes, tris, None, {"Shear modulus": MU, "Lame constants": MU, "Half space": False},
+                          mini_leaf=32)
+    tree2.calc_Hmatrix_ACA(d)
+    assert np.array_equal(tree2.blocks_process_MVM(x, None, "A1s"), y1)
+
+
+def test_hmatrix_halfspace_product_matches_dense(cuda):
+    """Half-space H-matrix (ACA on the half-space GF) of a 60-degree dipping
+    fault reaching the free surface, against the dense half-space FP64
+    operator (parity-checked against the reference in test_gf_gpu.py)."""
+    nodes, tris = mesh.planar_fault(24.0, 12.0, 40, 20)
+    nodes = nodes.copy()
+    nodes[:, 1] = nodes[:, 2] / np.tan(np.radians(60.0))
+    N = tris.shape[0]
+    H = HMatrix(nodes, tris, MU, MU, min_size=32, mini_leaf=32, tol=1e-4, device=cuda, halfspace=True)
+    assert H.stats["lowrank_blocks"] > 0
+    K64, _ = gf.assemble_dense(nodes, tris, MU, MU, halfspace=True, fp32_copy=False, device=cuda)
+    Kfs, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
+    X = torch.as_tensor(np.random.default_rng(0).standard_normal((2, 2 * N)), device=cuda)
+    Y = H.apply(X)
+    for r in range(2):
+        assert _rel(X[r] @ K64.T, Y[r]) < 1e-4, r
+        assert _rel(X[r] @ Kfs.T, Y[r]) > 1e-3     # not the full-space operator
+    tree = createHmatrix(None, nodes, tris, None, {"Shear modulus": MU, "Lame constants": MU, "Half space": "True"},
+                         mini_leaf=32)
+    tree.calc_Hmatrix_ACA()
+    x = np.random.default_rng(2).standard_normal(N)
+    y = tree.blocks_process_MVM(x, None, "Bd")
+    ref = (gf.split_ops(K64)["Bd"] @ torch.as_tensor(x, device=cuda)).cpu().numpy()
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-4
