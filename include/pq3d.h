@@ -149,7 +149,25 @@ typedef struct pq3d_dense_sim {
     /* scalars */
     double V0, Vpl, eta;   /* eta = mu / (2 cs) */
     int fix_Tn;
+    /* Pore-pressure dilatancy (src/QDsim_gpu.py:611-671), all NULL when off:
+     * P, dPdt [N] (Pa, Pa/s) enter the right-hand side; Parr [ndepth + 1][N]
+     * is the fault-normal pressure profile of every cell (row k = depth node
+     * k, the last row the fixed far-field value); dila = the table built by
+     * pq3d_dilatancy_table.  After every accepted step each cell takes one
+     * implicit diffusion step (tridiagonal, ndepth unknowns). */
+    int32_t ndepth;
+    double *P, *dPdt, *Parr;
+    const double *dila;
 } pq3d_dense_sim;
+
+/* Dilatancy table for pq3d_dense_sim.dila from the depth nodes z[ndepth + 1]
+ * (the reference's zp = log(1 + yp / 1e-2), yp logspace(-3, 10, 60)) and the
+ * parameter-file values (hydraulic diffusivity c_hyd, dilatancy coefficient,
+ * shear-zone thickness, effective compressibility, far-field pressure P0 in
+ * Pa).  out[pq3d_dilatancy_table_len(ndepth)] (host memory). */
+size_t pq3d_dilatancy_table_len(int ndepth);
+int pq3d_dilatancy_table(const double *z, int ndepth, double c_hyd, double dilatancy, double thickness,
+                         double compressibility, double P0, double *out);
 
 /* Device control block of the stepper (one per simulation, device memory).
  * The host writes dttry/time/status before the first step; the stepper clears

@@ -9,6 +9,9 @@ Followed line by line (reference file:line):
   * right-hand side                      src/QDsim_gpu.py:772-828 (derivative)
   * Dormand-Prince 5(4) attempt          src/QDsim_gpu.py:1266-1397
   * step control and state update        src/QDsim_gpu.py:1029-1122 (simu_forward)
+  * pore-pressure dilatancy (optional)   src/QDsim_gpu.py:332-349 (set-up), 611-626
+                                         (Calc_Pmatrix), 628-671 (Calc_P_implicit, after
+                                         every accepted step, 1119-1120)
 
 Quirks kept on purpose: the traction product K.(V - Vpl) and the slip rate in
 the aging law are frozen at the step start; 7 right-hand-side evaluations per
@@ -58,7 +61,11 @@ class DenseStepper:
     (row = receiver, column = source).  table: (N, 10) per-cell table.
     """
 
-    def __init__(self, K, table, *, mu, density, V0=1e-6, Vpl=1e-9, fix_Tn=False):
+    def __init__(self, K, table, *, mu, density, V0=1e-6, Vpl=1e-9, fix_Tn=False, dilatancy=None):
+        """dilatancy: None, or dict with the parameter-file values 'Dilatancy
+        coefficient', 'Hydraulic diffusivity', 'Actively shearing zone
+        thickness', 'Effective compressibility', 'Constant porepressure' and
+        'Initial porepressure' (MPa)."""
         self.K = K
         self.mu = float(mu)
         self.Cs = np.sqrt(self.mu / float(density))
@@ -68,12 +75,70 @@ class DenseStepper:
         N = table.shape[0]
         self.P = np.zeros(N)
         self.dPdt0 = np.zeros(N)
+        self.Ifdila = dilatancy is not None
+        if self.Ifdila:
+            self._setup_dilatancy(dilatancy, N)
         self.slipvC = np.ones(N) * self.Vpl_con
         self.time = 0.0
         self._read_parameter(table)
         self.slip1 = np.zeros(N)
         self.slip2 = np.zeros(N)
         self.slip = np.zeros(N)
+
+    # src/QDsim_gpu.py:332-349, 161-165
+    def _setup_dilatancy(self, d, N):
+        self.DilatancyC = float(d["Dilatancy coefficient"])
+        self.Chyd = float(d["Hydraulic diffusivity"])
+        self.hs = float(d["Actively shearing zone thickness"])
+        self.EPermeability = float(d["Effective compressibility"])
+        c = 1e-2
+        num = 60
+        self.P0 = float(d["Constant porepressure"]) * 1e6
+        self.P = np.ones(N) * float(d["Initial porepressure"]) * 1e6
+        yp = np.logspace(start=-3, stop=10, num=num, base=10)
+        self.zp = np.log(1 + yp / c)
+        self.Parr = np.ones([N, num]) * float(d["Initial porepressure"]) * 1e6
+        self.Pmatrix = np.zeros([num, num])
+        self._calc_pmatrix()
+
+    # src/QDsim_gpu.py:611-626
+    def _calc_pmatrix(self):
+        K = len(self.zp)
+        z = self.zp
+        c = self.Chyd
+        dz = np.diff(self.zp)
+        for i in range(K - 1):
+            if i == 0:
+                self.Pmatrix[0, 0] = c * (np.exp(-(2 * z[0] - dz[0] / 2)) + np.exp(-(2 * z[0] + dz[0] / 2))) / (dz[0] * dz[0])
+                self.Pmatrix[0, 1] = -c * (np.exp(-(2 * z[0] - dz[0] / 2)) + np.exp(-(2 * z[0] + dz[0] / 2))) / (dz[0] * dz[0])
+            else:
+                self.Pmatrix[i, i] = c * (np.exp(-(2 * z[i] - dz[i] / 2)) + np.exp(-(2 * z[i] + dz[i] / 2))) / (dz[i] * dz[i])
+                self.Pmatrix[i, i + 1] = -c * np.exp(-(2 * z[i] + dz[i] / 2)) / (dz[i] * dz[i])
+                self.Pmatrix[i, i - 1] = -c * np.exp(-(2 * z[i] - dz[i] / 2)) / (dz[i] * dz[i])
+
+    # src/QDsim_gpu.py:628-671: one implicit step of the fault-normal pore
+    # pressure diffusion per cell, flux from the dilatant state evolution
+    def calc_p_implicit(self, dt):
+        from scipy.linalg import lu_factor, lu_solve
+        e, h, beta, c_hyd, dc, z = self.DilatancyC, self.hs, self.EPermeability, self.Chyd, self.dc, self.zp
+        dz = np.diff(z)
+        K = len(z)
+        dt = float(dt)
+        M = self.Pmatrix[:-1, :-1] * dt + np.eye(K - 1)
+        lu, piv = lu_factor(M)
+        theta = self.dc / self.V0 * np.exp((self.state - self.f0) / self.b)
+        dthetadt = 1.0 - self.slipv * theta / dc
+        g = -e * h / (2.0 * beta * c_hyd * theta) * dthetadt
+        for i in range(self.Tno.shape[0]):
+            b = np.copy(self.Parr[i, :-1])
+            b[0] = b[0] - 2.0 * c_hyd * np.exp(-(z[0] - dz[0] / 2)) * g[i] * dt / dz[0]
+            b[-1] = b[-1] + dt / (dz[-1] * dz[-1]) * c_hyd * np.exp(-(z[-2] - dz[-1] / 2)) * self.P0
+            x = lu_solve((lu, piv), b)
+            self.Parr[i, :-1] = np.copy(x)
+            term1 = -np.exp(-(z[0] - dz[0] / 2)) * (self.Parr[i, 0] - self.Parr[i, 1] + 2 * dz[0] * g[i] * np.exp(z[0]))
+            term2 = np.exp(-(z[0] + dz[0] / 2)) * (self.Parr[i, 1] - self.Parr[i, 0])
+            self.dPdt0[i] = c_hyd * np.exp(-z[0]) * (term1 + term2) / dz[0] ** 2
+            self.P[i] = self.Parr[i, 0]
 
     # src/QDsim_gpu.py:714-770
     def _read_parameter(self, values):
@@ -203,6 +268,8 @@ class DenseStepper:
             if h < 1.e-15 or nrjct > 20:
                 raise StepFailure("dt is too small")
         self.accept(h, Tno_y, Tt1o_y, Tt2o_y, state_y)
+        if self.Ifdila:
+            self.calc_p_implicit(h)
         return h, dtnext, nrjct + 1
 
     def accept(self, h, Tno_y, Tt1o_y, Tt2o_y, state_y):

@@ -20,7 +20,7 @@ raises :class:`StepError`.
 
 Supported inputs: per-cell parameter files (``InputHetoparamter: True``,
 layout of src/QDsim_gpu.py:714-770), full- or half-space (``Half space``),
-no dilatancy.  Other
+pore-pressure dilatancy (``If Dilatancy``; dense stepper).  Other
 parameter-file options raise ``NotImplementedError`` rather than silently
 computing something else.
 """
@@ -93,11 +93,24 @@ STATE_FIELDS = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "ra
 PARAM_FIELDS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "rake0")
 
 
+DILATANCY_KEYS = ("Dilatancy coefficient", "Hydraulic diffusivity", "Actively shearing zone thickness",
+                  "Effective compressibility", "Constant porepressure", "Initial porepressure")
+
+
+def dilatancy_depths(num=60, c=1e-2):
+    """Fault-normal nodes of the pore-pressure profile (src/QDsim_gpu.py:342-343)."""
+    yp = np.logspace(start=-3, stop=10, num=num, base=10)
+    return np.log(1 + yp / c)
+
+
 class DenseDeviceSim:
     """Device state of one dense simulation + the launch structure of
-    ``pq3d_dense_step``.  ``K`` is the (3N, 2N) FP64 or FP32 operator."""
+    ``pq3d_dense_step``.  ``K`` is the (3N, 2N) FP64 or FP32 operator.
+    ``dilatancy``: None, or a dict of the parameter-file values
+    (DILATANCY_KEYS, pressures in MPa) -- pore pressure P (initial value,
+    also in ``init``'s initial state) and the per-cell diffusion profile."""
 
-    def __init__(self, K, init, *, mu, Cs, V0, Vpl, fix_Tn=False, dttry=1e-3, device=None):
+    def __init__(self, K, init, *, mu, Cs, V0, Vpl, fix_Tn=False, dttry=1e-3, device=None, dilatancy=None):
         self.device = K.device if device is None else device
         N = K.shape[1] // 2
         self.N = N
@@ -126,6 +139,23 @@ class DenseDeviceSim:
             raise TypeError("operator must be float64 or float32")
         S.ctrl = self.ctrl_t.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = self.V0, self.Vpl, self.eta, int(self.fix_Tn)
+        if dilatancy is not None:
+            L = _lib.load()
+            z = dilatancy_depths()
+            nd = len(z) - 1
+            P0 = float(dilatancy["Constant porepressure"]) * 1e6
+            Pin = float(dilatancy["Initial porepressure"]) * 1e6
+            tab = np.zeros(L.pq3d_dilatancy_table_len(nd))
+            _lib.check(L.pq3d_dilatancy_table(z.ctypes.data, nd, float(dilatancy["Hydraulic diffusivity"]),
+                                              float(dilatancy["Dilatancy coefficient"]),
+                                              float(dilatancy["Actively shearing zone thickness"]),
+                                              float(dilatancy["Effective compressibility"]), P0, tab.ctypes.data))
+            self.t["dila"] = torch.as_tensor(tab, device=dev)
+            self.t["P"] = torch.full((N,), Pin, dtype=f64, device=dev)
+            self.t["dPdt"] = torch.zeros(N, dtype=f64, device=dev)
+            self.t["Parr"] = torch.full((nd + 1, N), Pin, dtype=f64, device=dev)   # [depth node][cell]
+            S.ndepth = nd
+            S.P, S.dPdt, S.Parr, S.dila = (self.t[k].data_ptr() for k in ("P", "dPdt", "Parr", "dila"))
         self.S = S
 
     def set_ctrl(self, dttry, time):
@@ -193,8 +223,6 @@ class QDsim:
         self.Vpl_con = float(P["Plate loading rate"])
         if not self.InputHetoparamter:
             raise NotImplementedError("only per-cell parameter files (InputHetoparamter: True) are supported")
-        if self.Ifdila:
-            raise NotImplementedError("pore-pressure dilatancy coupling is not supported")
         self.device = torch.device(device) if device is not None else torch.device("cuda")
         self.operator_dtype = operator_dtype
         self.read_parameter(P["Inputparamter file"])
@@ -204,7 +232,10 @@ class QDsim:
         path = fname if os.path.isabs(fname) else os.path.join(self.dirname, fname)
         values = np.loadtxt(path, ndmin=2)
         N = self.eleVec.shape[0]
-        self.init = initial_state(values[:N], self.V0, self.Vpl_con)
+        # pore pressure (Pa): the initial value with dilatancy, else 0 (src/QDsim_gpu.py:332-348)
+        self.dilatancy = {k: float(self.Para0[k]) for k in DILATANCY_KEYS} if self.Ifdila else None
+        self.P = np.ones(N) * self.dilatancy["Initial porepressure"] * 1e6 if self.Ifdila else np.zeros(N)
+        self.init = initial_state(values[:N], self.V0, self.Vpl_con, P=self.P)
         for k, v in self.init.items():
             setattr(self, k, v.copy())
         self.maxslipv0 = np.max(self.slipv)
@@ -234,7 +265,7 @@ class QDsim:
     def initGPUvariable(self):
         K = self.K64 if self.operator_dtype == torch.float64 else self.K32
         self.dev = DenseDeviceSim(K, self.init, mu=self.mu, Cs=self.Cs, V0=self.V0, Vpl=self.Vpl_con,
-                                  fix_Tn=self.fix_Tn, dttry=self.htry, device=self.device)
+                                  fix_Tn=self.fix_Tn, dttry=self.htry, device=self.device, dilatancy=self.dilatancy)
         for k, v in self.dev.t.items():
             setattr(self, k + "_gpu", v)
 

@@ -45,7 +45,8 @@ class DenseSim(ctypes.Structure):
                                  "slipv1", "slipv2", "slipv", "rake", "slip1", "slip2", "slip", "Tt", "fric",
                                  "a", "b", "dc", "f0", "shear_loading", "normal_loading", "rake0",
                                  "rates", "vprime", "cand", "K64", "K32", "ctrl")] + \
-        [("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", c_int)]
+        [("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", c_int), ("ndepth", ctypes.c_int32)] + \
+        [(n, c_void_p) for n in ("P", "dPdt", "Parr", "dila")]
 
 
 class RunCtrl(ctypes.Structure):
@@ -105,6 +106,8 @@ _SIGS = {
     "pq3d_dense_matvec_f64": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_matvec_f32": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_dense_step": (c_int, [ctypes.POINTER(DenseSim), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pq3d_dilatancy_table_len": (c_size, [c_int]),
+    "pq3d_dilatancy_table": (c_int, [c_void_p, c_int, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_void_p]),
     "pq3d_batch_operator_bytes": (c_size, [c_i64]),
     "pq3d_batch_pack_operator": (c_int, [c_void_p, c_i64, c_void_p, c_void_p]),
     "pq3d_batch_rhs_bytes": (c_size, [c_i64, c_int]),

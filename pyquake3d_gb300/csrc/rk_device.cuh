@@ -1,8 +1,9 @@
 // Rate-and-state right-hand side and one Dormand-Prince 5(4) attempt of one
 // cell, shared by the single-simulation and the batched steppers.
 //
-// Reference: src/QDsim_gpu.py:830-891 (derivative_gpu), 1128-1262
-// (RungeKutte_solve_Dormand_Prince_gpu); pore pressure is zero (dilatancy off).
+// Reference: src/QDsim_gpu.py:772-828 (derivative, with the pore pressure P
+// and its rate dPdt of the dilatancy model; both zero when it is off),
+// 830-891 (derivative_gpu), 1128-1262 (RungeKutte_solve_Dormand_Prince_gpu).
 #pragma once
 
 #include <math.h>
@@ -23,11 +24,12 @@ constexpr double B81 = 5179. / 57600., B83 = 7571. / 16695., B84 = 393. / 640., 
 constexpr double kRelTol = 1e-4;
 
 // ---------------------------------------------------------------------------
-// right-hand side of one cell (src/QDsim_gpu.py:830-891), pore pressure 0
+// right-hand side of one cell (src/QDsim_gpu.py:772-828)
 
 struct Cell {
     double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
     double inv_a, inv_b, bdc;   // 1/a, 1/b, b/dc (used by the mixed-precision right-hand side)
+    double P, dPdt;             // pore pressure (Pa) and its rate (Pa/s); 0 without dilatancy
 };
 
 __device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
@@ -35,7 +37,7 @@ __device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0
 __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
                                     double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
 {
-    const double Tn = Tno * 1e6, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
+    const double Tn = Tno * 1e6 - c.P, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;   // effective normal stress
     const double es = exp(clip700(-state / c.a));
     const double aTn = c.a * Tn;
     const double x1 = clip700(T1 / aTn), x2 = clip700(T2 / aTn);
@@ -50,8 +52,9 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     const double dV1dstate = -2 * V0 / c.a * es * sh1;
     const double dV2dstate = -2 * V0 / c.a * es * sh2;
     dstate = c.b / c.dc * (V0 * exp(clip700((c.f0 - state) / c.b)) - c.slipv);
-    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * c.dsig + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
-    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * c.dsig + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    const double ds = c.dsig - c.dPdt;
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
     dsig = c.dsig / 1e6;
     dtau1 = t1 / 1e6;
     dtau2 = t2 / 1e6;
@@ -79,7 +82,7 @@ __device__ __forceinline__ double fexp(double x)
 __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
                                           double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
 {
-    const double Tn = Tno * 1e6, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
+    const double Tn = Tno * 1e6 - c.P, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
     const double inv_aTn = 1.0 / (c.a * Tn);
     const double x1 = clip700(T1 * inv_aTn), x2 = clip700(T2 * inv_aTn);
     const double sp = clip700(-state * c.inv_a);
@@ -93,8 +96,9 @@ __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, 
     const double dV1dstate = -twoV0 * c.inv_a * (0.5 * (e1p - e1m));
     const double dV2dstate = -twoV0 * c.inv_a * (0.5 * (e2p - e2m));
     dstate = c.bdc * (V0 * fexp((c.f0 - state) * c.inv_b) - c.slipv);
-    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * c.dsig + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
-    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * c.dsig + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    const double ds = c.dsig - c.dPdt;
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
     dsig = c.dsig * 1e-6;
     dtau1 = t1 * 1e-6;
     dtau2 = t2 * 1e-6;

@@ -140,11 +140,71 @@ __global__ void __launch_bounds__(256) matvec_kernel(const void *__restrict__ K,
     }
 }
 
+// ---------------------------------------------------------------------------
+// pore-pressure dilatancy (src/QDsim_gpu.py:611-671)
+
+constexpr int kMaxDepth = 64;   // tridiagonal unknowns per cell (the reference uses 59)
+
+// table layout (pq3d_dilatancy_table): lower, diag, upper of the diffusion
+// matrix (n each; M = dt * this + I), then the scalars below
+enum DilaScalar { D_BC0, D_BCN, D_G, D_T1, D_T2, D_TG, D_DP, D_NSCAL };
+
+// One implicit step for every cell of this thread (called by all threads of
+// every block with the same h): the Thomas factorisation of M is formed once
+// per block in shared memory (M is diagonally dominant by rows, so no
+// pivoting is needed; the reference factorises with partial pivoting).
+__device__ __noinline__ void dilatancy_step(const pq3d_dense_sim &S, double h, double *cp, double *inv)
+{
+    const int n = S.ndepth;
+    const double *lo = S.dila, *di = lo + n, *up = di + n, *sc = up + n;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double prev = 0.0;
+        for (int k = 0; k < n; ++k) {
+            const double den = (1.0 + di[k] * h) - (k ? lo[k] * h * prev : 0.0);
+            inv[k] = 1.0 / den;
+            prev = (k + 1 < n) ? up[k] * h * inv[k] : 0.0;
+            cp[k] = prev;
+        }
+    }
+    __syncthreads();
+    const int64_t N = S.N;
+    const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += gsz) {
+        const double theta = S.dc[i] / S.V0 * exp((S.state[i] - S.f0[i]) / S.b[i]);
+        const double dthetadt = 1.0 - S.slipv[i] * theta / S.dc[i];
+        const double g = -sc[D_G] / theta * dthetadt;
+        double *col = S.Parr + i;   // Parr[k * N + i]
+        // forward sweep: d'_k into Parr
+        double dprev = 0.0;
+        for (int k = 0; k < n; ++k) {
+            double b = col[k * N];
+            if (k == 0) b -= sc[D_BC0] * g * h;
+            if (k == n - 1) b += h * sc[D_BCN];
+            const double d = (b - (k ? lo[k] * h * dprev : 0.0)) * inv[k];
+            col[k * N] = d;
+            dprev = d;
+        }
+        // back substitution
+        double x = dprev;
+        for (int k = n - 2; k >= 0; --k) {
+            x = col[k * N] - cp[k] * x;
+            col[k * N] = x;
+        }
+        const double x0 = col[0], x1 = col[N];
+        const double term1 = -sc[D_T1] * (x0 - x1 + sc[D_TG] * g);
+        const double term2 = sc[D_T2] * (x1 - x0);
+        S.dPdt[i] = sc[D_DP] * (term1 + term2);
+        S.P[i] = x0;
+    }
+}
+
 template <bool kF32>
 __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist,
                                                          const double *h_force)
 {
     __shared__ double red[8];
+    __shared__ double dil_cp[kMaxDepth], dil_inv[kMaxDepth];
     pq3d_step_ctrl *C = S.ctrl;
     const int64_t N = S.N;
     const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
@@ -191,7 +251,8 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             double m1 = 0.0, m2 = 0.0;
             for (int64_t i = gtid; i < N; i += gsz) {
                 Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
-                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2], 0.0, 0.0, 0.0};
+                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2], 0.0, 0.0, 0.0,
+                       S.P ? S.P[i] : 0.0, S.dPdt ? S.dPdt[i] : 0.0};
                 const double y[4] = {S.Tno[i], S.Tt1o[i], S.Tt2o[i], S.state[i]};
                 double yo[4], e1, e2;
                 dp_attempt(c, S.V0, S.eta, h, y, yo, e1, e2);
@@ -249,13 +310,16 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             const double s1 = S.slip1[i] + v1 * h, s2 = S.slip2[i] + v2 * h;
             S.slip1[i] = s1; S.slip2[i] = s2;
             S.slip[i] = sqrt(s1 * s1 + s2 * s2);
-            S.fric[i] = S.Tt[i] / Tno;
+            S.fric[i] = S.P ? S.Tt[i] / (Tno - S.P[i] * 1e-6) : S.Tt[i] / Tno;   // pressure before its update
             const double w1 = v1 - S.Vpl * cos(S.rake0[i]), w2 = v2 - S.Vpl * sin(S.rake0[i]);
             if (kF32) vs[i] = split_v(w1, w2);
             else vp[i] = make_double2(w1, w2);
         }
         vmax = block_max(vmax, red);
         if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, dbits(vmax));
+        // (3b) pore-pressure diffusion of every cell with the new state and
+        // slip rate (src/QDsim_gpu.py:628-671, after the update 1119-1120)
+        if (S.Parr) dilatancy_step(S, h, dil_cp, dil_inv);
         time = time + h;
         dttry = dtnext;
         if (lead) {
@@ -271,6 +335,50 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
         C->maxv = __longlong_as_double((long long)C->maxv_bits);
     }
 }
+
+}  // namespace step
+}  // namespace pq3d
+
+extern "C" size_t pq3d_dilatancy_table_len(int ndepth) { return ndepth > 0 ? (size_t)3 * ndepth + pq3d::step::D_NSCAL : 0; }
+
+// The reference's matrix (src/QDsim_gpu.py:611-626) and right-hand-side
+// constants (628-671) for depth nodes z[0..ndepth].
+extern "C" int pq3d_dilatancy_table(const double *z, int ndepth, double c_hyd, double dilatancy, double thickness,
+                                    double compressibility, double P0, double *out)
+{
+    using namespace pq3d;
+    using namespace pq3d::step;
+    clear_error();
+    PQ3D_REQUIRE(z && out && ndepth >= 2 && ndepth <= kMaxDepth, "pq3d_dilatancy_table: bad arguments (ndepth %d)",
+                 ndepth);
+    const int n = ndepth;
+    double *lo = out, *di = lo + n, *up = di + n, *sc = up + n;
+    for (int i = 0; i < n; ++i) {
+        const double dz = z[i + 1] - z[i];
+        const double em = exp(-(2 * z[i] - dz / 2)), ep = exp(-(2 * z[i] + dz / 2));
+        if (i == 0) {
+            di[0] = c_hyd * (em + ep) / (dz * dz);
+            up[0] = -c_hyd * (em + ep) / (dz * dz);
+            lo[0] = 0.0;
+        } else {
+            di[i] = c_hyd * (em + ep) / (dz * dz);
+            up[i] = (i + 1 < n) ? -c_hyd * ep / (dz * dz) : 0.0;
+            lo[i] = -c_hyd * em / (dz * dz);
+        }
+    }
+    const double dz0 = z[1] - z[0], dzl = z[n] - z[n - 1];
+    sc[D_BC0] = 2.0 * c_hyd * exp(-(z[0] - dz0 / 2)) / dz0;
+    sc[D_BCN] = 1.0 / (dzl * dzl) * c_hyd * exp(-(z[n - 1] - dzl / 2)) * P0;
+    sc[D_G] = dilatancy * thickness / (2.0 * compressibility * c_hyd);
+    sc[D_T1] = exp(-(z[0] - dz0 / 2));
+    sc[D_T2] = exp(-(z[0] + dz0 / 2));
+    sc[D_TG] = 2 * dz0 * exp(z[0]);
+    sc[D_DP] = c_hyd * exp(-z[0]) / (dz0 * dz0);
+    return PQ3D_OK;
+}
+
+namespace pq3d {
+namespace step {
 
 struct LaunchCfg {
     int device = -1;
@@ -338,6 +446,9 @@ extern "C" int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_
     PQ3D_REQUIRE(aligned16(sim->vprime) && aligned16(sim->cand) && aligned16(sim->K64 ? (const void *)sim->K64
                                                                                       : (const void *)sim->K32),
                  "pq3d_dense_step: vprime, cand and K must be 16-byte aligned");
+    if (sim->Parr)
+        PQ3D_REQUIRE(sim->P && sim->dPdt && sim->dila && sim->ndepth >= 2 && sim->ndepth <= kMaxDepth,
+                     "pq3d_dense_step: dilatancy needs P, dPdt, dila and 2 <= ndepth <= %d", kMaxDepth);
     if (nsteps == 0) return PQ3D_OK;
     const bool f32 = sim->K32 != nullptr;
     int grid = 0;

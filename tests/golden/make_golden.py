@@ -189,7 +189,7 @@ Shear modulus: {mu}
 Rock density: {rho}
 InputHetoparamter: True
 Inputparamter file: cells.dat
-If Dilatancy:False
+If Dilatancy:{dila}
 Dilatancy coefficient: 3e-4
 Hydraulic diffusivity: 1e-5
 Actively shearing zone thickness: 3e-3
@@ -220,10 +220,11 @@ Plate loading rate: 1e-9
 RHO = MU / 3464.0 ** 2  # cs = 3.464 km/s
 
 
-def reference_sim(QDsim_gpu, nodes, tris, table, workdir, half=False):
+def reference_sim(QDsim_gpu, nodes, tris, table, workdir, half=False, dila=False):
     core = os.path.join(workdir, "core")
     with open(os.path.join(workdir, "parameter.txt"), "w") as f:
-        f.write(PARAM_TXT.format(core=core, lam=LAM, mu=MU, rho=RHO, half="True" if half else "False"))
+        f.write(PARAM_TXT.format(core=core, lam=LAM, mu=MU, rho=RHO, half="True" if half else "False",
+                                 dila="True" if dila else "False"))
     mesh.write_parameter_file(os.path.join(workdir, "cells.dat"), table)
     cwd = os.getcwd()
     os.chdir(workdir)
@@ -369,6 +370,40 @@ def main_halfspace_only():
     print("hs_dense_small.npz: N = %d, reference NumPy vs C++ max rel %.2e" % (tris.shape[0], d))
 
 
+DILA = {"Dilatancy coefficient": 3e-4, "Hydraulic diffusivity": 1e-5, "Actively shearing zone thickness": 3e-3,
+        "Effective compressibility": 8e-11, "Constant porepressure": 2.0, "Initial porepressure": 2.0}
+
+
+def main_dilatancy_only():
+    """The reference CPU stepper with pore-pressure dilatancy (If Dilatancy:
+    True, the parameter values of PARAM_TXT) on the planar N=64 mesh: 200
+    accepted steps with checkpoints of the state, P and dPdt."""
+    QDsim_gpu = import_reference_python()
+    nodes, tris = mesh.planar_fault(8.0, 4.0, 8, 4)
+    _, xg = mesh.element_frames(nodes, tris)
+    table = mesh.friction_table(xg, 8e3, 4e3, v_nuc=3e-2, seed=0)   # fast nucleation: dilatant weakening
+    out = {"nodes": nodes, "tris": tris, "table": table, "mu": MU, "rho": RHO}
+    for k, v in DILA.items():
+        out["dila_" + k.replace(" ", "_")] = v
+    with tempfile.TemporaryDirectory() as td:
+        sim = reference_sim(QDsim_gpu, nodes, tris, table, td, dila=True)
+        out["P_init"] = np.array(sim.P)
+        out["state_init"] = np.array(sim.state)
+        hs, ts = [], []
+        dttry = sim.htry
+        for i in range(200):
+            h, dttry = sim.simu_forward(dttry)
+            hs.append(h)
+            ts.append(sim.time)
+            if (i + 1) in (1, 10, 50, 100, 200):
+                for k in ("Tno", "Tt1o", "state", "slipv", "slip1", "P", "dPdt0"):
+                    out[f"s{i + 1}_{k}"] = np.array(getattr(sim, k))
+        out["h"], out["t"] = np.array(hs), np.array(ts)
+        out["Parr_200"] = np.array(sim.Parr)
+    np.savez_compressed(os.path.join(HERE, "traj_dila.npz"), **out)
+    print("traj_dila.npz: t_end = %.6e s, P range %.6e .. %.6e" % (ts[-1], out["s200_P"].min(), out["s200_P"].max()))
+
+
 def main():
     rng = np.random.default_rng(20251203)
     lib = load_ref_lib()
@@ -433,5 +468,7 @@ if __name__ == "__main__":
         main_hmatrix_only()
     elif "--halfspace-only" in sys.argv:
         main_halfspace_only()
+    elif "--dilatancy-only" in sys.argv:
+        main_dilatancy_only()
     else:
         main()

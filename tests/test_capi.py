@@ -37,7 +37,7 @@ def test_struct_layouts_match_header(tmp_path):
     fields = {"pq3d_batch_sim": ("BatchSim", ["N", "B", "precision", "Tno", "rates", "nsplit", "cand", "vop", "K",
                                               "ctrl", "V0", "eta", "fix_Tn", "N_total", "cell0"]),
               "pq3d_dense_sim": ("DenseSim", ["N", "Tno", "fric", "a", "rake0", "rates", "cand", "K64", "K32", "ctrl",
-                                              "V0", "eta", "fix_Tn"]),
+                                              "V0", "eta", "fix_Tn", "ndepth", "P", "Parr", "dila"]),
               "pq3d_run_ctrl": ("RunCtrl", ["h", "time", "attempts", "max_steps", "err2_bits", "status", "accepted"]),
               "pq3d_step_ctrl": ("StepCtrl", ["dttry", "status", "attempts", "err_slot", "maxv_bits", "bar_gen"]),
               "pq3d_hmat": ("HMat", ["N", "nblocks", "nleaves", "t_rows", "perm", "data", "t_blk", "leaf_blocks"])}

@@ -101,3 +101,21 @@ def test_oracle_step_failure_raises():
     st.state[:] = np.nan
     with pytest.raises(StepFailure):
         st.simu_forward(1e-3)
+
+
+def test_oracle_dilatancy_reproduces_reference_bitwise(golden):
+    """Pore-pressure dilatancy: the oracle's stepping (with its implicit
+    pressure diffusion) against 200 steps of the reference CPU run with
+    "If Dilatancy: True" (golden traj_dila.npz): bit for bit."""
+    from oracle.stepping import DenseStepper
+    d = golden("dense_small.npz")
+    g = golden("traj_dila.npz")
+    K = {k: d["planar_" + k] for k in oracle.OPS}
+    dila = {k.replace("dila_", "").replace("_", " "): float(g[k]) for k in g.files if k.startswith("dila_")}
+    st = DenseStepper(K, g["table"], mu=float(g["mu"]), density=float(g["rho"]), dilatancy=dila)
+    assert np.array_equal(st.P, g["P_init"]) and np.array_equal(st.state, g["state_init"])
+    hist = st.run(200)
+    assert np.array_equal(hist[:, 0], g["h"])
+    for k in ("Tno", "Tt1o", "state", "slipv", "slip1", "P", "dPdt0"):
+        assert np.array_equal(getattr(st, k), g["s200_" + k]), k
+    assert np.array_equal(st.Parr, g["Parr_200"])

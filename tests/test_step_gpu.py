@@ -177,3 +177,60 @@ def test_nan_state_reports_step_failure(cuda, golden):
     # the context is still usable
     _, ok = _golden_sim(golden, cuda)
     ok.step(2)
+
+
+def _dila_params(g):
+    return {k.replace("dila_", "").replace("_", " "): float(g[k]) for k in g.files if k.startswith("dila_")}
+
+
+def test_dilatancy_reproduces_reference_trajectory(cuda, golden):
+    """Pore-pressure dilatancy (src/QDsim_gpu.py:611-671): the persistent
+    stepper with the per-cell implicit pressure diffusion after every
+    accepted step, against the reference CPU run with "If Dilatancy: True"
+    (golden traj_dila.npz; the oracle reproduces it bit for bit,
+    test_oracle.py).  While the step sequences coincide (50 steps): state and
+    slip <= 1e-9, pore pressure <= 1e-12 (it sits near 2 MPa), dP/dt <= 1e-6,
+    slip rate <= 1e-7; step sizes <= 1e-9."""
+    g = golden("traj_dila.npz")
+    d = golden("dense_small.npz")
+    K = torch.as_tensor(gf.join_ops({k: d["planar_" + k] for k in oracle.OPS}), device=cuda).contiguous()
+    dila = _dila_params(g)
+    P0 = np.ones(g["table"].shape[0]) * dila["Initial porepressure"] * 1e6
+    init = initial_state(g["table"], 1e-6, 1e-9, P=P0)
+    assert np.array_equal(init["state"], g["state_init"])
+    sim = DenseDeviceSim(K, init, mu=float(g["mu"]), Cs=np.sqrt(float(g["mu"]) / float(g["rho"])), V0=1e-6,
+                         Vpl=1e-9, dilatancy=dila)
+    hs = []
+    done = 0
+    tol = {"Tno": 1e-9, "Tt1o": 1e-9, "state": 1e-9, "slip1": 1e-9, "slipv": 1e-7, "P": 1e-12, "dPdt0": 1e-6}
+    for stop in (1, 10, 50):
+        h, _, _ = sim.step(stop - done)
+        hs.extend(h)
+        done = stop
+        for k, tk in tol.items():
+            got = sim.t["dPdt" if k == "dPdt0" else k].cpu().numpy()
+            assert normwise_rel(g[f"s{stop}_{k}"], got) < tk, (stop, k)
+    assert np.allclose(hs, g["h"][:50], rtol=1e-9, atol=0)
+    assert np.any(sim.t["dPdt"].cpu().numpy() != 0.0)
+
+
+def test_dilatancy_through_qdsim(cuda, golden, tmp_path):
+    """"If Dilatancy: True" in the parameter file of the drop-in QDsim."""
+    from pyquake3d_gb300.QDsim_gpu import QDsim
+    g = golden("traj_dila.npz")
+    dila = _dila_params(g)
+    txt = ("Shear modulus: %r\nLame constants: %r\nRock density: %r\nInputHetoparamter: True\n"
+           "Inputparamter file: cells.dat\nHalf space: False\nIf Dilatancy:True\nFix_Tn: False\n"
+           "Reference slip rate: 1e-6\nPlate loading rate: 1e-9\n" % (float(g["mu"]), float(g["mu"]), float(g["rho"])))
+    txt += "".join("%s: %r\n" % (k, v) for k, v in dila.items())
+    (tmp_path / "parameter.txt").write_text(txt)
+    mesh.write_parameter_file(str(tmp_path / "cells.dat"), g["table"])
+    sim = QDsim(g["tris"], g["nodes"], str(tmp_path / "parameter.txt"))
+    sim.initGPUvariable()
+    dttry = sim.htry
+    hs = []
+    for _ in range(10):
+        h, dttry = sim.simu_forwardGPU(dttry)
+        hs.append(h)
+    assert np.allclose(hs, g["h"][:10], rtol=1e-9)
+    assert normwise_rel(g["s10_P"], sim.P_gpu.cpu().numpy()) < 1e-12
