@@ -661,6 +661,42 @@ def L_ws_bytes(N):
     return _lib.load().pq3d_gf_workspace_bytes(N)
 
 
+def profile_case(case):
+    """Small single-kernel cases for ncu captures (no timing, no JSON):
+    hs_assembly  half-space assembly, rough 20x10 km to the surface, N=1,600 (2 launches)
+    hmat_product H-matrix product, rough 200x40 km, N=100,000, B=1 (13 products)
+    tc_gemm      tcgen05 BF16x6 product, planar 60x50 km, N=6,000, B=64 (4 iterations)"""
+    import torch
+    from pyquake3d_gb300 import gf, mesh
+    if case == "hs_assembly":
+        nodes, tris = mesh.rough_fault(20.0, 10.0, 40, 20, seed=0)
+        K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, halfspace=True)
+        gf.assemble_dense(nodes, tris, MU, LAM, halfspace=True, out64=K64, out32=K32)
+    elif case == "hmat_product":
+        from pyquake3d_gb300.hmatrix import HMatrix
+        nodes, tris = mesh.rough_fault(200.0, 40.0, 500, 100, seed=0)
+        H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4)
+        v = torch.randn(1, 2 * H.N, dtype=torch.float64, device="cuda")
+        ws = torch.empty(H.workspace_bytes(1), dtype=torch.uint8, device="cuda")
+        out = torch.empty(1, 3 * H.N, dtype=torch.float64, device="cuda")
+        for _ in range(13):
+            H.apply(v, out, ws)
+    elif case == "tc_gemm":
+        from pyquake3d_gb300.ensemble import Ensemble, PackedOperator
+        nodes, tris = mesh.planar_fault(60.0, 50.0, 60, 50)
+        K64, _ = gf.assemble_dense(nodes, tris, MU, LAM, fp32_copy=False)
+        P = PackedOperator(K64)
+        del K64
+        torch.cuda.empty_cache()
+        _, xg = mesh.element_frames(nodes, tris)
+        tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
+        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x6").iterate(4)
+    else:
+        raise SystemExit("unknown --case " + case)
+    torch.cuda.synchronize()
+    print("case %s done" % case)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -682,7 +718,11 @@ def main():
     ap.add_argument("--nsplit", type=int, default=None)
     ap.add_argument("--graph-iters", type=int, default=25)
     ap.add_argument("--batch-iters", type=int, default=300)
+    ap.add_argument("--case", default=None, help="profiling case only (hs_assembly, hmat_product, tc_gemm)")
     args = ap.parse_args()
+    if args.case:
+        profile_case(args.case)
+        return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return

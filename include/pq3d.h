@@ -317,7 +317,8 @@ typedef struct pq3d_hmat {
     const float *data;            /* FP32: dense block (3m x 2n, column-major) or U (3m x k, column-major)
                                      then V (k x 2n, row-major) */
     const int32_t *lr_ids;        /* low-rank block ids, in order */
-    const int32_t *t_blk;         /* [t_rows] block of each rank row (low-rank blocks in lr_ids order) */
+    const int64_t *t_info;        /* [t_rows][2] per rank row (low-rank blocks in lr_ids order): offset of its V
+                                     row in data, then (first column 2 c0) | (row length 2n) << 32 */
     const int64_t *t_off;         /* [nblocks]: first rank row of the block in the product workspace */
     const int64_t *leaf;          /* [nleaves][2]: permuted ranges of the leaf row clusters */
     const int64_t *leaf_ptr;      /* [nleaves + 1] */
@@ -350,6 +351,11 @@ int pq3d_hmat_pack_factors(const double *UV, const int64_t *uv_off, const int64_
  * arithmetic.  Replaces blocks_process_MVM (src/Hmatrix.py:1773-1866), all six
  * operator types at once. */
 size_t pq3d_hmat_workspace_bytes(const pq3d_hmat *H, int B);
+/* The same for the runs r with run_active[r * active_stride] != 0 only (device
+ * int32 flags, e.g. the `active` field of a pq3d_run_ctrl array; the rows of
+ * the other runs are left untouched). */
+int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B, double *Y, const int32_t *run_active,
+                           int active_stride, void *workspace, size_t workspace_bytes, void *stream);
 int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, double *Y, void *workspace, size_t workspace_bytes,
                     void *stream);
 

@@ -71,7 +71,7 @@ class BatchSim(ctypes.Structure):
 class HMat(ctypes.Structure):
     """Mirror of pq3d_hmat."""
     _fields_ = [("N", c_i64), ("nblocks", ctypes.c_int32), ("nleaves", ctypes.c_int32), ("t_rows", c_i64)] + \
-        [(n, c_void_p) for n in ("perm", "blk", "rank", "off", "data", "lr_ids", "t_blk", "t_off", "leaf", "leaf_ptr",
+        [(n, c_void_p) for n in ("perm", "blk", "rank", "off", "data", "lr_ids", "t_info", "t_off", "leaf", "leaf_ptr",
                                  "leaf_blocks")]
 
 
@@ -122,6 +122,8 @@ _SIGS = {
                                        c_void_p, c_void_p]),
     "pq3d_hmat_workspace_bytes": (c_size, [ctypes.POINTER(HMat), c_int]),
     "pq3d_hmat_apply": (c_int, [ctypes.POINTER(HMat), c_void_p, c_int, c_void_p, c_void_p, c_size, c_void_p]),
+    "pq3d_hmat_apply_masked": (c_int, [ctypes.POINTER(HMat), c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p,
+                                       c_size, c_void_p]),
     "pq3d_batch_prepare": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
     "pq3d_batch_iterate": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
     "pq3d_batch_iterate_begin": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),

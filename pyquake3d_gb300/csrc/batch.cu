@@ -363,8 +363,10 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
         if (rc) return rc;
     } else {
         // the H-matrix product needs no padding runs: the first B rows only
-        rc = pq3d_hmat_apply((const pq3d_hmat *)S.K, (const double *)S.vop, S.B, S.rates, workspace, workspace_bytes,
-                             stream);
+        // inactive runs (free slots, finished runs) skip the product
+        rc = pq3d_hmat_apply_masked((const pq3d_hmat *)S.K, (const double *)S.vop, S.B, S.rates, &S.ctrl[0].active,
+                                    (int)(sizeof(pq3d_run_ctrl) / sizeof(int32_t)), workspace, workspace_bytes,
+                                    stream);
         if (rc) return rc;
     }
     PQ3D_CUDA_TRY(cudaGetLastError());

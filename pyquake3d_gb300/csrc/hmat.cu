@@ -326,39 +326,41 @@ __device__ __forceinline__ float2 split2(double x)
 }
 
 // X (FP64, [B][2N], element order) -> Xs ([B][2N] float (hi, lo) pairs, permuted order)
+// run r takes part iff act == NULL or act[r * act_stride] != 0
+__device__ __forceinline__ bool run_on(const int32_t *act, int act_stride, int r)
+{
+    return act == nullptr || act[(int64_t)r * act_stride] != 0;
+}
+
 __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t *__restrict__ perm, int64_t N, int B,
-                                     float2 *__restrict__ Xs)
+                                     float2 *__restrict__ Xs, const int32_t *act, int act_stride)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int r = blockIdx.y;
-    if (i >= 2 * N || r >= B) return;
+    if (i >= 2 * N || r >= B || !run_on(act, act_stride, r)) return;
     const int64_t q = i >> 1;
     Xs[(int64_t)r * 2 * N + i] = split2(X[(int64_t)r * 2 * N + 2 * perm[q] + (i & 1)]);
 }
 
-// T[(t_off[b] + l) * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo)
-// pair; one warp per (rank row, run), t_blk[w] = the block of rank row w.
-// Runs are the fastest-varying part of the block index, so the B CTAs that
-// read the same factor rows run together and share them in L2.
+// T[w * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo) pair for rank
+// row w (row l of low-rank block b); one warp per (rank row, run).  The row's
+// storage offset, first x column and length come in one 16-byte record
+// (t_info), so a warp starts streaming after a single dependent load.  Runs
+// are the fastest-varying part of the block index, so the B CTAs that read
+// the same factor rows run together and share them in L2.
 __global__ void __launch_bounds__(256)
-lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off, const int64_t *__restrict__ blk,
-                 const int32_t *__restrict__ rank, const int32_t *__restrict__ t_blk, int64_t t_rows,
-                 const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T,
-                 const int64_t *__restrict__ t_off)
+lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info, int64_t t_rows,
+                 const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T, const int32_t *act,
+                 int act_stride)
 {
     const int lane = threadIdx.x & 31;
     const int r = (int)(blockIdx.x % (unsigned)B);
     const int64_t w = ((blockIdx.x / (unsigned)B) * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (w >= t_rows) return;
-    const int b = t_blk[w];
-    const int64_t t0 = t_off[b];
-    const int l = (int)(w - t0);
-    const int k = rank[b];
-    const int64_t c0 = blk[4 * b + 2];
-    const int Nc = 2 * (int)(blk[4 * b + 3] - c0);
-    const int M = 3 * (int)(blk[4 * b + 1] - blk[4 * b]);
-    const float *v = data + off[b] + (int64_t)M * k + (int64_t)l * Nc;
-    const float2 *x = Xs + (int64_t)r * 2 * N + 2 * c0;
+    if (w >= t_rows || !run_on(act, act_stride, r)) return;
+    const longlong2 info = t_info[w];
+    const float *v = data + info.x;
+    const float2 *x = Xs + (int64_t)r * 2 * N + (int32_t)(info.y & 0xffffffffll);
+    const int Nc = (int)(info.y >> 32);
     FF sum{0.f, 0.f};
     for (int c0k = 0; c0k < Nc; c0k += 1024) {
         const int cend = min(Nc, c0k + 1024);
@@ -380,7 +382,7 @@ lowrank_T_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
         sum = ff_add(sum, FF{__fadd_rn(a0.c, a1.c), 0.f});
     }
     sum = warp_sum_ff(sum);
-    if (lane == 0) T[(t0 + l) * (int64_t)B + r] = make_float2(sum.hi, sum.lo);
+    if (lane == 0) T[w * (int64_t)B + r] = make_float2(sum.hi, sum.lo);
 }
 
 // One CTA per (leaf row cluster, run), the run fastest in the block index so
@@ -476,12 +478,13 @@ leaf_rows_kernel(const float *__restrict__ data, const int64_t *__restrict__ off
                  const int32_t *__restrict__ rank, const int64_t *__restrict__ leaf, const int64_t *__restrict__ leaf_ptr,
                  const int32_t *__restrict__ leaf_blocks, const int64_t *__restrict__ perm, const float2 *__restrict__ Xs,
                  const float2 *__restrict__ T, const int64_t *__restrict__ t_off, int64_t N, int B,
-                 double *__restrict__ Y)
+                 double *__restrict__ Y, const int32_t *act, int act_stride)
 {
     __shared__ BlkDesc desc[kMaxLeafBlocks];
     __shared__ int wpre[kMaxLeafBlocks + 1];
     __shared__ double red[kWarps][kPassRows];
     const int L = (int)(blockIdx.x / (unsigned)B), r = (int)(blockIdx.x % (unsigned)B);
+    if (!run_on(act, act_stride, r)) return;   // uniform per CTA: before any barrier
     const int64_t p0 = leaf[2 * L], p1 = leaf[2 * L + 1];
     const int rows = 3 * (int)(p1 - p0);
     const int64_t q0 = leaf_ptr[L], q1 = leaf_ptr[L + 1];
@@ -613,8 +616,9 @@ extern "C" int pq3d_hmat_pack_factors(const double *UV, const int64_t *uv_off, c
     return PQ3D_OK;
 }
 
-extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, double *Y, void *workspace,
-                               size_t workspace_bytes, void *stream)
+extern "C" int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B, double *Y,
+                                      const int32_t *run_active, int active_stride, void *workspace,
+                                      size_t workspace_bytes, void *stream)
 {
     clear_error();
     PQ3D_REQUIRE(H && X && Y && workspace && B >= 1, "pq3d_hmat_apply: bad arguments");
@@ -626,21 +630,27 @@ extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, doubl
     float2 *Xs = (float2 *)workspace;
     float2 *T = (float2 *)((char *)workspace + (size_t)B * 2 * N * sizeof(float2));
     dim3 g1((unsigned)((2 * N + 255) / 256), (unsigned)B);
-    permute_split_kernel<<<g1, 256, 0, st>>>(X, H->perm, N, B, Xs);
+    permute_split_kernel<<<g1, 256, 0, st>>>(X, H->perm, N, B, Xs, run_active, active_stride);
     // all runs in one launch, run fastest in the block index; a run's result
     // does not depend on B
     if (H->t_rows > 0) {
         const int64_t nT = (H->t_rows * 32 + 255) / 256 * B;
         PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
-        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, H->off, H->blk, H->rank, H->t_blk, H->t_rows, Xs, N,
-                                                       B, T, H->t_off);
+        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_rows, Xs, N, B, T,
+                                                       run_active, active_stride);
     }
     PQ3D_REQUIRE((int64_t)H->nleaves * B < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many leaves x runs");
     const unsigned gL = (unsigned)(H->nleaves * B);
     leaf_rows_kernel<<<gL, kThreads, 0, st>>>(H->data, H->off, H->blk, H->rank, H->leaf, H->leaf_ptr, H->leaf_blocks,
-                                              H->perm, Xs, T, H->t_off, N, B, Y);
+                                              H->perm, Xs, T, H->t_off, N, B, Y, run_active, active_stride);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
+}
+
+extern "C" int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, double *Y, void *workspace,
+                               size_t workspace_bytes, void *stream)
+{
+    return pq3d_hmat_apply_masked(H, X, B, Y, nullptr, 0, workspace, workspace_bytes, stream);
 }
 
 extern "C" size_t pq3d_hmat_workspace_bytes(const pq3d_hmat *H, int B)

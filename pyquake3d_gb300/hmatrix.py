@@ -210,8 +210,17 @@ class HMatrix:
         self.t_rows = int(prefix[-1])
         self.lr_ids = torch.as_tensor(lr_ids if len(lr_ids) else np.zeros(1, np.int32), device=dev)
         self.t_off = torch.as_tensor(t_off, device=dev)
-        t_blk = np.repeat(lr_ids, ranks) if len(lr_ids) else np.zeros(1, np.int32)
-        self.t_blk = torch.as_tensor(np.ascontiguousarray(t_blk, dtype=np.int32), device=dev)
+        # per rank row: offset of its V row, and (2 c0) | (2n) << 32
+        if len(lr_ids):
+            bl = np.repeat(lr_ids, ranks)
+            l = np.arange(self.t_rows, dtype=np.int64) - np.repeat(prefix[:-1], ranks)
+            Mb, Nb = 3 * m[bl].astype(np.int64), 2 * n[bl].astype(np.int64)
+            info = np.empty((self.t_rows, 2), dtype=np.int64)
+            info[:, 0] = off[bl] + Mb * rank[bl].astype(np.int64) + l * Nb
+            info[:, 1] = 2 * blocks[bl, 2].astype(np.int64) | (Nb << 32)
+        else:
+            info = np.zeros((1, 2), dtype=np.int64)
+        self.t_info = torch.as_tensor(info, device=dev)
         nl = leaves.shape[0]
         leaf_start = leaves[:, 0]
         lists = [[] for _ in range(nl)]
@@ -232,7 +241,7 @@ class HMatrix:
                       "bytes": int(self.data.numel() * 4), "dense_fp32_bytes": int(6 * N * N * 4),
                       "leaves": int(nl)}
 
-    _ARRAYS = ("perm", "blk", "rank", "off", "data", "lr_ids", "t_blk", "t_off", "leaf", "leaf_ptr", "leaf_blocks")
+    _ARRAYS = ("perm", "blk", "rank", "off", "data", "lr_ids", "t_info", "t_off", "leaf", "leaf_ptr", "leaf_blocks")
 
     def _make_struct(self):
         H = _lib.HMat()
@@ -266,17 +275,25 @@ class HMatrix:
     def workspace_bytes(self, B):
         return _lib.load().pq3d_hmat_workspace_bytes(ctypes.byref(self.H), int(B))
 
-    def apply(self, X, out=None, workspace=None):
+    def apply(self, X, out=None, workspace=None, active=None):
         """Y = H X for X of shape (B, 2N) (FP64, element order, interleaved
-        strike/dip); returns Y (B, 3N)."""
+        strike/dip); returns Y (B, 3N).  ``active``: optional int32 device
+        tensor of B flags; runs with flag 0 are skipped (their rows of ``out``
+        are left as they are)."""
         L = _lib.load()
         X = X.contiguous()
         B = X.shape[0]
         Y = out if out is not None else torch.empty((B, 3 * self.N), dtype=torch.float64, device=self.device)
         ws = workspace if workspace is not None else torch.empty(self.workspace_bytes(B), dtype=torch.uint8,
                                                                  device=self.device)
-        _lib.check(L.pq3d_hmat_apply(ctypes.byref(self.H), X.data_ptr(), B, Y.data_ptr(), ws.data_ptr(), ws.numel(),
-                                     torch.cuda.current_stream(self.device).cuda_stream))
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        if active is None:
+            _lib.check(L.pq3d_hmat_apply(ctypes.byref(self.H), X.data_ptr(), B, Y.data_ptr(), ws.data_ptr(),
+                                         ws.numel(), st))
+        else:
+            assert active.dtype == torch.int32 and active.numel() == B
+            _lib.check(L.pq3d_hmat_apply_masked(ctypes.byref(self.H), X.data_ptr(), B, Y.data_ptr(),
+                                                active.data_ptr(), 1, ws.data_ptr(), ws.numel(), st))
         return Y
 
     def matvec(self, v):

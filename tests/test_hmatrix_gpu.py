@@ -39,6 +39,10 @@ def test_hmatrix_product_matches_dense(cuda, leaf):
     # a run alone gives the same bits as in the batch
     Y1 = H.apply(X[1:2])
     assert torch.equal(Y1[0], Y[1])
+    # masked runs are skipped, the others unchanged
+    Ym = torch.full_like(Y, 7.0)
+    H.apply(X, out=Ym, active=torch.tensor([1, 0, 1], dtype=torch.int32, device=cuda))
+    assert torch.equal(Ym[0], Y[0]) and torch.equal(Ym[2], Y[2]) and bool(torch.all(Ym[1] == 7.0))
 
 
 def test_hmatrix_error_not_worse_than_reference(cuda):
