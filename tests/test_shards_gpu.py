@@ -60,3 +60,35 @@ def test_shard_rejects_tensor_core_product(cuda, golden):
     tabs = _tables(golden("traj_small.npz"), 1)
     with pytest.raises(ValueError):
         Ensemble(K[:96].contiguous(), tabs[:, :32], mu=MU, Cs=CS, precision="bf16x6", shard=(0, 64))
+
+
+def test_dist_exchange_over_nccl_world1(cuda, golden):
+    """The torch.distributed exchange on device tensors (NCCL) with one rank
+    (one GPU here): the collective calls run and the result equals the
+    unsharded ensemble bitwise.  Several ranks are covered on CPU (gloo)."""
+    import socket
+
+    import torch.distributed as dist
+    from pyquake3d_gb300.shards import DistExchange, receiver_partition
+    if not dist.is_nccl_available():
+        pytest.fail("NCCL backend missing")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    dist.init_process_group("nccl", init_method="tcp://127.0.0.1:%d" % port, rank=0, world_size=1)
+    try:
+        d = golden("dense_small.npz")
+        g = golden("traj_small.npz")
+        K = torch.as_tensor(gf.join_ops({k: d["planar_" + k] for k in oracle.OPS}), device=cuda).contiguous()
+        tabs = _tables(g, 2)
+        N = tabs.shape[1]
+        whole = Ensemble(K, tabs, mu=MU, Cs=CS, precision="fp64")
+        whole.iterate(60)
+        bounds = receiver_partition(N, 1)
+        shard = Ensemble(K, tabs, mu=MU, Cs=CS, precision="fp64", shard=(0, N))
+        iterate_sharded([shard], DistExchange(bounds), 60)
+        torch.cuda.synchronize()
+        assert torch.equal(shard.t["slip1"], whole.t["slip1"])
+        assert [c.steps for c in shard.read_ctrl()] == [c.steps for c in whole.read_ctrl()]
+    finally:
+        dist.destroy_process_group()
