@@ -265,6 +265,10 @@ __global__ void decide_kernel(pq3d_run_ctrl *ctrl, int B)
     }
 }
 
+// kMixed: the slip rate 2 V0 e^{-psi/a} sinh(tau / (sigma a)) formed as
+// V0 (e^{x - psi/a} - e^{-x - psi/a}) with fexp (2.5e-7 relative, as the
+// mixed right-hand side); the FP64 arm keeps the reference formula.
+template <bool kMixed>
 __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
 {
     __shared__ int acc;
@@ -282,9 +286,18 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
     const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[idx];
     S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
-    const double e = (2.0 * S.V0) * exp(-st / a);
-    const double v1 = e * sinh(T1 / Tno / a);
-    const double v2 = e * sinh(T2 / Tno / a);
+    double v1, v2;
+    if (kMixed) {
+        const double inv_a = 1.0 / a, sp = -st * inv_a;
+        const double q = inv_a / Tno;
+        const double x1 = clip700(T1 * q), x2 = clip700(T2 * q);
+        v1 = S.V0 * (fexp(sp + x1) - fexp(sp - x1));
+        v2 = S.V0 * (fexp(sp + x2) - fexp(sp - x2));
+    } else {
+        const double e = (2.0 * S.V0) * exp(-st / a);
+        v1 = e * sinh(T1 / Tno / a);
+        v2 = e * sinh(T2 / Tno / a);
+    }
     double v = sqrt(v1 * v1 + v2 * v2);
     if (v < 1e-30) v = 1e-30;
     S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
@@ -388,7 +401,8 @@ extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
     // 3-4. decide, update
     decide_kernel<<<(S.B + 127) / 128, 128, 0, st>>>(S.ctrl, S.B);
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
-    update_kernel<<<grid, 256, 0, st>>>(S);
+    if (S.precision == PQ3D_BATCH_FP64) update_kernel<false><<<grid, 256, 0, st>>>(S);
+    else update_kernel<true><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

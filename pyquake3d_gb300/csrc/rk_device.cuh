@@ -97,8 +97,11 @@ __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, 
     const double dV2dstate = -twoV0 * c.inv_a * (0.5 * (e2p - e2m));
     dstate = c.bdc * (V0 * fexp((c.f0 - state) * c.inv_b) - c.slipv);
     const double ds = c.dsig - c.dPdt;
-    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
-    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    // one reciprocal for both radiation-damping denominators
+    const double den1 = 1.0 + eta * dV1dtau, den2 = 1.0 + eta * dV2dtau;
+    const double inv12 = 1.0 / (den1 * den2);
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) * (den2 * inv12);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) * (den1 * inv12);
     dsig = c.dsig * 1e-6;
     dtau1 = t1 * 1e-6;
     dtau2 = t2 * 1e-6;

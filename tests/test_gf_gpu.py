@@ -211,3 +211,25 @@ def test_halfspace_rough_fault_against_reference(cuda, golden):
     err_gpu = np.abs(got.ravel()[idx] - true).sum()
     err_ref = np.abs(ref.ravel()[idx] - true).sum()
     assert err_gpu <= err_ref, (err_gpu, err_ref)
+
+
+def test_qdsim_halfspace_parameter(cuda, golden, tmp_path):
+    """"Half space: True" in the drop-in QDsim's parameter file assembles the
+    half-space operator (the reference's dense half-space path, golden)."""
+    from pyquake3d_gb300.QDsim_gpu import QDsim
+    g = golden("hs_dense_small.npz")
+    nodes, tris = g["nodes"], g["tris"]
+    mu = float(g["mu"])
+    _, xg = mesh.element_frames(nodes, tris)
+    table = mesh.friction_table(xg, 8e3, 4e3, v_nuc=1e-3, seed=0)
+    (tmp_path / "parameter.txt").write_text(
+        "Shear modulus: %r\nLame constants: %r\nRock density: %r\nInputHetoparamter: True\n"
+        "Inputparamter file: cells.dat\nHalf space: True\nIf Dilatancy: False\nFix_Tn: False\n"
+        "Reference slip rate: 1e-6\nPlate loading rate: 1e-9\n" % (mu, float(g["lam"]), mu / 3464.0 ** 2))
+    mesh.write_parameter_file(str(tmp_path / "cells.dat"), table)
+    sim = QDsim(tris, nodes, str(tmp_path / "parameter.txt"))
+    ref = gf.join_ops({k: g["py_" + k] for k in oracle.OPS})
+    assert normwise_rel(ref, sim.K64.cpu().numpy()) < 1e-10
+    sim.initGPUvariable()
+    h, _ = sim.simu_forwardGPU(sim.htry)
+    assert h > 0 and np.all(np.isfinite(sim.slip1_gpu.cpu().numpy()))
