@@ -214,7 +214,12 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
         const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
         const double a = S.a[idx], b = S.b[idx], dc = S.dc[idx];
         Cell c{a, b, dc, S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig, 0.0, 0.0, 0.0};
-        if (kMixed) { c.inv_a = 1.0 / a; c.inv_b = 1.0 / b; c.bdc = b / dc; }
+        if (kMixed) {
+            c.inv_a = 1.0 / a; c.inv_b = 1.0 / b; c.bdc = b / dc;
+            c.L1 = (float)(-c.AdotV1 + c.shear);
+            c.L2 = (float)(-c.AdotV2 + c.shear);
+            c.dsf = (float)(c.dsig - c.dPdt);
+        }
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
         double yo[4], e1, e2;
         dp_attempt<kMixed>(c, S.V0, S.eta, hs, y, yo, e1, e2);

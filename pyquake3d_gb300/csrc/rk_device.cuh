@@ -30,6 +30,7 @@ struct Cell {
     double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
     double inv_a, inv_b, bdc;   // 1/a, 1/b, b/dc (used by the mixed-precision right-hand side)
     double P, dPdt;             // pore pressure (Pa) and its rate (Pa/s); 0 without dilatancy
+    float L1, L2, dsf;          // mixed right-hand side: -AdotV1 + shear, -AdotV2 + shear, dsig - dPdt
 };
 
 __device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
@@ -75,10 +76,27 @@ __device__ __forceinline__ double fexp(double x)
     return (double)exp2f(f) * scale;
 }
 
+// e^x as FP32: the argument reduced in FP64 as in fexp, 2^f from exp2f and
+// the exact power-of-two scaling in FP32 (ldexpf: underflow to 0 where the
+// term is negligible).
+__device__ __forceinline__ float fexpf(double x)
+{
+    x = fmin(fmax(x, -700.0), 700.0);
+    const double t = x * 1.4426950408889634;
+    const double n = rint(t);
+    return ldexpf(exp2f((float)(t - n)), (int)fmax(fmin(n, 300.0), -300.0));
+}
+
 // Mixed-precision right-hand side (batched mixed modes).  Same equations as
-// rhs(); the factors e^{-psi/a} cosh(x), e^{-psi/a} sinh(x) are formed as
-// (e^{x - psi/a} +- e^{-x - psi/a}) / 2 with fexp, and the divisions share
-// one reciprocal per stage.  The state and its increments stay FP64.
+// rhs().  What needs FP64 stays FP64: the state, the exponent arguments
+// tau/(a sigma) and -psi/a (large and nearly cancelling: they are summed in
+// FP64 before the exponential) and everything downstream of the right-hand
+// side (stage sums, increments, error norm).  The factors e^{-psi/a} cosh(x),
+// e^{-psi/a} sinh(x) are formed as (e^{x - psi/a} +- e^{-x - psi/a}) / 2 with
+// fexpf, and the algebra after the exponentials (slip-rate derivatives,
+// aging law, radiation-damping quotient; relative error ~1e-7, the level of
+// the product's) runs in FP32 -- GB300's FP64 rate is 1/64 of FP32.
+// Cell-constant loads (-AdotV + shear, sigma rate - P rate) come in as FP32.
 __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
                                           double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
 {
@@ -86,25 +104,25 @@ __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, 
     const double inv_aTn = 1.0 / (c.a * Tn);
     const double x1 = clip700(T1 * inv_aTn), x2 = clip700(T2 * inv_aTn);
     const double sp = clip700(-state * c.inv_a);
-    const double e1p = fexp(sp + x1), e1m = fexp(sp - x1), e2p = fexp(sp + x2), e2m = fexp(sp - x2);
-    const double twoV0 = 2.0 * V0;
-    const double dV1dtau = twoV0 * inv_aTn * (0.5 * (e1p + e1m));
-    const double dV2dtau = twoV0 * inv_aTn * (0.5 * (e2p + e2m));
-    const double inv_Tn = c.a * inv_aTn;
-    const double dV1dsigma = -dV1dtau * T1 * inv_Tn;
-    const double dV2dsigma = -dV2dtau * T2 * inv_Tn;
-    const double dV1dstate = -twoV0 * c.inv_a * (0.5 * (e1p - e1m));
-    const double dV2dstate = -twoV0 * c.inv_a * (0.5 * (e2p - e2m));
-    dstate = c.bdc * (V0 * fexp((c.f0 - state) * c.inv_b) - c.slipv);
-    const double ds = c.dsig - c.dPdt;
-    // one reciprocal for both radiation-damping denominators
-    const double den1 = 1.0 + eta * dV1dtau, den2 = 1.0 + eta * dV2dtau;
-    const double inv12 = 1.0 / (den1 * den2);
-    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) * (den2 * inv12);
-    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) * (den1 * inv12);
+    const float e1p = fexpf(sp + x1), e1m = fexpf(sp - x1), e2p = fexpf(sp + x2), e2m = fexpf(sp - x2);
+    const float ed = fexpf((c.f0 - state) * c.inv_b);
+    const float V0f = (float)V0, iaT = (float)inv_aTn, inv_a = (float)c.inv_a, etaf = (float)eta;
+    const float inv_Tn = (float)(c.a * inv_aTn);
+    const float dV1dtau = V0f * iaT * (e1p + e1m);
+    const float dV2dtau = V0f * iaT * (e2p + e2m);
+    const float dV1dsigma = -dV1dtau * (float)T1 * inv_Tn;
+    const float dV2dsigma = -dV2dtau * (float)T2 * inv_Tn;
+    const float dV1dstate = -V0f * inv_a * (e1p - e1m);
+    const float dV2dstate = -V0f * inv_a * (e2p - e2m);
+    const float ds_dt = (float)c.bdc * (V0f * ed - (float)c.slipv);
+    const float den1 = 1.0f + etaf * dV1dtau, den2 = 1.0f + etaf * dV2dtau;
+    const float inv12 = 1.0f / (den1 * den2);
+    const float t1 = (c.L1 - etaf * (dV1dsigma * c.dsf + dV1dstate * ds_dt)) * (den2 * inv12);
+    const float t2 = (c.L2 - etaf * (dV2dsigma * c.dsf + dV2dstate * ds_dt)) * (den1 * inv12);
+    dstate = (double)ds_dt;
     dsig = c.dsig * 1e-6;
-    dtau1 = t1 * 1e-6;
-    dtau2 = t2 * 1e-6;
+    dtau1 = (double)t1 * 1e-6;
+    dtau2 = (double)t2 * 1e-6;
 }
 
 template <bool kMixed>
