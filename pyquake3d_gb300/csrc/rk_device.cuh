@@ -97,8 +97,8 @@ __device__ __forceinline__ float fexpf(double x)
 // aging law, radiation-damping quotient; relative error ~1e-7, the level of
 // the product's) runs in FP32 -- GB300's FP64 rate is 1/64 of FP32.
 // Cell-constant loads (-AdotV + shear, sigma rate - P rate) come in as FP32.
-__device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
-                                          double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+__device__ __forceinline__ void rhs_mixed_f(const Cell &c, double V0, double eta, double Tno, double Tt1o,
+                                            double Tt2o, double state, float &dstate, float &dtau1, float &dtau2)
 {
     const double Tn = Tno * 1e6 - c.P, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
     const double inv_aTn = 1.0 / (c.a * Tn);
@@ -119,10 +119,20 @@ __device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, 
     const float inv12 = 1.0f / (den1 * den2);
     const float t1 = (c.L1 - etaf * (dV1dsigma * c.dsf + dV1dstate * ds_dt)) * (den2 * inv12);
     const float t2 = (c.L2 - etaf * (dV2dsigma * c.dsf + dV2dstate * ds_dt)) * (den1 * inv12);
-    dstate = (double)ds_dt;
+    dstate = ds_dt;
+    dtau1 = t1 * 1e-6f;
+    dtau2 = t2 * 1e-6f;
+}
+
+__device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
+                                          double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+{
+    float ds, t1, t2;
+    rhs_mixed_f(c, V0, eta, Tno, Tt1o, Tt2o, state, ds, t1, t2);
+    dstate = ds;
     dsig = c.dsig * 1e-6;
-    dtau1 = (double)t1 * 1e-6;
-    dtau2 = (double)t2 * 1e-6;
+    dtau1 = t1;
+    dtau2 = t2;
 }
 
 template <bool kMixed>
@@ -135,10 +145,69 @@ __device__ __forceinline__ void rhs_sel(const Cell &c, double V0, double eta, do
 
 // One Dormand-Prince attempt of one cell; y = (Tno, Tt1o, Tt2o, state).
 // Writes the 5th-order solution to yo and returns the two relative errors.
+// Mixed attempt: the stage derivatives come from rhs_mixed_f as FP32 and
+// their weighted sums are formed in FP32 (they carry the derivatives' ~1e-7
+// relative error already); each stage state is y + h * sum with one FP64
+// multiply-add, and the 5th-minus-4th-order difference is summed directly
+// (h * sum (b_i - b*_i) k_i) instead of subtracting two FP64 states.  The
+// normal-stress rate is constant over the step.
+__device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, double eta, double h, const double y[4],
+                                                 double yo[4], double &e1, double &e2)
+{
+    float s[7], t[7], u[7];
+    const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
+    const double dn = c.dsig * 1e-6;   // d(Tno)/dt, MPa/s
+    const float A[6][6] = {{(float)B21, 0, 0, 0, 0, 0},
+                           {(float)B31, (float)B32, 0, 0, 0, 0},
+                           {(float)B41, (float)B42, (float)B43, 0, 0, 0},
+                           {(float)B51, (float)B52, (float)B53, (float)B54, 0, 0},
+                           {(float)B61, (float)B62, (float)B63, (float)B64, (float)B65, 0},
+                           {(float)B71, 0.f, (float)B73, (float)B74, (float)B75, (float)B76}};
+    rhs_mixed_f(c, V0, eta, Tno, Tt1o, Tt2o, st, s[0], t[0], u[0]);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        float ds = 0.f, dt1 = 0.f, dt2 = 0.f;
+#pragma unroll
+        for (int l = 0; l <= j; ++l) {
+            ds = fmaf(A[j][l], s[l], ds);
+            dt1 = fmaf(A[j][l], t[l], dt1);
+            dt2 = fmaf(A[j][l], u[l], dt2);
+        }
+        const double wsum[6] = {B21, B31 + B32, B41 + B42 + B43, B51 + B52 + B53 + B54, B61 + B62 + B63 + B64 + B65,
+                                B71 + B73 + B74 + B75 + B76};
+        const double Tn_j = Tno + h * (wsum[j] * dn);   // the normal-stress rate is constant
+        const double T1_j = Tt1o + h * (double)dt1, T2_j = Tt2o + h * (double)dt2, st_j = st + h * (double)ds;
+        if (j == 5) { yo[0] = Tn_j; yo[1] = T1_j; yo[2] = T2_j; yo[3] = st_j; }
+        rhs_mixed_f(c, V0, eta, Tn_j, T1_j, T2_j, st_j, s[j + 1], t[j + 1], u[j + 1]);
+    }
+    // 4th-order minus 5th-order solution: h * sum (B8i - B7i) k_i
+    const float D[7] = {(float)(B81 - B71), 0.f, (float)(B83 - B73), (float)(B84 - B74), (float)(B85 - B75),
+                        (float)(B86 - B76), (float)B87};
+    float es = 0.f, e1t = 0.f, e2t = 0.f;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) {
+        es = fmaf(D[l], s[l], es);
+        e1t = fmaf(D[l], t[l], e1t);
+        e2t = fmaf(D[l], u[l], e2t);
+    }
+    const double wn = (B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76);
+    const double st8 = yo[3] + h * (double)es;
+    const double T18 = yo[1] + h * (double)e1t, T28 = yo[2] + h * (double)e2t, Tn8 = yo[0] + h * (wn * dn);
+    e1 = fabs(fabs(h * (double)es) / st8);
+    const double ea = fabs(fabs(h * (double)e1t) / T18);
+    const double eb = fabs(fabs(h * (double)e2t) / T28);
+    const double ec = fabs(fabs(h * (wn * dn)) / Tn8);
+    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
+}
+
 template <bool kMixed = false>
 __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
                                            double yo[4], double &e1, double &e2)
 {
+    if (kMixed) {
+        dp_attempt_mixed(c, V0, eta, h, y, yo, e1, e2);
+        return;
+    }
     double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
         u7;
     const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
