@@ -323,6 +323,8 @@ typedef struct pq3d_hmat {
     const int64_t *leaf;          /* [nleaves][2]: permuted ranges of the leaf row clusters */
     const int64_t *leaf_ptr;      /* [nleaves + 1] */
     const int32_t *leaf_blocks;   /* blocks whose row range covers each leaf row cluster, fixed order */
+    const int32_t *t_sched;       /* [t_rows] rank rows: those of at most 8192 columns, then the longer ones */
+    int64_t t_nlong;              /* number of the longer rows (the tail of t_sched) */
 } pq3d_hmat;
 
 /* ACA (partial pivoting, relative Frobenius tolerance `tol`) of the listed

@@ -343,37 +343,53 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
 }
 
 // T[w * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo) pair for rank
-// row w (row l of low-rank block b); one warp per (rank row, run).  The row's
-// storage offset, first x column and length come in one 16-byte record
-// (t_info), so a warp starts streaming after a single dependent load.  Runs
-// are the fastest-varying part of the block index, so the B CTAs that read
-// the same factor rows run together and share them in L2.
-__global__ void __launch_bounds__(256)
-lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info, int64_t t_rows,
-                 const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T, const int32_t *act,
-                 int act_stride)
+// row w (row l of low-rank block b).  The row's storage offset, first x
+// column and length come in one 16-byte record (t_info), so a warp starts
+// streaming after a single dependent load.  Work list t_sched: the rows of
+// at most kLongRow columns first, one warp each (8 per CTA), then the longer
+// rows, one CTA each with the columns cut into 8 contiguous pieces (a warp
+// streams only a few KB in flight, so a long row on one warp would be the
+// tail) and the 8 partial sums added in warp order.  Runs are the
+// fastest-varying part of the block index, so the B CTAs that read the same
+// factor rows run together and share them in L2.
+constexpr int kLongRow = 8192;
+
+__device__ __forceinline__ FF t_row_part(const float *__restrict__ v, const float2 *__restrict__ x, int c_begin,
+                                         int c_end, int lane)
 {
-    const int lane = threadIdx.x & 31;
-    const int r = (int)(blockIdx.x % (unsigned)B);
-    const int64_t w = ((blockIdx.x / (unsigned)B) * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (w >= t_rows || !run_on(act, act_stride, r)) return;
-    const longlong2 info = t_info[w];
-    const float *v = data + info.x;
-    const float2 *x = Xs + (int64_t)r * 2 * N + (int32_t)(info.y & 0xffffffffll);
-    const int Nc = (int)(info.y >> 32);
     FF sum{0.f, 0.f};
-    for (int c0k = 0; c0k < Nc; c0k += 1024) {
-        const int cend = min(Nc, c0k + 1024);
+    for (int c0k = c_begin; c0k < c_end; c0k += 1024) {
+        const int cend = min(c_end, c0k + 1024);
         Acc2 a0{0.f, 0.f}, a1{0.f, 0.f};
         int col = c0k + lane;
+        // 16 columns per lane in flight: an average rank row (~630 columns)
+        // is one or two rounds
+        for (; col + 480 < cend; col += 512) {
+            float k[16];
+            float2 xv[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                k[u] = __ldg(v + col + 32 * u);
+                xv[u] = x[col + 32 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < 16; u += 2) {
+                acc2_add(a0, k[u], xv[u]);
+                acc2_add(a1, k[u + 1], xv[u + 1]);
+            }
+        }
         for (; col + 96 < cend; col += 128) {
-            const float k0 = __ldg(v + col), k1 = __ldg(v + col + 32), k2 = __ldg(v + col + 64),
-                        k3 = __ldg(v + col + 96);
-            const float2 x0 = x[col], x1 = x[col + 32], x2 = x[col + 64], x3 = x[col + 96];
-            acc2_add(a0, k0, x0);
-            acc2_add(a1, k1, x1);
-            acc2_add(a0, k2, x2);
-            acc2_add(a1, k3, x3);
+            float k[4];
+            float2 xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                k[u] = __ldg(v + col + 32 * u);
+                xv[u] = x[col + 32 * u];
+            }
+            acc2_add(a0, k[0], xv[0]);
+            acc2_add(a1, k[1], xv[1]);
+            acc2_add(a0, k[2], xv[2]);
+            acc2_add(a1, k[3], xv[3]);
         }
         for (; col < cend; col += 32) acc2_add(a0, __ldg(v + col), x[col]);
         // the hi and lo parts of the FP32 partial sums of this chunk
@@ -381,8 +397,45 @@ lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t
         sum = ff_add(sum, FF{a1.s, 0.f});
         sum = ff_add(sum, FF{__fadd_rn(a0.c, a1.c), 0.f});
     }
-    sum = warp_sum_ff(sum);
-    if (lane == 0) T[w * (int64_t)B + r] = make_float2(sum.hi, sum.lo);
+    return warp_sum_ff(sum);
+}
+
+__global__ void __launch_bounds__(256)
+lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info,
+                 const int32_t *__restrict__ t_sched, int64_t nshort, int64_t nlong, int64_t short_ctas,
+                 const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T, const int32_t *act,
+                 int act_stride)
+{
+    __shared__ FF part[8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int r = (int)(blockIdx.x % (unsigned)B);
+    const int64_t cta = blockIdx.x / (unsigned)B;
+    if (!run_on(act, act_stride, r)) return;   // uniform per CTA
+    const float2 *xr = Xs + (int64_t)r * 2 * N;
+    if (cta < short_ctas) {
+        const int64_t q = cta * 8 + wid;
+        if (q >= nshort) return;
+        const int w = t_sched[q];
+        const longlong2 info = t_info[w];
+        const FF s = t_row_part(data + info.x, xr + (int32_t)(info.y & 0xffffffffll), 0, (int)(info.y >> 32), lane);
+        if (lane == 0) T[w * (int64_t)B + r] = make_float2(s.hi, s.lo);
+        return;
+    }
+    const int64_t q = cta - short_ctas;
+    if (q >= nlong) return;   // uniform per CTA
+    const int w = t_sched[nshort + q];
+    const longlong2 info = t_info[w];
+    const int Nc = (int)(info.y >> 32);
+    const int piece = (Nc / 8 + 31) / 32 * 32;
+    const int c_begin = min(Nc, wid * piece), c_end = min(Nc, (wid + 1) * piece);
+    const FF s = t_row_part(data + info.x, xr + (int32_t)(info.y & 0xffffffffll), c_begin, c_end, lane);
+    if (lane == 0) part[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        FF t = part[0];
+        for (int k = 1; k < 8; ++k) t = ff_add(t, part[k]);
+        T[w * (int64_t)B + r] = make_float2(t.hi, t.lo);
+    }
 }
 
 // One CTA per (leaf row cluster, run), the run fastest in the block index so
@@ -634,10 +687,13 @@ extern "C" int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B
     // all runs in one launch, run fastest in the block index; a run's result
     // does not depend on B
     if (H->t_rows > 0) {
-        const int64_t nT = (H->t_rows * 32 + 255) / 256 * B;
+        const int64_t nshort = H->t_rows - H->t_nlong;
+        const int64_t short_ctas = (nshort + 7) / 8;
+        const int64_t nT = (short_ctas + H->t_nlong) * B;
         PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
-        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_rows, Xs, N, B, T,
-                                                       run_active, active_stride);
+        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_sched, nshort,
+                                                       H->t_nlong, short_ctas, Xs, N, B, T, run_active,
+                                                       active_stride);
     }
     PQ3D_REQUIRE((int64_t)H->nleaves * B < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many leaves x runs");
     const unsigned gL = (unsigned)(H->nleaves * B);

@@ -221,6 +221,7 @@ class HMatrix:
         else:
             info = np.zeros((1, 2), dtype=np.int64)
         self.t_info = torch.as_tensor(info, device=dev)
+        self._make_sched(info)
         nl = leaves.shape[0]
         leaf_start = leaves[:, 0]
         lists = [[] for _ in range(nl)]
@@ -243,11 +244,22 @@ class HMatrix:
 
     _ARRAYS = ("perm", "blk", "rank", "off", "data", "lr_ids", "t_info", "t_off", "leaf", "leaf_ptr", "leaf_blocks")
 
+    LONG_ROW = 8192   # columns above which a rank row gets a whole CTA in the product
+
+    def _make_sched(self, info):
+        Nc = (np.asarray(info)[:, 1] >> 32) if self.t_rows else np.zeros(0, np.int64)
+        rows = np.arange(len(Nc), dtype=np.int32)
+        longm = Nc > self.LONG_ROW
+        sched = np.concatenate([rows[~longm], rows[longm]]) if len(Nc) else np.zeros(1, np.int32)
+        self.t_sched = torch.as_tensor(np.ascontiguousarray(sched, dtype=np.int32), device=self.device)
+        self.t_nlong = int(longm.sum())
+
     def _make_struct(self):
         H = _lib.HMat()
         H.N, H.nblocks, H.nleaves, H.t_rows = self.N, int(self.blk.shape[0]), int(self.leaf.shape[0]), self.t_rows
         for k in self._ARRAYS:
             setattr(H, k, getattr(self, k).data_ptr())
+        H.t_sched, H.t_nlong = self.t_sched.data_ptr(), self.t_nlong
         self.H = H
 
     def save(self, path):
@@ -269,6 +281,7 @@ class HMatrix:
         self.halfspace = bool(g["halfspace"]) if "halfspace" in g else False
         for k in cls._ARRAYS:
             setattr(self, k, torch.as_tensor(g[k], device=self.device))
+        self._make_sched(g["t_info"])
         self._make_struct()
         return self
 
