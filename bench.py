@@ -374,7 +374,32 @@ def bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks):
                                           "achieved": bytes_step * acc / dt / 1e9, "peak": peaks["hbm_gbs"],
                                           "frac": bytes_step * acc / dt / 1e9 / peaks["hbm_gbs"],
                                           "note": "operator bytes per accepted step / step time (whole step)"}}
+    if not args.no_cpu:
+        res["cpu_baseline"] = cpu_stepping_sample(torch, K64, tab, seconds=min(args.ref_seconds, 12.0))
     return res
+
+
+def cpu_stepping_sample(torch, K64, tab, seconds=12.0):
+    """The reference's CPU stepping algorithm (the oracle's NumPy
+    restatement, bit for bit equal to QDsim_gpu.simu_forward) on the same
+    operator and table, BLAS on all host threads, for about `seconds`."""
+    import oracle
+    from oracle.stepping import DenseStepper
+    from pyquake3d_gb300 import gf
+    ops = {k: np.ascontiguousarray(v.cpu().numpy()) for k, v in gf.split_ops(K64).items()}
+    st = DenseStepper(ops, tab, mu=MU, density=MU / 3464.0 ** 2)
+    st.run(1)
+    t0 = time.perf_counter()
+    att = 0
+    steps = 0
+    dttry = 1e-3
+    while time.perf_counter() - t0 < seconds:
+        h, dttry, a = st.simu_forward(dttry)
+        att += a
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": 7.0 * att / dt, "unit": "RK stages/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d accepted steps (%d attempts) of the N=%d stepping, %.1f s" % (steps, att, tab.shape[0], dt)}
 
 
 def bench_batched(torch, dev, args, peaks):
