@@ -282,12 +282,6 @@ __device__ __forceinline__ void acc2_add(Acc2 &a, float k, float2 x)
     a.c = fmaf(k, x.y, a.c);
 }
 
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // Float-float (unevaluated sum hi + lo) accumulation with FP32 operations
 // only (Knuth's TwoSum), for the reductions of the low-rank product: GB300's
@@ -345,15 +339,14 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
 // T[w * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo) pair for rank
 // row w (row l of low-rank block b).  The row's storage offset, first x
 // column and length come in one 16-byte record (t_info), so a warp starts
-// streaming after a single dependent load.  Work list t_sched: the rows of
-// at most kLongRow columns first, one warp each (8 per CTA), then the longer
+// streaming after a single dependent load.  Work list t_sched (built by the
+// host; the split is at 8,192 columns): the shorter rows first, one warp each
+// (8 per CTA), then the longer
 // rows, one CTA each with the columns cut into 8 contiguous pieces (a warp
 // streams only a few KB in flight, so a long row on one warp would be the
 // tail) and the 8 partial sums added in warp order.  Runs are the
 // fastest-varying part of the block index, so the B CTAs that read the same
 // factor rows run together and share them in L2.
-constexpr int kLongRow = 8192;
-
 __device__ __forceinline__ FF t_row_part(const float *__restrict__ v, const float2 *__restrict__ x, int c_begin,
                                          int c_end, int lane)
 {
