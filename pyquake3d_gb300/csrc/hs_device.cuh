@@ -152,7 +152,7 @@ struct FscTrig {
 };
 
 __device__ __forceinline__ void fsc_unit_disp(Dv y1, Dv y2, Dv y3, const FscTrig &T, double nu, double a,
-                                                       Dv u[3][3])
+                                              Dv u[3][3])
 {
     const double s = T.s, c = T.c, ct = T.ct, ic = 1.0 / c;
     const double n1 = 1.0 - 2.0 * nu, n2 = 1.0 - nu;
@@ -162,7 +162,7 @@ __device__ __forceinline__ void fsc_unit_disp(Dv y1, Dv y2, Dv y3, const FscTrig
     const Dv z3b = y3b * c - y1 * s;
     const Dv rb = dsqrt(y1 * y1 + y2 * y2 + y3b * y3b);
     const Dv irb = dinv(rb);
-    const Dv irb2 = irb * irb, irb3 = irb2 * irb;
+    const Dv irb2 = irb * irb;
     const Dv P = rb + y3b, Q = rb + z3b;
     const Dv iP = dinv(P), iQ = dinv(Q);
     const Dv h = y3b - a;
@@ -171,46 +171,56 @@ __device__ __forceinline__ void fsc_unit_disp(Dv y1, Dv y2, Dv y3, const FscTrig
     const Dv Fib = 2.0 * datan_ratio(-y2, y1 - P * T.cth);
     const Dv lP = dlog(P), lQ = dlog(Q);
     const Dv y1s = y1 * y1, y2s = y2 * y2;
-    const Dv car = c + ar;                 // cos + a / rb
+    // shared products (each formed once; the expressions below scale them)
+    const Dv car = c + ar, nar = nu + ar, tar = 2.0 * nu + ar, ar1 = 1.0 + ar;
     const Dv hirb = h * irb;
     const Dv rsy = rb * s - y1;
+    const Dv y1P = y1 * iP, y2P = y2 * iP, y2Q = y2 * iQ, z1Q = z1b * iQ;
+    const Dv G = y2 * hirb, GP = G * iP, GQ = G * iQ;        // y2 h / rb, / P, / Q
+    const Dv Y1h = y1 * hirb;                                // y1 h / rb
+    const Dv HP = h * iP, HQ = h * iQ;
+    const Dv WQ = W * iQ;
+    const Dv airb2 = a * irb2;                              // a / rb^2
+    const Dv ay3 = y3b * airb2;                             // a y3b / rb^2
+    const Dv aic = (a * ic) * irb;                          // a / (rb cos)
+    const Dv WQcar = WQ * car;
+    const Dv y2Qcar = y2Q * car;
     // b1
-    u[0][0] = (-2.0 * n2 * n1 * ct2) * Fib + n1 * y2 * iP * ((n1 - ar) * ct - y1 * iP * (nu + ar))
-              + (n1 * c * ct) * y2 * iQ * car + (a * ct) * y2 * h * irb3
-              + y2 * hirb * iP * (-n1 * ct + y1 * iP * (2.0 * nu + ar) + a * y1 * irb2)
-              + y2 * hirb * iQ * (c * iQ * (W * (n1 * c - ar) * ct + (2.0 * n2 * c) * rsy) - (a * c * ct) * y3b * irb2);
+    u[0][0] = (-2.0 * n2 * n1 * ct2) * Fib + n1 * (y2P * ((n1 - ar) * ct - y1P * nar)) + (n1 * c * ct) * y2Qcar
+              + (a * ct) * (G * irb2)
+              + GP * (-n1 * ct + y1P * tar + y1 * airb2)
+              + GQ * ((c * ct) * (WQ * (n1 * c - ar)) + (2.0 * n2 * c * c) * (rsy * iQ) - (c * ct) * ay3);
     u[0][1] = n1 * ((2.0 * n2 * ct2 - nu) * lP - ((2.0 * n2 * ct2 + n1) * c) * lQ)
-              - n1 * iP * (y1 * ct * (n1 - ar) + nu * y3b - a + y2s * iP * (nu + ar))
-              - (n1 * ct) * z1b * iQ * car - (a * ct) * y1 * h * irb3
-              + h * iP * (-2.0 * nu + (n1 * ct * y1 - a) * irb + y2s * irb * iP * (2.0 * nu + ar) + a * y2s * irb3)
-              + h * iQ * (c * c - ((n1 * ct) * z1b + a * c) * irb + (a * ct) * y3b * z1b * irb3
-                          - (y2s * (c * c) - (a * ct) * z1b * irb * W) * irb * iQ);
-    u[0][2] = (2.0 * n2) * ((n1 * ct) * Fib + y2 * iP * (2.0 * nu + ar) - c * y2 * iQ * car)
-              + y2 * hirb * (2.0 * nu * iP + a * irb2)
-              + c * y2 * hirb * iQ * (n1 - W * iQ * car - a * y3b * irb2);
+              - n1 * (iP * (ct * (y1 * (n1 - ar)) + nu * y3b - a + y2s * (iP * nar)))
+              - (n1 * ct) * (z1Q * car) - (a * ct) * (Y1h * irb2)
+              + HP * (-2.0 * nu + irb * ((n1 * ct) * y1 - a) + (y2s * irb) * (iP * tar) + y2s * (airb2 * irb))
+              + HQ * (c * c - irb * ((n1 * ct) * z1b + a * c) + (a * ct) * (z1b * (y3b * (irb2 * irb)))
+                      - (irb * iQ) * ((c * c) * y2s - (a * ct) * (z1b * (irb * W))));
+    u[0][2] = (2.0 * n2) * ((n1 * ct) * Fib + y2P * tar - c * y2Qcar)
+              + G * (2.0 * nu * iP + airb2)
+              + c * (GQ * (n1 - WQcar - ay3));
     // b2
     u[1][0] = n1 * ((2.0 * n2 * ct2 + nu) * lP - ((2.0 * n2 * ct2 + 1.0) * c) * lQ)
-              + n1 * iP * (-(n1 * ct) * y1 + nu * y3b - a + (a * ct) * y1 * irb + y1s * iP * (nu + ar))
-              - (n1 * ct) * iQ * (c * z1b - (a * ic) * rsy * irb) - (a * ct) * y1 * h * irb3
-              + h * iP * (2.0 * nu + ((n1 * ct) * y1 + a) * irb - y1s * irb * iP * (2.0 * nu + ar) - a * y1s * irb3)
-              + ct * h * iQ * (-c * s + (a * ic) * y1 * y3b * irb3
-                               + rsy * irb * ((2.0 * n2 * c) - W * iQ * (1.0 + (a * ic) * irb)));
-    u[1][1] = (2.0 * n2 * n1 * ct2) * Fib + n1 * y2 * iP * (-(n1 - ar) * ct + y1 * iP * (nu + ar))
-              - (n1 * ct) * y2 * iQ * (1.0 + (a * ic) * irb) - (a * ct) * y2 * h * irb3
-              + y2 * hirb * iP * (n1 * ct - 2.0 * nu * y1 * iP - a * y1 * irb * (irb + iP))
-              + ct * y2 * hirb * iQ * (-2.0 * n2 * c + W * iQ * (1.0 + (a * ic) * irb) + (a * ic) * y3b * irb2);
-    u[1][2] = (-2.0 * n2 * n1 * ct) * (lP - c * lQ) - (2.0 * n2) * y1 * iP * (2.0 * nu + ar)
-              + (2.0 * n2) * z1b * iQ * car + hirb * (n1 * ct - 2.0 * nu * y1 * iP - a * y1 * irb2)
-              - h * iQ * (c * s + ct * W * irb * (2.0 * n2 * c - W * iQ)
-                          + a * irb * (s - y3b * z1b * irb2 - z1b * W * irb * iQ));
+              + n1 * (iP * (-(n1 * ct) * y1 + nu * y3b - a + (a * ct) * (y1 * irb) + y1s * (iP * nar)))
+              - (n1 * ct) * (iQ * (c * z1b - rsy * aic)) - (a * ct) * (Y1h * irb2)
+              + HP * (2.0 * nu + irb * ((n1 * ct) * y1 + a) - (y1s * irb) * (iP * tar) - y1s * (airb2 * irb))
+              + ct * (HQ * (-c * s + ic * (y1 * (ay3 * irb)) + (rsy * irb) * ((2.0 * n2 * c) - WQ * (1.0 + aic))));
+    u[1][1] = (2.0 * n2 * n1 * ct2) * Fib + n1 * (y2P * (-(n1 - ar) * ct + y1P * nar))
+              - (n1 * ct) * (y2Q * (1.0 + aic)) - (a * ct) * (G * irb2)
+              + GP * (n1 * ct - 2.0 * nu * y1P - (a * y1) * (irb * (irb + iP)))
+              + ct * (GQ * (-2.0 * n2 * c + WQ * (1.0 + aic) + ic * ay3));
+    u[1][2] = (-2.0 * n2 * n1 * ct) * (lP - c * lQ) - (2.0 * n2) * (y1P * tar)
+              + (2.0 * n2) * (z1Q * car) + hirb * (n1 * ct - 2.0 * nu * y1P - y1 * airb2)
+              - HQ * (c * s + ct * (W * irb) * (2.0 * n2 * c - WQ)
+                      + ar * (s - z1b * (y3b * irb2) - z1b * (W * irb) * iQ));
     // b3
-    u[2][0] = n1 * (y2 * iP * (1.0 + ar) - c * y2 * iQ * car) - y2 * hirb * (a * irb2 + iP)
-              + c * y2 * hirb * iQ * (W * iQ * car + a * y3b * irb2);
-    u[2][1] = n1 * (-s * lQ - y1 * iP * (1.0 + ar) + z1b * iQ * car) + y1 * hirb * (a * irb2 + iP)
-              - h * iQ * (s * (c - ar) + z1b * irb * (1.0 + a * y3b * irb2)
-                          - ((c * s) * y2s - a * z1b * irb * W) * irb * iQ);
-    u[2][2] = (2.0 * n2) * Fib + (2.0 * n2 * s) * y2 * iQ * car
-              + s * y2 * hirb * iQ * (1.0 + W * iQ * car + a * y3b * irb2);
+    u[2][0] = n1 * (y2P * ar1 - c * y2Qcar) - G * (airb2 + iP)
+              + c * (GQ * (WQcar + ay3));
+    u[2][1] = n1 * (-s * lQ - y1P * ar1 + z1Q * car) + Y1h * (airb2 + iP)
+              - HQ * (s * (c - ar) + (z1b * irb) * (1.0 + ay3)
+                      - (irb * iQ) * ((c * s) * y2s - a * (z1b * (irb * W))));
+    u[2][2] = (2.0 * n2) * Fib + (2.0 * n2 * s) * y2Qcar
+              + s * (GQ * (1.0 + WQcar + ay3));
 }
 
 // d/dy of the harmonic displacement at one end point for NB Burgers vectors b
