@@ -194,10 +194,14 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
 {
     __shared__ double red[8];
     __shared__ int act;
-    __shared__ double hs;
+    __shared__ double hs, log_etaV0;
     const int r = blockIdx.y;
     pq3d_run_ctrl *C = S.ctrl + r;
-    if (threadIdx.x == 0) { act = C->active; hs = C->h; }
+    if (threadIdx.x == 0) {
+        act = C->active;
+        hs = C->h;
+        if (kMixed) log_etaV0 = log(S.eta * S.V0);
+    }
     __syncthreads();
     if (!act) return;
     const int64_t N = S.N;
@@ -212,17 +216,12 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
             q0 += p[0]; q1 += p[1]; q2 += p[2];
         }
         const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
-        const double a = S.a[idx], b = S.b[idx], dc = S.dc[idx];
-        Cell c{a, b, dc, S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig, 0.0, 0.0, 0.0};
-        if (kMixed) {
-            c.inv_a = 1.0 / a; c.inv_b = 1.0 / b; c.bdc = b / dc;
-            c.L1 = (float)(-c.AdotV1 + c.shear);
-            c.L2 = (float)(-c.AdotV2 + c.shear);
-            c.dsf = (float)(c.dsig - c.dPdt);
-        }
+        const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
+                     0.0, 0.0};
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
         double yo[4], e1, e2;
-        dp_attempt<kMixed>(c, S.V0, S.eta, hs, y, yo, e1, e2);
+        if (kMixed) dp_attempt_mixed(c, S.V0, log_etaV0, hs, y, yo, e1, e2);
+        else dp_attempt(c, S.V0, S.eta, hs, y, yo, e1, e2);
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
         m1 = e1;
         m2 = e2;
@@ -388,7 +387,7 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
         if (rc) return rc;
     }
     PQ3D_CUDA_TRY(cudaGetLastError());
-    // 2. attempt (FP64 arm: the reference right-hand side; mixed arms: rhs_mixed)
+    // 2. attempt (FP64 arm: the reference arithmetic; mixed arms: dp_attempt_mixed)
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
     if (S.precision == PQ3D_BATCH_FP64) attempt_kernel<false><<<grid, 256, 0, st>>>(S);
     else attempt_kernel<true><<<grid, 256, 0, st>>>(S);

@@ -28,9 +28,7 @@ constexpr double kRelTol = 1e-4;
 
 struct Cell {
     double a, b, dc, f0, shear, slipv, AdotV1, AdotV2, dsig;
-    double inv_a, inv_b, bdc;   // 1/a, 1/b, b/dc (used by the mixed-precision right-hand side)
-    double P, dPdt;             // pore pressure (Pa) and its rate (Pa/s); 0 without dilatancy
-    float L1, L2, dsf;          // mixed right-hand side: -AdotV1 + shear, -AdotV2 + shear, dsig - dPdt
+    double P, dPdt;   // pore pressure (Pa) and its rate (Pa/s); 0 without dilatancy
 };
 
 __device__ __forceinline__ double clip700(double x) { return fmin(fmax(x, -700.0), 700.0); }
@@ -61,11 +59,11 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     dtau2 = t2 / 1e6;
 }
 
-// e^x for the mixed-precision right-hand side: x = (n + f) / log2(e) with n
-// integer and |f| <= 1/2 (Cody-Waite range reduction); 2^f from the FP32
-// exp2f, 2^n exact.  Relative error ~2.5e-7 (that of exp2f), 6 FP64
-// operations instead of the ~20 of an FP64 exp.  The argument is clipped to
-// +-700 like the reference's safe_exp.
+// e^x with x = (n + f) / log2(e), n integer and |f| <= 1/2 (Cody-Waite
+// range reduction); 2^f from the FP32 exp2f, 2^n exact.  Relative error
+// ~2.5e-7 (that of exp2f), 6 FP64 operations instead of the ~20 of an FP64
+// exp.  The argument is clipped to +-700 like the reference's safe_exp.
+// Used by the mixed-precision slip-rate update.
 __device__ __forceinline__ double fexp(double x)
 {
     x = fmin(fmax(x, -700.0), 700.0);
@@ -76,103 +74,178 @@ __device__ __forceinline__ double fexp(double x)
     return (double)exp2f(f) * scale;
 }
 
-// 1/d for the mixed right-hand side: the FP32 reciprocal refined by one
-// Newton-Raphson step r <- r (2 - d r) in FP64 (the relative error squares:
-// ~4e-15), two FMAs instead of a full FP64 division.  d > 0, in FP32 range.
+// 1/d: the FP32 reciprocal refined by one Newton-Raphson step
+// r <- r (2 - d r) in FP64 (the relative error squares: ~4e-15), two FMAs
+// instead of a full FP64 division.  d in FP32 range.
 __device__ __forceinline__ double rcp_nr(double d)
 {
     const double r = (double)__frcp_rn((float)d);
     return fma(r, fma(-d, r, 1.0), r);
 }
 
-// e^x as FP32: the argument reduced in FP64 as in fexp, 2^f from exp2f and
-// the exact power-of-two scaling in FP32 (ldexpf: underflow to 0 where the
-// term is negligible).
-__device__ __forceinline__ float fexpf(double x)
+// ---------------------------------------------------------------------------
+// Mixed-precision attempt (batched mixed modes).
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate, so the seven right-hand sides of
+// an attempt run in FP32 and only per-attempt set-up and the final state
+// update are FP64.  Two reformulations keep FP32 both accurate and in range:
+//
+// (1) Increments.  A stage state is the attempt's start state y0 plus an
+//     increment h * sum_l A_jl k_l that is formed in FP32 (relative error
+//     ~1e-7 of the increment, not of the state).  The large exponent
+//     arguments -psi/a and tau/(a sigma) (~200, nearly cancelling) are
+//     evaluated once per attempt in FP64 at y0; at a stage only their
+//     change is added, in FP32, to a float-float (hi + lo) copy of the
+//     FP64 value, so the exponent keeps ~1e-7 absolute accuracy.
+//
+// (2) Scale.  With u = -psi/a + |x|, x = tau/(a sigma), r = e^{-2|x|} and
+//     W = eta V0 e^u the traction rate of the right-hand side (the
+//     reference's dtau/dt, src/QDsim_gpu.py:772-828) is
+//         dtau/dt = (L + W M) / (1 + W D),
+//         D = (1 + r) / (a sigma),   M = D (tau/sigma) dsigma/dt
+//                                      + sign(x) (1 - r)/a * dpsi/dt,
+//     L = -K.v' + shear loading.  W spans e^{+-100} within one attempt
+//     (an intermediate Dormand-Prince stage can overshoot by >100 in u;
+//     FP64 stays finite there and may still accept the step), so the form
+//     is evaluated with w = e^{-|ln W|} <= 1: (L + w M)/(1 + w D) when
+//     W < 1, (L w + M)/(w + D) when W >= 1.  Nothing overflows.
+//
+// Derivatives then match the FP64 right-hand side to ~2e-7 relative and the
+// error norms to ~1e-6.  A stage whose FP32 arithmetic still leaves the
+// float range (psi itself running away, e^{(f0-psi)/b} > 1e38) gives an
+// infinite error, i.e. a rejection with dt halved, which is what the FP64
+// arithmetic decides for such a stage; a NaN in the inputs stays NaN.
+
+struct FF {   // hi + lo, |lo| <= ulp(hi) / 2
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_split(double x)
 {
-    x = fmin(fmax(x, -700.0), 700.0);
-    const double t = x * 1.4426950408889634;
-    const double n = rint(t);
-    return ldexpf(exp2f((float)(t - n)), (int)fmax(fmin(n, 300.0), -300.0));
+    const float h = (float)x;
+    return FF{h, (float)(x - (double)h)};
 }
 
-// Mixed-precision right-hand side (batched mixed modes).  Same equations as
-// rhs().  What needs FP64 stays FP64: the state, the exponent arguments
-// tau/(a sigma) and -psi/a (large and nearly cancelling: they are summed in
-// FP64 before the exponential) and everything downstream of the right-hand
-// side (stage sums, increments, error norm).  The factors e^{-psi/a} cosh(x),
-// e^{-psi/a} sinh(x) are formed as (e^{x - psi/a} +- e^{-x - psi/a}) / 2 with
-// fexpf, and the algebra after the exponentials (slip-rate derivatives,
-// aging law, radiation-damping quotient; relative error ~1e-7, the level of
-// the product's) runs in FP32 -- GB300's FP64 rate is 1/64 of FP32.
-// Cell-constant loads (-AdotV + shear, sigma rate - P rate) come in as FP32.
-__device__ __forceinline__ void rhs_mixed_f(const Cell &c, double V0, double eta, double Tno, double Tt1o,
-                                            double Tt2o, double state, float &dstate, float &dtau1, float &dtau2)
+// (b.hi + b.lo) + d as (s, lo); TwoSum with explicit rounding so that the
+// compiler does not contract it
+__device__ __forceinline__ FF ff_add(FF b, float d)
 {
-    const double Tn = Tno * 1e6 - c.P, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
-    const double inv_aTn = rcp_nr(c.a * Tn);
-    const double x1 = clip700(T1 * inv_aTn), x2 = clip700(T2 * inv_aTn);
-    const double sp = clip700(-state * c.inv_a);
-    const float e1p = fexpf(sp + x1), e1m = fexpf(sp - x1), e2p = fexpf(sp + x2), e2m = fexpf(sp - x2);
-    const float ed = fexpf((c.f0 - state) * c.inv_b);
-    const float V0f = (float)V0, iaT = (float)inv_aTn, inv_a = (float)c.inv_a, etaf = (float)eta;
-    const float inv_Tn = (float)(c.a * inv_aTn);
-    const float dV1dtau = V0f * iaT * (e1p + e1m);
-    const float dV2dtau = V0f * iaT * (e2p + e2m);
-    const float dV1dsigma = -dV1dtau * (float)T1 * inv_Tn;
-    const float dV2dsigma = -dV2dtau * (float)T2 * inv_Tn;
-    const float dV1dstate = -V0f * inv_a * (e1p - e1m);
-    const float dV2dstate = -V0f * inv_a * (e2p - e2m);
-    const float ds_dt = (float)c.bdc * (V0f * ed - (float)c.slipv);
-    const float den1 = 1.0f + etaf * dV1dtau, den2 = 1.0f + etaf * dV2dtau;
-    const float inv12 = 1.0f / (den1 * den2);
-    const float t1 = (c.L1 - etaf * (dV1dsigma * c.dsf + dV1dstate * ds_dt)) * (den2 * inv12);
-    const float t2 = (c.L2 - etaf * (dV2dsigma * c.dsf + dV2dstate * ds_dt)) * (den1 * inv12);
+    const float s = __fadd_rn(b.hi, d);
+    const float bp = __fsub_rn(s, b.hi);
+    const float e = __fadd_rn(__fsub_rn(b.hi, __fsub_rn(s, bp)), __fsub_rn(d, bp));
+    return FF{s, __fadd_rn(e, b.lo)};
+}
+
+// e^{-|v|} of v = hi + lo: e^{-|hi|} (1 -+ lo), |lo| ~ 1e-6 at most
+__device__ __forceinline__ float ff_exp_neg_abs(FF v)
+{
+    const float e = expf(-fabsf(v.hi));
+    return v.hi >= 0.f ? e * (1.f - v.lo) : e * (1.f + v.lo);
+}
+
+__device__ __forceinline__ float ff_exp(FF v) { return expf(v.hi) * (1.f + v.lo); }
+
+// per-attempt constants of one cell
+struct MixedBase {
+    float Tn0;          // effective normal stress at y0 (MPa)
+    float q0[2];        // tau_k / sigma at y0
+    float x0[2];        // tau_k / (a sigma) at y0 (hi part: sign and r only)
+    FF Sp[2], Sm[2];    // -psi0/a + ln(eta V0) +- x0_k
+    FF g0;              // (f0 - psi0) / b
+    float a, inv_a, inv_b, bdc, V0, slipv, dsf;
+    float L[2];         // -K.v' + shear loading (Pa/s)
+};
+
+__device__ __forceinline__ MixedBase mixed_base(const Cell &c, double V0, double log_etaV0, const double y[4])
+{
+    MixedBase m;
+    const double Tn0 = y[0] - c.P * 1e-6;   // MPa
+    const double r0 = rcp_nr(Tn0), inv_a = rcp_nr(c.a), inv_b = rcp_nr(c.b);
+    const double q1 = y[1] * r0, q2 = y[2] * r0;
+    const double x1 = q1 * inv_a, x2 = q2 * inv_a;
+    const double sp = fma(-y[3], inv_a, log_etaV0);
+    m.Tn0 = (float)Tn0;
+    m.q0[0] = (float)q1; m.q0[1] = (float)q2;
+    m.x0[0] = (float)x1; m.x0[1] = (float)x2;
+    m.Sp[0] = ff_split(sp + x1); m.Sm[0] = ff_split(sp - x1);
+    m.Sp[1] = ff_split(sp + x2); m.Sm[1] = ff_split(sp - x2);
+    m.g0 = ff_split((c.f0 - y[3]) * inv_b);
+    m.a = (float)c.a;
+    m.inv_a = (float)inv_a;
+    m.inv_b = (float)inv_b;
+    m.bdc = (float)c.b / (float)c.dc;
+    m.V0 = (float)V0;
+    m.slipv = (float)c.slipv;
+    m.dsf = (float)(c.dsig - c.dPdt);
+    m.L[0] = (float)(-c.AdotV1 + c.shear);
+    m.L[1] = (float)(-c.AdotV2 + c.shear);
+    return m;
+}
+
+// Right-hand side at y0 + (dTn, dT1, dT2, dpsi) (MPa, MPa, MPa, state):
+// dpsi/dt and dtau_k/dt (MPa/s).
+__device__ __forceinline__ void mixed_rhs(const MixedBase &m, float dTn, float dT1, float dT2, float dpsi,
+                                          float &dstate, float &dtau1, float &dtau2)
+{
+    const float rTn = __frcp_rn(m.Tn0 + dTn);
+    const float iaTn = m.inv_a * rTn;                          // 1 / (a sigma), 1/MPa
+    const float ed = ff_exp(ff_add(m.g0, -dpsi * m.inv_b));    // e^{(f0 - psi)/b}
+    const float ds_dt = m.bdc * (m.V0 * ed - m.slipv);
+    const float dpa = dpsi * m.inv_a;
+    float out[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float dx = ((k ? dT2 : dT1) - m.q0[k] * dTn) * iaTn;   // change of tau/(a sigma)
+        const float xs = m.x0[k] + dx;
+        const bool pos = xs >= 0.f;
+        const float em = expm1f(-2.f * fabsf(xs));                  // r - 1
+        const FF lw = ff_add(pos ? m.Sp[k] : m.Sm[k], (pos ? dx : -dx) - dpa);   // ln W
+        const float w = ff_exp_neg_abs(lw);
+        const float q = m.q0[k] + m.a * dx;                         // tau / sigma
+        const float D = (2.f + em) * iaTn * 1e-6f;                  // (1 + r) / (a sigma), 1/Pa
+        const float M = D * q * m.dsf + m.inv_a * (pos ? -em : em) * ds_dt;
+        const float L = m.L[k];
+        out[k] = (lw.hi >= 0.f) ? __fdiv_rn(fmaf(L, w, M), w + D) : __fdiv_rn(fmaf(w, M, L), fmaf(w, D, 1.f));
+    }
     dstate = ds_dt;
-    dtau1 = t1 * 1e-6f;
-    dtau2 = t2 * 1e-6f;
+    dtau1 = out[0] * 1e-6f;
+    dtau2 = out[1] * 1e-6f;
 }
 
-__device__ __forceinline__ void rhs_mixed(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
-                                          double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+// |num| / |den| in FP32 where den is in float range, else in FP64
+__device__ __forceinline__ double rel_err(float num, double den)
 {
-    float ds, t1, t2;
-    rhs_mixed_f(c, V0, eta, Tno, Tt1o, Tt2o, state, ds, t1, t2);
-    dstate = ds;
-    dsig = c.dsig * 1e-6;
-    dtau1 = t1;
-    dtau2 = t2;
+    const double ad = fabs(den);
+    if (ad >= 1e-30 && ad <= 1e30) return (double)__fdiv_rn(fabsf(num), (float)ad);
+    return fabs((double)num) / ad;
 }
 
-template <bool kMixed>
-__device__ __forceinline__ void rhs_sel(const Cell &c, double V0, double eta, double Tno, double Tt1o, double Tt2o,
-                                        double state, double &dstate, double &dsig, double &dtau1, double &dtau2)
+__device__ __forceinline__ bool finite_cell(const Cell &c, const double y[4])
 {
-    if (kMixed) rhs_mixed(c, V0, eta, Tno, Tt1o, Tt2o, state, dstate, dsig, dtau1, dtau2);
-    else rhs(c, V0, eta, Tno, Tt1o, Tt2o, state, dstate, dsig, dtau1, dtau2);
+    return isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) && isfinite(c.AdotV1) &&
+           isfinite(c.AdotV2) && isfinite(c.dsig) && isfinite(c.slipv);
 }
 
-// One Dormand-Prince attempt of one cell; y = (Tno, Tt1o, Tt2o, state).
-// Writes the 5th-order solution to yo and returns the two relative errors.
-// Mixed attempt: the stage derivatives come from rhs_mixed_f as FP32 and
-// their weighted sums are formed in FP32 (they carry the derivatives' ~1e-7
-// relative error already); each stage state is y + h * sum with one FP64
-// multiply-add, and the 5th-minus-4th-order difference is summed directly
-// (h * sum (b_i - b*_i) k_i) instead of subtracting two FP64 states.  The
-// normal-stress rate is constant over the step.
-__device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, double eta, double h, const double y[4],
-                                                 double yo[4], double &e1, double &e2)
+// One Dormand-Prince attempt of one cell in the mixed arithmetic above.
+// log_etaV0 = ln(eta V0).  Writes the 5th-order solution to yo and returns
+// the two relative errors (as the FP64 attempt below).
+__device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, double log_etaV0, double h,
+                                                 const double y[4], double yo[4], double &e1, double &e2)
 {
-    float s[7], t[7], u[7];
-    const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
-    const double dn = c.dsig * 1e-6;   // d(Tno)/dt, MPa/s
+    const MixedBase m = mixed_base(c, V0, log_etaV0, y);
+    const float hf = (float)h;
+    const float dn = (float)(c.dsig * 1e-6);   // d(Tno)/dt, MPa/s, constant over the step
     const float A[6][6] = {{(float)B21, 0, 0, 0, 0, 0},
                            {(float)B31, (float)B32, 0, 0, 0, 0},
                            {(float)B41, (float)B42, (float)B43, 0, 0, 0},
                            {(float)B51, (float)B52, (float)B53, (float)B54, 0, 0},
                            {(float)B61, (float)B62, (float)B63, (float)B64, (float)B65, 0},
                            {(float)B71, 0.f, (float)B73, (float)B74, (float)B75, (float)B76}};
-    rhs_mixed_f(c, V0, eta, Tno, Tt1o, Tt2o, st, s[0], t[0], u[0]);
+    const float wsum[6] = {(float)B21, (float)(B31 + B32), (float)(B41 + B42 + B43), (float)(B51 + B52 + B53 + B54),
+                           (float)(B61 + B62 + B63 + B64 + B65), (float)(B71 + B73 + B74 + B75 + B76)};
+    float s[7], t[7], u[7];
+    float inc[4] = {0.f, 0.f, 0.f, 0.f};
+    mixed_rhs(m, 0.f, 0.f, 0.f, 0.f, s[0], t[0], u[0]);
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         float ds = 0.f, dt1 = 0.f, dt2 = 0.f;
@@ -182,13 +255,14 @@ __device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, doubl
             dt1 = fmaf(A[j][l], t[l], dt1);
             dt2 = fmaf(A[j][l], u[l], dt2);
         }
-        const double wsum[6] = {B21, B31 + B32, B41 + B42 + B43, B51 + B52 + B53 + B54, B61 + B62 + B63 + B64 + B65,
-                                B71 + B73 + B74 + B75 + B76};
-        const double Tn_j = Tno + h * (wsum[j] * dn);   // the normal-stress rate is constant
-        const double T1_j = Tt1o + h * (double)dt1, T2_j = Tt2o + h * (double)dt2, st_j = st + h * (double)ds;
-        if (j == 5) { yo[0] = Tn_j; yo[1] = T1_j; yo[2] = T2_j; yo[3] = st_j; }
-        rhs_mixed_f(c, V0, eta, Tn_j, T1_j, T2_j, st_j, s[j + 1], t[j + 1], u[j + 1]);
+        const float dTn = hf * (wsum[j] * dn), dT1 = hf * dt1, dT2 = hf * dt2, dps = hf * ds;
+        if (j == 5) { inc[0] = dTn; inc[1] = dT1; inc[2] = dT2; inc[3] = dps; }
+        mixed_rhs(m, dTn, dT1, dT2, dps, s[j + 1], t[j + 1], u[j + 1]);
     }
+    yo[0] = y[0] + (double)inc[0];
+    yo[1] = y[1] + (double)inc[1];
+    yo[2] = y[2] + (double)inc[2];
+    yo[3] = y[3] + (double)inc[3];
     // 4th-order minus 5th-order solution: h * sum (B8i - B7i) k_i
     const float D[7] = {(float)(B81 - B71), 0.f, (float)(B83 - B73), (float)(B84 - B74), (float)(B85 - B75),
                         (float)(B86 - B76), (float)B87};
@@ -199,37 +273,39 @@ __device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, doubl
         e1t = fmaf(D[l], t[l], e1t);
         e2t = fmaf(D[l], u[l], e2t);
     }
+    es *= hf; e1t *= hf; e2t *= hf;
     const double wn = (B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76);
-    const double st8 = yo[3] + h * (double)es;
-    const double T18 = yo[1] + h * (double)e1t, T28 = yo[2] + h * (double)e2t, Tn8 = yo[0] + h * (wn * dn);
-    e1 = fabs(fabs(h * (double)es) / st8);
-    const double ea = fabs(fabs(h * (double)e1t) / T18);
-    const double eb = fabs(fabs(h * (double)e2t) / T28);
-    const double ec = fabs(fabs(h * (wn * dn)) / Tn8);
+    const double en = h * (wn * (c.dsig * 1e-6));
+    e1 = rel_err(es, yo[3] + (double)es);
+    const double ea = rel_err(e1t, yo[1] + (double)e1t);
+    const double eb = rel_err(e2t, yo[2] + (double)e2t);
+    const double ec = fabs(en) / fabs(yo[0] + en);
     e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
+    if (!(isfinite(e1) && isfinite(e2)) && finite_cell(c, y)) {
+        if (!isfinite(e1)) e1 = INFINITY;
+        if (!isfinite(e2)) e2 = INFINITY;
+    }
 }
 
-template <bool kMixed = false>
+// One Dormand-Prince attempt of one cell in FP64, the reference arithmetic
+// (src/QDsim_gpu.py:1266-1397).  Writes the 5th-order solution to yo and
+// returns the two relative errors.
 __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
                                            double yo[4], double &e1, double &e2)
 {
-    if (kMixed) {
-        dp_attempt_mixed(c, V0, eta, h, y, yo, e1, e2);
-        return;
-    }
     double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
         u7;
     const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
-    rhs_sel<kMixed>(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
-    rhs_sel<kMixed>(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
-    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
+    rhs(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
+    rhs(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
+    rhs(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),
         st + h * (B31 * s1 + B32 * s2), s3, n3, t3, u3);
-    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
+    rhs(c, V0, eta, Tno + h * (B41 * n1 + B42 * n2 + B43 * n3), Tt1o + h * (B41 * t1 + B42 * t2 + B43 * t3),
         Tt2o + h * (B41 * u1 + B42 * u2 + B43 * u3), st + h * (B41 * s1 + B42 * s2 + B43 * s3), s4, n4, t4, u4);
-    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
+    rhs(c, V0, eta, Tno + h * (B51 * n1 + B52 * n2 + B53 * n3 + B54 * n4),
         Tt1o + h * (B51 * t1 + B52 * t2 + B53 * t3 + B54 * t4), Tt2o + h * (B51 * u1 + B52 * u2 + B53 * u3 + B54 * u4),
         st + h * (B51 * s1 + B52 * s2 + B53 * s3 + B54 * s4), s5, n5, t5, u5);
-    rhs_sel<kMixed>(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
+    rhs(c, V0, eta, Tno + h * (B61 * n1 + B62 * n2 + B63 * n3 + B64 * n4 + B65 * n5),
         Tt1o + h * (B61 * t1 + B62 * t2 + B63 * t3 + B64 * t4 + B65 * t5),
         Tt2o + h * (B61 * u1 + B62 * u2 + B63 * u3 + B64 * u4 + B65 * u5),
         st + h * (B61 * s1 + B62 * s2 + B63 * s3 + B64 * s4 + B65 * s5), s6, n6, t6, u6);
@@ -237,7 +313,7 @@ __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta,
     yo[1] = Tt1o + h * (B71 * t1 + B73 * t3 + B74 * t4 + B75 * t5 + B76 * t6);
     yo[2] = Tt2o + h * (B71 * u1 + B73 * u3 + B74 * u4 + B75 * u5 + B76 * u6);
     yo[3] = st + h * (B71 * s1 + B73 * s3 + B74 * s4 + B75 * s5 + B76 * s6);
-    rhs_sel<kMixed>(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
+    rhs(c, V0, eta, yo[0], yo[1], yo[2], yo[3], s7, n7, t7, u7);
     const double Tn8 = Tno + h * (B81 * n1 + B83 * n3 + B84 * n4 + B85 * n5 + B86 * n6 + B87 * n7);
     const double T18 = Tt1o + h * (B81 * t1 + B83 * t3 + B84 * t4 + B85 * t5 + B86 * t6 + B87 * t7);
     const double T28 = Tt2o + h * (B81 * u1 + B83 * u3 + B84 * u4 + B85 * u5 + B86 * u6 + B87 * u7);

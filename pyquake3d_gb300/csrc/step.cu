@@ -250,9 +250,9 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             const int slot = (int)(attempt % 3);
             double m1 = 0.0, m2 = 0.0;
             for (int64_t i = gtid; i < N; i += gsz) {
-                Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
-                       S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2], 0.0, 0.0, 0.0,
-                       S.P ? S.P[i] : 0.0, S.dPdt ? S.dPdt[i] : 0.0};
+                const Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
+                             S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2],
+                             S.P ? S.P[i] : 0.0, S.dPdt ? S.dPdt[i] : 0.0};
                 const double y[4] = {S.Tno[i], S.Tt1o[i], S.Tt2o[i], S.state[i]};
                 double yo[4], e1, e2;
                 dp_attempt(c, S.V0, S.eta, h, y, yo, e1, e2);

@@ -159,3 +159,103 @@ def test_failing_run_is_retired_alone(cuda, golden):
     assert c[1].status == _lib.PQ3D_ERR_STEP and c[1].active == 0 and c[1].attempts == 21
     for r in (0, 2):
         assert c[r].status == 0 and c[r].steps == 25
+
+
+# Cells recorded from RK45 stepping of the 200 x 40 km rough fault (N = 100,000,
+# H-matrix product, nucleation patch at 1e-3 m/s) at t = 26.2 s:
+# (a, b, dc, f0, Tno, Tt1o, Tt2o, state, V, AdotV1, AdotV2, dsigma/dt).  With
+# dt = 9.2124 s, stage 5 of the Dormand-Prince attempt overshoots the first
+# four cells' shear stress by ~11 MPa, i.e. the slip-rate exponent by ~100:
+# FP64 stays finite there (the step is rejected with a moderate error); FP32
+# e^x overflows unless the right-hand side is kept in scale.
+STAGE_OVERSHOOT_DT = 9.212423770310084
+STAGE_OVERSHOOT_CELLS = np.array([
+    (0.004, 0.03, 0.14, 0.6, 25.10468272887533, 20.86252722459316, -0.002760444839195026, 0.7992124489447135,
+     0.002841888671875, 71096.96010955973, -5694.026039135735, 6560.18839958655),
+    (0.004, 0.03, 0.14, 0.6, 25.01407476670933, 20.789991456525662, -0.0022071424474962094, 0.7989258258571602,
+     0.003138430908203125, 94074.79105999242, -6539.926320837528, 821.216190121016),
+    (0.004, 0.03, 0.14, 0.6, 25.010806663905637, 20.783066464523046, -0.003983947056773062, 0.7986710025369866,
+     0.00320707470703125, 71442.20331160886, -4145.00307035588, 765.1998111441719),
+    (0.004, 0.03, 0.14, 0.6, 24.979281731662297, 20.754842854125048, -0.0017027261935954384, 0.7982971840641563,
+     0.0034505085449218747, 78594.30492606362, -4672.568136799041, -1424.6719326721313),
+    (0.007839999999999993, 0.03, 0.14, 0.6, 25.00000776405218, 18.827723270419693, -3.647291134394441e-05,
+     0.8072326583603793, 1.0041975183412432e-09, -43.931460405325566, 1.9563141481575645, 0.42981355991842674),
+    (0.02656, 0.03, 0.14, 0.6, 25.000243771293796, 15.601184432203162, 0.0024916621398196393, 0.8072326583459437,
+     1.0105451801791787e-09, -351.2858186715674, -130.83729749546245, 11.993399799267007),
+    (0.04000000000000001, 0.03, 0.14, 0.6, 25.000001389555507, 13.273161081080296, 7.962887358376142e-06,
+     0.8072326583692505, 1.000099233348689e-09, -5.346188035257384, -0.4267521966803598, 0.0764763278500351),
+    (0.004, 0.03, 0.14, 0.6, 24.999990713881537, 19.50592064913241, 0.0011329691141147916, 0.8072326580016972,
+     1.1721852933987974e-09, -803.5071173343583, -67.20042687143759, -1.0927068774489872)])
+
+
+def _recorded_cells_ensemble(cuda, precision, h, rows):
+    """One run over the recorded cells: state written directly, and a
+    (3n x 2n) operator with one non-zero column per cell so that K.v'
+    reproduces the recorded traction rates."""
+    cells = STAGE_OVERSHOOT_CELLS[rows]
+    n = len(cells)
+    tab = np.zeros((1, n, 10))
+    tab[0, :, 1:5] = cells[:, 0:4]
+    tab[0, :, 6] = cells[:, 4]
+    tab[0, :, 7] = cells[:, 8]
+    vp = cells[:, 8] - 1e-9                     # v' = V - Vpl (rake 0)
+    K = np.zeros((3 * n, 2 * n))
+    for i in range(n):
+        K[3 * i:3 * i + 3, 2 * i] = cells[i, 9:12] / vp[i]
+    Kt = torch.as_tensor(K, device=cuda)
+    if precision == "fp32":
+        Kt = Kt.float().contiguous()
+    ens = Ensemble(Kt, tab, mu=MU, Cs=CS, precision=precision, dttry=h)
+    for k, col in (("Tno", 4), ("Tt1o", 5), ("Tt2o", 6), ("state", 7), ("slipv", 8), ("slipv1", 8)):
+        ens.t[k][0].copy_(torch.as_tensor(cells[:, col]))
+    ens.t["slipv2"].zero_()
+    ens.prepare()
+    return ens, cells
+
+
+def _oracle_attempt(cells, h):
+    """The reference's FP64 attempt on the recorded cells (per cell)."""
+    from oracle.stepping import DenseStepper
+    s = object.__new__(DenseStepper)
+    s.mu, s.Cs, s.V0 = MU, CS, 1e-6
+    s.a, s.b, s.dc, s.f0 = (cells[:, k].copy() for k in range(4))
+    s.Tno, s.Tt1o, s.Tt2o, s.state, s.slipv = (cells[:, k].copy() for k in range(4, 9))
+    s.AdotV1, s.AdotV2, s.dsigmadt = cells[:, 9].copy(), cells[:, 10].copy(), cells[:, 11].copy()
+    s.shear_loading = np.zeros(len(cells))
+    s.P = np.zeros(len(cells))
+    s.dPdt0 = np.zeros(len(cells))
+    return s.rk_attempt_raw(h)
+
+
+@pytest.mark.parametrize("rows,h", [(slice(0, 4), STAGE_OVERSHOOT_DT), (slice(0, 8), STAGE_OVERSHOOT_DT / 2),
+                                    (slice(4, 8), STAGE_OVERSHOOT_DT), (slice(0, 8), 0.5)])
+def test_mixed_attempt_in_range_through_stage_overshoot(cuda, rows, h):
+    """The mixed-precision attempt against the FP64 one on the recorded cells:
+    error norms within 1e-4 relative or 1e-8 absolute (they decide accept /
+    reject and the next dt against the tolerance 1e-4), candidate state
+    within 1e-6 of the step's increment, no NaN or inf from finite inputs --
+    including the attempt whose stage 5 overshoots."""
+    ref = _oracle_attempt(STAGE_OVERSHOOT_CELLS[rows], h)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        ens, cells = _recorded_cells_ensemble(cuda, prec, h, rows)
+        ens.begin()
+        w = ens.error_words()[0].cpu().numpy()
+        err = w.view(np.float64)
+        cand = ens.t["cand"].view(-1, 4).cpu().numpy()
+        ens.end()
+        res[prec] = (err, cand, ens.read_ctrl()[0])
+    e64, c64, k64 = res["fp64"]
+    e32, c32, k32 = res["fp32"]
+    assert np.all(np.isfinite(e32)) and np.all(np.isfinite(c32))
+    # FP64 arm = the reference arithmetic (the state error is a difference of
+    # two states ~0.8 apart by ~1e-10: ~1e-15 of rounding)
+    assert abs(e64[0] - ref[4]) <= 1e-6 * ref[4] + 1e-14
+    assert abs(e64[1] - ref[5]) <= 1e-9 * ref[5] + 1e-15
+    assert abs(e32[0] - e64[0]) <= 1e-4 * e64[0] + 1e-8
+    assert abs(e32[1] - e64[1]) <= 1e-4 * e64[1] + 1e-8
+    y0 = STAGE_OVERSHOOT_CELLS[rows][:, [4, 5, 6, 7]]
+    inc = np.abs(c64 - y0)
+    assert np.all(np.abs(c32 - c64) <= 1e-6 * inc + 1e-13 * np.abs(y0))
+    assert k32.accepted == k64.accepted
+    assert abs(k32.h - k64.h) <= 1e-4 * k64.h
