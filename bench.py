@@ -690,7 +690,8 @@ def profile_case(case):
     """Small single-kernel cases for ncu captures (no timing, no JSON):
     hs_assembly  half-space assembly, rough 20x10 km to the surface, N=1,600 (2 launches)
     hmat_product H-matrix product, rough 200x40 km, N=100,000, B=1 (13 products)
-    tc_gemm      tcgen05 BF16x6 product, planar 60x50 km, N=6,000, B=64 (4 iterations)"""
+    tc_gemm      batched iterations (tcgen05 BF16x6 product, attempt, decision, update),
+                 planar 60x50 km, N=6,000, B=64 (12 iterations)"""
     import torch
     from pyquake3d_gb300 import gf, mesh
     if case == "hs_assembly":
@@ -715,7 +716,7 @@ def profile_case(case):
         torch.cuda.empty_cache()
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
-        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x6").iterate(4)
+        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x6").iterate(12)
     else:
         raise SystemExit("unknown --case " + case)
     torch.cuda.synchronize()

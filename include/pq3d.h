@@ -256,7 +256,14 @@ typedef struct pq3d_batch_sim {
      * means an unsharded simulation (N_total = N, cell0 = 0). */
     int64_t N_total;
     int64_t cell0;
+    /* Mixed precisions (FP32, BF16X6, HMAT): the cells' start-of-step
+     * constants of the mixed-precision Dormand-Prince attempt, FP32
+     * [PQ3D_BATCH_BASE_FIELDS][B][N], written by pq3d_batch_prepare and by
+     * the update of every accepted step.  NULL (unused) for FP64. */
+    float *base;
 } pq3d_batch_sim;
+
+#define PQ3D_BATCH_BASE_FIELDS 20
 
 /* Packed operator of the tensor-core product: the FP64 operator split into
  * three BF16 pieces, stored as [3N/128 tiles][2N/32 blocks][3][128 x 32]
@@ -275,8 +282,10 @@ int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, 
  * sim->rates; this is what the tensor-core product needs besides). */
 size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim);
 
-/* Prepare the operator right-hand side from the current slip rates (run once
- * before the first iteration and after any host-side change of the state). */
+/* Prepare the operator right-hand side from the current slip rates and, for
+ * the mixed precisions, the start-of-step constants from the current state
+ * (run once before the first iteration and after any host-side change of
+ * the state). */
 int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream);
 
 /* One batched iteration on `stream`, graph-capturable: the operator product

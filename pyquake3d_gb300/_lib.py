@@ -65,7 +65,7 @@ class BatchSim(ctypes.Structure):
                                  "rates")] + \
         [("nsplit", ctypes.c_int32), ("pad0", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
          ("ctrl", c_void_p), ("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", ctypes.c_int32),
-         ("pad1", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64)]
+         ("pad1", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64), ("base", c_void_p)]
 
 
 class HMat(ctypes.Structure):
@@ -79,6 +79,7 @@ PQ3D_BATCH_FP64 = 0
 PQ3D_BATCH_FP32 = 1
 PQ3D_BATCH_BF16X6 = 2
 PQ3D_BATCH_HMAT = 3
+PQ3D_BATCH_BASE_FIELDS = 20   # floats per cell and run of pq3d_batch_sim.base
 
 
 class StepCtrl(ctypes.Structure):

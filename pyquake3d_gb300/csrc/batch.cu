@@ -40,14 +40,14 @@ __device__ __forceinline__ void vprime(const pq3d_batch_sim &S, int64_t idx, dou
     v2 = S.slipv2[idx] - S.Vpl * S.sin_rake0[idx];
 }
 
-// 3-piece BF16 split of an FP64 value: x ~= p0 + p1 + p2 (24 significant bits).
-__device__ __forceinline__ void split3(double x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
+// 3-piece BF16 split of an FP32 value: x = p0 + p1 + p2 exactly (each
+// residual is exact in FP32 and has 8 fewer significant bits than the last)
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
 {
-    p0 = __double2bfloat16(x);
-    const double r1 = x - (double)__bfloat162float(p0);
-    p1 = __double2bfloat16(r1);
-    const double r2 = r1 - (double)__bfloat162float(p1);
-    p2 = __double2bfloat16(r2);
+    p0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p0);
+    p1 = __float2bfloat16_rn(r1);
+    p2 = __float2bfloat16_rn(r1 - __bfloat162float(p1));
 }
 
 // i: local cell of the shard; v' goes to the mesh-wide position cell0 + i
@@ -66,8 +66,8 @@ __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_
         __nv_bfloat16 *P = (__nv_bfloat16 *)S.vop + (k / tc::kBlockK) * tc::kPieces * img +
                            tc::image_offset(r, (int)(k % tc::kBlockK));
         __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-        split3(v1, a0, a1, a2);
-        split3(v2, b0, b1, b2);
+        split3((float)v1, a0, a1, a2);   // v' to 24 bits, like the operator's pieces
+        split3((float)v2, b0, b1, b2);
         __nv_bfloat162 q;
         q.x = a0; q.y = b0; reinterpret_cast<__nv_bfloat162 *>(P)[0] = q;
         q.x = a1; q.y = b1; reinterpret_cast<__nv_bfloat162 *>(P + img)[0] = q;
@@ -75,13 +75,24 @@ __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_
     }
 }
 
+__device__ __forceinline__ double log_eta_v0(const pq3d_batch_sim &S) { return log(S.eta * S.V0); }
+
 __global__ void prepare_kernel(pq3d_batch_sim S)
 {
     const int r = blockIdx.y;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= S.N) return;
     double v1 = 0.0, v2 = 0.0;
-    if (r < S.B) vprime(S, (int64_t)r * S.N + i, v1, v2);   // padding runs stay zero
+    if (r < S.B) {   // padding runs stay zero
+        const int64_t idx = (int64_t)r * S.N + i;
+        vprime(S, idx, v1, v2);
+        if (S.base) {
+            MixedBase m = mixed_base(S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx], S.a[idx], S.b[idx],
+                                     S.dc[idx], S.f0[idx], log_eta_v0(S));
+            m.slipv = (float)S.slipv[idx];
+            store_base(S.base + idx, (int64_t)S.B * S.N, m);
+        }
+    }
     write_vop(S, r, i, v1, v2);
 }
 
@@ -192,21 +203,26 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__
 template <bool kMixed>
 __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
 {
-    __shared__ double red[8];
+    __shared__ unsigned long long red[32];
     __shared__ int act;
-    __shared__ double hs, log_etaV0;
+    __shared__ double hs;
+    __shared__ float hsf, V0f;
     const int r = blockIdx.y;
     pq3d_run_ctrl *C = S.ctrl + r;
     if (threadIdx.x == 0) {
         act = C->active;
         hs = C->h;
-        if (kMixed) log_etaV0 = log(S.eta * S.V0);
+        if (kMixed) {
+            hsf = (float)hs;
+            V0f = (float)S.V0;
+        }
     }
     __syncthreads();
     if (!act) return;
     const int64_t N = S.N;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double m1 = 0.0, m2 = 0.0;
+    float f1 = 0.f, f2 = 0.f;
     if (i < N) {
         const int64_t idx = (int64_t)r * N + i;
         const int Bp = padded_runs(S.B);
@@ -216,21 +232,39 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
             q0 += p[0]; q1 += p[1]; q2 += p[2];
         }
         const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
-        const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
-                     0.0, 0.0};
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
-        double yo[4], e1, e2;
-        if (kMixed) dp_attempt_mixed(c, S.V0, log_etaV0, hs, y, yo, e1, e2);
-        else dp_attempt(c, S.V0, S.eta, hs, y, yo, e1, e2);
+        double yo[4];
+        if (kMixed) {
+            MixedBase m = load_base(S.base + idx, (int64_t)S.B * N);
+            const double shear = S.shear_loading[idx];
+            m.V0 = V0f;
+            m.dsf = (float)dsig;
+            m.L[0] = (float)(shear - q0);
+            m.L[1] = (float)(shear - q1);
+            dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
+        } else {
+            const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
+                         0.0, 0.0};
+            dp_attempt(c, S.V0, S.eta, hs, y, yo, m1, m2);
+        }
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
-        m1 = e1;
-        m2 = e2;
     }
-    m1 = block_max(m1, red);
-    m2 = block_max(m2, red);
-    if (threadIdx.x == 0) {
-        atomicMax((unsigned long long *)&C->err1_bits, dbits(m1));
-        atomicMax((unsigned long long *)&C->err2_bits, dbits(m2));
+    if (kMixed) {
+        // float maxima, widened to FP64 once per block
+        unsigned *red32 = reinterpret_cast<unsigned *>(red);
+        const unsigned b1 = block_max_bits32(f1, red32);
+        const unsigned b2 = block_max_bits32(f2, red32);
+        if (threadIdx.x == 0) {
+            atomicMax((unsigned long long *)&C->err1_bits, dbits((double)__uint_as_float(b1)));
+            atomicMax((unsigned long long *)&C->err2_bits, dbits((double)__uint_as_float(b2)));
+        }
+    } else {
+        const unsigned long long b1 = block_max_bits(dbits(m1), red);
+        const unsigned long long b2 = block_max_bits(dbits(m2), red);
+        if (threadIdx.x == 0) {
+            atomicMax((unsigned long long *)&C->err1_bits, b1);
+            atomicMax((unsigned long long *)&C->err2_bits, b2);
+        }
     }
 }
 
@@ -269,17 +303,28 @@ __global__ void decide_kernel(pq3d_run_ctrl *ctrl, int B)
     }
 }
 
-// kMixed: the slip rate 2 V0 e^{-psi/a} sinh(tau / (sigma a)) formed as
-// V0 (e^{x - psi/a} - e^{-x - psi/a}) with fexp (2.5e-7 relative, as the
-// mixed right-hand side); the FP64 arm keeps the reference formula.
+// kMixed: the new state's start-of-step constants (the FP64 work of the
+// mixed attempts, done once per accepted step) and from them the slip rate
+// 2 V0 e^{-psi/a} sinh(tau / (sigma a)) in float-float exponent arithmetic
+// (~2e-7 relative, as the mixed right-hand side); FP64 for the slip
+// accumulation.  The FP64 arm keeps the reference formula
+// (src/QDsim_gpu.py:994-1027).
 template <bool kMixed>
 __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
 {
     __shared__ int acc;
-    __shared__ double hs;
+    __shared__ double hs, log_etaV0;
+    __shared__ float inv_eta;
     const int r = blockIdx.y;
     const pq3d_run_ctrl *C = S.ctrl + r;
-    if (threadIdx.x == 0) { acc = C->accepted; hs = C->h_last; }
+    if (threadIdx.x == 0) {
+        acc = C->accepted;
+        hs = C->h_last;
+        if (kMixed) {
+            log_etaV0 = log_eta_v0(S);
+            inv_eta = (float)(1.0 / S.eta);
+        }
+    }
     __syncthreads();
     if (!acc) return;
     const int64_t N = S.N;
@@ -290,19 +335,23 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
     const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[idx];
     S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
-    double v1, v2;
+    double v1, v2, v;
     if (kMixed) {
-        const double inv_a = 1.0 / a, sp = -st * inv_a;
-        const double q = inv_a / Tno;
-        const double x1 = clip700(T1 * q), x2 = clip700(T2 * q);
-        v1 = S.V0 * (fexp(sp + x1) - fexp(sp - x1));
-        v2 = S.V0 * (fexp(sp + x2) - fexp(sp - x2));
+        MixedBase m = mixed_base(Tno, T1, T2, st, a, S.b[idx], S.dc[idx], S.f0[idx], log_etaV0);
+        const float f1 = base_slip_rate(m, 0, inv_eta), f2 = base_slip_rate(m, 1, inv_eta);
+        // |V| without under/overflow of the squares
+        const float p = fmaxf(fabsf(f1), fabsf(f2)), q = fminf(fabsf(f1), fabsf(f2));
+        const float t = p > 0.f ? q / p : 0.f;
+        const float vf = fmaxf(p * sqrtf(fmaf(t, t, 1.f)), 1e-30f);
+        m.slipv = vf;
+        store_base(S.base + idx, (int64_t)S.B * N, m);
+        v1 = f1; v2 = f2; v = vf;
     } else {
         const double e = (2.0 * S.V0) * exp(-st / a);
         v1 = e * sinh(T1 / Tno / a);
         v2 = e * sinh(T2 / Tno / a);
+        v = sqrt(v1 * v1 + v2 * v2);
     }
-    double v = sqrt(v1 * v1 + v2 * v2);
     if (v < 1e-30) v = 1e-30;
     S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
     S.slip1[idx] += v1 * h;
@@ -320,6 +369,8 @@ static int check_sim(const pq3d_batch_sim *S)
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
     PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
     if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
+    if (S->precision != PQ3D_BATCH_FP64)
+        PQ3D_REQUIRE(S->base != nullptr && aligned16(S->base), "pq3d_batch: mixed precisions need the base array");
     PQ3D_REQUIRE(S->N_total >= 0 && S->cell0 >= 0, "pq3d_batch: bad shard");
     if (S->N_total > 0 && (S->N_total != S->N || S->cell0 != 0)) {
         PQ3D_REQUIRE(S->precision == PQ3D_BATCH_FP64 || S->precision == PQ3D_BATCH_FP32,

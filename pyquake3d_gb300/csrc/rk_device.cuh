@@ -145,41 +145,81 @@ __device__ __forceinline__ float ff_exp_neg_abs(FF v)
 
 __device__ __forceinline__ float ff_exp(FF v) { return expf(v.hi) * (1.f + v.lo); }
 
-// per-attempt constants of one cell
+// Constants of one cell at the start of a step (y0), shared by all the
+// attempts of the step: computed once per accepted step (the FP64 set-up:
+// GB300's FP64 pipe also executes the FP64<->FP32 conversions and the FP64
+// compares, at the FP64 rate) and stored as kBaseFields floats per cell.
 struct MixedBase {
     float Tn0;          // effective normal stress at y0 (MPa)
     float q0[2];        // tau_k / sigma at y0
-    float x0[2];        // tau_k / (a sigma) at y0 (hi part: sign and r only)
-    FF Sp[2], Sm[2];    // -psi0/a + ln(eta V0) +- x0_k
+    float x0[2];        // tau_k / (a sigma) at y0 (FP32: sign and r only)
+    FF Sp[2], Sm[2];    // -psi0/a + ln(eta V0) +- tau_k / (a sigma)
     FF g0;              // (f0 - psi0) / b
-    float a, inv_a, inv_b, bdc, V0, slipv, dsf;
+    float a, inv_a, inv_b, bdc;
+    float slipv;        // slip rate at the start of the step
+    // per attempt (not stored)
+    float V0, dsf;      // V0; dsigma/dt - dP/dt (Pa/s)
     float L[2];         // -K.v' + shear loading (Pa/s)
 };
+constexpr int kBaseFields = 20;
 
-__device__ __forceinline__ MixedBase mixed_base(const Cell &c, double V0, double log_etaV0, const double y[4])
+// Tn0: effective normal stress (MPa); T1, T2 shear stresses (MPa); psi state
+__device__ __forceinline__ MixedBase mixed_base(double Tn0, double T1, double T2, double psi, double a, double b,
+                                                double dc, double f0, double log_etaV0)
 {
     MixedBase m;
-    const double Tn0 = y[0] - c.P * 1e-6;   // MPa
-    const double r0 = rcp_nr(Tn0), inv_a = rcp_nr(c.a), inv_b = rcp_nr(c.b);
-    const double q1 = y[1] * r0, q2 = y[2] * r0;
+    const double r0 = rcp_nr(Tn0), inv_a = rcp_nr(a), inv_b = rcp_nr(b);
+    const double q1 = T1 * r0, q2 = T2 * r0;
     const double x1 = q1 * inv_a, x2 = q2 * inv_a;
-    const double sp = fma(-y[3], inv_a, log_etaV0);
+    const double sp = fma(-psi, inv_a, log_etaV0);
     m.Tn0 = (float)Tn0;
     m.q0[0] = (float)q1; m.q0[1] = (float)q2;
-    m.x0[0] = (float)x1; m.x0[1] = (float)x2;
+    m.inv_a = (float)inv_a;
+    m.x0[0] = m.q0[0] * m.inv_a; m.x0[1] = m.q0[1] * m.inv_a;
     m.Sp[0] = ff_split(sp + x1); m.Sm[0] = ff_split(sp - x1);
     m.Sp[1] = ff_split(sp + x2); m.Sm[1] = ff_split(sp - x2);
-    m.g0 = ff_split((c.f0 - y[3]) * inv_b);
-    m.a = (float)c.a;
-    m.inv_a = (float)inv_a;
+    m.g0 = ff_split((f0 - psi) * inv_b);
+    m.a = (float)a;
     m.inv_b = (float)inv_b;
-    m.bdc = (float)c.b / (float)c.dc;
-    m.V0 = (float)V0;
-    m.slipv = (float)c.slipv;
-    m.dsf = (float)(c.dsig - c.dPdt);
-    m.L[0] = (float)(-c.AdotV1 + c.shear);
-    m.L[1] = (float)(-c.AdotV2 + c.shear);
+    m.bdc = (float)b / (float)dc;
+    m.slipv = 0.f;
     return m;
+}
+
+// stored as [kBaseFields][cells] (field-major: coalesced)
+__device__ __forceinline__ void store_base(float *p, int64_t stride, const MixedBase &m)
+{
+    const float v[kBaseFields] = {m.Tn0, m.q0[0], m.q0[1], m.x0[0], m.x0[1], m.Sp[0].hi, m.Sp[0].lo, m.Sp[1].hi,
+                                  m.Sp[1].lo, m.Sm[0].hi, m.Sm[0].lo, m.Sm[1].hi, m.Sm[1].lo, m.g0.hi, m.g0.lo,
+                                  m.a, m.inv_a, m.inv_b, m.bdc, m.slipv};
+#pragma unroll
+    for (int k = 0; k < kBaseFields; ++k) p[k * stride] = v[k];
+}
+
+__device__ __forceinline__ MixedBase load_base(const float *__restrict__ p, int64_t stride)
+{
+    float v[kBaseFields];
+#pragma unroll
+    for (int k = 0; k < kBaseFields; ++k) v[k] = __ldg(p + k * stride);
+    MixedBase m;
+    m.Tn0 = v[0];
+    m.q0[0] = v[1]; m.q0[1] = v[2];
+    m.x0[0] = v[3]; m.x0[1] = v[4];
+    m.Sp[0] = FF{v[5], v[6]}; m.Sp[1] = FF{v[7], v[8]};
+    m.Sm[0] = FF{v[9], v[10]}; m.Sm[1] = FF{v[11], v[12]};
+    m.g0 = FF{v[13], v[14]};
+    m.a = v[15]; m.inv_a = v[16]; m.inv_b = v[17]; m.bdc = v[18]; m.slipv = v[19];
+    return m;
+}
+
+// slip rate 2 V0 e^{-psi/a} sinh(x), x = tau/(a sigma), from the constants:
+// V0 sign(x) e^{-psi/a + |x|} (1 - e^{-2|x|}) = sign(x) W (1 - r) / eta
+__device__ __forceinline__ float base_slip_rate(const MixedBase &m, int k, float inv_eta)
+{
+    const float x = m.x0[k];
+    const FF lw = x >= 0.f ? m.Sp[k] : m.Sm[k];
+    const float v = ff_exp(lw) * inv_eta * -expm1f(-2.f * fabsf(x));
+    return x < 0.f ? -v : v;
 }
 
 // Right-hand side at y0 + (dTn, dT1, dT2, dpsi) (MPa, MPa, MPa, state):
@@ -212,29 +252,29 @@ __device__ __forceinline__ void mixed_rhs(const MixedBase &m, float dTn, float d
     dtau2 = out[1] * 1e-6f;
 }
 
-// |num| / |den| in FP32 where den is in float range, else in FP64
-__device__ __forceinline__ double rel_err(float num, double den)
+// |num| / |yo + num|: in FP32 where yo + num is in float range, else in FP64
+__device__ __forceinline__ float rel_err(float num, double yo)
 {
-    const double ad = fabs(den);
-    if (ad >= 1e-30 && ad <= 1e30) return (double)__fdiv_rn(fabsf(num), (float)ad);
-    return fabs((double)num) / ad;
+    const float ay = fabsf((float)yo + num);
+    if (ay >= 1e-30f && ay <= 1e30f) return __fdiv_rn(fabsf(num), ay);
+    return (float)(fabs((double)num) / fabs(yo + (double)num));
 }
 
-__device__ __forceinline__ bool finite_cell(const Cell &c, const double y[4])
+__device__ __forceinline__ bool finite_inputs(const MixedBase &m, const double y[4], double dsig)
 {
-    return isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) && isfinite(c.AdotV1) &&
-           isfinite(c.AdotV2) && isfinite(c.dsig) && isfinite(c.slipv);
+    return isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) && isfinite(m.L[0]) &&
+           isfinite(m.L[1]) && isfinite(dsig) && isfinite(m.slipv);
 }
 
-// One Dormand-Prince attempt of one cell in the mixed arithmetic above.
-// log_etaV0 = ln(eta V0).  Writes the 5th-order solution to yo and returns
-// the two relative errors (as the FP64 attempt below).
-__device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, double log_etaV0, double h,
-                                                 const double y[4], double yo[4], double &e1, double &e2)
+// One Dormand-Prince attempt of one cell in the mixed arithmetic above, from
+// the cell's start-of-step constants m (with V0, dsf and L set) and its
+// normal-stress rate dsig (Pa/s).  Writes the 5th-order solution to yo and
+// returns the two relative errors (as the FP64 attempt below; as floats:
+// they only decide accept / reject and the next dt).
+__device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, double dsig, float hf, const double y[4],
+                                                 double yo[4], float &e1, float &e2)
 {
-    const MixedBase m = mixed_base(c, V0, log_etaV0, y);
-    const float hf = (float)h;
-    const float dn = (float)(c.dsig * 1e-6);   // d(Tno)/dt, MPa/s, constant over the step
+    const float dn = (float)(dsig * 1e-6);   // d(Tno)/dt, MPa/s, constant over the step
     const float A[6][6] = {{(float)B21, 0, 0, 0, 0, 0},
                            {(float)B31, (float)B32, 0, 0, 0, 0},
                            {(float)B41, (float)B42, (float)B43, 0, 0, 0},
@@ -274,14 +314,14 @@ __device__ __forceinline__ void dp_attempt_mixed(const Cell &c, double V0, doubl
         e2t = fmaf(D[l], u[l], e2t);
     }
     es *= hf; e1t *= hf; e2t *= hf;
-    const double wn = (B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76);
-    const double en = h * (wn * (c.dsig * 1e-6));
-    e1 = rel_err(es, yo[3] + (double)es);
-    const double ea = rel_err(e1t, yo[1] + (double)e1t);
-    const double eb = rel_err(e2t, yo[2] + (double)e2t);
-    const double ec = fabs(en) / fabs(yo[0] + en);
-    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
-    if (!(isfinite(e1) && isfinite(e2)) && finite_cell(c, y)) {
+    // the normal stress: its rate is constant, the two orders differ by the
+    // rounding of the weight sums
+    const float wn = (float)((B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76));
+    const float en = hf * (wn * dn);
+    e1 = rel_err(es, yo[3]);
+    const float ea = rel_err(e1t, yo[1]), eb = rel_err(e2t, yo[2]), ec = rel_err(en, yo[0]);
+    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmaxf(fmaxf(ea, eb), ec);
+    if (!(isfinite(e1) && isfinite(e2)) && finite_inputs(m, y, dsig)) {
         if (!isfinite(e1)) e1 = INFINITY;
         if (!isfinite(e2)) e2 = INFINITY;
     }
@@ -326,25 +366,46 @@ __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta,
     e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
 }
 
-// max over non-negative doubles (and NaN, which wins) through their bit patterns
+// max over non-negative doubles (and NaN, which wins) through their bit
+// patterns: for such values unsigned order is numeric order and a NaN's
+// pattern lies above +inf's, so a NaN wins as in numpy's max
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(fabs(x)); }
 
-__device__ __forceinline__ double block_max(double v, double *red)
+// block-wide max of such bit patterns (blockDim.x a multiple of 32, at most
+// 1024; red[32] in shared memory); valid in thread 0
+__device__ __forceinline__ unsigned long long block_max_bits(unsigned long long v, unsigned long long *red)
 {
-    // NaN-propagating max across the block
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (isnan(v) || isnan(u)) ? NAN : fmax(v, u);
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u > v ? u : v;
     }
+    __syncthreads();   // red may still be read by a previous call
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+            v = u > v ? u : v;
+        }
+    }
+    return v;
+}
+
+// the same for non-negative floats (or NaN): 32-bit patterns, warp max in
+// one reduction instruction
+__device__ __forceinline__ unsigned block_max_bits32(float x, unsigned *red)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned v = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(x)));
     __syncthreads();
     if (lane == 0) red[w] = v;
     __syncthreads();
-    double m = 0.0;
-    const int nw = blockDim.x >> 5;
-    for (int q = 0; q < nw; ++q) m = (isnan(m) || isnan(red[q])) ? NAN : fmax(m, red[q]);
-    return m;
+    if (w == 0) v = __reduce_max_sync(0xffffffffu, lane < (int)(blockDim.x >> 5) ? red[lane] : 0u);
+    return v;
 }
 
 __device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }

@@ -203,7 +203,7 @@ template <bool kF32>
 __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int nsteps, double *h_hist, double *t_hist,
                                                          const double *h_force)
 {
-    __shared__ double red[8];
+    __shared__ unsigned long long red[32];
     __shared__ double dil_cp[kMaxDepth], dil_inv[kMaxDepth];
     pq3d_step_ctrl *C = S.ctrl;
     const int64_t N = S.N;
@@ -260,11 +260,11 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
                 m1 = (isnan(m1) || isnan(e1)) ? NAN : fmax(m1, e1);
                 m2 = (isnan(m2) || isnan(e2)) ? NAN : fmax(m2, e2);
             }
-            m1 = block_max(m1, red);
-            m2 = block_max(m2, red);
+            const unsigned long long b1 = block_max_bits(dbits(m1), red);
+            const unsigned long long b2 = block_max_bits(dbits(m2), red);
             if (threadIdx.x == 0) {
-                atomicMax((unsigned long long *)&C->err_slot[2 * slot], dbits(m1));
-                atomicMax((unsigned long long *)&C->err_slot[2 * slot + 1], dbits(m2));
+                atomicMax((unsigned long long *)&C->err_slot[2 * slot], b1);
+                atomicMax((unsigned long long *)&C->err_slot[2 * slot + 1], b2);
             }
             if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
             const double err1 = __longlong_as_double((long long)*((volatile unsigned long long *)&C->err_slot[2 * slot])) + 1e-10;
@@ -315,8 +315,8 @@ __global__ void __launch_bounds__(256) dense_step_kernel(pq3d_dense_sim S, int n
             if (kF32) vs[i] = split_v(w1, w2);
             else vp[i] = make_double2(w1, w2);
         }
-        vmax = block_max(vmax, red);
-        if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, dbits(vmax));
+        const unsigned long long bv = block_max_bits(dbits(vmax), red);
+        if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, bv);
         // (3b) pore-pressure diffusion of every cell with the new state and
         // slip rate (src/QDsim_gpu.py:628-671, after the update 1119-1120)
         if (S.Parr) dilatancy_step(S, h, dil_cp, dil_inv);

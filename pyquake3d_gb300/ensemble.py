@@ -111,6 +111,8 @@ class Ensemble:
         self.t["sin_rake0"] = torch.sin(torch.as_tensor(np.stack([s["rake0"] for s in inits]), **f64)).contiguous()
         self.t["rates"] = torch.zeros(self.nsplit * self.Bp * 3 * N, **f64)
         self.t["cand"] = torch.zeros(B * N * 4, **f64)
+        if precision != "fp64":   # start-of-step constants of the mixed-precision attempt
+            self.t["base"] = torch.zeros(_lib.PQ3D_BATCH_BASE_FIELDS * B * N, dtype=torch.float32, device=dev)
         if precision in ("fp64", "hmat"):
             self.vop = torch.zeros(self.Bp * 2 * Nt, **f64)
         elif precision == "fp32":
@@ -123,6 +125,7 @@ class Ensemble:
         for k in STATE + PARAMS + ("rates", "cand"):
             setattr(S, k, self.t[k].data_ptr())
         S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
+        S.base = self.t["base"].data_ptr() if "base" in self.t else None
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
         if shard is not None:

@@ -35,7 +35,7 @@ def test_struct_layouts_match_header(tmp_path):
     import subprocess
     src = tmp_path / "probe.c"
     fields = {"pq3d_batch_sim": ("BatchSim", ["N", "B", "precision", "Tno", "rates", "nsplit", "cand", "vop", "K",
-                                              "ctrl", "V0", "eta", "fix_Tn", "N_total", "cell0"]),
+                                              "ctrl", "V0", "eta", "fix_Tn", "N_total", "cell0", "base"]),
               "pq3d_dense_sim": ("DenseSim", ["N", "Tno", "fric", "a", "rake0", "rates", "cand", "K64", "K32", "ctrl",
                                               "V0", "eta", "fix_Tn", "ndepth", "P", "Parr", "dila"]),
               "pq3d_run_ctrl": ("RunCtrl", ["h", "time", "attempts", "max_steps", "err2_bits", "status", "accepted"]),
@@ -46,6 +46,7 @@ def test_struct_layouts_match_header(tmp_path):
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
         for f in fl:
             lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+    lines.append('printf("%d\\n", PQ3D_BATCH_BASE_FIELDS);')
     lines.append("return 0;}")
     src.write_text("\n".join(lines))
     exe = tmp_path / "probe"
@@ -59,3 +60,4 @@ def test_struct_layouts_match_header(tmp_path):
         for f in fl:
             assert getattr(cls, f).offset == vals[k], (cname, f)
             k += 1
+    assert vals[k] == _lib.PQ3D_BATCH_BASE_FIELDS
