@@ -318,7 +318,7 @@ def bench_ours(args):
                       "path": "pq3d_assemble_dense_host (C-ABI), 2 streams, D2H overlapped with assembly"}
         del host64
         # -- stepping on the assembled operator
-        out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks)
+        out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, dict(peaks, fp64_tflops=fp64))
         if not args.no_batch:
             out["batched"] = bench_batched(torch, dev, args, peaks)
         if not args.no_hmat:
@@ -374,8 +374,54 @@ def bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks):
                                           "achieved": bytes_step * acc / dt / 1e9, "peak": peaks["hbm_gbs"],
                                           "frac": bytes_step * acc / dt / 1e9 / peaks["hbm_gbs"],
                                           "note": "operator bytes per accepted step / step time (whole step)"}}
+    res["product"] = bench_dense_product(torch, dev, K64, K32, peaks)
     if not args.no_cpu:
         res["cpu_baseline"] = cpu_stepping_sample(torch, K64, tab, seconds=min(args.ref_seconds, 12.0))
+    return res
+
+
+def bench_dense_product(torch, dev, K64, K32, peaks):
+    """The stepping's traction product K.v' alone (pq3d_dense_matvec_f64 /
+    _f32, the kernels' own launches, CUDA events, operator larger than L2):
+    FP64 against the FP64 peak (GB300's FP64 rate, 1 DFMA per 8-byte entry,
+    is below its HBM rate), FP32 against HBM."""
+    from pyquake3d_gb300 import _lib
+    L_ = _lib.load()
+    N = K64.shape[1] // 2
+    st = torch.cuda.current_stream(dev).cuda_stream
+    g = torch.Generator(device=dev).manual_seed(0)
+    v = torch.randn(2 * N, dtype=torch.float64, device=dev, generator=g)
+    hi = v.float()
+    vs = torch.stack([hi[0::2], hi[1::2], (v - hi.double()).float()[0::2], (v - hi.double()).float()[1::2]], 1)
+    vs = vs.contiguous()
+    out = torch.empty(3 * N, dtype=torch.float64, device=dev)
+    res = {}
+    for label, call, nbytes in (
+            ("fp64", lambda: L_.pq3d_dense_matvec_f64(K64.data_ptr(), N, v.data_ptr(), out.data_ptr(), st),
+             K64.numel() * 8),
+            ("fp32", lambda: L_.pq3d_dense_matvec_f32(K32.data_ptr(), N, vs.data_ptr(), out.data_ptr(), st),
+             K32.numel() * 4)):
+        for _ in range(2):
+            _lib.check(call())
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 5
+        s.record()
+        for _ in range(n):
+            _lib.check(call())
+        e.record()
+        e.synchronize()
+        t = s.elapsed_time(e) / 1e3 / n
+        gbs = nbytes / t / 1e9
+        r = {"launch_s": t, "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"],
+                                    "unit": "GB/s", "algorithmic_bytes": int(nbytes)}}
+        if label == "fp64":
+            tf = 2.0 * K64.numel() / t / 1e12
+            r["bound"] = "fp64"
+            r["fp64"] = {"achieved": tf, "peak": peaks["fp64_tflops"], "frac": tf / peaks["fp64_tflops"],
+                         "unit": "TFLOP/s", "flops": 2.0 * K64.numel()}
+        else:
+            r["bound"] = "hbm"
+        res[label] = r
     return res
 
 
