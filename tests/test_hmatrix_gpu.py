@@ -45,6 +45,21 @@ def test_hmatrix_product_matches_dense(cuda, leaf):
     assert torch.equal(Ym[0], Y[0]) and torch.equal(Ym[2], Y[2]) and bool(torch.all(Ym[1] == 7.0))
 
 
+def test_mesh_smaller_than_a_leaf_is_one_dense_block(cuda):
+    """N = 18 cells under a 64-cell leaf: the partition is one dense block and
+    the product is the FP32-stored dense operator (~1e-7 relative)."""
+    nodes, tris = mesh.planar_fault(3.0, 3.0, 3, 3)
+    N = tris.shape[0]
+    H = HMatrix(nodes, tris, MU, MU, min_size=64, mini_leaf=64, tol=1e-4, device=cuda)
+    assert H.stats["blocks"] == 1 and H.stats["lowrank_blocks"] == 0
+    K64, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
+    X = torch.as_tensor(np.random.default_rng(1).standard_normal((2, 2 * N)), device=cuda)
+    Y = H.apply(X)
+    ref = X @ K64.T
+    for r in range(2):
+        assert _rel(ref[r], Y[r]) < 1e-6, r
+
+
 def test_hmatrix_error_not_worse_than_reference(cuda):
     """The reference's own H-matrix (ACA+, absolute tolerance 0.01, mini_leaf
     32) on the golden mesh vs ours (tol 1e-4, same partition), both measured
