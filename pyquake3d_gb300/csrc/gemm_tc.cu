@@ -27,6 +27,7 @@
 // No cluster, no multicast: each CTA reads its own tiles.
 #include <cuda_bf16.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 #include "gemm_tc.cuh"
@@ -125,7 +126,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ uint32_t tmem_cols(int Bp)
+__host__ __device__ inline uint32_t tmem_cols(int Bp)
 {
     uint32_t c = 32;
     while ((int)c < Bp) c <<= 1;
@@ -259,7 +260,9 @@ size_t gemm_bf16x6_workspace_bytes(int64_t, int, int) { return 256; }
 
 struct Cfg {
     int device = -1;
-    int max_smem = 0;
+    int max_smem = 0;      // per block (opt-in)
+    int sm_smem = 0;       // per SM
+    int ctas_per_sm = 2;   // PQ3D_TC_CTAS_PER_SM (1, 2 or 3)
 };
 static thread_local Cfg g_cfg;
 
@@ -275,15 +278,29 @@ int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int
     int dev;
     PQ3D_CUDA_TRY(cudaGetDevice(&dev));
     if (g_cfg.device != dev) {
-        int maxs = 0;
+        int maxs = 0, sms = 0;
         PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         PQ3D_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16x6_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
         g_cfg.device = dev;
         g_cfg.max_smem = maxs;
+        g_cfg.sm_smem = sms;
+        const char *env = getenv("PQ3D_TC_CTAS_PER_SM");
+        const int c = env ? atoi(env) : 2;
+        g_cfg.ctas_per_sm = c < 1 ? 1 : (c > 3 ? 3 : c);
     }
+    // Several CTAs per SM (default 2) while each still gets a pipeline of at
+    // least 2 stages and its tensor-memory columns: one CTA streams the
+    // operator while another fills its pipeline or drains its accumulator,
+    // and the last wave is finer; else one CTA with up to 6 stages.
     const size_t stage_bytes = (size_t)kPieces * (kImageA + (size_t)Bp * kBlockK * 2);
-    int stages = (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16));
-    if (stages > 6) stages = 6;
+    int stages = 0;
+    for (int c = g_cfg.ctas_per_sm; c >= 1 && stages == 0; --c) {
+        int s = (int)((g_cfg.sm_smem / c - 1024 - 16) / (stage_bytes + 16));
+        if (s > 6) s = 6;
+        if (s > (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16))) s = (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16));
+        if (s >= 2 && c * (int)tmem_cols(Bp) <= 512) stages = s;
+    }
     PQ3D_REQUIRE(stages >= 2, "gemm_bf16x6: not enough shared memory for B=%d", Bp);
     const size_t smem = (size_t)stages * stage_bytes + 16 * (size_t)stages + 16;
     dim3 grid((unsigned)m_tiles(N), (unsigned)nsplit);
