@@ -106,10 +106,13 @@ int pq3d_assemble_dense_noalloc(const double *nodes, const int64_t *tris, int64_
                                 double mu, double lambda_, int halfspace, double *K64, float *K32, void *stream);
 
 /* Host-buffer variant for callers that keep the mesh and the operator in host
- * memory (the reference keeps A1s..Bd as NumPy arrays): copies the mesh in,
- * assembles in row blocks on two streams and copies each block back while the
- * next one is computed.  K64_host: (3N)x(2N) doubles (pinned memory recommended);
- * K32_host may be NULL.  Allocates and frees its own device buffers. */
+ * memory (the reference keeps A1s..Bd as NumPy arrays): copies the mesh in and
+ * assembles.  Outputs in page-locked host memory mapped into the device address
+ * space (cudaHostAlloc, cudaHostRegister) are written by the assembly kernel
+ * directly; other (pageable) outputs are assembled in row blocks on two
+ * streams, each block copied back while the next one is computed.
+ * K64_host: (3N)x(2N) doubles; K32_host may be NULL.  Allocates and frees its
+ * own device buffers. */
 int pq3d_assemble_dense_host(const double *nodes_host, int64_t n_nodes, const int64_t *tris_host,
                              int64_t N, double mu, double lambda_, int halfspace,
                              double *K64_host, float *K32_host);

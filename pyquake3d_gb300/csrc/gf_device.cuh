@@ -176,18 +176,25 @@ __device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, Ad
     g.i_W2r = g.iW2 * ir;
     g.C = (r * ca - z) * g.i_Wr;
     g.S = (r * sa - y) * g.i_Wr;
+    // with 1/(r - zeta) = -1/W:
     const double q = 1.0 / (4.0 * kPi);
-    const T i_rzeta = -iW;   // 1/(r - zeta)
-    g.gx = q * (g.eta * ir * i_rzeta - y * g.i_rz);
-    g.gy = q * (x * g.i_rz - ca * x * ir * i_rzeta);
-    g.gz = q * (sa * x * ir * i_rzeta);
+    g.gx = -q * (g.eta * g.i_Wr + y * g.i_rz);
+    g.gy = (q * x) * (g.i_rz + ca * g.i_Wr);
+    g.gz = -(q * x) * (sa * g.i_Wr);
     const double p2 = 2.0 * nu + 1.0;
-    g.fx = p2 * g.i_Wr + g.x2 * g.i_W2r2 - g.x2 * g.i_Wr3;
+    g.fx = p2 * g.i_Wr + g.x2 * (g.i_W2r2 - g.i_Wr3);
     g.fy = g.i_Wr + g.S * g.S - g.y2 * g.i_Wr3;
     g.fz = g.i_Wr + g.C * g.C - g.z2 * g.i_Wr3;
 }
 
-// Strain of unit by (Ey) and unit bz (Ez) Burgers components.
+// Strain of unit by (Ey) and unit bz (Ez) Burgers components.  The
+// published expressions share many products; they are grouped here (same
+// mathematics, ~40 % fewer FP64 operations): with
+//   A = 1/(r(r-z))^2 + 1/(r^3 (r-z)),  Q3 = S (nu + x^2/(W r)) + y x^2/(W r^3),
+//   Q4 = C (nu + x^2/(W r)) + z x^2/(W r^3),
+//   P = sa ca / W^2 - (y ca + z sa)/(W^2 r) + y z (1/(W r)^2 - 1/(W r^3)),
+// the by-part uses Q3, Q4 and P scaled by cos(alpha) and the bz-part the same
+// three scaled by sin(alpha).
 template <class T>
 __device__ __forceinline__ void ad_parts_yz(const AdGeom<T> &g, double nu, double k, T Ey[6], T Ez[6])
 {
@@ -195,20 +202,25 @@ __device__ __forceinline__ void ad_parts_yz(const AdGeom<T> &g, double nu, doubl
     const double p2 = 2.0 * nu + 1.0;
     const T xk = x * k, sak = sa * k, xsak = xk * sa;
     const T yz = y * z;
-    Ey[0] = -xk * (g.fx * ca + p2 * g.i_rz - g.x2 * g.i_r2z2 - g.x2 * g.i_r3z);
-    Ey[1] = g.gy - xk * (g.i_rz - g.y2 * g.i_r2z2 - g.y2 * g.i_r3z + g.fy * ca);
+    const T A = g.i_r2z2 + g.i_r3z;
+    const T x2i = g.x2 * g.i_Wr, x2w3 = g.x2 * g.i_Wr3;
+    const T nux = nu + x2i;
+    const T Q3 = g.S * nux + y * x2w3;
+    const T Q4 = g.C * nux + z * x2w3;
+    const T P = sa * ca * g.iW2 - g.ycz * g.i_W2r + yz * (g.i_W2r2 - g.i_Wr3);
+    const T hgx = 0.5 * g.gx;
+    Ey[0] = -xk * (g.fx * ca + p2 * g.i_rz - g.x2 * A);
+    Ey[1] = g.gy - xk * (g.i_rz - g.y2 * A + g.fy * ca);
     Ey[2] = -xk * (g.fz * ca + z * g.ir3);
-    Ey[3] = 0.5 * g.gx + k * (g.x2 * y * g.i_r2z2 - nu * y * g.i_rz + g.x2 * y * g.i_r3z + nu * ca * g.S
-                              + g.x2 * y * ca * g.i_Wr3 + g.x2 * ca * g.S * g.i_Wr);
-    Ey[4] = k * (-g.x2 * g.ir3 + nu * g.ir + nu * ca * g.C + g.x2 * z * ca * g.i_Wr3 + g.x2 * ca * g.C * g.i_Wr);
-    Ey[5] = 0.5 * g.gz - xk * (y * g.ir3 + sa * ca * ca * g.iW2 - ca * g.ycz * g.i_W2r + yz * ca * g.i_W2r2
-                               - yz * ca * g.i_Wr3);
+    Ey[3] = hgx + k * (g.x2 * y * A - nu * y * g.i_rz + ca * Q3);
+    Ey[4] = k * (nu * g.ir - g.x2 * g.ir3 + ca * Q4);
+    Ey[5] = 0.5 * g.gz - xk * (y * g.ir3 + ca * P);
     Ez[0] = xsak * g.fx;
     Ez[1] = xsak * g.fy;
     Ez[2] = g.gz + xsak * g.fz;
-    Ez[3] = -sak * (nu * g.S + g.x2 * g.S * g.i_Wr + g.x2 * y * g.i_Wr3);
-    Ez[4] = 0.5 * g.gx - sak * (nu * g.C + g.x2 * g.C * g.i_Wr + g.x2 * z * g.i_Wr3);
-    Ez[5] = 0.5 * g.gy - xsak * (yz * g.i_Wr3 - sa * ca * g.iW2 + g.ycz * g.i_W2r - yz * g.i_W2r2);
+    Ez[3] = -sak * Q3;
+    Ez[4] = hgx - sak * Q4;
+    Ez[5] = 0.5 * g.gy + xsak * P;
 }
 
 // Strain of a unit bx (tensile) Burgers component.
@@ -229,17 +241,20 @@ __device__ __forceinline__ void ad_part_x(const AdGeom<double> &g, double nu, do
 }
 
 // acc += B^T T' B for the rotation B = [[1,0,0],[0,sz,-sy],[0,sy,sz]] about x
-// (the back-rotation of src/TDstressFS_C.cpp:240-255).
+// (the back-rotation of src/TDstressFS_C.cpp:240-255), with the double angle
+// (c2, s2) = (sz^2 - sy^2, 2 sy sz) of the unit vector (sy, sz): the yz-block
+// is its mean, plus its half difference and off-diagonal term rotated by 2x.
 template <class T>
-__device__ __forceinline__ void add_rot_x(T acc[6], const T t[6], T sy, T sz)
+__device__ __forceinline__ void add_rot_x(T acc[6], const T t[6], T sy, T sz, T c2, T s2)
 {
-    const T yy = sy * sy, zz = sz * sz, yz = sy * sz;
+    const T h = 0.5 * (t[1] + t[2]), d = 0.5 * (t[1] - t[2]);
+    const T u = c2 * d + s2 * t[5];
     acc[0] += t[0];
-    acc[1] += zz * t[1] + 2.0 * yz * t[5] + yy * t[2];
-    acc[2] += yy * t[1] - 2.0 * yz * t[5] + zz * t[2];
+    acc[1] += h + u;
+    acc[2] += h - u;
     acc[3] += sz * t[3] + sy * t[4];
-    acc[4] += -sy * t[3] + sz * t[4];
-    acc[5] += -yz * t[1] + (zz - yy) * t[5] + yz * t[2];
+    acc[4] += sz * t[4] - sy * t[3];
+    acc[5] += c2 * t[5] - s2 * d;
 }
 
 // Source fields through an accessor: F(i) returns field i.
@@ -279,8 +294,9 @@ __device__ __forceinline__ bool tdcs_strain_sd(const Src &F, T x, T y, T z, doub
             ts[i] = sz * Ey[i] + sy * Ez[i];    // strike: (by1, bz1) = (sz, sy)
             td[i] = -sy * Ey[i] + sz * Ez[i];   // dip:    (by1, bz1) = (-sy, sz)
         }
-        add_rot_x(Es, ts, sy, sz);
-        add_rot_x(Ed, td, sy, sz);
+        const T c2 = sz * sz - sy * sy, s2 = 2.0 * (sy * sz);
+        add_rot_x(Es, ts, sy, sz, c2, s2);
+        add_rot_x(Ed, td, sy, sz, c2, s2);
     }
     return true;
 }
@@ -313,7 +329,7 @@ __device__ __forceinline__ void tdcs_strain_general(const Src &F, double x, doub
         } else {
             for (int i = 0; i < 6; ++i) t[i] = by1 * Ey[i] + bz1 * Ez[i];
         }
-        add_rot_x(E, t, sy, sz);
+        add_rot_x(E, t, sy, sz, sz * sz - sy * sy, 2.0 * (sy * sz));
     }
 }
 

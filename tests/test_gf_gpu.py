@@ -111,11 +111,21 @@ def test_row_blocks_equal_full_assembly_and_are_deterministic(cuda):
 
 
 def test_host_buffer_assembly_matches_device(cuda):
+    """Pinned outputs (written by the kernel through the mapping) and pageable
+    outputs (staged row blocks) give the device assembly bit for bit."""
     nodes, tris = mesh.rough_fault(10.0, 5.0, 16, 9, seed=4)
     K, K32 = gf.assemble_dense(nodes, tris, MU, MU)
     Kh, K32h = gf.assemble_dense_host(nodes, tris, MU, MU, fp32_copy=True)
+    assert Kh.is_pinned()
     assert torch.equal(Kh, K.cpu())
     assert torch.equal(K32h, K32.cpu())
+    N = tris.shape[0]
+    P64 = torch.full((3 * N, 2 * N), 7.0, dtype=torch.float64)
+    P32 = torch.full((3 * N, 2 * N), 7.0, dtype=torch.float32)
+    assert not P64.is_pinned()
+    gf.assemble_dense_host(nodes, tris, MU, MU, fp32_copy=True, out64=P64, out32=P32)
+    assert torch.equal(P64, K.cpu())
+    assert torch.equal(P32, K32.cpu())
 
 
 def test_horizontal_source_is_finite(cuda):
