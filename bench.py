@@ -134,7 +134,7 @@ def fp64_peak_tflops(torch, dev):
 # FP64 operations of one (receiver, source) pair of the assembly kernel
 # (both unit slips, 6 entries): 357 add + 645 mul + 11 div + 3 sqrt, counted by
 # oracle/count_gf_flops.cpp on the kernel's own device math.
-GF_FLOP_PER_PAIR = 836
+GF_FLOP_PER_PAIR = 848
 # Stores per pair: 6 FP64 + 6 FP32 entries.
 GF_BYTES_PER_PAIR = 72
 

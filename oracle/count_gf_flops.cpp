@@ -31,6 +31,7 @@ inline bool operator==(C a, double b) { return a.v == b; }
 inline bool operator!=(C a, double b) { return a.v != b; }
 inline bool operator>(C a, C b) { return a.v > b.v; }
 inline C sqrt(C a) { ++g_ops.sqrt_; return C(std::sqrt(a.v)); }
+inline bool isfinite_t(C a) { return std::isfinite(a.v); }
 
 #include "../pyquake3d_gb300/csrc/gf_device.cuh"
 

@@ -30,6 +30,7 @@
 
 #ifndef __CUDACC__
 // Host compilation (operation counting in oracle/count_gf_flops.cpp).
+#include <cmath>
 #define __host__
 #define __device__
 #define __forceinline__ inline
@@ -139,6 +140,13 @@ __device__ __forceinline__ int tri_mode(T x, T y, T z, T p1y, T p1z, T p3y, T p3
     return m;
 }
 
+#ifdef __CUDACC__
+__device__ __forceinline__ bool isfinite_t(double v) { return isfinite(v); }
+#else
+inline bool isfinite_t(double v) { return std::isfinite(v); }
+inline bool isfinite_t(long double v) { return std::isfinite(v); }
+#endif
+
 // Shared geometric terms of one angular dislocation at (x, y, z) of its own
 // frame, opening angle with cos/sin (ca, sa).
 template <class T>
@@ -160,9 +168,23 @@ __device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, Ad
     g.x2 = x * x; g.y2 = y * y; g.z2 = z * z;
     const T r2 = g.x2 + g.y2 + g.z2;
     const T r = sqrt(r2);
-    const T ir = 1.0 / r;
-    const T irz = 1.0 / (r - z);
-    const T iW = 1.0 / (zeta - r);
+    const T rz = r - z, W = zeta - r;
+    // the three reciprocals from one division (a division is ~9 FP64-pipe
+    // instructions, a product one); the plain quotients where the product is
+    // zero or not finite (singular lines of the dislocation)
+    T ir, irz, iW;
+    const T rrz = r * rz, p = rrz * W;
+    if (p != 0.0 && isfinite_t(p)) {
+        const T ip = 1.0 / p;
+        const T iWp = ip * W;
+        ir = iWp * rz;
+        irz = iWp * r;
+        iW = ip * rrz;
+    } else {
+        ir = 1.0 / r;
+        irz = 1.0 / rz;
+        iW = 1.0 / W;
+    }
     const T ir2 = ir * ir;
     g.ir = ir;
     g.ir3 = ir2 * ir;
