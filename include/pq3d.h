@@ -236,7 +236,10 @@ typedef struct pq3d_batch_sim {
     int32_t precision;     /* PQ3D_BATCH_* */
     double *Tno, *Tt1o, *Tt2o, *state, *slipv1, *slipv2, *slipv, *slip1, *slip2;
     const double *a, *b, *dc, *f0, *shear_loading, *normal_loading, *cos_rake0, *sin_rake0;
-    double *rates;         /* [nsplit][B][3N] partial traction rates, summed in FP64 by the stepper */
+    double *rates;         /* partial traction rates, room for nsplit x Bp x 3N doubles: FP64 [Bp][3N]
+                              (nsplit = 1) for FP64, FP32 and HMAT; for BF16X6 FP32 [nsplit][Bp][3N],
+                              the K slices' tensor-memory accumulators, summed in float-float by the
+                              stepper */
     int32_t nsplit;        /* K-slices of the operator product (>= 1) */
     int32_t pad0;
     double *cand;          /* [B][N][4] candidate state */
@@ -276,9 +279,9 @@ size_t pq3d_batch_operator_bytes(int64_t N);
 int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpacked, void *stream);
 /* Bytes of the packed right-hand side for B runs (BF16X6). */
 size_t pq3d_batch_rhs_bytes(int64_t N, int B);
-/* The tensor-core product alone: out[(s*Bp + n)*3N + m] (s < nsplit K slices,
- * Bp = B rounded up to 16) from the packed operator and right-hand side. */
-int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, double *out,
+/* The tensor-core product alone: FP32 out[(s*Bp + n)*3N + m] (s < nsplit K
+ * slices, Bp = B rounded up to 16) from the packed operator and right-hand side. */
+int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
                            void *workspace, size_t workspace_bytes, void *stream);
 
 /* Device workspace bytes of one batched iteration (GEMM split-K partials live in

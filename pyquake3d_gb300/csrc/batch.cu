@@ -226,23 +226,42 @@ __global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
     if (i < N) {
         const int64_t idx = (int64_t)r * N + i;
         const int Bp = padded_runs(S.B);
-        double q0 = 0.0, q1 = 0.0, q2 = 0.0;
-        for (int s = 0; s < S.nsplit; ++s) {
-            const double *p = S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
-            q0 += p[0]; q1 += p[1]; q2 += p[2];
-        }
-        const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
         double yo[4];
         if (kMixed) {
+            // traction rates: the BF16X6 product leaves FP32 partials per K
+            // slice (added here in float-float, slice order), the other mixed
+            // products one FP64 value
+            FF q[3];
+            if (S.precision == PQ3D_BATCH_BF16X6) {
+                const float *pr = (const float *)S.rates + (int64_t)r * 3 * N + 3 * i;
+                const int64_t sstride = (int64_t)Bp * 3 * N;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = FF{pr[c], 0.f};
+                for (int sl = 1; sl < S.nsplit; ++sl)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) q[c] = ff_add(q[c], pr[sl * sstride + c]);
+            } else {
+                const double *pr = S.rates + (int64_t)r * 3 * N + 3 * i;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = ff_split(pr[c]);
+            }
             MixedBase m = load_base(S.base + idx, (int64_t)S.B * N);
-            const double shear = S.shear_loading[idx];
+            const float shear = (float)S.shear_loading[idx];
+            const float dsig = S.fix_Tn ? (float)S.normal_loading[idx]
+                                        : (q[2].hi + (q[2].lo + (float)S.normal_loading[idx]));
             m.V0 = V0f;
-            m.dsf = (float)dsig;
-            m.L[0] = (float)(shear - q0);
-            m.L[1] = (float)(shear - q1);
+            m.dsf = dsig;
+            m.L[0] = (shear - q[0].hi) - q[0].lo;
+            m.L[1] = (shear - q[1].hi) - q[1].lo;
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
         } else {
+            double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+            for (int s = 0; s < S.nsplit; ++s) {
+                const double *p = S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
+                q0 += p[0]; q1 += p[1]; q2 += p[2];
+            }
+            const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
             const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
                          0.0, 0.0};
             dp_attempt(c, S.V0, S.eta, hs, y, yo, m1, m2);
@@ -426,7 +445,7 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
         dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
         gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
-        rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.rates, workspace,
+        rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, (float *)S.rates, workspace,
                                    workspace_bytes, st);
         if (rc) return rc;
     } else {

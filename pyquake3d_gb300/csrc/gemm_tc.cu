@@ -8,7 +8,8 @@
 // the six cross products x_i * y_j with i + j <= 2 are accumulated in FP32 in
 // tensor memory.  Their sum carries the operands to ~2^-24 (the FP32 operator
 // copy's own rounding), while two-piece "BF16x3" carries them to ~2^-16.
-// Slices of the reduction (split-K) are added in FP64 by the consumer.
+// Slices of the reduction (split-K) are written as the FP32 tensor-memory
+// accumulators and added in float-float by the consumer.
 //
 // Data path (one CTA = one 128-row tile of K x one K slice, all runs):
 //   * the operator pieces are packed once, after assembly, into ready-made
@@ -20,7 +21,7 @@
 //   * warp 0 lane 0 produces stages, warp 1 lane 0 issues 12 tcgen05.mma
 //     (M=128, N=B, K=16; 6 products x 2 K-steps) per stage and frees the stage
 //     with tcgen05.commit; all 4 warps drain the FP32 accumulator from tensor
-//     memory (tcgen05.ld 32x32b) and store FP64.
+//     memory (tcgen05.ld 32x32b) and store it (FP32).
 //   * every mbarrier wait is bounded; a wait that gives up records an error
 //     word in the workspace, the kernel still waits (bounded) for its own
 //     tensor-core work, frees its tensor memory and returns.
@@ -139,7 +140,7 @@ __constant__ int kPairB[6] = {0, 1, 0, 2, 1, 0};
 
 __global__ void __launch_bounds__(128, 1)
 gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bp, int nsplit,
-                   double *__restrict__ out, int *__restrict__ err, int stages)
+                   float *__restrict__ out, int *__restrict__ err, int stages)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -223,7 +224,7 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
             if (m < M) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    out[((int64_t)slice * Bp + c0 + j) * M + m] = (double)__uint_as_float(r[j]);
+                    out[((int64_t)slice * Bp + c0 + j) * M + m] = __uint_as_float(r[j]);
             }
         }
     } else if (lane == 0) {
@@ -266,7 +267,7 @@ struct Cfg {
 };
 static thread_local Cfg g_cfg;
 
-int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, double *out, void *workspace,
+int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, float *out, void *workspace,
                 size_t workspace_bytes, cudaStream_t stream)
 {
     PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x6: null pointer");
@@ -335,7 +336,7 @@ extern "C" int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpac
 }
 
 extern "C" int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit,
-                                      double *out, void *workspace, size_t workspace_bytes, void *stream)
+                                      float *out, void *workspace, size_t workspace_bytes, void *stream)
 {
     clear_error();
     return tc::gemm_bf16x6(Kpacked, Vpacked, N, (B + 15) / 16 * 16, nsplit, out, workspace, workspace_bytes,

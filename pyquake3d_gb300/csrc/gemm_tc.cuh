@@ -36,8 +36,8 @@ size_t gemm_bf16x6_workspace_bytes(int64_t N, int Bp, int nsplit);
 
 // out[(s * Bp + n) * 3N + m] = sum over the columns k of slice s of K[m][k] * V[n][k],
 // from the packed operator and right-hand side; FP32 accumulation in tensor
-// memory, FP64 output.  Returns a PQ3D status.
-int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, double *out,
+// memory, FP32 output (the accumulator).  Returns a PQ3D status.
+int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, float *out,
                 void *workspace, size_t workspace_bytes, cudaStream_t stream);
 
 }  // namespace tc

@@ -260,7 +260,7 @@ __device__ __forceinline__ float rel_err(float num, double yo)
     return (float)(fabs((double)num) / fabs(yo + (double)num));
 }
 
-__device__ __forceinline__ bool finite_inputs(const MixedBase &m, const double y[4], double dsig)
+__device__ __forceinline__ bool finite_inputs(const MixedBase &m, const double y[4], float dsig)
 {
     return isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) && isfinite(m.L[0]) &&
            isfinite(m.L[1]) && isfinite(dsig) && isfinite(m.slipv);
@@ -271,10 +271,10 @@ __device__ __forceinline__ bool finite_inputs(const MixedBase &m, const double y
 // normal-stress rate dsig (Pa/s).  Writes the 5th-order solution to yo and
 // returns the two relative errors (as the FP64 attempt below; as floats:
 // they only decide accept / reject and the next dt).
-__device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, double dsig, float hf, const double y[4],
+__device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, float dsig, float hf, const double y[4],
                                                  double yo[4], float &e1, float &e2)
 {
-    const float dn = (float)(dsig * 1e-6);   // d(Tno)/dt, MPa/s, constant over the step
+    const float dn = dsig * 1e-6f;   // d(Tno)/dt, MPa/s, constant over the step
     const float A[6][6] = {{(float)B21, 0, 0, 0, 0, 0},
                            {(float)B31, (float)B32, 0, 0, 0, 0},
                            {(float)B41, (float)B42, (float)B43, 0, 0, 0},

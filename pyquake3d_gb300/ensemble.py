@@ -173,6 +173,17 @@ class Ensemble:
         sz = ctypes.sizeof(_lib.RunCtrl)
         self.ctrl_t[slot * sz:(slot + 1) * sz].copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
 
+    def traction_rates(self):
+        """(B, 3N) FP64 traction rates K.v' of the last product: the FP32
+        K-slice partials of the tensor-core product added, or the one FP64
+        partial of the other products."""
+        n = self.nsplit * self.Bp * 3 * self.N
+        if self.precision == "bf16x6":
+            r = self.t["rates"].view(torch.float32)[:n].view(self.nsplit, self.Bp, 3 * self.N).double().sum(0)
+        else:
+            r = self.t["rates"][:n].view(self.nsplit, self.Bp, 3 * self.N).sum(0)
+        return r[:self.B]
+
     def state_bytes(self):
         """Device bytes of the per-run state, rates, right-hand side and control."""
         return sum(t.numel() * t.element_size() for t in self.t.values()) + self.vop.numel() * self.vop.element_size() \

@@ -39,8 +39,7 @@ def _tables(g, B, seed=0):
 
 
 def _rates(ens):
-    r = ens.t["rates"].view(ens.nsplit, ens.Bp, 3 * ens.N).sum(0)
-    return r[:ens.B].cpu().numpy()
+    return ens.traction_rates().cpu().numpy()
 
 
 @pytest.mark.parametrize("N,B,nsplit", [(64, 16, 1), (64, 5, 3), (700, 64, 2), (1000, 40, 7)])
