@@ -299,6 +299,12 @@ def bench_ours(args):
         # DRAM bytes of one launch: ncu on the N=2,000 case measured 56.9 B/pair
         # (226.3 MB written + 1.4 MB read for 4e6 pairs, part of the 288 MB of
         # stores still dirty in L2 at kernel end); scaled to this launch.
+        # the FP64 pipe is the bound: DGEMM issues only 2-flop DFMAs, this
+        # kernel averages ~1.3 flops per FP64-pipe instruction; ncu on the
+        # N = 2,000 case: FP64 pipe 88 % busy (active cycles)
+        roof["fp64_pipe_active_pct"] = 88.3
+        roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, N=2000 case "
+                             "(profiles/gf_assembly_rough_N2000.md)")
         roof["traffic"] = 56.9 * N * N
         roof["traffic_note"] = ("ncu dram__bytes_read+write at N=2000 (56.9 B/pair) scaled by pairs; "
                                 "algorithmic stores are %d B/pair" % GF_BYTES_PER_PAIR)

@@ -59,21 +59,6 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     dtau2 = t2 / 1e6;
 }
 
-// e^x with x = (n + f) / log2(e), n integer and |f| <= 1/2 (Cody-Waite
-// range reduction); 2^f from the FP32 exp2f, 2^n exact.  Relative error
-// ~2.5e-7 (that of exp2f), 6 FP64 operations instead of the ~20 of an FP64
-// exp.  The argument is clipped to +-700 like the reference's safe_exp.
-// Used by the mixed-precision slip-rate update.
-__device__ __forceinline__ double fexp(double x)
-{
-    x = fmin(fmax(x, -700.0), 700.0);
-    const double t = x * 1.4426950408889634;
-    const double n = rint(t);
-    const float f = (float)(t - n);
-    const double scale = __longlong_as_double((long long)((int)n + 1023) << 52);
-    return (double)exp2f(f) * scale;
-}
-
 // 1/d: the FP32 reciprocal refined by one Newton-Raphson step
 // r <- r (2 - d r) in FP64 (the relative error squares: ~4e-15), two FMAs
 // instead of a full FP64 division.  d in FP32 range.
