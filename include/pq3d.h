@@ -225,7 +225,8 @@ typedef struct pq3d_run_ctrl {
 #define PQ3D_BATCH_FP32 1      /* FP32 operator, FP32 FMA (CUDA cores), FP64 across chunks */
 #define PQ3D_BATCH_BF16X6 2    /* FP32 operator split on the fly into 3 BF16 pieces, v' into 3 BF16
                                   pieces, the 6 leading cross products on tcgen05 tensor cores,
-                                  FP32 accumulation in tensor memory, FP64 across K slices */
+                                  FP32 accumulation in tensor memory, K slices added in
+                                  float-float */
 #define PQ3D_BATCH_HMAT 3      /* H-matrix product (pq3d_hmat_apply); K points to a host pq3d_hmat */
 
 /* Device state of B simulations sharing one mesh.  Arrays are run-major
