@@ -270,7 +270,7 @@ typedef struct pq3d_batch_sim {
     float *base;
 } pq3d_batch_sim;
 
-#define PQ3D_BATCH_BASE_FIELDS 20
+#define PQ3D_BATCH_BASE_FIELDS 24
 
 /* Packed operator of the tensor-core product: the FP64 operator split into
  * three BF16 pieces, stored as [3N/128 tiles][2N/32 blocks][3][128 x 32]

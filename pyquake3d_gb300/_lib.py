@@ -79,7 +79,7 @@ PQ3D_BATCH_FP64 = 0
 PQ3D_BATCH_FP32 = 1
 PQ3D_BATCH_BF16X6 = 2
 PQ3D_BATCH_HMAT = 3
-PQ3D_BATCH_BASE_FIELDS = 20   # floats per cell and run of pq3d_batch_sim.base
+PQ3D_BATCH_BASE_FIELDS = 24   # floats per cell and run of pq3d_batch_sim.base
 
 
 class StepCtrl(ctypes.Structure):

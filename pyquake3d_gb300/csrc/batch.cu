@@ -87,10 +87,13 @@ __global__ void prepare_kernel(pq3d_batch_sim S)
         const int64_t idx = (int64_t)r * S.N + i;
         vprime(S, idx, v1, v2);
         if (S.base) {
-            MixedBase m = mixed_base(S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx], S.a[idx], S.b[idx],
-                                     S.dc[idx], S.f0[idx], log_eta_v0(S));
-            m.slipv = (float)S.slipv[idx];
-            store_base(S.base + idx, (int64_t)S.B * S.N, m);
+            float *pb = S.base + idx;
+            const int64_t stride = (int64_t)S.B * S.N;
+            store_base_constants(pb, stride, S.a[idx], S.b[idx], S.dc[idx], S.f0[idx]);
+            MixedBase m;
+            store_base_state(pb, stride, S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx],
+                             ff_split(log_eta_v0(S)), m);
+            pb[19 * stride] = (float)S.slipv[idx];
         }
     }
     write_vop(S, r, i, v1, v2);
@@ -322,25 +325,26 @@ __global__ void decide_kernel(pq3d_run_ctrl *ctrl, int B)
     }
 }
 
-// kMixed: the new state's start-of-step constants (the FP64 work of the
-// mixed attempts, done once per accepted step) and from them the slip rate
-// 2 V0 e^{-psi/a} sinh(tau / (sigma a)) in float-float exponent arithmetic
-// (~2e-7 relative, as the mixed right-hand side); FP64 for the slip
-// accumulation.  The FP64 arm keeps the reference formula
-// (src/QDsim_gpu.py:994-1027).
+// kMixed: the new state's start-of-step constants (in float-float from the
+// FP64 state, once per accepted step for all the attempts of the next step)
+// and from them the slip rate 2 V0 e^{-psi/a} sinh(tau / (sigma a)) (~2e-7
+// relative, as the mixed right-hand side); FP64 for the slip accumulation.
+// The FP64 arm keeps the reference formula (src/QDsim_gpu.py:994-1027).
 template <bool kMixed>
 __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
 {
     __shared__ int acc;
-    __shared__ double hs, log_etaV0;
-    __shared__ float inv_eta;
+    __shared__ double hs;
+    __shared__ float inv_eta, c0hi, c0lo;
     const int r = blockIdx.y;
     const pq3d_run_ctrl *C = S.ctrl + r;
     if (threadIdx.x == 0) {
         acc = C->accepted;
         hs = C->h_last;
         if (kMixed) {
-            log_etaV0 = log_eta_v0(S);
+            const FF c0 = ff_split(log_eta_v0(S));
+            c0hi = c0.hi;
+            c0lo = c0.lo;
             inv_eta = (float)(1.0 / S.eta);
         }
     }
@@ -352,20 +356,23 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     const int64_t idx = (int64_t)r * N + i;
     const double h = hs;
     const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
-    const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[idx];
+    const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w;
     S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
     double v1, v2, v;
     if (kMixed) {
-        MixedBase m = mixed_base(Tno, T1, T2, st, a, S.b[idx], S.dc[idx], S.f0[idx], log_etaV0);
+        float *pb = S.base + idx;
+        const int64_t stride = (int64_t)S.B * N;
+        MixedBase m;
+        store_base_state(pb, stride, Tno, T1, T2, st, FF{c0hi, c0lo}, m);
         const float f1 = base_slip_rate(m, 0, inv_eta), f2 = base_slip_rate(m, 1, inv_eta);
         // |V| without under/overflow of the squares
         const float p = fmaxf(fabsf(f1), fabsf(f2)), q = fminf(fabsf(f1), fabsf(f2));
         const float t = p > 0.f ? q / p : 0.f;
         const float vf = fmaxf(p * sqrtf(fmaf(t, t, 1.f)), 1e-30f);
-        m.slipv = vf;
-        store_base(S.base + idx, (int64_t)S.B * N, m);
+        pb[19 * stride] = vf;
         v1 = f1; v2 = f2; v = vf;
     } else {
+        const double a = S.a[idx];
         const double e = (2.0 * S.V0) * exp(-st / a);
         v1 = e * sinh(T1 / Tno / a);
         v2 = e * sinh(T2 / Tno / a);

@@ -59,14 +59,6 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     dtau2 = t2 / 1e6;
 }
 
-// 1/d: the FP32 reciprocal refined by one Newton-Raphson step
-// r <- r (2 - d r) in FP64 (the relative error squares: ~4e-15), two FMAs
-// instead of a full FP64 division.  d in FP32 range.
-__device__ __forceinline__ double rcp_nr(double d)
-{
-    const double r = (double)__frcp_rn((float)d);
-    return fma(r, fma(-d, r, 1.0), r);
-}
 
 // ---------------------------------------------------------------------------
 // Mixed-precision attempt (batched mixed modes).
@@ -130,10 +122,50 @@ __device__ __forceinline__ float ff_exp_neg_abs(FF v)
 
 __device__ __forceinline__ float ff_exp(FF v) { return expf(v.hi) * (1.f + v.lo); }
 
+// float-float arithmetic (Dekker / Knuth error-free transforms with FMA; ~2^-46
+// relative), FP32 pipes only; the explicit rounding intrinsics keep the
+// compiler from contracting the transforms
+__device__ __forceinline__ FF ff_norm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ FF ff_add2(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bp = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return ff_norm(s, e);
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return ff_norm(p, e);
+}
+
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
+
+// 1/d: the FP32 reciprocal r and one Newton step r + r (1 - d r), the
+// residual 1 - d r formed exactly with FMAs
+__device__ __forceinline__ FF ff_rcp(FF d)
+{
+    const float r = __frcp_rn(d.hi);
+    float e = __fmaf_rn(-d.hi, r, 1.f);
+    e = __fmaf_rn(-d.lo, r, e);
+    return ff_norm(r, __fmul_rn(r, e));
+}
+
 // Constants of one cell at the start of a step (y0), shared by all the
-// attempts of the step: computed once per accepted step (the FP64 set-up:
-// GB300's FP64 pipe also executes the FP64<->FP32 conversions and the FP64
-// compares, at the FP64 rate) and stored as kBaseFields floats per cell.
+// attempts of the step: computed once per accepted step, in float-float from
+// the FP64 state (GB300's FP64 pipe, which also executes the FP64<->FP32
+// conversions and the FP64 compares, is 1/64 of the FP32 rate), and stored as
+// kBaseFields floats per cell.
 struct MixedBase {
     float Tn0;          // effective normal stress at y0 (MPa)
     float q0[2];        // tau_k / sigma at y0
@@ -146,46 +178,57 @@ struct MixedBase {
     float V0, dsf;      // V0; dsigma/dt - dP/dt (Pa/s)
     float L[2];         // -K.v' + shear loading (Pa/s)
 };
-constexpr int kBaseFields = 20;
+// stored per cell: the 20 fields above, then the cell constants 1/a, 1/b and
+// f0 as float-float lo parts / pairs (fields 20-23: 1/a lo, 1/b lo, f0 hi, f0 lo)
+constexpr int kBaseFields = 24;
 
-// Tn0: effective normal stress (MPa); T1, T2 shear stresses (MPa); psi state
-__device__ __forceinline__ MixedBase mixed_base(double Tn0, double T1, double T2, double psi, double a, double b,
-                                                double dc, double f0, double log_etaV0)
+// The cell's constants, set once (FP64 quotients, split), fields 15-18, 20-23.
+__device__ __forceinline__ void store_base_constants(float *p, int64_t stride, double a, double b, double dc,
+                                                     double f0)
 {
-    MixedBase m;
-    const double r0 = rcp_nr(Tn0), inv_a = rcp_nr(a), inv_b = rcp_nr(b);
-    const double q1 = T1 * r0, q2 = T2 * r0;
-    const double x1 = q1 * inv_a, x2 = q2 * inv_a;
-    const double sp = fma(-psi, inv_a, log_etaV0);
-    m.Tn0 = (float)Tn0;
-    m.q0[0] = (float)q1; m.q0[1] = (float)q2;
-    m.inv_a = (float)inv_a;
-    m.x0[0] = m.q0[0] * m.inv_a; m.x0[1] = m.q0[1] * m.inv_a;
-    m.Sp[0] = ff_split(sp + x1); m.Sm[0] = ff_split(sp - x1);
-    m.Sp[1] = ff_split(sp + x2); m.Sm[1] = ff_split(sp - x2);
-    m.g0 = ff_split((f0 - psi) * inv_b);
-    m.a = (float)a;
-    m.inv_b = (float)inv_b;
-    m.bdc = (float)b / (float)dc;
-    m.slipv = 0.f;
-    return m;
+    const FF ia = ff_split(1.0 / a), ib = ff_split(1.0 / b), ff0 = ff_split(f0);
+    p[15 * stride] = (float)a;
+    p[16 * stride] = ia.hi;
+    p[17 * stride] = ib.hi;
+    p[18 * stride] = (float)b / (float)dc;
+    p[20 * stride] = ia.lo;
+    p[21 * stride] = ib.lo;
+    p[22 * stride] = ff0.hi;
+    p[23 * stride] = ff0.lo;
 }
 
-// stored as [kBaseFields][cells] (field-major: coalesced)
-__device__ __forceinline__ void store_base(float *p, int64_t stride, const MixedBase &m)
+// The state-dependent constants (fields 0-14) of the state (Tn0, T1, T2, psi)
+// (MPa, MPa, MPa, state), in float-float from the FP64 state: the FP64 work is
+// the four splits.  c0 = ln(eta V0) as float-float.
+__device__ __forceinline__ void store_base_state(float *p, int64_t stride, double Tn0, double T1, double T2,
+                                                 double psi, FF c0, MixedBase &m)
 {
-    const float v[kBaseFields] = {m.Tn0, m.q0[0], m.q0[1], m.x0[0], m.x0[1], m.Sp[0].hi, m.Sp[0].lo, m.Sp[1].hi,
-                                  m.Sp[1].lo, m.Sm[0].hi, m.Sm[0].lo, m.Sm[1].hi, m.Sm[1].lo, m.g0.hi, m.g0.lo,
-                                  m.a, m.inv_a, m.inv_b, m.bdc, m.slipv};
+    const float *q = p;
+    const FF ia{q[16 * stride], q[20 * stride]}, ib{q[17 * stride], q[21 * stride]};
+    const FF f0{q[22 * stride], q[23 * stride]};
+    const FF tn = ff_split(Tn0), t1 = ff_split(T1), t2 = ff_split(T2), ps = ff_split(psi);
+    const FF r0 = ff_rcp(tn);
+    const FF q1 = ff_mul(t1, r0), q2 = ff_mul(t2, r0);
+    const FF x1 = ff_mul(q1, ia), x2 = ff_mul(q2, ia);
+    const FF sp = ff_add2(ff_neg(ff_mul(ps, ia)), c0);
+    m.Tn0 = tn.hi;
+    m.q0[0] = q1.hi; m.q0[1] = q2.hi;
+    m.inv_a = ia.hi;
+    m.x0[0] = m.q0[0] * m.inv_a; m.x0[1] = m.q0[1] * m.inv_a;
+    m.Sp[0] = ff_add2(sp, x1); m.Sm[0] = ff_add2(sp, ff_neg(x1));
+    m.Sp[1] = ff_add2(sp, x2); m.Sm[1] = ff_add2(sp, ff_neg(x2));
+    m.g0 = ff_mul(ff_add2(f0, ff_neg(ps)), ib);
+    const float v[15] = {m.Tn0, m.q0[0], m.q0[1], m.x0[0], m.x0[1], m.Sp[0].hi, m.Sp[0].lo, m.Sp[1].hi,
+                         m.Sp[1].lo, m.Sm[0].hi, m.Sm[0].lo, m.Sm[1].hi, m.Sm[1].lo, m.g0.hi, m.g0.lo};
 #pragma unroll
-    for (int k = 0; k < kBaseFields; ++k) p[k * stride] = v[k];
+    for (int k = 0; k < 15; ++k) p[k * stride] = v[k];
 }
 
 __device__ __forceinline__ MixedBase load_base(const float *__restrict__ p, int64_t stride)
 {
-    float v[kBaseFields];
+    float v[20];
 #pragma unroll
-    for (int k = 0; k < kBaseFields; ++k) v[k] = __ldg(p + k * stride);
+    for (int k = 0; k < 20; ++k) v[k] = __ldg(p + k * stride);
     MixedBase m;
     m.Tn0 = v[0];
     m.q0[0] = v[1]; m.q0[1] = v[2];
