@@ -341,6 +341,9 @@ typedef struct pq3d_hmat {
     const int32_t *leaf_blocks;   /* blocks whose row range covers each leaf row cluster, fixed order */
     const int32_t *t_sched;       /* [t_rows] rank rows: those of at most 8192 columns, then the longer ones */
     int64_t t_nlong;              /* number of the longer rows (the tail of t_sched) */
+    const int32_t *t_grp;         /* [t_ngrp] groups of up to 4 consecutive shorter rank rows of one block
+                                     (they share their x values): first position in t_sched | size << 28 */
+    int64_t t_ngrp;
 } pq3d_hmat;
 
 /* ACA (partial pivoting, relative Frobenius tolerance `tol`) of the listed

@@ -72,7 +72,7 @@ class HMat(ctypes.Structure):
     """Mirror of pq3d_hmat."""
     _fields_ = [("N", c_i64), ("nblocks", ctypes.c_int32), ("nleaves", ctypes.c_int32), ("t_rows", c_i64)] + \
         [(n, c_void_p) for n in ("perm", "blk", "rank", "off", "data", "lr_ids", "t_info", "t_off", "leaf", "leaf_ptr",
-                                 "leaf_blocks", "t_sched")] + [("t_nlong", c_i64)]
+                                 "leaf_blocks", "t_sched")] + [("t_nlong", c_i64), ("t_grp", c_void_p), ("t_ngrp", c_i64)]
 
 
 PQ3D_BATCH_FP64 = 0

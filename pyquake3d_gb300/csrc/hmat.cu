@@ -393,54 +393,58 @@ __device__ __forceinline__ FF t_row_part(const float *__restrict__ v, const floa
     return warp_sum_ff(sum);
 }
 
-// Two short rows at once on one warp (A and B), 8 columns of each per lane in
-// flight: a warp keeps twice the bytes in flight of a one-row walk for the
-// same registers (the short rows, ~630 columns on average, were bound by
-// their round trips).  Columns beyond a row's end are predicated off (zero
-// terms); partial sums move to float-float every 1024 columns.
-__device__ __forceinline__ void t_row_pair(const float *__restrict__ vA, const float2 *__restrict__ xA, int nA,
-                                           const float *__restrict__ vB, const float2 *__restrict__ xB, int nB,
-                                           int lane, FF &outA, FF &outB)
+// Up to 4 consecutive short rank rows of one block on one warp: the rows
+// share their x values, so a lane loads x once per column for all of them and
+// keeps 8 columns of every row in flight; a warp therefore moves ~4x the bytes
+// per memory round trip of a one-row walk (the ~630-column rows were bound by
+// their round trips).  Row j starts at v + j * nc.  Columns beyond the end
+// are predicated off (zero terms); partial sums move to float-float every
+// 1024 columns.
+__device__ __forceinline__ void t_row_group(const float *__restrict__ v, int nc, int g, const float2 *__restrict__ x,
+                                            int lane, FF (&out)[4])
 {
-    FF sA{0.f, 0.f}, sB{0.f, 0.f};
-    const int n = max(nA, nB);
-    for (int c0k = 0; c0k < n; c0k += 1024) {
-        Acc2 a0{0.f, 0.f}, a1{0.f, 0.f}, b0{0.f, 0.f}, b1{0.f, 0.f};
-        const int cend = min(n, c0k + 1024);
+    FF sum[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sum[j] = FF{0.f, 0.f};
+    for (int c0k = 0; c0k < nc; c0k += 1024) {
+        Acc2 a0[4], a1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { a0[j] = Acc2{0.f, 0.f}; a1[j] = Acc2{0.f, 0.f}; }
+        const int cend = min(nc, c0k + 1024);
         for (int col = c0k + lane; col - lane < cend; col += 256) {
-            float ka[8], kb[8];
-            float2 xa[8], xb[8];
+            float2 xv[8];
+            float k[4][8];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 const int c = col + 32 * u;
-                const bool oa = c < nA && c < cend, ob = c < nB && c < cend;
-                ka[u] = oa ? __ldg(vA + c) : 0.f;
-                xa[u] = oa ? xA[c] : make_float2(0.f, 0.f);
-                kb[u] = ob ? __ldg(vB + c) : 0.f;
-                xb[u] = ob ? xB[c] : make_float2(0.f, 0.f);
+                const bool ok = c < cend;
+                xv[u] = ok ? x[c] : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) k[j][u] = (ok && j < g) ? __ldg(v + (int64_t)j * nc + c) : 0.f;
             }
 #pragma unroll
-            for (int u = 0; u < 8; u += 2) {
-                acc2_add(a0, ka[u], xa[u]);
-                acc2_add(a1, ka[u + 1], xa[u + 1]);
-                acc2_add(b0, kb[u], xb[u]);
-                acc2_add(b1, kb[u + 1], xb[u + 1]);
-            }
+            for (int u = 0; u < 8; u += 2)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    acc2_add(a0[j], k[j][u], xv[u]);
+                    acc2_add(a1[j], k[j][u + 1], xv[u + 1]);
+                }
         }
-        sA = ff_add(sA, FF{a0.s, 0.f});
-        sA = ff_add(sA, FF{a1.s, 0.f});
-        sA = ff_add(sA, FF{__fadd_rn(a0.c, a1.c), 0.f});
-        sB = ff_add(sB, FF{b0.s, 0.f});
-        sB = ff_add(sB, FF{b1.s, 0.f});
-        sB = ff_add(sB, FF{__fadd_rn(b0.c, b1.c), 0.f});
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            sum[j] = ff_add(sum[j], FF{a0[j].s, 0.f});
+            sum[j] = ff_add(sum[j], FF{a1[j].s, 0.f});
+            sum[j] = ff_add(sum[j], FF{__fadd_rn(a0[j].c, a1[j].c), 0.f});
+        }
     }
-    outA = warp_sum_ff(sA);
-    outB = warp_sum_ff(sB);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[j] = warp_sum_ff(sum[j]);
 }
 
 __global__ void __launch_bounds__(256)
 lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info,
-                 const int32_t *__restrict__ t_sched, int64_t nshort, int64_t nlong, int64_t short_ctas,
+                 const int32_t *__restrict__ t_sched, const int32_t *__restrict__ t_grp, int64_t ngrp,
+                 int64_t nshort, int64_t nlong, int64_t short_ctas,
                  const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T, const int32_t *act,
                  int act_stride)
 {
@@ -451,24 +455,17 @@ lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t
     if (!run_on(act, act_stride, r)) return;   // uniform per CTA
     const float2 *xr = Xs + (int64_t)r * 2 * N;
     if (cta < short_ctas) {
-        // 16 short rows per CTA, two per warp
-        const int64_t qa = cta * 16 + wid, qb = qa + 8;
-        if (qa >= nshort) return;
-        const int wa = t_sched[qa];
-        const longlong2 ia = t_info[wa];
-        int wb = -1;
-        longlong2 ib = make_longlong2(0, 0);
-        if (qb < nshort) {
-            wb = t_sched[qb];
-            ib = t_info[wb];
-        }
-        FF sa, sb;
-        t_row_pair(data + ia.x, xr + (int32_t)(ia.y & 0xffffffffll), (int)(ia.y >> 32), data + ib.x,
-                   xr + (int32_t)(ib.y & 0xffffffffll), wb >= 0 ? (int)(ib.y >> 32) : 0, lane, sa, sb);
-        if (lane == 0) {
-            T[wa * (int64_t)B + r] = make_float2(sa.hi, sa.lo);
-            if (wb >= 0) T[wb * (int64_t)B + r] = make_float2(sb.hi, sb.lo);
-        }
+        // 8 groups of short rows per CTA, one per warp
+        const int64_t gi = cta * 8 + wid;
+        if (gi >= ngrp) return;
+        const int e = t_grp[gi];
+        const int q0 = e & 0x0FFFFFFF, g = e >> 28;
+        const int w0 = t_sched[q0];
+        const longlong2 info = t_info[w0];
+        FF sg[4];
+        t_row_group(data + info.x, (int)(info.y >> 32), g, xr + (int32_t)(info.y & 0xffffffffll), lane, sg);
+        if (lane == 0)
+            for (int j = 0; j < g; ++j) T[(w0 + j) * (int64_t)B + r] = make_float2(sg[j].hi, sg[j].lo);
         return;
     }
     const int64_t q = cta - short_ctas;
@@ -738,10 +735,11 @@ extern "C" int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B
     // does not depend on B
     if (H->t_rows > 0) {
         const int64_t nshort = H->t_rows - H->t_nlong;
-        const int64_t short_ctas = (nshort + 15) / 16;
+        const int64_t short_ctas = (H->t_ngrp + 7) / 8;
         const int64_t nT = (short_ctas + H->t_nlong) * B;
         PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
-        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_sched, nshort,
+        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_sched, H->t_grp,
+                                                       H->t_ngrp, nshort,
                                                        H->t_nlong, short_ctas, Xs, N, B, T, run_active,
                                                        active_stride);
     }

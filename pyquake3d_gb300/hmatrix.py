@@ -259,6 +259,8 @@ class HMatrix:
 
     LONG_ROW = 8192   # columns above which a rank row gets a whole CTA in the product
 
+    T_GROUP = 4       # short rank rows of one block handled together (they share the x values)
+
     def _make_sched(self, info):
         Nc = (np.asarray(info)[:, 1] >> 32) if self.t_rows else np.zeros(0, np.int64)
         rows = np.arange(len(Nc), dtype=np.int32)
@@ -266,6 +268,21 @@ class HMatrix:
         sched = np.concatenate([rows[~longm], rows[longm]]) if len(Nc) else np.zeros(1, np.int32)
         self.t_sched = torch.as_tensor(np.ascontiguousarray(sched, dtype=np.int32), device=self.device)
         self.t_nlong = int(longm.sum())
+        # groups of up to T_GROUP consecutive short rows of one low-rank block
+        # (all rows of a block have the same length): first position in
+        # t_sched | group size << 28
+        grp = []
+        if self.t_rows:
+            ranks = self.rank.cpu().numpy()[self.lr_ids.cpu().numpy()].astype(np.int64) if len(Nc) else []
+            pos = np.cumsum(~longm) - 1
+            first = 0
+            for k in ranks:
+                if k > 0 and not longm[first]:
+                    for j in range(0, int(k), self.T_GROUP):
+                        grp.append(int(pos[first + j]) | (min(self.T_GROUP, int(k) - j) << 28))
+                first += int(k)
+        self.t_grp = torch.as_tensor(np.asarray(grp if grp else [0], dtype=np.int32), device=self.device)
+        self.t_ngrp = len(grp)
 
     def _make_struct(self):
         H = _lib.HMat()
@@ -273,6 +290,7 @@ class HMatrix:
         for k in self._ARRAYS:
             setattr(H, k, getattr(self, k).data_ptr())
         H.t_sched, H.t_nlong = self.t_sched.data_ptr(), self.t_nlong
+        H.t_grp, H.t_ngrp = self.t_grp.data_ptr(), self.t_ngrp
         self.H = H
 
     def save(self, path):

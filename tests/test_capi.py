@@ -40,7 +40,7 @@ def test_struct_layouts_match_header(tmp_path):
                                               "V0", "eta", "fix_Tn", "ndepth", "P", "Parr", "dila"]),
               "pq3d_run_ctrl": ("RunCtrl", ["h", "time", "attempts", "max_steps", "err2_bits", "status", "accepted"]),
               "pq3d_step_ctrl": ("StepCtrl", ["dttry", "status", "attempts", "err_slot", "maxv_bits", "bar_gen"]),
-              "pq3d_hmat": ("HMat", ["N", "nblocks", "nleaves", "t_rows", "perm", "data", "t_info", "t_sched", "t_nlong", "leaf_blocks"])}
+              "pq3d_hmat": ("HMat", ["N", "nblocks", "nleaves", "t_rows", "perm", "data", "t_info", "t_sched", "t_nlong", "t_grp", "t_ngrp", "leaf_blocks"])}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "pq3d.h"', "int main(void){"]
     for cname, (_, fl) in fields.items():
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
