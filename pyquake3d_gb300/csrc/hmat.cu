@@ -441,7 +441,7 @@ __device__ __forceinline__ void t_row_group(const float *__restrict__ v, int nc,
     for (int j = 0; j < 4; ++j) out[j] = warp_sum_ff(sum[j]);
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info,
                  const int32_t *__restrict__ t_sched, const int32_t *__restrict__ t_grp, int64_t ngrp,
                  int64_t nshort, int64_t nlong, int64_t short_ctas,
