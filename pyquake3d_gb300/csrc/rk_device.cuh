@@ -64,16 +64,18 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
 // Mixed-precision attempt (batched mixed modes).
 //
 // GB300 runs FP64 at 1/64 of the FP32 rate, so the seven right-hand sides of
-// an attempt run in FP32 and only per-attempt set-up and the final state
-// update are FP64.  Two reformulations keep FP32 both accurate and in range:
+// an attempt run in FP32; FP64 is kept for the state itself (start state and
+// the accepted update).  Two reformulations keep FP32 both accurate and in
+// range:
 //
 // (1) Increments.  A stage state is the attempt's start state y0 plus an
 //     increment h * sum_l A_jl k_l that is formed in FP32 (relative error
 //     ~1e-7 of the increment, not of the state).  The large exponent
 //     arguments -psi/a and tau/(a sigma) (~200, nearly cancelling) are
-//     evaluated once per attempt in FP64 at y0; at a stage only their
-//     change is added, in FP32, to a float-float (hi + lo) copy of the
-//     FP64 value, so the exponent keeps ~1e-7 absolute accuracy.
+//     evaluated once per step at y0, in float-float arithmetic from the
+//     split FP64 state (MixedBase, stored per cell); at a stage only their
+//     change is added, in FP32, to that float-float value, so the exponent
+//     keeps ~1e-7 absolute accuracy.
 //
 // (2) Scale.  With u = -psi/a + |x|, x = tau/(a sigma), r = e^{-2|x|} and
 //     W = eta V0 e^u the traction rate of the right-hand side (the
