@@ -38,7 +38,7 @@ extern "C" {
 #define PQ3D_ERR_CUDA 2         /* a CUDA call failed */
 #define PQ3D_ERR_TIMEOUT 3      /* a bounded device-side wait gave up */
 #define PQ3D_ERR_STEP 4         /* dt < 1e-15 or more than 20 rejected attempts */
-#define PQ3D_ERR_UNSUPPORTED 5  /* a feature this build does not provide */
+#define PQ3D_ERR_UNSUPPORTED 5  /* a feature the library does not provide */
 
 /* Text of the last error raised on the calling host thread ("" if none). */
 const char *pq3d_last_error(void);

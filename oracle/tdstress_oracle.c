@@ -16,7 +16,7 @@
  *   - configuration test (+1/-1/0)    src/TDstressFS_C.cpp:125-166 (trimodefinder)
  *   - per-side frame rotation         src/TDstressFS_C.cpp:185-256 (TDSetupS)
  *   - tensor rotation T' = A^T T A    src/TDstressFS_C.cpp:21-49   (TensTrans)
- *   - full-space driver               src/TDstressFS_C.cpp:274-521 (TDstressFS)
+ *   - full-space entry point          src/TDstressFS_C.cpp:274-521 (TDstressFS)
  *   - receivers exactly on a side line in the triangle plane (mode 0) keep zero
  *     strain, as the C++ does (src/TDstressFS_C.cpp:446-477); the NumPy twin
  *     writes NaN there instead (src/SH_greenfunction.py:297-302).

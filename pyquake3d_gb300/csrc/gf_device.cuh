@@ -6,7 +6,7 @@
 //   angular-dislocation strain   src/TDstressFS_C.cpp:51-121
 //   configuration test           src/TDstressFS_C.cpp:125-166
 //   per-side rotation            src/TDstressFS_C.cpp:185-256
-//   full-space driver            src/TDstressFS_C.cpp:274-521
+//   full-space entry point       src/TDstressFS_C.cpp:274-521
 //   traction projection          src/QDsim_gpu.py:1400-1417
 //   receiver frames              src/readmsh.py:75-134
 //
