@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__
 // attempt / decide / update
 
 template <bool kMixed>
-__global__ void __launch_bounds__(256) attempt_kernel(pq3d_batch_sim S)
+__global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch_sim S)
 {
     __shared__ unsigned long long red[32];
     __shared__ int act;
