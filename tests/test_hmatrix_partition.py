@@ -51,3 +51,36 @@ def test_oracle_partition_matches_reference_golden():
     assert got == ref
     lr = [lowrank for _, _, lowrank in ohm.leaf_blocks(xg, 16, int(g["mini_leaf"]))]
     assert np.array_equal(np.array(lr), g["aca"])
+
+
+def test_low_rank_row_schedule_and_groups():
+    """Host-side work lists of the low-rank product: short rows first (row
+    order), long rows after; groups of up to 4 consecutive short rows of one
+    block, each group's rows contiguous in the schedule."""
+    import torch
+    from pyquake3d_gb300.hmatrix import HMatrix
+    H = HMatrix.__new__(HMatrix)
+    H.device = torch.device("cpu")
+    # four low-rank blocks (ids 1, 2, 4, 5 of 6): ranks 5, 3, 9, 1; block 4's rows are long
+    rank = np.array([-1, 5, 3, -1, 9, 1], dtype=np.int32)
+    lr = np.array([1, 2, 4, 5], dtype=np.int32)
+    H.rank, H.lr_ids = torch.as_tensor(rank), torch.as_tensor(lr)
+    ranks = rank[lr]
+    H.t_rows = int(ranks.sum())
+    Nc = np.concatenate([np.full(k, nc) for k, nc in zip(ranks, (300, 64, 20000, 8))]).astype(np.int64)
+    info = np.stack([np.arange(H.t_rows, dtype=np.int64) * 1000, Nc << 32], 1)
+    H._make_sched(info)
+    sched = H.t_sched.numpy()
+    short = np.nonzero(Nc <= H.LONG_ROW)[0]
+    assert np.array_equal(sched[:len(short)], short) and H.t_nlong == 9
+    assert np.array_equal(np.sort(sched[len(short):]), np.nonzero(Nc > H.LONG_ROW)[0])
+    grp = H.t_grp.numpy()
+    q0, g = grp & 0x0FFFFFFF, grp >> 28
+    assert list(g) == [4, 1, 3, 1] and H.t_ngrp == 4
+    covered = np.concatenate([sched[a:a + n] for a, n in zip(q0, g)])
+    assert np.array_equal(np.sort(covered), short)
+    # rows of a group are consecutive rows of one block
+    block_of = np.repeat(np.arange(len(lr)), ranks)
+    for a, n in zip(q0, g):
+        rows = sched[a:a + n]
+        assert np.all(np.diff(rows) == 1) and len(set(block_of[rows])) == 1
