@@ -459,7 +459,7 @@ def bench_batched(torch, dev, args, peaks):
     1 km squares), per-run friction draws (seed 0), BF16x6 tensor-core traction
     product vs the plain FP64 single-simulation stepper on the same mesh."""
     import ctypes
-    from pyquake3d_gb300 import _lib, gf, mesh
+    from pyquake3d_gb300 import _lib, autotune, gf, mesh
     from pyquake3d_gb300.ensemble import Ensemble, PackedOperator
     from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
     L_ = _lib.load()
@@ -471,6 +471,12 @@ def bench_batched(torch, dev, args, peaks):
     tabs = mesh.ensemble_tables(xg, Lkm * 1e3, Wkm * 1e3, B=B, seed=0, v_nuc=1e-3)
     K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
     P = PackedOperator(K64)
+    # launch shape of the tensor-core product (K slices, CTAs per SM) from the
+    # project's autotuner, before anything is timed
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    shape = autotune.tune_bf16x6(P, B)
+    tune_s = time.perf_counter() - t0
     res = {"workload": "batched ensemble: planar %dx%d km, N=%d, B=%d runs, per-run a-b, Dc, sigma_n, nucleation "
                        "patch from seed 0; RK stages = 7 x attempted steps, all runs" % (Lkm, Wkm, N, B)}
     out = {}
@@ -500,12 +506,12 @@ def bench_batched(torch, dev, args, peaks):
             # the tensor-core product alone, CUDA events over repeated launches
             st = torch.cuda.current_stream(dev).cuda_stream
             for _ in range(3):
-                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit, ens.tc_ctas,
                                           ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
             nl = 20
             s.record()
             for _ in range(nl):
-                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit, ens.tc_ctas,
                                           ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
             e.record()
             e.synchronize()
@@ -513,7 +519,10 @@ def bench_batched(torch, dev, args, peaks):
             Bp = ens.Bp
             op_bytes = P.data.numel()
             flops = 6 * 2.0 * (3 * N) * (2 * N) * Bp
-            out[prec]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit,
+            out[prec]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit, "ctas_per_sm": ens.tc_ctas,
+                                 "autotune": {"nsplit": shape["nsplit"], "ctas_per_sm": shape["ctas_per_sm"],
+                                              "tune_s": tune_s, "candidates": "nsplit 1..16 x CTAs per SM "
+                                              "(1, 2, 3) at 64 runs, then CTAs per SM at this run count"},
                                  "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": op_bytes / tg / 1e9,
                                               "peak": peaks["hbm_gbs"], "frac": op_bytes / tg / 1e9 / peaks["hbm_gbs"],
                                               "algorithmic_bytes": op_bytes,
@@ -538,10 +547,83 @@ def bench_batched(torch, dev, args, peaks):
                                 "ms_per_step": dt / max(1, c1.steps_done - c0.steps_done) * 1e3}
     out["ratio_bf16x6_vs_plain_fp64"] = out["bf16x6"]["rk_stages_per_s"] / plain
     out["ratio_fp32_vs_plain_fp64"] = out["fp32"]["rk_stages_per_s"] / plain
+    if args.acc_runs > 0:
+        out["accuracy_vs_fp64"] = batched_accuracy(torch, K64, K32, P, tabs[:args.acc_runs], args.acc_steps)
     res.update(out)
     del K64, K32, P
     torch.cuda.empty_cache()
     return res
+
+
+def batched_accuracy(torch, K64, K32, P, tabs, max_steps, every=5):
+    """Slip error of the mixed-precision ensembles against the FP64 batched
+    stepper (the reference arithmetic, FP64 operator) on the same runs, in
+    lockstep: each iteration runs as its two halves (pq3d_batch_iterate_begin /
+    _end) and between them every other ensemble takes the FP64 ensemble's
+    error norms (the hand-over row shards use for their reduced norms), so all
+    take the same accept/reject decisions and step sizes and reach the same
+    times; the differences are the arithmetic's alone.  Beside the mixed
+    products runs the FP64 stepper itself with each run's initial slip rates
+    perturbed by 1e-12 (relative, random sign): the floor set by the
+    sensitivity of the trajectories (nucleation amplifies any perturbation by
+    orders of magnitude).  Reported per variant: the accepted steps up to which
+    the normwise relative slip error of every run stays within 1e-5, and the
+    error at fixed step counts (null once a run's forced acceptance of a step
+    its own arithmetic would reject has made it non-finite)."""
+    import numpy as np
+    from pyquake3d_gb300.ensemble import Ensemble
+    B = tabs.shape[0]
+    pert = tabs.copy()
+    pert[:, :, 7] *= 1.0 + 1e-12 * np.random.default_rng(7).choice([-1.0, 1.0], size=pert[:, :, 7].shape)
+    kw = dict(mu=MU, Cs=3464.0, max_steps=max_steps)
+    runs = {"fp64": Ensemble(K64, tabs, precision="fp64", **kw),
+            "bf16x6": Ensemble(P, tabs, precision="bf16x6", **kw),
+            "fp32": Ensemble(K32, tabs, precision="fp32", **kw),
+            "fp64_perturbed_1e-12": Ensemble(K64, pert, precision="fp64", **kw)}
+    ref = runs["fp64"]
+    others = [k for k in runs if k != "fp64"]
+    marks = [m for m in (10, 25, 50, 100, 200, 400) if m <= max_steps]
+    out = {k: {"steps_within_1e-5": 0, "slip_rel_err_at_steps": {}, "max_slip_rate_rel_err_within": 0.0}
+           for k in others}
+    ok = {k: True for k in others}
+    done = False
+    for _ in range(40 * max_steps // every):
+        for _ in range(every):
+            for e in runs.values():
+                e.begin()
+            wr = ref.error_words()
+            for k in others:
+                runs[k].set_error_words(wr)
+            for e in runs.values():
+                e.end()
+        cr = ref.read_ctrl()
+        steps = min(c.steps for c in cr)
+        s_ref = torch.cat([ref.t["slip1"], ref.t["slip2"]], 1)
+        v_ref = torch.cat([ref.t["slipv1"], ref.t["slipv2"]], 1)
+        for k in others:
+            e = runs[k]
+            s = torch.cat([e.t["slip1"], e.t["slip2"]], 1)
+            v = torch.cat([e.t["slipv1"], e.t["slipv2"]], 1)
+            es = ((s - s_ref).norm(dim=1) / s_ref.norm(dim=1)).max().item()
+            ev = ((v - v_ref).norm(dim=1) / v_ref.norm(dim=1)).max().item()
+            O = out[k]
+            if ok[k] and es <= 1e-5:
+                O["steps_within_1e-5"] = steps
+                O["max_slip_rate_rel_err_within"] = max(O["max_slip_rate_rel_err_within"], ev)
+            else:
+                ok[k] = False
+            for m in marks:
+                if steps >= m and str(m) not in O["slip_rel_err_at_steps"]:
+                    O["slip_rel_err_at_steps"][str(m)] = es if es == es and es < float("inf") else None
+        if done:
+            break
+        done = not any(c.active for c in cr)
+    for k in others:
+        out[k]["failed_runs"] = int(sum(c.status != 0 for c in runs[k].read_ctrl()))
+    return {"runs": B, "accepted_steps": max_steps, "rk_stages_per_run": int(7 * max(c.attempts for c in cr)),
+            "simulated_time_s": max(c.time for c in cr), "bar": 1e-5, **out,
+            "method": "lockstep with the FP64 batched stepper (same step sizes and decisions: the FP64 error norms "
+                      "handed over between the halves of each iteration); checkpoints every %d iterations" % every}
 
 
 def bench_hmatrix(torch, dev, args, peaks):
@@ -796,6 +878,8 @@ def main():
     ap.add_argument("--nsplit", type=int, default=None)
     ap.add_argument("--graph-iters", type=int, default=25)
     ap.add_argument("--batch-iters", type=int, default=300)
+    ap.add_argument("--acc-runs", type=int, default=16, help="runs of the slip-accuracy check (0: skip)")
+    ap.add_argument("--acc-steps", type=int, default=200)
     ap.add_argument("--case", default=None, help="profiling case only (hs_assembly, hmat_product, tc_gemm)")
     args = ap.parse_args()
     if args.case:

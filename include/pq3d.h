@@ -242,7 +242,8 @@ typedef struct pq3d_batch_sim {
                               the K slices' tensor-memory accumulators, summed in float-float by the
                               stepper */
     int32_t nsplit;        /* K-slices of the operator product (>= 1) */
-    int32_t pad0;
+    int32_t tc_ctas;       /* BF16X6: CTAs per SM of the tensor-core product, 0 (= 2) or 1..3; the launch
+                              shape only, results do not depend on it */
     double *cand;          /* [B][N][4] candidate state */
     void *vop;             /* operator-product right-hand side of all runs, padded to Bp = B rounded up
                               to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], or for
@@ -253,7 +254,8 @@ typedef struct pq3d_batch_sim {
     pq3d_run_ctrl *ctrl;   /* [B] */
     double V0, Vpl, eta;
     int32_t fix_Tn;
-    int32_t pad1;
+    int32_t attempt64;     /* FP32, BF16X6, HMAT: 1 = Dormand-Prince stages in the reference FP64
+                              arithmetic (base unused, may be NULL), 0 = mixed precision */
     /* Receiver-row shard (FP64 and FP32 only): this process steps cells
      * [cell0, cell0 + N) of an N_total-cell mesh.  The per-cell arrays, cand
      * and rates hold the shard's N cells; K holds the shard's 3N rows of the
@@ -263,10 +265,10 @@ typedef struct pq3d_batch_sim {
      * means an unsharded simulation (N_total = N, cell0 = 0). */
     int64_t N_total;
     int64_t cell0;
-    /* Mixed precisions (FP32, BF16X6, HMAT): the cells' start-of-step
-     * constants of the mixed-precision Dormand-Prince attempt, FP32
-     * [PQ3D_BATCH_BASE_FIELDS][B][N], written by pq3d_batch_prepare and by
-     * the update of every accepted step.  NULL (unused) for FP64. */
+    /* Mixed precisions (FP32, BF16X6, HMAT with attempt64 = 0): the cells'
+     * start-of-step constants of the mixed-precision Dormand-Prince attempt,
+     * FP32 [PQ3D_BATCH_BASE_FIELDS][B][N], written by pq3d_batch_prepare and
+     * by the update of every accepted step.  NULL (unused) otherwise. */
     float *base;
 } pq3d_batch_sim;
 
@@ -281,9 +283,16 @@ int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpacked, void *
 /* Bytes of the packed right-hand side for B runs (BF16X6). */
 size_t pq3d_batch_rhs_bytes(int64_t N, int B);
 /* The tensor-core product alone: FP32 out[(s*Bp + n)*3N + m] (s < nsplit K
- * slices, Bp = B rounded up to 16) from the packed operator and right-hand side. */
-int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
-                           void *workspace, size_t workspace_bytes, void *stream);
+ * slices, Bp = B rounded up to 16) from the packed operator and right-hand
+ * side.  nsplit sets the order in which the slices' sums are added (and so
+ * the bits of the result); ctas_per_sm (0 = 2, else 1..3) is the launch shape
+ * only. */
+int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, int ctas_per_sm,
+                           float *out, void *workspace, size_t workspace_bytes, void *stream);
+/* The launch of that product for B runs on the current device: plan[0] = CTAs
+ * per SM actually launched for the requested ctas_per_sm (fewer where shared
+ * or tensor memory does not fit them), plan[1] = pipeline stages per CTA. */
+int pq3d_batch_gemm_bf16x6_plan(int B, int ctas_per_sm, int32_t *plan);
 
 /* Device workspace bytes of one batched iteration (GEMM split-K partials live in
  * sim->rates; this is what the tensor-core product needs besides). */

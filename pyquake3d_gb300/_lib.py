@@ -63,9 +63,9 @@ class BatchSim(ctypes.Structure):
         [(n, c_void_p) for n in ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2",
                                  "a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0",
                                  "rates")] + \
-        [("nsplit", ctypes.c_int32), ("pad0", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
+        [("nsplit", ctypes.c_int32), ("tc_ctas", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
          ("ctrl", c_void_p), ("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", ctypes.c_int32),
-         ("pad1", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64), ("base", c_void_p)]
+         ("attempt64", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64), ("base", c_void_p)]
 
 
 class HMat(ctypes.Structure):
@@ -112,7 +112,9 @@ _SIGS = {
     "pq3d_batch_operator_bytes": (c_size, [c_i64]),
     "pq3d_batch_pack_operator": (c_int, [c_void_p, c_i64, c_void_p, c_void_p]),
     "pq3d_batch_rhs_bytes": (c_size, [c_i64, c_int]),
-    "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size, c_void_p]),
+    "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_int, c_void_p, c_void_p, c_size,
+                                       c_void_p]),
+    "pq3d_batch_gemm_bf16x6_plan": (c_int, [c_int, c_int, c_void_p]),
     "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
     "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_void_p, c_size, c_void_p]),
     "pq3d_hmat_aca": (c_int, [c_void_p, c_i64, c_void_p, c_int, c_void_p, c_void_p, c_dbl, c_dbl, c_dbl, c_int,

@@ -42,12 +42,14 @@ __device__ __forceinline__ void vprime(const pq3d_batch_sim &S, int64_t idx, dou
 
 // 3-piece BF16 split of an FP32 value: x = p0 + p1 + p2 exactly (each
 // residual is exact in FP32 and has 8 fewer significant bits than the last)
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
+// x = p0 + p1 + p2 to ~2^-26 relative (each piece rounds the remainder of the
+// previous ones to BF16), the remainders formed exactly in FP64
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
 {
-    p0 = __float2bfloat16_rn(x);
-    const float r1 = x - __bfloat162float(p0);
-    p1 = __float2bfloat16_rn(r1);
-    p2 = __float2bfloat16_rn(r1 - __bfloat162float(p1));
+    p0 = __double2bfloat16(x);
+    const double r1 = x - (double)__bfloat162float(p0);
+    p1 = __double2bfloat16(r1);
+    p2 = __double2bfloat16(r1 - (double)__bfloat162float(p1));
 }
 
 // i: local cell of the shard; v' goes to the mesh-wide position cell0 + i
@@ -66,8 +68,8 @@ __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_
         __nv_bfloat16 *P = (__nv_bfloat16 *)S.vop + (k / tc::kBlockK) * tc::kPieces * img +
                            tc::image_offset(r, (int)(k % tc::kBlockK));
         __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-        split3((float)v1, a0, a1, a2);   // v' to 24 bits, like the operator's pieces
-        split3((float)v2, b0, b1, b2);
+        split3(v1, a0, a1, a2);   // v' to ~26 bits, like the operator's pieces
+        split3(v2, b0, b1, b2);
         __nv_bfloat162 q;
         q.x = a0; q.y = b0; reinterpret_cast<__nv_bfloat162 *>(P)[0] = q;
         q.x = a1; q.y = b1; reinterpret_cast<__nv_bfloat162 *>(P + img)[0] = q;
@@ -260,9 +262,16 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
         } else {
             double q0 = 0.0, q1 = 0.0, q2 = 0.0;
-            for (int s = 0; s < S.nsplit; ++s) {
-                const double *p = S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
-                q0 += p[0]; q1 += p[1]; q2 += p[2];
+            if (S.precision == PQ3D_BATCH_BF16X6) {   // FP32 K-slice partials, added in FP64
+                for (int s = 0; s < S.nsplit; ++s) {
+                    const float *p = (const float *)S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
+                    q0 += (double)p[0]; q1 += (double)p[1]; q2 += (double)p[2];
+                }
+            } else {
+                for (int s = 0; s < S.nsplit; ++s) {
+                    const double *p = S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
+                    q0 += p[0]; q1 += p[1]; q2 += p[2];
+                }
             }
             const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
             const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
@@ -385,6 +394,11 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     write_vop(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
 }
 
+// The Dormand-Prince attempt and update in mixed precision (FP32 stages on the
+// FP64 state), or in the reference FP64 arithmetic: always for the FP64
+// product, on request (attempt64) for the others.
+static bool mixed_attempt(const pq3d_batch_sim &S) { return S.precision != PQ3D_BATCH_FP64 && !S.attempt64; }
+
 static int check_sim(const pq3d_batch_sim *S)
 {
     PQ3D_REQUIRE(S && S->N > 0 && S->B > 0 && S->B <= 1024 && S->ctrl && S->K && S->vop && S->rates && S->cand,
@@ -393,9 +407,11 @@ static int check_sim(const pq3d_batch_sim *S)
     if (S->precision == PQ3D_BATCH_HMAT)
         PQ3D_REQUIRE(((const pq3d_hmat *)S->K)->N == S->N, "pq3d_batch: H-matrix size differs from N");
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
+    PQ3D_REQUIRE(S->tc_ctas >= 0 && S->tc_ctas <= 3, "pq3d_batch: tc_ctas must be 0 (default) or 1..3");
     PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
     if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
-    if (S->precision != PQ3D_BATCH_FP64)
+    PQ3D_REQUIRE(S->attempt64 == 0 || S->attempt64 == 1, "pq3d_batch: attempt64 must be 0 or 1");
+    if (mixed_attempt(*S))
         PQ3D_REQUIRE(S->base != nullptr && aligned16(S->base), "pq3d_batch: mixed precisions need the base array");
     PQ3D_REQUIRE(S->N_total >= 0 && S->cell0 >= 0, "pq3d_batch: bad shard");
     if (S->N_total > 0 && (S->N_total != S->N || S->cell0 != 0)) {
@@ -452,8 +468,8 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
         dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
         gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
-        rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, (float *)S.rates, workspace,
-                                   workspace_bytes, st);
+        rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.tc_ctas, (float *)S.rates,
+                                   workspace, workspace_bytes, st);
         if (rc) return rc;
     } else {
         // the H-matrix product needs no padding runs: the first B rows only
@@ -466,8 +482,8 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
     PQ3D_CUDA_TRY(cudaGetLastError());
     // 2. attempt (FP64 arm: the reference arithmetic; mixed arms: dp_attempt_mixed)
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
-    if (S.precision == PQ3D_BATCH_FP64) attempt_kernel<false><<<grid, 256, 0, st>>>(S);
-    else attempt_kernel<true><<<grid, 256, 0, st>>>(S);
+    if (mixed_attempt(S)) attempt_kernel<true><<<grid, 256, 0, st>>>(S);
+    else attempt_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }
@@ -482,8 +498,8 @@ extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
     // 3-4. decide, update
     decide_kernel<<<(S.B + 127) / 128, 128, 0, st>>>(S.ctrl, S.B);
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
-    if (S.precision == PQ3D_BATCH_FP64) update_kernel<false><<<grid, 256, 0, st>>>(S);
-    else update_kernel<true><<<grid, 256, 0, st>>>(S);
+    if (mixed_attempt(S)) update_kernel<true><<<grid, 256, 0, st>>>(S);
+    else update_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

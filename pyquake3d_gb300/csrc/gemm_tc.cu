@@ -6,10 +6,17 @@
 // Precision ("BF16x6"): the FP64 operator and the FP64 right-hand side are
 // split into three BF16 pieces each (x = x0 + x1 + x2, 24 significant bits);
 // the six cross products x_i * y_j with i + j <= 2 are accumulated in FP32 in
-// tensor memory.  Their sum carries the operands to ~2^-24 (the FP32 operator
-// copy's own rounding), while two-piece "BF16x3" carries them to ~2^-16.
-// Slices of the reduction (split-K) are written as the FP32 tensor-memory
-// accumulators and added in float-float by the consumer.
+// tensor memory.  Their sum carries the operands to ~2^-26 (the dropped
+// products are x_1 y_2, x_2 y_1, x_2 y_2), while two-piece "BF16x3" carries
+// them to ~2^-16.  The leading product x_0 y_0 and the five corrections go to
+// two accumulators, added (round to nearest) when drained: the tensor-memory
+// accumulation loses more than an FP32 FMA chain would when small terms are
+// added to a large accumulator, and the corrections are 2^-8 of the leading
+// product and less.  (On the N = 10,000 planar operator with a nucleation
+// patch, one accumulator for all six products gave a 2.7e-6 normwise error,
+// the leading product alone 7.4e-7, FP32 FMA 3.7e-7, the pieces' exact sum
+// 1.6e-8.)  Slices of the reduction (split-K) are written as FP32 and added
+// in float-float by the consumer.
 //
 // Data path (one CTA = one 128-row tile of K x one K slice, all runs):
 //   * the operator pieces are packed once, after assembly, into ready-made
@@ -20,8 +27,8 @@
 //     copies (cp.async.bulk, completion on an mbarrier), no tensor map.
 //   * warp 0 lane 0 produces stages, warp 1 lane 0 issues 12 tcgen05.mma
 //     (M=128, N=B, K=16; 6 products x 2 K-steps) per stage and frees the stage
-//     with tcgen05.commit; all 4 warps drain the FP32 accumulator from tensor
-//     memory (tcgen05.ld 32x32b) and store it (FP32).
+//     with tcgen05.commit; all 4 warps drain the two FP32 accumulators from
+//     tensor memory (tcgen05.ld 32x32b) and store their sum (FP32).
 //   * every mbarrier wait is bounded; a wait that gives up records an error
 //     word in the workspace, the kernel still waits (bounded) for its own
 //     tensor-core work, frees its tensor memory and returns.
@@ -156,7 +163,7 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
     uint8_t *bars = smem + (size_t)stages * stage_bytes;
     const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * stages, done = full0 + 16 * stages;
     uint32_t *tmem_slot = (uint32_t *)(bars + 16 * stages + 8);
-    const uint32_t ncols = tmem_cols(Bp);
+    const uint32_t ncols = tmem_cols(Bp);   // per accumulator; two accumulators
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < stages; ++s) {
@@ -168,7 +175,7 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(ncols)
+                     "r"(2 * ncols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -203,7 +210,10 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
                 for (int p = 0; p < 6; ++p) {
                     const uint64_t ad = smem_desc(sa + kPairA[p] * kImageA + ks * 256, 128, 512);
                     const uint64_t bd = smem_desc(sb + kPairB[p] * b_img + ks * 256, 128, 512);
-                    mma_bf16(tmem, ad, bd, idesc, (it > 0 || ks > 0 || p > 0) ? 1u : 0u);
+                    // leading product into the first accumulator, the five
+                    // corrections (2^-8 of it and less) into the second
+                    const uint32_t acc = it > 0 || ks > 0 || p > 1;
+                    mma_bf16(p == 0 ? tmem : tmem + ncols, ad, bd, idesc, p == 0 ? (uint32_t)(it > 0 || ks > 0) : acc);
                 }
             }
             mma_commit(empty0 + 8 * st);
@@ -219,12 +229,13 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
     const int64_t m = mt * kTileM + 32 * warp + lane;
     if (got) {
         for (int c0 = 0; c0 < Bp; c0 += 16) {
-            uint32_t r[16];
+            uint32_t r[16], q[16];
             tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, r);
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + ncols + (uint32_t)c0, q);
             if (m < M) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    out[((int64_t)slice * Bp + c0 + j) * M + m] = __uint_as_float(r[j]);
+                    out[((int64_t)slice * Bp + c0 + j) * M + m] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
             }
         }
     } else if (lane == 0) {
@@ -232,7 +243,8 @@ gemm_bf16x6_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ V
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * ncols) : "memory");
 }
 
 // FP64 operator -> three BF16 pieces in the tile-image layout.
@@ -261,21 +273,13 @@ size_t gemm_bf16x6_workspace_bytes(int64_t, int, int) { return 256; }
 
 struct Cfg {
     int device = -1;
-    int max_smem = 0;      // per block (opt-in)
-    int sm_smem = 0;       // per SM
-    int ctas_per_sm = 2;   // PQ3D_TC_CTAS_PER_SM (1, 2 or 3)
+    int max_smem = 0;   // per block (opt-in)
+    int sm_smem = 0;    // per SM
 };
 static thread_local Cfg g_cfg;
 
-int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, float *out, void *workspace,
-                size_t workspace_bytes, cudaStream_t stream)
+static int device_cfg()
 {
-    PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x6: null pointer");
-    PQ3D_REQUIRE(workspace_bytes >= 256 && aligned16(workspace), "gemm_bf16x6: workspace must be >= 256 bytes");
-    PQ3D_REQUIRE(Bp >= 16 && Bp <= 256 && Bp % 16 == 0, "gemm_bf16x6: padded run count must be 16..256, multiple of 16");
-    PQ3D_REQUIRE(aligned16(Kpacked) && aligned16(Vpacked), "gemm_bf16x6: operands must be 16-byte aligned");
-    const int64_t KB = k_blocks(N);
-    PQ3D_REQUIRE(nsplit >= 1 && nsplit <= KB, "gemm_bf16x6: nsplit must be in [1, %lld]", (long long)KB);
     int dev;
     PQ3D_CUDA_TRY(cudaGetDevice(&dev));
     if (g_cfg.device != dev) {
@@ -286,23 +290,50 @@ int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int
         g_cfg.device = dev;
         g_cfg.max_smem = maxs;
         g_cfg.sm_smem = sms;
-        const char *env = getenv("PQ3D_TC_CTAS_PER_SM");
-        const int c = env ? atoi(env) : 2;
-        g_cfg.ctas_per_sm = c < 1 ? 1 : (c > 3 ? 3 : c);
     }
-    // Several CTAs per SM (default 2) while each still gets a pipeline of at
-    // least 2 stages and its tensor-memory columns: one CTA streams the
-    // operator while another fills its pipeline or drains its accumulator,
-    // and the last wave is finer; else one CTA with up to 6 stages.
+    return PQ3D_OK;
+}
+
+// Launch plan for `ctas_per_sm` requested CTAs per SM (0 = 2): the most CTAs
+// per SM, not above the request, for which each CTA still gets a pipeline of
+// at least 2 stages and its tensor-memory columns, with up to 6 stages each.
+// Several CTAs per SM let one stream the operator while another fills its
+// pipeline or drains its accumulator, and make the last wave finer.
+int plan_bf16x6(int Bp, int ctas_per_sm, int *ctas, int *stages)
+{
+    int rc = device_cfg();
+    if (rc) return rc;
+    const int want = ctas_per_sm == 0 ? 2 : ctas_per_sm;
     const size_t stage_bytes = (size_t)kPieces * (kImageA + (size_t)Bp * kBlockK * 2);
-    int stages = 0;
-    for (int c = g_cfg.ctas_per_sm; c >= 1 && stages == 0; --c) {
+    *ctas = 0;
+    *stages = 0;
+    for (int c = want; c >= 1 && *stages == 0; --c) {
         int s = (int)((g_cfg.sm_smem / c - 1024 - 16) / (stage_bytes + 16));
         if (s > 6) s = 6;
         if (s > (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16))) s = (int)((g_cfg.max_smem - 1024) / (stage_bytes + 16));
-        if (s >= 2 && c * (int)tmem_cols(Bp) <= 512) stages = s;
+        if (s >= 2 && c * 2 * (int)tmem_cols(Bp) <= 512) {
+            *stages = s;
+            *ctas = c;
+        }
     }
-    PQ3D_REQUIRE(stages >= 2, "gemm_bf16x6: not enough shared memory for B=%d", Bp);
+    PQ3D_REQUIRE(*stages >= 2, "gemm_bf16x6: not enough shared memory for B=%d", Bp);
+    return PQ3D_OK;
+}
+
+int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, int ctas_per_sm, float *out,
+                void *workspace, size_t workspace_bytes, cudaStream_t stream)
+{
+    PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x6: null pointer");
+    PQ3D_REQUIRE(workspace_bytes >= 256 && aligned16(workspace), "gemm_bf16x6: workspace must be >= 256 bytes");
+    PQ3D_REQUIRE(Bp >= 16 && Bp <= 256 && Bp % 16 == 0, "gemm_bf16x6: padded run count must be 16..256, multiple of 16");
+    PQ3D_REQUIRE(aligned16(Kpacked) && aligned16(Vpacked), "gemm_bf16x6: operands must be 16-byte aligned");
+    PQ3D_REQUIRE(ctas_per_sm >= 0 && ctas_per_sm <= 3, "gemm_bf16x6: ctas_per_sm must be 0 (default) or 1..3");
+    const int64_t KB = k_blocks(N);
+    PQ3D_REQUIRE(nsplit >= 1 && nsplit <= KB, "gemm_bf16x6: nsplit must be in [1, %lld]", (long long)KB);
+    int ctas, stages;
+    int rc = plan_bf16x6(Bp, ctas_per_sm, &ctas, &stages);
+    if (rc) return rc;
+    const size_t stage_bytes = (size_t)kPieces * (kImageA + (size_t)Bp * kBlockK * 2);
     const size_t smem = (size_t)stages * stage_bytes + 16 * (size_t)stages + 16;
     dim3 grid((unsigned)m_tiles(N), (unsigned)nsplit);
     gemm_bf16x6_kernel<<<grid, 128, smem, stream>>>((const uint8_t *)Kpacked, (const uint8_t *)Vpacked, N, Bp, nsplit,
@@ -336,9 +367,23 @@ extern "C" int pq3d_batch_pack_operator(const double *K64, int64_t N, void *Kpac
 }
 
 extern "C" int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit,
-                                      float *out, void *workspace, size_t workspace_bytes, void *stream)
+                                      int ctas_per_sm, float *out, void *workspace, size_t workspace_bytes,
+                                      void *stream)
 {
     clear_error();
-    return tc::gemm_bf16x6(Kpacked, Vpacked, N, (B + 15) / 16 * 16, nsplit, out, workspace, workspace_bytes,
-                           (cudaStream_t)stream);
+    return tc::gemm_bf16x6(Kpacked, Vpacked, N, (B + 15) / 16 * 16, nsplit, ctas_per_sm, out, workspace,
+                           workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int pq3d_batch_gemm_bf16x6_plan(int B, int ctas_per_sm, int32_t *plan)
+{
+    clear_error();
+    PQ3D_REQUIRE(plan && B >= 1 && B <= 256, "pq3d_batch_gemm_bf16x6_plan: bad arguments");
+    PQ3D_REQUIRE(ctas_per_sm >= 0 && ctas_per_sm <= 3, "pq3d_batch_gemm_bf16x6_plan: ctas_per_sm must be 0..3");
+    int ctas, stages;
+    int rc = tc::plan_bf16x6((B + 15) / 16 * 16, ctas_per_sm, &ctas, &stages);
+    if (rc) return rc;
+    plan[0] = ctas;
+    plan[1] = stages;
+    return PQ3D_OK;
 }

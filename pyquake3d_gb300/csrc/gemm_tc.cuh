@@ -36,9 +36,13 @@ size_t gemm_bf16x6_workspace_bytes(int64_t N, int Bp, int nsplit);
 
 // out[(s * Bp + n) * 3N + m] = sum over the columns k of slice s of K[m][k] * V[n][k],
 // from the packed operator and right-hand side; FP32 accumulation in tensor
-// memory, FP32 output (the accumulator).  Returns a PQ3D status.
-int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, float *out,
+// memory, FP32 output (the accumulator); ctas_per_sm (0 = 2, else 1..3) CTAs
+// resident per SM, fewer where shared or tensor memory does not fit them (the
+// launch shape only: the result does not depend on it).  Returns a PQ3D status.
+int gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, int ctas_per_sm, float *out,
                 void *workspace, size_t workspace_bytes, cudaStream_t stream);
+// CTAs per SM and pipeline stages that gemm_bf16x6 launches with.
+int plan_bf16x6(int Bp, int ctas_per_sm, int *ctas, int *stages);
 
 }  // namespace tc
 }  // namespace pq3d

@@ -12,9 +12,19 @@ Precisions of the traction product (``precision=``):
   "fp32"   FP32 operator copy on CUDA cores ("plain FP32")
   "bf16x6" the operator and v' each split into three BF16 pieces, the six
            leading cross products on the tcgen05 tensor cores with FP32
-           accumulation in tensor memory; K slices added in FP64
+           accumulation in tensor memory; K slices added in float-float;
+           launch shape (K slices, CTAs per SM) from :mod:`.autotune`
   "hmat"   an :class:`~pyquake3d_gb300.hmatrix.HMatrix` (large meshes)
 Time, slip, the state and the RK error norm stay FP64 in every mode.
+
+The Dormand-Prince attempt (``attempt=``): "mixed" (default for the mixed
+products) runs the seven right-hand sides in FP32 on the FP64 start state
+with float-float exponent arguments; "fp64" runs them in the reference FP64
+arithmetic (always for precision "fp64").  The FP32 stages add ~1e-7 of each
+step's increment; during nucleation the slip rate's exponential dependence
+on the traction amplifies that, so runs that must track the FP64 trajectory
+closely over many steps take attempt="fp64" (the product keeps its
+precision).
 """
 from __future__ import annotations
 
@@ -23,7 +33,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, autotune
 from .QDsim_gpu import initial_state
 
 PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6,
@@ -34,16 +44,6 @@ PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", 
 
 def padded_runs(B: int) -> int:
     return (B + 15) // 16 * 16
-
-
-def auto_nsplit(N: int, device) -> int:
-    """K slices of the tensor-core product: about 7.5 waves of one-CTA-per-SM
-    tiles (3N/128 row tiles x slices), at least 1, at most 16 and at most the
-    number of 32-column blocks (N = 10,000 on 152 SMs -> 5, measured best)."""
-    sms = torch.cuda.get_device_properties(device).multi_processor_count
-    tiles = (3 * N + 127) // 128
-    ns = int(round(7.5 * sms / tiles))
-    return max(1, min(16, ns, (2 * N + 31) // 32))
 
 
 class PackedOperator:
@@ -71,11 +71,14 @@ class Ensemble:
     N_total-cell mesh ("fp64" / "fp32"); K is then the shard's (3N, 2 N_total)
     row block and :mod:`pyquake3d_gb300.shards` drives the iterations."""
 
-    def __init__(self, K, tables, *, mu, Cs, V0=1e-6, Vpl=1e-9, precision="bf16x6", nsplit=None, dttry=1e-3,
-                 max_steps=2 ** 62, t_end=float("inf"), fix_Tn=False, shard=None):
+    def __init__(self, K, tables, *, mu, Cs, V0=1e-6, Vpl=1e-9, precision="bf16x6", attempt="mixed", nsplit=None,
+                 tc_ctas=None, dttry=1e-3, max_steps=2 ** 62, t_end=float("inf"), fix_Tn=False, shard=None):
         L = _lib.load()
         self.precision = precision
         prec = PRECISIONS[precision]
+        if attempt not in ("mixed", "fp64"):
+            raise ValueError("attempt must be 'mixed' or 'fp64'")
+        self.attempt = "fp64" if precision == "fp64" else attempt
         tables = np.asarray(tables, dtype=np.float64)
         B, N = tables.shape[0], tables.shape[1]
         self.B, self.N, self.Bp = B, N, padded_runs(B)
@@ -93,8 +96,10 @@ class Ensemble:
         elif precision == "bf16x6":
             assert isinstance(K, PackedOperator) and K.N == N
             kop = K.data
-            if nsplit is None:
-                nsplit = auto_nsplit(N, dev)
+            if nsplit is None or tc_ctas is None:
+                shape = autotune.tune_bf16x6(K, B)
+                nsplit = shape["nsplit"] if nsplit is None else nsplit
+                tc_ctas = shape["ctas_per_sm"] if tc_ctas is None else tc_ctas
         else:
             assert isinstance(K, torch.Tensor) and K.shape == (3 * N, 2 * Nt) and K.is_contiguous()
             assert K.dtype == (torch.float64 if precision == "fp64" else torch.float32)
@@ -102,6 +107,7 @@ class Ensemble:
             nsplit = 1
         self.K = kop
         self.nsplit = int(nsplit)
+        self.tc_ctas = int(tc_ctas or 0)
         inits = [initial_state(t, V0, Vpl) for t in tables]
         f64 = dict(dtype=torch.float64, device=dev)
         self.t = {}
@@ -111,7 +117,7 @@ class Ensemble:
         self.t["sin_rake0"] = torch.sin(torch.as_tensor(np.stack([s["rake0"] for s in inits]), **f64)).contiguous()
         self.t["rates"] = torch.zeros(self.nsplit * self.Bp * 3 * N, **f64)
         self.t["cand"] = torch.zeros(B * N * 4, **f64)
-        if precision != "fp64":   # start-of-step constants of the mixed-precision attempt
+        if self.attempt == "mixed":   # start-of-step constants of the mixed-precision attempt
             self.t["base"] = torch.zeros(_lib.PQ3D_BATCH_BASE_FIELDS * B * N, dtype=torch.float32, device=dev)
         if precision in ("fp64", "hmat"):
             self.vop = torch.zeros(self.Bp * 2 * Nt, **f64)
@@ -121,13 +127,14 @@ class Ensemble:
             self.vop = torch.zeros(L.pq3d_batch_rhs_bytes(N, B), dtype=torch.uint8, device=dev)
         self.ctrl_t = torch.zeros(B * ctypes.sizeof(_lib.RunCtrl), dtype=torch.uint8, device=dev)
         S = _lib.BatchSim()
-        S.N, S.B, S.precision, S.nsplit = N, B, prec, self.nsplit
+        S.N, S.B, S.precision, S.nsplit, S.tc_ctas = N, B, prec, self.nsplit, self.tc_ctas
         for k in STATE + PARAMS + ("rates", "cand"):
             setattr(S, k, self.t[k].data_ptr())
         S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
         S.base = self.t["base"].data_ptr() if "base" in self.t else None
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
+        S.attempt64 = int(self.attempt == "fp64" and precision != "fp64")
         if shard is not None:
             S.N_total, S.cell0 = Nt, self.cell0
         self.S = S

@@ -57,7 +57,7 @@ def test_tensor_core_product_matches_fp64(cuda, N, B, nsplit):
     ens = Ensemble(PackedOperator(K), tabs, mu=MU, Cs=CS, precision="bf16x6", nsplit=nsplit)
     L = _lib.load()
     st = torch.cuda.current_stream().cuda_stream
-    _lib.check(L.pq3d_batch_gemm_bf16x6(ens.K.data_ptr(), ens.vop.data_ptr(), N, B, nsplit,
+    _lib.check(L.pq3d_batch_gemm_bf16x6(ens.K.data_ptr(), ens.vop.data_ptr(), N, B, nsplit, ens.tc_ctas,
                                         ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st))
     torch.cuda.synchronize()
     assert ens.error_word() == 0
@@ -68,6 +68,43 @@ def test_tensor_core_product_matches_fp64(cuda, N, B, nsplit):
     got = _rates(ens)
     for r in range(B):
         assert normwise_rel(ref[r], got[r]) < 5e-6, r
+
+
+def test_autotuned_launch_shape_and_ctas_do_not_change_bits(cuda):
+    """The autotuner returns a valid launch shape, caches it per mesh size
+    (nsplit) and per run count (CTAs per SM), and the CTA count is the launch
+    shape only: the product's bits are the same for 1, 2 and 3 CTAs per SM."""
+    from pyquake3d_gb300 import autotune
+    autotune.clear()
+    N, B = 600, 20
+    rng = np.random.default_rng(5)
+    K = torch.as_tensor(rng.standard_normal((3 * N, 2 * N)), device=cuda)
+    P = PackedOperator(K)
+    shape = autotune.tune_bf16x6(P, B)
+    assert shape["tuned"] and 1 <= shape["nsplit"] <= 16 and shape["ctas_per_sm"] in (1, 2, 3)
+    again = autotune.tune_bf16x6(P, 30)      # same padded width (32)
+    assert not again["tuned"] and again["nsplit"] == shape["nsplit"]
+    wide = autotune.tune_bf16x6(P, 200)      # another width: same nsplit, its own CTA count
+    assert wide["nsplit"] == shape["nsplit"]
+    tabs = np.zeros((B, N, 10))
+    tabs[:, :, 1] = 0.01; tabs[:, :, 2] = 0.015; tabs[:, :, 3] = 0.1; tabs[:, :, 4] = 0.6; tabs[:, :, 6] = 30.0
+    tabs[:, :, 7] = 10 ** rng.uniform(-12, -1, size=(B, N))
+    ens = Ensemble(P, tabs, mu=MU, Cs=CS, precision="bf16x6")
+    assert (ens.nsplit, ens.tc_ctas) == (shape["nsplit"], shape["ctas_per_sm"])
+    L = _lib.load()
+    st = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for c in (1, 2, 3):
+        ens.t["rates"].zero_()
+        _lib.check(L.pq3d_batch_gemm_bf16x6(ens.K.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit, c,
+                                            ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st))
+        outs.append(ens.t["rates"].clone())
+    torch.cuda.synchronize()
+    assert ens.error_word() == 0
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+    plan = np.zeros(2, dtype=np.int32)
+    _lib.check(L.pq3d_batch_gemm_bf16x6_plan(256, 3, plan.ctypes.data))
+    assert plan[0] in (1, 2) and plan[1] >= 2     # 3 CTAs of 256 runs do not fit tensor memory
 
 
 def test_batched_fp64_matches_single_simulation(cuda, golden):
@@ -101,6 +138,24 @@ def test_bf16x6_traction_rates_and_early_trajectory(cuda, golden):
     b.iterate(150)
     for r in range(4):
         assert normwise_rel(a.t["slip1"][r].cpu().numpy(), b.t["slip1"][r].cpu().numpy()) < 1e-5, r
+    assert b.error_word() == 0
+
+
+def test_bf16x6_product_with_fp64_attempt(cuda, golden):
+    """attempt="fp64": the tensor-core product with the reference FP64
+    Dormand-Prince arithmetic (no start-of-step constants); over the first 30
+    accepted steps slip within 1e-5 of the FP64 batched stepper, like the
+    mixed attempt."""
+    g, K = _golden(golden, cuda)
+    tabs = _tables(g, 4, seed=1)
+    a = Ensemble(K, tabs, mu=float(g["mu"]), Cs=CS, precision="fp64", max_steps=30)
+    b = Ensemble(PackedOperator(K), tabs, mu=float(g["mu"]), Cs=CS, precision="bf16x6", attempt="fp64", max_steps=30)
+    assert "base" not in b.t and b.S.attempt64 == 1
+    a.iterate(150)
+    b.iterate(150)
+    for r in range(4):
+        assert normwise_rel(a.t["slip1"][r].cpu().numpy(), b.t["slip1"][r].cpu().numpy()) < 1e-5, r
+    assert all(c.steps == 30 and c.status == 0 for c in b.read_ctrl())
     assert b.error_word() == 0
 
 
