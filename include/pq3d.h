@@ -193,11 +193,13 @@ typedef struct pq3d_step_ctrl {
  * each step.  h_force (device, nsteps doubles, normally NULL) replays a
  * prescribed step sequence: step s takes h_force[s] in one attempt, whatever
  * its error (used to compare arithmetic precisions on identical steps; the
- * reference has no such mode).  One cooperative persistent kernel does, per accepted step, the
- * traction product, the retry loop of Dormand-Prince attempts with the
- * max-relative error norm, and the state update (src/QDsim_gpu.py:942-1027,
- * 1128-1262).  Asynchronous on `stream`: the return value reports the launch;
- * the outcome of the steps is ctrl->status (read it after the stream). */
+ * reference has no such mode).  Per accepted step two launches are queued:
+ * the traction product, then one cooperative kernel with the retry loop of
+ * Dormand-Prince attempts (max-relative error norm) and the state update
+ * (src/QDsim_gpu.py:942-1027, 1128-1262); dt, time and the attempt count
+ * carry over in ctrl.  Asynchronous on `stream`: the return value reports the
+ * launches; the outcome of the steps is ctrl->status (read it after the
+ * stream; after a failed step the remaining launches return at once). */
 int pq3d_dense_step(const pq3d_dense_sim *sim, int nsteps, double *h_hist, double *t_hist,
                     const double *h_force, void *stream);
 
