@@ -154,11 +154,12 @@ constexpr int kMaxDepth = 64;   // tridiagonal unknowns per cell (the reference 
 // matrix (n each; M = dt * this + I), then the scalars below
 enum DilaScalar { D_BC0, D_BCN, D_G, D_T1, D_T2, D_TG, D_DP, D_NSCAL };
 
-// One implicit step for every cell of this thread (called by all threads of
-// every block with the same h): the Thomas factorisation of M is formed once
+// One implicit step for the cells [cell0, cell1) of this block (called by all
+// threads of every block with the same h): the Thomas factorisation of M is formed once
 // per block in shared memory (M is diagonally dominant by rows, so no
 // pivoting is needed; the reference factorises with partial pivoting).
-__device__ __noinline__ void dilatancy_step(const pq3d_dense_sim &S, double h, double *cp, double *inv)
+__device__ __noinline__ void dilatancy_step(const pq3d_dense_sim &S, double h, double *cp, double *inv, int64_t cell0,
+                                            int64_t cell1)
 {
     const int n = S.ndepth;
     const double *lo = S.dila, *di = lo + n, *up = di + n, *sc = up + n;
@@ -174,8 +175,7 @@ __device__ __noinline__ void dilatancy_step(const pq3d_dense_sim &S, double h, d
     }
     __syncthreads();
     const int64_t N = S.N;
-    const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += gsz) {
+    for (int64_t i = cell0 + threadIdx.x; i < cell1; i += blockDim.x) {
         const double theta = S.dc[i] / S.V0 * exp((S.state[i] - S.f0[i]) / S.b[i]);
         const double dthetadt = 1.0 - S.slipv[i] * theta / S.dc[i];
         const double g = -sc[D_G] / theta * dthetadt;
@@ -254,13 +254,15 @@ __global__ void __launch_bounds__(256) dense_attempt_kernel(pq3d_dense_sim S, in
     const double dttry = *(volatile double *)&C->dttry, time = *(volatile double *)&C->time;
     int64_t attempt = *(volatile int64_t *)&C->attempts;      // rotates the error slots
     const int64_t N = S.N;
-    const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
-    const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     unsigned *bc = &C->bar_count, *bg = &C->bar_gen;
     const unsigned nb = gridDim.x;
     double2 *vp = (double2 *)S.vprime;
     float4 *vs = (float4 *)S.vprime;
+    // cells of this block: a contiguous share of N / gridDim, so that every SM
+    // gets cells (N is often below the grid's thread count)
+    const int64_t chunk = (N + nb - 1) / nb;
+    const int64_t cell0 = (int64_t)blockIdx.x * chunk, cell1 = cell0 + chunk < N ? cell0 + chunk : N;
     if (lead) C->maxv_bits = 0ull;   // the update's atomicMax comes after at least one grid barrier
 
     // (2) attempts until one is accepted
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(256) dense_attempt_kernel(pq3d_dense_sim S, in
     for (;;) {
         const int slot = (int)(attempt % 3);
         double m1 = 0.0, m2 = 0.0;
-        for (int64_t i = gtid; i < N; i += gsz) {
+        for (int64_t i = cell0 + threadIdx.x; i < cell1; i += blockDim.x) {
             const Cell c{S.a[i], S.b[i], S.dc[i], S.f0[i], S.shear_loading[i], S.slipv[i],
                          S.rates[3 * i], S.rates[3 * i + 1], S.rates[3 * i + 2],
                          S.P ? S.P[i] : 0.0, S.dPdt ? S.dPdt[i] : 0.0};
@@ -314,7 +316,7 @@ __global__ void __launch_bounds__(256) dense_attempt_kernel(pq3d_dense_sim S, in
 
     // (3) state update (src/QDsim_gpu.py:994-1027)
     double vmax = 0.0;
-    for (int64_t i = gtid; i < N; i += gsz) {
+    for (int64_t i = cell0 + threadIdx.x; i < cell1; i += blockDim.x) {
         const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[i];
         const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w, a = S.a[i];
         S.Tno[i] = Tno; S.Tt1o[i] = T1; S.Tt2o[i] = T2; S.state[i] = st;
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(256) dense_attempt_kernel(pq3d_dense_sim S, in
     if (threadIdx.x == 0) atomicMax((unsigned long long *)&C->maxv_bits, bv);
     // (3b) pore-pressure diffusion of every cell with the new state and
     // slip rate (src/QDsim_gpu.py:628-671, after the update 1119-1120)
-    if (S.Parr) dilatancy_step(S, h, dil_cp, dil_inv);
+    if (S.Parr) dilatancy_step(S, h, dil_cp, dil_inv, cell0, cell1);
     if (!grid_barrier(bc, bg, nb)) { if (threadIdx.x == 0) C->status = PQ3D_ERR_TIMEOUT; return; }
     if (lead) {
         if (h_hist) h_hist[step] = h;
