@@ -134,49 +134,65 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const double2 *__restrict
     }
 }
 
-// FP32: CTA tile 128 rows x 64 runs, K chunks of 32 through shared memory,
-// FP32 FMAs with the partial sums moved to FP64 every 256 columns.  N
-// receivers of the shard (3N rows), Nt sources of the mesh (2 Nt columns).
+// FP32: CTA tile 128 rows x 64 runs, K chunks of 32 through shared memory
+// (the next chunk is loaded into registers while the current one is used),
+// FP32 FMAs with the partial sums moved to FP64 every 256 columns; the FP64
+// sums live in dynamic shared memory (64 KB per CTA), which keeps the kernel
+// at 2 CTAs per SM.  N receivers of the shard (3N rows), Nt sources of the
+// mesh (2 Nt columns).
 constexpr int kF32Rows = 128, kF32Runs = 64, kF32K = 32;
+constexpr int kF32Smem = 32 * 256 * (int)sizeof(double);
 
-__global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__ K, const float *__restrict__ V,
-                                                       int64_t N, int64_t Nt, int Bp, double *__restrict__ out)
+__global__ void __launch_bounds__(256, 2) gemm_f32_kernel(const float *__restrict__ K, const float *__restrict__ V,
+                                                          int64_t N, int64_t Nt, int Bp, double *__restrict__ out)
 {
     __shared__ float As[kF32K][kF32Rows + 4];
     __shared__ float Vs[kF32K][kF32Runs + 4];
+    extern __shared__ double acc64s[];   // [32][256]: FP64 sum j of thread t at j * 256 + t
     const int t = threadIdx.x;
     const int tr = t & 31, tn = t >> 5;       // rows tr*4..+3, runs tn*8..+7
     const int64_t M = 3 * N, Kd = 2 * Nt;
     const int64_t m0 = (int64_t)blockIdx.x * kF32Rows;
     const int n0 = blockIdx.y * kF32Runs;
     float acc[4][8];
-    double acc64[4][8];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) { acc[a][b] = 0.f; acc64[a][b] = 0.0; }
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc64s[j * 256 + t] = 0.0;
+    // this thread's share of a chunk: K rows (t >> 5) + 8u and runs (t >> 5) + 8u, column t & 31
+    const int kk = t & 31, g = t >> 5;
+    float pk[16], pv[8];
+    auto load = [&](int64_t k0) {
+        const int64_t k = k0 + kk;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int64_t m = m0 + g + 8 * u;
+            pk[u] = (m < M && k < Kd) ? K[m * Kd + k] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int n = n0 + g + 8 * u;
+            pv[u] = (n < Bp && k < Kd) ? V[(int64_t)n * Kd + k] : 0.f;
+        }
+    };
+    load(0);
     int chunk = 0;
     for (int64_t k0 = 0; k0 < Kd; k0 += kF32K, ++chunk) {
-        // K tile: 128 x 32 floats, 16 per thread (row-major, contiguous along k)
-        for (int q = t; q < kF32Rows * kF32K; q += 256) {
-            const int mm = q / kF32K, kk = q % kF32K;
-            const int64_t m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < Kd) ? K[m * Kd + k] : 0.f;
-        }
-        for (int q = t; q < kF32Runs * kF32K; q += 256) {
-            const int nn = q / kF32K, kk = q % kF32K;
-            const int n = n0 + nn;
-            const int64_t k = k0 + kk;
-            Vs[kk][nn] = (n < Bp && k < Kd) ? V[(int64_t)n * Kd + k] : 0.f;
-        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) As[kk][g + 8 * u] = pk[u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) Vs[kk][g + 8 * u] = pv[u];
         __syncthreads();
+        if (k0 + kF32K < Kd) load(k0 + kF32K);
 #pragma unroll 8
-        for (int kk = 0; kk < kF32K; ++kk) {
+        for (int c = 0; c < kF32K; ++c) {
             float a[4], b[8];
 #pragma unroll
-            for (int x = 0; x < 4; ++x) a[x] = As[kk][tr * 4 + x];
+            for (int x = 0; x < 4; ++x) a[x] = As[c][tr * 4 + x];
 #pragma unroll
-            for (int y = 0; y < 8; ++y) b[y] = Vs[kk][tn * 8 + y];
+            for (int y = 0; y < 8; ++y) b[y] = Vs[c][tn * 8 + y];
 #pragma unroll
             for (int x = 0; x < 4; ++x)
 #pragma unroll
@@ -187,7 +203,10 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__
 #pragma unroll
             for (int x = 0; x < 4; ++x)
 #pragma unroll
-                for (int y = 0; y < 8; ++y) { acc64[x][y] += (double)acc[x][y]; acc[x][y] = 0.f; }
+                for (int y = 0; y < 8; ++y) {
+                    acc64s[(x * 8 + y) * 256 + t] += (double)acc[x][y];
+                    acc[x][y] = 0.f;
+                }
         }
     }
 #pragma unroll
@@ -197,7 +216,7 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(const float *__restrict__
 #pragma unroll
         for (int y = 0; y < 8; ++y) {
             const int n = n0 + tn * 8 + y;
-            if (n < Bp) out[(int64_t)n * M + m] = acc64[x][y] + (double)acc[x][y];
+            if (n < Bp) out[(int64_t)n * M + m] = acc64s[(x * 8 + y) * 256 + t] + (double)acc[x][y];
         }
     }
 }
@@ -466,7 +485,14 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
             (const double2 *)S.K, (const double2 *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_FP32) {
         dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
-        gemm_f32_kernel<<<grid, 256, 0, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
+        static thread_local int smem_dev = -1;
+        int dev;
+        PQ3D_CUDA_TRY(cudaGetDevice(&dev));
+        if (smem_dev != dev) {
+            PQ3D_CUDA_TRY(cudaFuncSetAttribute(gemm_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kF32Smem));
+            smem_dev = dev;
+        }
+        gemm_f32_kernel<<<grid, 256, kF32Smem, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
         rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.tc_ctas, (float *)S.rates,
                                    workspace, workspace_bytes, st);
