@@ -52,7 +52,21 @@ __device__ __forceinline__ void split3(double x, __nv_bfloat16 &p0, __nv_bfloat1
     p2 = __double2bfloat16(r1 - (double)__bfloat162float(p1));
 }
 
+// the same for an FP32 value (exact: 24 bits in three 8-bit pieces), on the
+// FP32 pipe
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &p0, __nv_bfloat16 &p1, __nv_bfloat16 &p2)
+{
+    p0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p0);
+    p1 = __float2bfloat16_rn(r1);
+    p2 = __float2bfloat16_rn(r1 - __bfloat162float(p1));
+}
+
 // i: local cell of the shard; v' goes to the mesh-wide position cell0 + i
+// kExactV: v' carries an FP64 slip rate (the FP64 attempt and update) and is
+// split from FP64; otherwise the slip rate is the mixed update's FP32 value,
+// v' has its 24 bits at most and the split runs on the FP32 pipe.
+template <bool kExactV>
 __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_t i, double v1, double v2)
 {
     const int Bp = padded_runs(S.B);
@@ -68,8 +82,13 @@ __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_
         __nv_bfloat16 *P = (__nv_bfloat16 *)S.vop + (k / tc::kBlockK) * tc::kPieces * img +
                            tc::image_offset(r, (int)(k % tc::kBlockK));
         __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-        split3(v1, a0, a1, a2);   // v' to ~26 bits, like the operator's pieces
-        split3(v2, b0, b1, b2);
+        if (kExactV) {
+            split3(v1, a0, a1, a2);   // v' to ~26 bits, like the operator's pieces
+            split3(v2, b0, b1, b2);
+        } else {
+            split3((float)v1, a0, a1, a2);
+            split3((float)v2, b0, b1, b2);
+        }
         __nv_bfloat162 q;
         q.x = a0; q.y = b0; reinterpret_cast<__nv_bfloat162 *>(P)[0] = q;
         q.x = a1; q.y = b1; reinterpret_cast<__nv_bfloat162 *>(P + img)[0] = q;
@@ -98,7 +117,10 @@ __global__ void prepare_kernel(pq3d_batch_sim S)
             pb[19 * stride] = (float)S.slipv[idx];
         }
     }
-    write_vop(S, r, i, v1, v2);
+    // the split the update of this precision writes, so that a prepare (a run
+    // loaded into another slot) leaves the other runs' v' bit for bit as it was
+    if (S.precision != PQ3D_BATCH_FP64 && !S.attempt64) write_vop<false>(S, r, i, v1, v2);
+    else write_vop<true>(S, r, i, v1, v2);
 }
 
 // ---------------------------------------------------------------------------
@@ -410,7 +432,7 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
     S.slip1[idx] += v1 * h;
     S.slip2[idx] += v2 * h;
-    write_vop(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
+    write_vop<!kMixed>(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
 }
 
 // The Dormand-Prince attempt and update in mixed precision (FP32 stages on the
