@@ -62,3 +62,12 @@ def test_unreadable_cache_file_is_ignored(tmp_path, monkeypatch):
 @pytest.mark.parametrize("B,Bp", [(1, 16), (16, 16), (17, 32), (64, 64)])
 def test_padded_runs(B, Bp):
     assert autotune.padded_runs(B) == Bp
+
+
+def test_ensemble_rejects_unknown_attempt_arithmetic():
+    import numpy as np
+    import torch
+    from pyquake3d_gb300.ensemble import Ensemble
+    K = torch.zeros((3 * 4, 2 * 4), dtype=torch.float64)
+    with pytest.raises(ValueError):
+        Ensemble(K, np.zeros((1, 4, 10)), mu=3e10, Cs=3464.0, precision="fp64", attempt="fp16")
