@@ -825,7 +825,9 @@ def profile_case(case):
     hs_assembly  half-space assembly, rough 20x10 km to the surface, N=1,600 (2 launches)
     hmat_product H-matrix product, rough 200x40 km, N=100,000, B=1 (13 products)
     tc_gemm      batched iterations (tcgen05 BF16x6 product, attempt, decision, update),
-                 planar 60x50 km, N=6,000, B=64 (12 iterations)"""
+                 planar 60x50 km, N=6,000, B=64 (12 iterations)
+    f32_gemm     batched iterations with the plain FP32 product on CUDA cores, same
+                 mesh and runs (6 iterations)"""
     import torch
     from pyquake3d_gb300 import gf, mesh
     if case == "hs_assembly":
@@ -852,6 +854,15 @@ def profile_case(case):
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
         # a fixed launch shape (no tuning launches before the captured ones)
         Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x6", nsplit=8, tc_ctas=2).iterate(12)
+    elif case == "f32_gemm":
+        from pyquake3d_gb300.ensemble import Ensemble
+        nodes, tris = mesh.planar_fault(60.0, 50.0, 60, 50)
+        K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM)
+        del K64
+        torch.cuda.empty_cache()
+        _, xg = mesh.element_frames(nodes, tris)
+        tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
+        Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(6)
     else:
         raise SystemExit("unknown --case " + case)
     torch.cuda.synchronize()
@@ -881,7 +892,8 @@ def main():
     ap.add_argument("--batch-iters", type=int, default=300)
     ap.add_argument("--acc-runs", type=int, default=16, help="runs of the slip-accuracy check (0: skip)")
     ap.add_argument("--acc-steps", type=int, default=200)
-    ap.add_argument("--case", default=None, help="profiling case only (hs_assembly, hmat_product, tc_gemm)")
+    ap.add_argument("--case", default=None,
+                    help="profiling case only (hs_assembly, hmat_product, tc_gemm, f32_gemm)")
     args = ap.parse_args()
     if args.case:
         profile_case(args.case)

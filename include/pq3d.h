@@ -240,10 +240,12 @@ typedef struct pq3d_batch_sim {
     double *Tno, *Tt1o, *Tt2o, *state, *slipv1, *slipv2, *slipv, *slip1, *slip2;
     const double *a, *b, *dc, *f0, *shear_loading, *normal_loading, *cos_rake0, *sin_rake0;
     double *rates;         /* partial traction rates, room for nsplit x Bp x 3N doubles: FP64 [Bp][3N]
-                              (nsplit = 1) for FP64, FP32 and HMAT; for BF16X6 FP32 [nsplit][Bp][3N],
-                              the K slices' tensor-memory accumulators, summed in float-float by the
-                              stepper */
-    int32_t nsplit;        /* K-slices of the operator product (>= 1) */
+                              (nsplit = 1) for FP64 and HMAT; FP64 [nsplit][Bp][3N] for FP32 (the K
+                              slices' sums, added in slice order by the stepper); for BF16X6 FP32
+                              [nsplit][Bp][3N], the K slices' tensor-memory sums, added in
+                              float-float by the stepper */
+    int32_t nsplit;        /* K-slices of the operator product: >= 1 for BF16X6, 1..64 for FP32, 1 for
+                              FP64 and HMAT */
     int32_t tc_ctas;       /* BF16X6: CTAs per SM of the tensor-core product, 0 (= 2) or 1..3; the launch
                               shape only, results do not depend on it */
     double *cand;          /* [B][N][4] candidate state */

@@ -156,18 +156,25 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const double2 *__restrict
     }
 }
 
-// FP32: CTA tile 128 rows x 64 runs, K chunks of 32 through shared memory
-// (the next chunk is loaded into registers while the current one is used),
-// FP32 FMAs with the partial sums moved to FP64 every 256 columns; the FP64
-// sums live in dynamic shared memory (64 KB per CTA), which keeps the kernel
-// at 2 CTAs per SM.  N receivers of the shard (3N rows), Nt sources of the
-// mesh (2 Nt columns).
+// FP32: CTA tile 128 rows x 64 runs x one K slice (split-K over gridDim.z:
+// the 3N x B outputs alone fill only part of the SMs), K chunks of 32 through
+// shared memory (the next chunk is loaded into registers while the current
+// one is used), FP32 FMAs with the partial sums moved to FP64 every 256
+// columns; the FP64 sums live in dynamic shared memory (64 KB per CTA), which
+// keeps the kernel at 2 CTAs per SM.  Each slice writes its FP64 sums; the
+// attempt adds them in slice order.  N receivers of the shard (3N rows), Nt
+// sources of the mesh (2 Nt columns).
 constexpr int kF32Rows = 128, kF32Runs = 64, kF32K = 32;
 constexpr int kF32Smem = 32 * 256 * (int)sizeof(double);
 
 __global__ void __launch_bounds__(256, 2) gemm_f32_kernel(const float *__restrict__ K, const float *__restrict__ V,
                                                           int64_t N, int64_t Nt, int Bp, double *__restrict__ out)
 {
+    // K slice blockIdx.z of gridDim.z: 32-column chunks [c0, c1) of the 2 Nt
+    // columns, its sums to out + z * Bp * 3N
+    const int64_t nch = (2 * Nt + kF32K - 1) / kF32K;
+    const int64_t kbeg = nch * blockIdx.z / gridDim.z * kF32K, kend = nch * (blockIdx.z + 1) / gridDim.z * kF32K;
+    out += (int64_t)blockIdx.z * Bp * 3 * N;
     __shared__ float As[kF32K][kF32Rows + 4];
     __shared__ float Vs[kF32K][kF32Runs + 4];
     extern __shared__ double acc64s[];   // [32][256]: FP64 sum j of thread t at j * 256 + t
@@ -199,15 +206,15 @@ __global__ void __launch_bounds__(256, 2) gemm_f32_kernel(const float *__restric
             pv[u] = (n < Bp && k < Kd) ? V[(int64_t)n * Kd + k] : 0.f;
         }
     };
-    load(0);
+    if (kbeg < kend) load(kbeg);
     int chunk = 0;
-    for (int64_t k0 = 0; k0 < Kd; k0 += kF32K, ++chunk) {
+    for (int64_t k0 = kbeg; k0 < kend; k0 += kF32K, ++chunk) {
 #pragma unroll
         for (int u = 0; u < 16; ++u) As[kk][g + 8 * u] = pk[u];
 #pragma unroll
         for (int u = 0; u < 8; ++u) Vs[kk][g + 8 * u] = pv[u];
         __syncthreads();
-        if (k0 + kF32K < Kd) load(k0 + kF32K);
+        if (k0 + kF32K < kend) load(k0 + kF32K);
 #pragma unroll 8
         for (int c = 0; c < kF32K; ++c) {
             float a[4], b[8];
@@ -287,10 +294,15 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
                 for (int sl = 1; sl < S.nsplit; ++sl)
 #pragma unroll
                     for (int c = 0; c < 3; ++c) q[c] = ff_add(q[c], pr[sl * sstride + c]);
-            } else {
+            } else {   // FP64 partial sums per K slice (one for H-matrix products)
                 const double *pr = S.rates + (int64_t)r * 3 * N + 3 * i;
+                const int64_t sstride = (int64_t)Bp * 3 * N;
+                double t[3] = {pr[0], pr[1], pr[2]};
+                for (int sl = 1; sl < S.nsplit; ++sl)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) q[c] = ff_split(pr[c]);
+                    for (int c = 0; c < 3; ++c) t[c] += pr[sl * sstride + c];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = ff_split(t[c]);
             }
             MixedBase m = load_base(S.base + idx, (int64_t)S.B * N);
             const float shear = (float)S.shear_loading[idx];
@@ -450,7 +462,10 @@ static int check_sim(const pq3d_batch_sim *S)
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
     PQ3D_REQUIRE(S->tc_ctas >= 0 && S->tc_ctas <= 3, "pq3d_batch: tc_ctas must be 0 (default) or 1..3");
     PQ3D_REQUIRE(aligned16(S->cand) && aligned16(S->vop) && aligned16(S->K), "pq3d_batch: buffers must be 16-byte aligned");
-    if (S->precision != PQ3D_BATCH_BF16X6) PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: CUDA-core products use nsplit = 1");
+    if (S->precision == PQ3D_BATCH_FP64 || S->precision == PQ3D_BATCH_HMAT)
+        PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: the FP64 and H-matrix products use nsplit = 1");
+    if (S->precision == PQ3D_BATCH_FP32)
+        PQ3D_REQUIRE(S->nsplit <= 64, "pq3d_batch: the FP32 product takes at most 64 K slices");
     PQ3D_REQUIRE(S->attempt64 == 0 || S->attempt64 == 1, "pq3d_batch: attempt64 must be 0 or 1");
     if (mixed_attempt(*S))
         PQ3D_REQUIRE(S->base != nullptr && aligned16(S->base), "pq3d_batch: mixed precisions need the base array");
@@ -506,7 +521,8 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
         gemm_f64_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
             (const double2 *)S.K, (const double2 *)S.vop, S.N, Nt, Bp, S.rates);
     } else if (S.precision == PQ3D_BATCH_FP32) {
-        dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs));
+        dim3 grid((unsigned)((3 * S.N + kF32Rows - 1) / kF32Rows), (unsigned)((Bp + kF32Runs - 1) / kF32Runs),
+                  (unsigned)S.nsplit);
         static thread_local int smem_dev = -1;
         int dev;
         PQ3D_CUDA_TRY(cudaGetDevice(&dev));

@@ -42,6 +42,12 @@ STATE = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "
 PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0")
 
 
+# K slices of the FP32 CUDA-core product: its 3N x B sums alone give too few
+# threads to fill the SMs.  A constant, so that the summation order (and the
+# bits) is the same for every batch, mesh size and row shard.
+FP32_NSPLIT = 4
+
+
 def padded_runs(B: int) -> int:
     return (B + 15) // 16 * 16
 
@@ -104,7 +110,7 @@ class Ensemble:
             assert isinstance(K, torch.Tensor) and K.shape == (3 * N, 2 * Nt) and K.is_contiguous()
             assert K.dtype == (torch.float64 if precision == "fp64" else torch.float32)
             kop = K
-            nsplit = 1
+            nsplit = 1 if precision == "fp64" else (FP32_NSPLIT if nsplit is None else int(nsplit))
         self.K = kop
         self.nsplit = int(nsplit)
         self.tc_ctas = int(tc_ctas or 0)
