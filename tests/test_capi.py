@@ -61,3 +61,31 @@ def test_struct_layouts_match_header(tmp_path):
             assert getattr(cls, f).offset == vals[k], (cname, f)
             k += 1
     assert vals[k] == _lib.PQ3D_BATCH_BASE_FIELDS
+
+
+def test_batch_structure_checks_need_no_gpu():
+    """pq3d_batch_prepare validates the simulation structure before any CUDA
+    call: K-slice counts per product, the CTA count and the attempt flag."""
+    import numpy as np
+    L = _lib.load()
+    buf = np.zeros(64, dtype=np.float64)          # 16-byte aligned stand-in pointers (never dereferenced)
+    p = buf.ctypes.data
+
+    def sim(**kw):
+        S = _lib.BatchSim()
+        S.N, S.B, S.precision, S.nsplit = 8, 2, _lib.PQ3D_BATCH_FP64, 1
+        for k in ("Tno", "rates", "cand", "vop", "K", "ctrl", "base"):
+            setattr(S, k, p)
+        for k, v in kw.items():
+            setattr(S, k, v)
+        return S
+
+    cases = [(dict(nsplit=2), "nsplit"),
+             (dict(precision=_lib.PQ3D_BATCH_FP32, nsplit=65), "64 K slices"),
+             (dict(precision=_lib.PQ3D_BATCH_BF16X6, tc_ctas=4), "tc_ctas"),
+             (dict(precision=_lib.PQ3D_BATCH_FP32, attempt64=2), "attempt64"),
+             (dict(precision=_lib.PQ3D_BATCH_FP32, base=None), "base array")]
+    for kw, text in cases:
+        S = sim(**kw)
+        assert L.pq3d_batch_prepare(ctypes.byref(S), None) == _lib.PQ3D_ERR_ARG, kw
+        assert text in L.pq3d_last_error().decode(), (kw, L.pq3d_last_error())
