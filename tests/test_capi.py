@@ -89,3 +89,18 @@ def test_batch_structure_checks_need_no_gpu():
         S = sim(**kw)
         assert L.pq3d_batch_prepare(ctypes.byref(S), None) == _lib.PQ3D_ERR_ARG, kw
         assert text in L.pq3d_last_error().decode(), (kw, L.pq3d_last_error())
+
+
+def test_tensor_core_launch_arguments_checked_without_gpu():
+    import numpy as np
+    L = _lib.load()
+    plan = np.zeros(2, dtype=np.int32)
+    assert L.pq3d_batch_gemm_bf16x6_plan(0, 2, plan.ctypes.data) == _lib.PQ3D_ERR_ARG
+    assert L.pq3d_batch_gemm_bf16x6_plan(64, 4, plan.ctypes.data) == _lib.PQ3D_ERR_ARG
+    buf = np.zeros(64, dtype=np.float64)
+    p = buf.ctypes.data
+    # CTAs per SM outside 0..3, then a K-slice count above the column blocks (N = 64: 4 blocks)
+    assert L.pq3d_batch_gemm_bf16x6(p, p, 64, 16, 1, 4, p, p, 256, None) == _lib.PQ3D_ERR_ARG
+    assert "ctas_per_sm" in L.pq3d_last_error().decode()
+    assert L.pq3d_batch_gemm_bf16x6(p, p, 64, 16, 5, 2, p, p, 256, None) == _lib.PQ3D_ERR_ARG
+    assert "nsplit" in L.pq3d_last_error().decode()
