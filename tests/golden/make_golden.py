@@ -19,6 +19,10 @@ What it records:
                     (QDsim_gpu.simu_forward, src/QDsim_gpu.py:1029-1122) on the
                     small planar mesh: step sizes, times and the state at
                     checkpoints.
+  traj_config1.npz  the same for the planar N = 1,600 workload (40 x 20 km
+                    vertical strike-slip fault, 1 km squares, velocity-
+                    weakening rectangle, 4 x 4 km nucleation square at
+                    0.03 m/s): 300 accepted steps (``--config1-only``).
 
 The reference Python imports matplotlib, mpi4py, h5py, pyvista and vtk, which
 are not installed; empty stand-in modules are injected into sys.modules before
@@ -404,6 +408,30 @@ def main_dilatancy_only():
     print("traj_dila.npz: t_end = %.6e s, P range %.6e .. %.6e" % (ts[-1], out["s200_P"].min(), out["s200_P"].max()))
 
 
+def main_config1_only():
+    """The reference CPU stepping on the N = 1,600 planar workload: 300
+    accepted steps from the reference's own dense operators (its Python GF)."""
+    QDsim_gpu = import_reference_python()
+    nodes, tris = mesh.planar_fault(40.0, 20.0, 40, 20)
+    _, xg = mesh.element_frames(nodes, tris)
+    table = mesh.friction_table(xg, 40e3, 20e3, seed=0)
+    out = {"nodes": nodes, "tris": tris, "table": table, "mu": MU, "rho": RHO}
+    with tempfile.TemporaryDirectory() as td:
+        sim = reference_sim(QDsim_gpu, nodes, tris, table, td)
+        hs, ts = [], []
+        dttry = sim.htry
+        for i in range(300):
+            h, dttry = sim.simu_forward(dttry)
+            hs.append(h)
+            ts.append(sim.time)
+            if (i + 1) in (1, 25, 50, 100, 150, 200, 250, 300):
+                for k in ("Tno", "Tt1o", "state", "slipv1", "slipv", "slip1", "slip"):
+                    out[f"s{i + 1}_{k}"] = np.array(getattr(sim, k))
+        out["h"], out["t"] = np.array(hs), np.array(ts)
+    np.savez_compressed(os.path.join(HERE, "traj_config1.npz"), **out)
+    print("traj_config1.npz: t_end = %.6e s, max V = %.3e" % (ts[-1], np.max(sim.slipv)))
+
+
 def main():
     rng = np.random.default_rng(20251203)
     lib = load_ref_lib()
@@ -470,5 +498,7 @@ if __name__ == "__main__":
         main_halfspace_only()
     elif "--dilatancy-only" in sys.argv:
         main_dilatancy_only()
+    elif "--config1-only" in sys.argv:
+        main_config1_only()
     else:
         main()

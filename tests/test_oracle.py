@@ -119,3 +119,31 @@ def test_oracle_dilatancy_reproduces_reference_bitwise(golden):
     for k in ("Tno", "Tt1o", "state", "slipv", "slip1", "P", "dPdt0"):
         assert np.array_equal(getattr(st, k), g["s200_" + k]), k
     assert np.array_equal(st.Parr, g["Parr_200"])
+
+
+def test_oracle_stepping_matches_reference_run_config1(golden):
+    """The N = 1,600 planar workload (40 x 20 km, 1 km squares): the oracle
+    (its own C-restated operator, which differs from the reference's Python
+    Green's functions at ~1e-14) against 300 accepted steps of the reference
+    CPU run.  The step sequences coincide for the first 60 steps, where the
+    states agree to 1e-11; after that ulp-level differences flip step
+    decisions, so the reference's own 300-step sequence is replayed and held
+    to its conditioning floor (measured 7.6e-7 in slip)."""
+    g = golden("traj_config1.npz")
+    Ko = oracle.assemble_dense(g["nodes"], g["tris"], float(g["mu"]), float(g["mu"]), nthreads=4)
+    ops = {name: Ko[k] for k, name in enumerate(oracle.OPS)}
+    st = DenseStepper(ops, g["table"], mu=float(g["mu"]), density=float(g["rho"]))
+    dt = 1e-3
+    for i in range(50):
+        h, dt, _ = st.simu_forward(dt)
+        assert h == pytest.approx(g["h"][i], rel=1e-10)
+    for k in ("slip1", "slipv1", "state", "Tt1o", "Tno"):
+        assert normwise_rel(g["s50_" + k], getattr(st, k)) < 1e-11, k
+    st = DenseStepper(ops, g["table"], mu=float(g["mu"]), density=float(g["rho"]))
+    done = 0
+    for stop in (100, 200, 300):
+        st.replay(g["h"][done:stop])
+        done = stop
+        for k, tol in (("slip1", 1e-5), ("slip", 1e-5), ("state", 1e-6), ("Tt1o", 1e-6), ("slipv", 1e-5)):
+            assert normwise_rel(g[f"s{stop}_{k}"], getattr(st, k)) < tol, (stop, k)
+    assert st.time == pytest.approx(g["t"][-1], rel=1e-13)

@@ -234,3 +234,28 @@ def test_dilatancy_through_qdsim(cuda, golden, tmp_path):
         hs.append(h)
     assert np.allclose(hs, g["h"][:10], rtol=1e-9)
     assert normwise_rel(g["s10_P"], sim.P_gpu.cpu().numpy()) < 1e-12
+
+
+def test_stepper_vs_reference_run_config1(cuda, golden):
+    """The N = 1,600 planar workload against 300 accepted steps of the
+    reference CPU run itself (traj_config1.npz), with the GPU-assembled
+    operator: free-running, the step sizes and the state agree while the two
+    step sequences coincide (first 50 steps: 1e-9, slip rate 1e-7); the
+    reference's 300-step sequence replayed stays within 10x the conditioning
+    floor the oracle measures against the same run (7.6e-7 in slip)."""
+    g = golden("traj_config1.npz")
+    K64, _ = gf.assemble_dense(g["nodes"], g["tris"], float(g["mu"]), float(g["mu"]), device=cuda)
+    cs = np.sqrt(float(g["mu"]) / float(g["rho"]))
+    free = DenseDeviceSim(K64, initial_state(g["table"], 1e-6, 1e-9), mu=float(g["mu"]), Cs=cs, V0=1e-6, Vpl=1e-9)
+    h, _, _ = free.step(50)
+    assert np.allclose(h, g["h"][:50], rtol=1e-8, atol=0)
+    for k, tk in TOL.items():
+        assert normwise_rel(g["s50_" + k], free.t[k].cpu().numpy()) < tk, k
+    rep = DenseDeviceSim(K64, initial_state(g["table"], 1e-6, 1e-9), mu=float(g["mu"]), Cs=cs, V0=1e-6, Vpl=1e-9)
+    done = 0
+    for stop in (100, 200, 300):
+        rep.step(stop - done, h_force=g["h"][done:stop])
+        done = stop
+        for k, tk in (("slip1", 1e-5), ("slip", 1e-5), ("state", 1e-6), ("Tt1o", 1e-6), ("slipv", 1e-5)):
+            assert normwise_rel(g[f"s{stop}_{k}"], rep.t[k].cpu().numpy()) < tk, (stop, k)
+    assert np.isclose(rep.read_ctrl().time, g["t"][-1], rtol=1e-13)
