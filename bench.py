@@ -206,21 +206,45 @@ def _ref_assemble(path, cores, nodes, tris):
 
 
 def bench_reference(args):
+    """The reference algorithm on the host cores.  One step = the GF assembly
+    of a fixed sample of source columns (all receivers), sized in the warm-up
+    to ~``--ref-step-seconds``; ``value`` = GF entries/s of that work (the
+    rate a full assembly runs at: every source column costs the same), and
+    ``ms_per_step`` is the time of the sample actually computed."""
+    import oracle
     name, L, W, nodes, tris = workload(args.quick)
     N = tris.shape[0]
-    samples = []
-    cb = None
-    for _ in range(args.warmup):
-        pass
-    for _ in range(max(1, args.steps)):
-        cb = cpu_gf_sample(nodes, tris, seconds=args.ref_seconds)
-        samples.append(cb["value"])
-    val = statistics.median(samples)
-    cb["value"] = val
+    cores = os.cpu_count() or 1
+    ref_so = os.path.join(HERE, "oracle", "_ref", "libTDstressFS_ref.so")
+    if os.path.exists(ref_so):
+        fn, kind = _ref_assemble(ref_so, cores, nodes, tris), "reference"
+    else:
+        fn, kind = (lambda c0, c1: oracle.assemble_dense(nodes, tris, MU, LAM, cols=(c0, c1), nthreads=cores)), "port"
+    # warm-up: calibration slices; the last one sizes the timed sample
+    ncols = min(N, 4 * cores)
+    for _ in range(max(1, args.warmup)):
+        t0 = time.perf_counter()
+        fn(0, ncols)
+        dt = time.perf_counter() - t0
+        ncols = int(min(N, max(4 * cores, ncols * args.ref_step_seconds / max(dt, 1e-3))))
+    times = []
+    for k in range(max(1, args.steps)):
+        c0 = (k * ncols) % max(1, N - ncols + 1)
+        t0 = time.perf_counter()
+        fn(c0, c0 + ncols)
+        times.append(time.perf_counter() - t0)
+    entries = 6.0 * N * ncols
+    val = entries * len(times) / sum(times)
+    cb = {"value": val, "unit": "GF entries/s", "cores": cores, "kind": kind,
+          "sample": "each step: %d of %d source columns x all %d receivers (%.3g GF entries), %d steps, "
+                    "%.1f s in all" % (ncols, N, N, entries, len(times), sum(times))}
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GF entries/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 6.0 * N * N / val * 1e3,
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": sum(times) / len(times) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "N": N, "entries_per_step": 6 * N * N, "halfspace": False},
+            "config": {"workload": name, "N": N, "sample_columns": ncols, "entries_per_step": int(entries),
+                       "full_assembly_entries": 6 * N * N, "halfspace": False,
+                       "note": "a step is a sample of the assembly (ms_per_step is its time); value is the rate, "
+                               "the same for the whole assembly"},
             "cpu_baseline": cb, "e2e": {"value": val, "unit": "GF entries/s", "h2d_bytes_per_step": 0,
                                          "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -344,10 +368,39 @@ def bench_ours(args):
                        "parallelism": "replicas" if world > 1 else "single"},
             "gpu_launches": 3 * args.steps}
     line.update(out)
+    if "batched" in out:
+        # the primary metric's numbers in one compact key, last in the line
+        line["batched_summary"] = batched_summary(out["batched"])
     if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def batched_summary(bt):
+    """RK stages/s of the batched arms over the plain FP64 stepper on the same
+    mesh, with how long each holds the 1e-5 slip bar against FP64 (lockstep)."""
+    acc = bt.get("accuracy_vs_fp64", {})
+    plain = bt["plain_fp64_single"]["rk_stages_per_s"]
+    arms = {}
+    for key, prec, acc_key in (("bf16x14_fp64_attempt", "bf16x14", "bf16x14_fp64_attempt"),
+                               ("bf16x6_mixed_attempt", "bf16x6", "bf16x6"),
+                               ("fp32_mixed_attempt", "fp32", "fp32")):
+        if prec not in bt:
+            continue
+        a = {"rk_stages_per_s": round(bt[prec]["rk_stages_per_s"]),
+             "ratio_vs_plain_fp64": round(bt[prec]["rk_stages_per_s"] / plain, 2)}
+        if acc_key in acc:
+            a["steps_within_1e-5"] = acc[acc_key]["steps_within_1e-5"]
+        if "gemm" in bt[prec]:
+            a["product_hbm_frac"] = round(bt[prec]["gemm"]["roofline"]["frac"], 3)
+        arms[key] = a
+    out = {"N": bt.get("N"), "B": bt.get("B"), "plain_fp64_rk_stages_per_s": round(plain), "arms": arms}
+    if acc:
+        out["lockstep"] = {"runs": acc.get("runs"), "accepted_steps": acc.get("accepted_steps"),
+                           "fp64_perturbed_1e-12_steps_within_1e-5":
+                               acc.get("fp64_perturbed_1e-12", {}).get("steps_within_1e-5")}
+    return out
 
 
 def bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, peaks):
@@ -456,11 +509,15 @@ def cpu_stepping_sample(torch, K64, tab, seconds=12.0):
 
 def bench_batched(torch, dev, args, peaks):
     """Config: batched ensemble, B runs on one planar N=10,000 mesh (100 x 50 km,
-    1 km squares), per-run friction draws (seed 0), BF16x6 tensor-core traction
-    product vs the plain FP64 single-simulation stepper on the same mesh."""
-    import ctypes
+    1 km squares), per-run friction draws (seed 0).  Arms, each against the
+    plain FP64 single-simulation stepper on the same mesh:
+      bf16x6   three-piece BF16 product on tcgen05, FP32 mixed attempt (fast);
+      bf16x14  exact fixed-point slices on tcgen05 (the FP64 product to ~1e-9
+               normwise), FP64 attempt: the arm that tracks the FP64
+               trajectory;
+      fp32     FP32 operator on CUDA cores, FP32 mixed attempt."""
     from pyquake3d_gb300 import _lib, autotune, gf, mesh
-    from pyquake3d_gb300.ensemble import Ensemble, PackedOperator
+    from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator, PackedOperator
     from pyquake3d_gb300.QDsim_gpu import DenseDeviceSim, initial_state
     L_ = _lib.load()
     Lkm, Wkm, nx, nz = (100.0, 50.0, 100, 50) if not args.quick else (40.0, 20.0, 40, 20)
@@ -471,17 +528,25 @@ def bench_batched(torch, dev, args, peaks):
     tabs = mesh.ensemble_tables(xg, Lkm * 1e3, Wkm * 1e3, B=B, seed=0, v_nuc=1e-3)
     K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
     P = PackedOperator(K64)
-    # launch shape of the tensor-core product (K slices, CTAs per SM) from the
-    # project's autotuner, before anything is timed
+    PF = PackedFixOperator(K64)
+    # launch shapes of the tensor-core products from the project's autotuner,
+    # before anything is timed
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     shape = autotune.tune_bf16x6(P, B)
+    shape_fix = autotune.tune_bf16x14(PF, min(B, 64))
     tune_s = time.perf_counter() - t0
     res = {"workload": "batched ensemble: planar %dx%d km, N=%d, B=%d runs, per-run a-b, Dc, sigma_n, nucleation "
-                       "patch from seed 0; RK stages = 7 x attempted steps, all runs" % (Lkm, Wkm, N, B)}
+                       "patch from seed 0; RK stages = 7 x attempted steps, all runs" % (Lkm, Wkm, N, B),
+           "N": N, "B": B}
     out = {}
-    for prec, K in (("bf16x6", P), ("fp32", K32)):
-        ens = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, nsplit=args.nsplit)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    arms = [("bf16x6", P, "mixed"), ("bf16x14", PF, "fp64"), ("fp32", K32, "mixed")]
+    for prec, K, attempt in arms:
+        if prec == "bf16x14" and B > 64:
+            continue
+        ens = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, attempt=attempt,
+                       nsplit=args.nsplit if prec == "bf16x6" else None)
         ens.iterate(2)
         torch.cuda.synchronize()
         ens.capture(args.graph_iters)
@@ -498,39 +563,50 @@ def bench_batched(torch, dev, args, peaks):
         dt = s.elapsed_time(e) / 1e3
         st1 = ens.stages()
         c = ens.read_ctrl()
-        out[prec] = {"rk_stages_per_s": (st1 - st0) / dt, "iterations": reps * args.graph_iters,
+        out[prec] = {"attempt": attempt, "rk_stages_per_s": (st1 - st0) / dt, "iterations": reps * args.graph_iters,
                      "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
                      "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
-                     "clocks": clk.summary(), "error_word": ens.error_word() if prec == "bf16x6" else 0}
-        if prec == "bf16x6":
+                     "clocks": clk.summary(), "error_word": ens.error_word() if prec != "fp32" else 0}
+        if prec in ("bf16x6", "bf16x14"):
             # the tensor-core product alone, CUDA events over repeated launches
-            st = torch.cuda.current_stream(dev).cuda_stream
+            if prec == "bf16x6":
+                launch = lambda: L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                                                           ens.tc_ctas, ens.t["rates"].data_ptr(), ens.ws.data_ptr(),
+                                                           ens.ws.numel(), st)
+                op_bytes = P.data.numel()
+                flops = 6 * 2.0 * (3 * N) * (2 * N) * ens.Bp
+                note = "packed BF16 3-piece operator streamed once per product"
+                fnote = "6 BF16 products x 2 x 3N x 2N x Bp"
+            else:
+                launch = lambda: L_.pq3d_batch_gemm_bf16x14(PF.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                                                            ens.t["rates"].data_ptr(), ens.ws.data_ptr(),
+                                                            ens.ws.numel(), st)
+                op_bytes = PF.data.numel()
+                flops = 14 * 2.0 * (3 * N) * (2 * N) * ens.Bp
+                note = "packed fixed-point operator (4 BF16 slices, 8 B per entry) streamed once per product"
+                fnote = "14 BF16 slice products x 2 x 3N x 2N x Bp"
             for _ in range(3):
-                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit, ens.tc_ctas,
-                                          ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
+                launch()
             nl = 20
             s.record()
             for _ in range(nl):
-                L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit, ens.tc_ctas,
-                                          ens.t["rates"].data_ptr(), ens.ws.data_ptr(), ens.ws.numel(), st)
+                launch()
             e.record()
             e.synchronize()
             tg = s.elapsed_time(e) / 1e3 / nl
-            Bp = ens.Bp
-            op_bytes = P.data.numel()
-            flops = 6 * 2.0 * (3 * N) * (2 * N) * Bp
+            sh = shape if prec == "bf16x6" else shape_fix
             out[prec]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit, "ctas_per_sm": ens.tc_ctas,
-                                 "autotune": {"nsplit": shape["nsplit"], "ctas_per_sm": shape["ctas_per_sm"],
-                                              "tune_s": tune_s, "candidates": "nsplit 1..16 x CTAs per SM "
-                                              "(1, 2, 3) at 64 runs, then CTAs per SM at this run count"},
+                                 "autotune": dict(sh, tune_s=tune_s),
                                  "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": op_bytes / tg / 1e9,
                                               "peak": peaks["hbm_gbs"], "frac": op_bytes / tg / 1e9 / peaks["hbm_gbs"],
-                                              "algorithmic_bytes": op_bytes,
-                                              "note": "packed BF16x3-piece operator streamed once per product"},
+                                              "algorithmic_bytes": op_bytes, "note": note},
                                  "tensor": {"achieved_tflops": flops / tg / 1e12, "peak_tflops": peaks["bf16_tflops"],
-                                            "frac": flops / tg / 1e12 / peaks["bf16_tflops"],
-                                            "flops": flops, "note": "6 BF16 products x 2 x 3N x 2N x Bp"}}
+                                            "frac": flops / tg / 1e12 / peaks["bf16_tflops"], "flops": flops,
+                                            "note": fnote}}
+            if ens.error_word() != 0:
+                out[prec]["error_word"] = ens.error_word()
         del ens
+        torch.cuda.empty_cache()
     # plain FP64 single simulation on the same mesh (run 0's parameters)
     sim = DenseDeviceSim(K64, initial_state(tabs[0], 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
     sim.step(3)
@@ -545,85 +621,48 @@ def bench_batched(torch, dev, args, peaks):
     plain = 7.0 * (c1.attempts - c0.attempts) / dt
     out["plain_fp64_single"] = {"rk_stages_per_s": plain, "accepted_steps": int(c1.steps_done - c0.steps_done),
                                 "ms_per_step": dt / max(1, c1.steps_done - c0.steps_done) * 1e3}
-    out["ratio_bf16x6_vs_plain_fp64"] = out["bf16x6"]["rk_stages_per_s"] / plain
-    out["ratio_fp32_vs_plain_fp64"] = out["fp32"]["rk_stages_per_s"] / plain
+    for prec, _, _ in arms:
+        if prec in out:
+            out["ratio_%s_vs_plain_fp64" % prec] = out[prec]["rk_stages_per_s"] / plain
     if args.acc_runs > 0:
-        out["accuracy_vs_fp64"] = batched_accuracy(torch, K64, K32, P, tabs[:args.acc_runs], args.acc_steps)
+        out["accuracy_vs_fp64"] = batched_accuracy(torch, K64, K32, P, PF, tabs[:args.acc_runs], args.acc_steps)
     res.update(out)
-    del K64, K32, P
+    del K64, K32, P, PF
     torch.cuda.empty_cache()
     return res
 
 
-def batched_accuracy(torch, K64, K32, P, tabs, max_steps, every=5):
+def batched_accuracy(torch, K64, K32, P, PF, tabs, max_steps, every=5):
     """Slip error of the mixed-precision ensembles against the FP64 batched
     stepper (the reference arithmetic, FP64 operator) on the same runs, in
-    lockstep: each iteration runs as its two halves (pq3d_batch_iterate_begin /
-    _end) and between them every other ensemble takes the FP64 ensemble's
-    error norms (the hand-over row shards use for their reduced norms), so all
-    take the same accept/reject decisions and step sizes and reach the same
-    times; the differences are the arithmetic's alone.  Beside the mixed
-    products runs the FP64 stepper itself with each run's initial slip rates
-    perturbed by 1e-12 (relative, random sign): the floor set by the
-    sensitivity of the trajectories (nucleation amplifies any perturbation by
-    orders of magnitude).  Reported per variant: the accepted steps up to which
-    the normwise relative slip error of every run stays within 1e-5, and the
-    error at fixed step counts (null once a run's forced acceptance of a step
-    its own arithmetic would reject has made it non-finite)."""
+    lockstep (pyquake3d_gb300.ensemble.lockstep: same step sizes and
+    decisions, so the differences are the arithmetic's alone).  Beside them
+    runs the FP64 stepper itself with each run's initial slip rates perturbed
+    by 1e-12 (relative, random sign): the floor set by the sensitivity of the
+    trajectories (nucleation amplifies any perturbation by orders of
+    magnitude).  Per variant: the accepted steps up to which the normwise
+    relative slip error of every run stays within 1e-5, and the error at fixed
+    step counts."""
     import numpy as np
-    from pyquake3d_gb300.ensemble import Ensemble
-    B = tabs.shape[0]
+    from pyquake3d_gb300.ensemble import Ensemble, lockstep
     pert = tabs.copy()
     pert[:, :, 7] *= 1.0 + 1e-12 * np.random.default_rng(7).choice([-1.0, 1.0], size=pert[:, :, 7].shape)
     kw = dict(mu=MU, Cs=3464.0, max_steps=max_steps)
-    runs = {"fp64": Ensemble(K64, tabs, precision="fp64", **kw),
-            "bf16x6": Ensemble(P, tabs, precision="bf16x6", **kw),
-            "fp32": Ensemble(K32, tabs, precision="fp32", **kw),
-            "fp64_perturbed_1e-12": Ensemble(K64, pert, precision="fp64", **kw)}
-    ref = runs["fp64"]
-    others = [k for k in runs if k != "fp64"]
-    marks = [m for m in (10, 25, 50, 100, 200, 400) if m <= max_steps]
-    out = {k: {"steps_within_1e-5": 0, "slip_rel_err_at_steps": {}, "max_slip_rate_rel_err_within": 0.0}
-           for k in others}
-    ok = {k: True for k in others}
-    done = False
-    for _ in range(40 * max_steps // every):
-        for _ in range(every):
-            for e in runs.values():
-                e.begin()
-            wr = ref.error_words()
-            for k in others:
-                runs[k].set_error_words(wr)
-            for e in runs.values():
-                e.end()
-        cr = ref.read_ctrl()
-        steps = min(c.steps for c in cr)
-        s_ref = torch.cat([ref.t["slip1"], ref.t["slip2"]], 1)
-        v_ref = torch.cat([ref.t["slipv1"], ref.t["slipv2"]], 1)
-        for k in others:
-            e = runs[k]
-            s = torch.cat([e.t["slip1"], e.t["slip2"]], 1)
-            v = torch.cat([e.t["slipv1"], e.t["slipv2"]], 1)
-            es = ((s - s_ref).norm(dim=1) / s_ref.norm(dim=1)).max().item()
-            ev = ((v - v_ref).norm(dim=1) / v_ref.norm(dim=1)).max().item()
-            O = out[k]
-            if ok[k] and es <= 1e-5:
-                O["steps_within_1e-5"] = steps
-                O["max_slip_rate_rel_err_within"] = max(O["max_slip_rate_rel_err_within"], ev)
-            else:
-                ok[k] = False
-            for m in marks:
-                if steps >= m and str(m) not in O["slip_rel_err_at_steps"]:
-                    O["slip_rel_err_at_steps"][str(m)] = es if es == es and es < float("inf") else None
-        if done:
-            break
-        done = not any(c.active for c in cr)
-    for k in others:
-        out[k]["failed_runs"] = int(sum(c.status != 0 for c in runs[k].read_ctrl()))
-    return {"runs": B, "accepted_steps": max_steps, "rk_stages_per_run": int(7 * max(c.attempts for c in cr)),
-            "simulated_time_s": max(c.time for c in cr), "bar": 1e-5, **out,
-            "method": "lockstep with the FP64 batched stepper (same step sizes and decisions: the FP64 error norms "
-                      "handed over between the halves of each iteration); checkpoints every %d iterations" % every}
+    ref = Ensemble(K64, tabs, precision="fp64", **kw)
+    others = {"bf16x14_fp64_attempt": Ensemble(PF, tabs, precision="bf16x14", attempt="fp64", **kw),
+              "bf16x14_mixed_attempt": Ensemble(PF, tabs, precision="bf16x14", attempt="mixed", **kw),
+              "bf16x6": Ensemble(P, tabs, precision="bf16x6", **kw),
+              "fp32": Ensemble(K32, tabs, precision="fp32", **kw),
+              "fp64_perturbed_1e-12": Ensemble(K64, pert, precision="fp64", **kw)}
+    r = lockstep(ref, others, max_steps, every=every)
+    info = r.pop("_ref")
+    out = {"runs": tabs.shape[0], **info, "bar": 1e-5,
+           "method": "lockstep with the FP64 batched stepper (same step sizes and decisions: the FP64 error norms "
+                     "handed over between the halves of each iteration); checkpoints every %d iterations" % every}
+    for k, v in r.items():
+        out[k] = {"steps_within_1e-5": v["steps_within"], "slip_rel_err_at_steps": v["slip_rel_err_at_steps"],
+                  "max_slip_rate_rel_err_within": v["max_slip_rate_err_within"], "failed_runs": v["failed_runs"]}
+    return out
 
 
 def bench_hmatrix(torch, dev, args, peaks):
@@ -644,7 +683,7 @@ def bench_hmatrix(torch, dev, args, peaks):
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
     res = {"workload": "H-matrix: rough %dx%d km, N=%d, leaf 64, eta 2, ACA tol 1e-4, FP32 factors" % (Lkm, Wkm, N),
-           "build_s": t_build, "stats": H.stats}
+           "build_s": t_build, "build_phases_s": H.build_phases, "partition": H.partition_info, "stats": H.stats}
     # product timing (B = 1)
     v = torch.randn(1, 2 * N, dtype=torch.float64, device=dev)
     ws = torch.empty(H.workspace_bytes(1), dtype=torch.uint8, device=dev)
@@ -765,53 +804,83 @@ def bench_serving(torch, dev, args):
     res = srv.run(reqs, time_limit_s=args.serve_time_limit)
     res["meshes"] = [{"N": int(sp["tris"].shape[0]), "kind": srv.kind[m], "operator_GB": srv.op_bytes[m] / 1e9,
                       "build_s": srv.build_s[m]} for m, sp in enumerate(meshes)]
-    # one-at-a-time on the plain path: plain FP64 stepping (dense) or a single
-    # H-matrix run, measured per mesh; each request's duration = its own stage
-    # count / that rate; FIFO one request at a time from its arrival
-    plain = {}
-    for m, sp in enumerate(meshes):
-        tab = reqs[0].table if reqs[0].mesh == m else None
-        _, xg = mesh.element_frames(sp["nodes"], sp["tris"])
-        tab = mesh.ensemble_tables(xg, sp["L"], sp["W"], B=1, seed=1, v_nuc=1e-3)[0]
-        if srv.kind[m] == "dense_bf16x6":
-            K64, _ = gf.assemble_dense(sp["nodes"], sp["tris"], MU, LAM, fp32_copy=False, device=dev)
-            sim = DenseDeviceSim(K64, initial_state(tab, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
-            sim.step(2)
-            c0 = sim.read_ctrl()
-            t0 = time.perf_counter()
-            sim.step(40)
-            dt = time.perf_counter() - t0
-            c1 = sim.read_ctrl()
-            plain[m] = 7.0 * (c1.attempts - c0.attempts) / dt
-            del K64, sim
-            torch.cuda.empty_cache()
-        else:
-            ens = Ensemble(srv.ens[m].hmat, tab[None], mu=MU, Cs=3464.0, precision="hmat")
-            ens.iterate(2)
-            torch.cuda.synchronize()
-            s0 = ens.stages()
-            t0 = time.perf_counter()
-            ens.iterate(60)
-            torch.cuda.synchronize()
-            plain[m] = (ens.stages() - s0) / (time.perf_counter() - t0)
-    t_free = 0.0
-    ttr = []
-    for r in sorted(reqs, key=lambda r: r.arrival_s):
-        if r.done_s is None:
-            continue
-        start = max(r.arrival_s, t_free)
-        t_free = start + 7.0 * r.attempts / plain[r.mesh]
-        ttr.append(t_free - r.arrival_s)
-    res["sequential_plain_estimate"] = {"p50_time_to_result_s": float(np.percentile(ttr, 50)) if ttr else None,
-                                        "p99_time_to_result_s": float(np.percentile(ttr, 99)) if ttr else None,
-                                        "plain_rk_stages_per_s": {str(srv.meshes[m]["tris"].shape[0]): v
-                                                                  for m, v in plain.items()},
-                                        "method": "per-mesh plain rates measured here x each served request's "
-                                                  "own attempt count, FIFO one at a time"}
-    res["workload"] = ("serving: %d requests, Poisson 4/s seed 0, 8 meshes N=%s, 16 slots/mesh, 150 GB budget, "
-                       "span U(1,20) yr, max %d steps/run" % (nreq, [m[0] for m in sizes], args.serve_max_steps))
+    # one at a time on the plain path, measured: each request (its own table
+    # and span) run alone, in arrival order, on the plain FP64 stepper (dense
+    # meshes) or a single-run H-matrix ensemble with the FP64 attempt, until
+    # its span or the step cap, while the measuring budget lasts; requests
+    # past the budget take their mesh's measured plain rate x their own
+    # served attempt count (stated in the result).  Time to result = FIFO.
     del srv
     torch.cuda.empty_cache()
+    durations, how = {}, {}
+    budget_end = time.perf_counter() + args.serve_plain_seconds
+    order = sorted([r for r in reqs if r.done_s is not None], key=lambda r: r.arrival_s)
+    rate = {}
+    for m, sp in enumerate(meshes):
+        mine = [r for r in order if r.mesh == m]
+        if not mine:
+            continue
+        N = int(sp["tris"].shape[0])
+        if res["meshes"][m]["kind"] == "dense_bf16x6":
+            K64, _ = gf.assemble_dense(sp["nodes"], sp["tris"], MU, LAM, fp32_copy=False, device=dev)
+            H = None
+        else:
+            from pyquake3d_gb300.hmatrix import HMatrix
+            K64, H = None, HMatrix(sp["nodes"], sp["tris"], MU, LAM, device=dev, min_size=64, mini_leaf=64, eta=2.0,
+                                   tol=1e-4)
+        st_all, t_all = 0, 0.0
+        for r in mine:
+            if time.perf_counter() > budget_end and st_all > 0:
+                continue
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if H is None:
+                sim = DenseDeviceSim(K64, initial_state(r.table, 1e-6, 1e-9), mu=MU, Cs=3464.0, V0=1e-6, Vpl=1e-9)
+                while True:
+                    sim.step(10)
+                    c = sim.read_ctrl()
+                    if c.time >= r.span_s or c.steps_done >= args.serve_max_steps or c.status != 0:
+                        break
+                att = int(c.attempts)
+                del sim
+            else:
+                ens = Ensemble(H, r.table[None], mu=MU, Cs=3464.0, precision="hmat", attempt="fp64", t_end=r.span_s,
+                               max_steps=args.serve_max_steps)
+                while ens.read_ctrl()[0].active:
+                    ens.iterate(50)
+                att = int(ens.read_ctrl()[0].attempts)
+                del ens
+            torch.cuda.synchronize()
+            durations[r.rid] = time.perf_counter() - t0
+            how[r.rid] = "measured"
+            st_all += 7 * att
+            t_all += durations[r.rid]
+        rate[m] = st_all / t_all if t_all > 0 else float("nan")
+        for r in mine:
+            if r.rid not in durations:
+                durations[r.rid] = 7.0 * r.attempts / rate[m]
+                how[r.rid] = "extrapolated"
+        del K64, H
+        torch.cuda.empty_cache()
+    t_free = 0.0
+    ttr = []
+    for r in order:
+        start = max(r.arrival_s, t_free)
+        t_free = start + durations[r.rid]
+        ttr.append(t_free - r.arrival_s)
+    nmeas = sum(1 for v in how.values() if v == "measured")
+    res["sequential_plain"] = {"p50_time_to_result_s": float(np.percentile(ttr, 50)) if ttr else None,
+                               "p99_time_to_result_s": float(np.percentile(ttr, 99)) if ttr else None,
+                               "requests_measured": nmeas, "requests_extrapolated": len(how) - nmeas,
+                               "plain_rk_stages_per_s": {str(int(meshes[m]["tris"].shape[0])): v
+                                                         for m, v in rate.items()},
+                               "method": "each request run alone in arrival order on the plain FP64 path (dense: "
+                                         "the FP64 stepper; H-matrix meshes: one H-matrix run with the FP64 "
+                                         "attempt) to its span or the step cap, wall-clocked, within a %.0f s "
+                                         "budget; the rest at their mesh's measured plain rate x their served "
+                                         "attempt count; FIFO one at a time from arrival" % args.serve_plain_seconds}
+    res["workload"] = ("serving: %d requests, Poisson 4/s seed 0, 8 meshes N=%s, 16 slots/mesh, 150 GB budget, "
+                       "span U(1,20) yr, max %d steps/run" % (nreq, [m[0] for m in sizes], args.serve_max_steps))
     return res
 
 
@@ -827,7 +896,11 @@ def profile_case(case):
     tc_gemm      batched iterations (tcgen05 BF16x6 product, attempt, decision, update),
                  planar 60x50 km, N=6,000, B=64 (12 iterations)
     f32_gemm     batched iterations with the plain FP32 product on CUDA cores, same
-                 mesh and runs (6 iterations)"""
+                 mesh and runs (6 iterations)
+    fix_gemm     batched iterations with the fixed-point BF16x14 product and the FP64
+                 attempt, same mesh and runs (6 iterations)
+    aca          H-matrix build (partition, ACA, dense blocks), rough 100x25 km, N=20,000,
+                 leaf 64, eta 2, tol 1e-4 (one ACA launch over all low-rank blocks)"""
     import torch
     from pyquake3d_gb300 import gf, mesh
     if case == "hs_assembly":
@@ -863,6 +936,21 @@ def profile_case(case):
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
         Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(6)
+    elif case == "fix_gemm":
+        from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator
+        nodes, tris = mesh.planar_fault(60.0, 50.0, 60, 50)
+        K64, _ = gf.assemble_dense(nodes, tris, MU, LAM, fp32_copy=False)
+        P = PackedFixOperator(K64)
+        del K64
+        torch.cuda.empty_cache()
+        _, xg = mesh.element_frames(nodes, tris)
+        tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
+        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x14", attempt="fp64", nsplit=6).iterate(6)
+    elif case == "aca":
+        from pyquake3d_gb300.hmatrix import HMatrix
+        nodes, tris = mesh.rough_fault(100.0, 25.0, 200, 50, seed=0)
+        H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4)
+        print(json.dumps({"stats": H.stats, "phases": H.build_phases}))
     else:
         raise SystemExit("unknown --case " + case)
     torch.cuda.synchronize()
@@ -876,8 +964,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="N=2,000 case (profiling)")
-    ap.add_argument("--rk-steps", type=int, default=200)
+    ap.add_argument("--rk-steps", type=int, default=1000)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=2.0,
+                    help="reference arm: CPU seconds of one step's assembly sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-hmat", action="store_true")
@@ -885,6 +975,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-max-steps", type=int, default=3000)
     ap.add_argument("--serve-time-limit", type=float, default=90.0)
+    ap.add_argument("--serve-plain-seconds", type=float, default=60.0,
+                    help="budget for measuring the one-at-a-time plain baseline of the serving stream")
     ap.add_argument("--hmat-stages", type=int, default=500)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--nsplit", type=int, default=None)

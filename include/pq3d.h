@@ -96,9 +96,11 @@ int pq3d_assemble_dense(const double *nodes, const int64_t *tris, int64_t N,
  * implicit device synchronisation and the failure modes of cudaMalloc/cudaFree
  * between its launches.  The source and receiver tables live in a fixed
  * 11.5 MB __device__ array inside this library, so N is limited to 32768
- * elements (larger N returns PQ3D_ERR_ARG).  The first call on a device looks
- * up the array's device address with that device current (cudaGetSymbolAddress)
- * and caches it; make that first call before any stream capture.  All calls
+ * elements (larger N returns PQ3D_ERR_ARG).  Every call looks up the array's
+ * device address with the calling device current (cudaGetSymbolAddress; no
+ * cached address, so a device reset between calls is harmless); the first
+ * call on a device may load the library's device code, so make it before any
+ * stream capture.  All calls
  * share the one array: calls that overlap on the GPU (other streams, other host
  * threads) race on it, so serialise them.  The caller still provides nodes,
  * tris, K64 and K32 as in pq3d_assemble_dense. */
@@ -230,6 +232,12 @@ typedef struct pq3d_run_ctrl {
                                   FP32 accumulation in tensor memory, K slices added in
                                   float-float */
 #define PQ3D_BATCH_HMAT 3      /* H-matrix product (pq3d_hmat_apply); K points to a host pq3d_hmat */
+#define PQ3D_BATCH_BF16X14 4   /* operator (32 bits) and v' (40 bits) as exact fixed-point BF16 slices,
+                                  one exponent per 1024-column chunk; 14 slice products on tcgen05
+                                  tensor cores with exact accumulation per chunk, chunks added in
+                                  float-float: the FP64 product to ~2^-32 of each chunk's largest
+                                  operator entry (static) and ~2^-40 of its largest v' (dynamic).
+                                  B <= 64, no row shards */
 
 /* Device state of B simulations sharing one mesh.  Arrays are run-major
  * [B][N] FP64 unless stated.  Same fields and units as pq3d_dense_sim. */
@@ -243,17 +251,20 @@ typedef struct pq3d_batch_sim {
                               (nsplit = 1) for FP64 and HMAT; FP64 [nsplit][Bp][3N] for FP32 (the K
                               slices' sums, added in slice order by the stepper); for BF16X6 FP32
                               [nsplit][Bp][3N], the K slices' tensor-memory sums, added in
-                              float-float by the stepper */
-    int32_t nsplit;        /* K-slices of the operator product: >= 1 for BF16X6, 1..64 for FP32, 1 for
-                              FP64 and HMAT */
+                              float-float by the stepper; for BF16X14 float2 (hi, lo)
+                              [nsplit][Bp][3N], float-float K-slice sums */
+    int32_t nsplit;        /* K-slices of the operator product: >= 1 for BF16X6 and BF16X14, 1..64 for
+                              FP32, 1 for FP64 and HMAT */
     int32_t tc_ctas;       /* BF16X6: CTAs per SM of the tensor-core product, 0 (= 2) or 1..3; the launch
                               shape only, results do not depend on it */
     double *cand;          /* [B][N][4] candidate state */
     void *vop;             /* operator-product right-hand side of all runs, padded to Bp = B rounded up
-                              to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], or for
-                              BF16X6 the packed pieces (pq3d_batch_rhs_bytes, zero-initialised) */
+                              to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], for
+                              BF16X6 the packed pieces (pq3d_batch_rhs_bytes, zero-initialised),
+                              for BF16X14 the packed fixed-point slices (pq3d_batch_rhs_fix_bytes) */
     const void *K;         /* operator: FP64 (3N)x(2N) for FP64, FP32 (3N)x(2N) for FP32, the
-                              packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6, a host
+                              packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6, the packed
+                              fixed-point slices (pq3d_batch_pack_operator_fix) for BF16X14, a host
                               pointer to a pq3d_hmat for HMAT (v' then FP64 [Bp][2N]) */
     pq3d_run_ctrl *ctrl;   /* [B] */
     double V0, Vpl, eta;
@@ -274,6 +285,15 @@ typedef struct pq3d_batch_sim {
      * FP32 [PQ3D_BATCH_BASE_FIELDS][B][N], written by pq3d_batch_prepare and
      * by the update of every accepted step.  NULL (unused) otherwise. */
     float *base;
+    /* BF16X14: the cell order of the fixed-point product (device int64, NULL =
+     * identity): fix_order[p] = cell at position p of the packed operator's
+     * rows and columns, fix_pos[cell] = its position.  A spatially compact
+     * order (pq3d_hmat_cluster_order) keeps each 1024-column chunk, whose
+     * largest |v'| sets the chunk's fixed-point grid, inside one region of
+     * the fault; the mesh order of a long fault puts far-apart cells in one
+     * chunk and costs the far receivers their relative precision. */
+    const int64_t *fix_order;
+    const int64_t *fix_pos;
 } pq3d_batch_sim;
 
 #define PQ3D_BATCH_BASE_FIELDS 24
@@ -298,6 +318,29 @@ int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, 
  * or tensor memory does not fit them), plan[1] = pipeline stages per CTA. */
 int pq3d_batch_gemm_bf16x6_plan(int B, int ctas_per_sm, int32_t *plan);
 
+/* Packed operator of the fixed-point tensor-core product (BF16X14): per operator
+ * row and 1024-column chunk one exponent e (|K| < 2^e over the chunk) and four
+ * BF16 slices d_p 2^(e-7-8p), |d_p| <= 128, stored as [3N/128 tiles][2N/32
+ * blocks][4][128 x 32] shared-memory images.  Bytes, and the packing kernel
+ * (once per mesh; the operator rounded to 32 bits of its chunk's largest entry). */
+size_t pq3d_batch_operator_fix_bytes(int64_t N);
+/* order (device int64 [N], NULL = identity): order[p] = cell at position p;
+ * the packed operator holds rows 3 order[p] + c and columns 2 order[q] + s at
+ * positions 3p + c and 2q + s, and the product's outputs come in that row
+ * order. */
+int pq3d_batch_pack_operator_fix(const double *K64, int64_t N, const int64_t *order, void *Kpacked, void *stream);
+/* Bytes of the packed fixed-point right-hand side for B <= 64 runs, and its
+ * packing from v ([B][2N] FP64 device array, v[r][2j + s]): per run and chunk
+ * five slices (40 bits of the chunk's largest |v|).  The batched stepper packs
+ * v' itself; this entry serves the product alone. */
+size_t pq3d_batch_rhs_fix_bytes(int64_t N, int B);
+int pq3d_batch_pack_rhs_fix(const double *v, int64_t N, int B, const int64_t *order, void *Vpacked, void *stream);
+/* The fixed-point tensor-core product alone: out[((s*Bp + n)*3N + m)*2 + {0,1}]
+ * = (hi, lo) FP32 with hi + lo = K slice s of sum_k K[m][k] v[n][k] (s < nsplit,
+ * Bp = B rounded up to 16, B <= 64), the exact product of the slices up to
+ * ~2^-44 relative.  One CTA per SM; nsplit sets the order of the slice sums. */
+int pq3d_batch_gemm_bf16x14(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
+                            void *workspace, size_t workspace_bytes, void *stream);
 /* Device workspace bytes of one batched iteration (GEMM split-K partials live in
  * sim->rates; this is what the tensor-core product needs besides). */
 size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim);
@@ -359,6 +402,25 @@ typedef struct pq3d_hmat {
     int64_t t_ngrp;
 } pq3d_hmat;
 
+/* Cluster and block tree of the H-matrix on the device (replaces the host
+ * recursions createHmatrix / build_block_tree / create_recursive_blocks,
+ * src/Hmatrix.py:143-192, 2077-2196, with their rules: bisection of the
+ * longest bounding-box axis at its midpoint, min_size points per leaf
+ * cluster, admissibility min(diam) <= eta * dist, mini_leaf).  xg: [N][3]
+ * centroids (device, FP64).  Outputs (device): perm[N] (element at each
+ * position of the depth-first leaf order), leaves [N][2] capacity (leaf
+ * cluster ranges, *n_leaves of them), blocks [cap_blocks][5] (r0, r1, c0, c1,
+ * lowrank; depth-first order, *n_blocks of them).  With a blocks array too
+ * small, returns PQ3D_ERR_ARG with *n_blocks set to the size needed.
+ * *depth (may be NULL) = cluster-tree levels.  Allocates its scratch; reads
+ * one count per level back to the host (synchronises `stream`). */
+/* The cluster tree alone: perm[N] (device) = the depth-first leaf order of
+ * the bisection tree with leaves of <= min_size points -- a spatially compact
+ * order of the elements (the BF16X14 product's fix_order). */
+int pq3d_hmat_cluster_order(const double *xg, int64_t N, int min_size, int64_t *perm, int32_t *depth, void *stream);
+int pq3d_hmat_partition(const double *xg, int64_t N, int min_size, int mini_leaf, double eta, int64_t *perm,
+                        int64_t *leaves, int64_t *n_leaves, int64_t *blocks, int64_t cap_blocks, int64_t *n_blocks,
+                        int32_t *depth, void *stream);
 /* ACA (partial pivoting, relative Frobenius tolerance `tol`) of the listed
  * admissible blocks, one CTA per block, rows and columns generated by the GF
  * kernel from `tables` (pq3d_gf_setup).  Per block b: kcap[b] = rank cap,
@@ -392,6 +454,22 @@ int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B, double *Y
                            int active_stride, void *workspace, size_t workspace_bytes, void *stream);
 int pq3d_hmat_apply(const pq3d_hmat *H, const double *X, int B, double *Y, void *workspace, size_t workspace_bytes,
                     void *stream);
+
+/* ---------------- self-tests of the bounded device waits ---------------- */
+/* No counterpart in the reference (it has no device waits).  A cooperative
+ * launch of `nblocks` blocks (<= 64) in which every block but `skip_block`
+ * arrives at one grid barrier -- the barrier of the dense stepper -- with the
+ * wait limit lowered to `spin_limit` iterations (~1 us each; <= 65536):
+ * returns PQ3D_ERR_TIMEOUT (the status the stepper records) once the waits
+ * give up; returned_host[b] (host, nblocks ints) = 1 if block b returned
+ * after giving up, 2 if it passed the barrier, 3 for the block that skipped
+ * it.  Allocates a small buffer. */
+int pq3d_selftest_barrier_timeout(int nblocks, int skip_block, unsigned spin_limit, int *returned_host);
+/* One block of 128 threads waits, with the bounded mbarrier wait of the
+ * tensor-core products and its limit lowered to `wait_limit` tries (<= 65536),
+ * on an mbarrier nobody arrives at: returns PQ3D_ERR_TIMEOUT with the error
+ * word set, *gave_up_host = the threads that gave up (128). */
+int pq3d_selftest_mbar_timeout(unsigned wait_limit, int *gave_up_host);
 
 #ifdef __cplusplus
 }

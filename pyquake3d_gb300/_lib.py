@@ -65,7 +65,8 @@ class BatchSim(ctypes.Structure):
                                  "rates")] + \
         [("nsplit", ctypes.c_int32), ("tc_ctas", ctypes.c_int32), ("cand", c_void_p), ("vop", c_void_p), ("K", c_void_p),
          ("ctrl", c_void_p), ("V0", c_dbl), ("Vpl", c_dbl), ("eta", c_dbl), ("fix_Tn", ctypes.c_int32),
-         ("attempt64", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64), ("base", c_void_p)]
+         ("attempt64", ctypes.c_int32), ("N_total", c_i64), ("cell0", c_i64), ("base", c_void_p),
+         ("fix_order", c_void_p), ("fix_pos", c_void_p)]
 
 
 class HMat(ctypes.Structure):
@@ -79,6 +80,7 @@ PQ3D_BATCH_FP64 = 0
 PQ3D_BATCH_FP32 = 1
 PQ3D_BATCH_BF16X6 = 2
 PQ3D_BATCH_HMAT = 3
+PQ3D_BATCH_BF16X14 = 4
 PQ3D_BATCH_BASE_FIELDS = 24   # floats per cell and run of pq3d_batch_sim.base
 
 
@@ -115,6 +117,12 @@ _SIGS = {
     "pq3d_batch_gemm_bf16x6": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_int, c_void_p, c_void_p, c_size,
                                        c_void_p]),
     "pq3d_batch_gemm_bf16x6_plan": (c_int, [c_int, c_int, c_void_p]),
+    "pq3d_batch_operator_fix_bytes": (c_size, [c_i64]),
+    "pq3d_batch_pack_operator_fix": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
+    "pq3d_batch_rhs_fix_bytes": (c_size, [c_i64, c_int]),
+    "pq3d_batch_pack_rhs_fix": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p]),
+    "pq3d_batch_gemm_bf16x14": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size,
+                                        c_void_p]),
     "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
     "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_void_p, c_size, c_void_p]),
     "pq3d_hmat_aca": (c_int, [c_void_p, c_i64, c_void_p, c_int, c_void_p, c_void_p, c_dbl, c_dbl, c_dbl, c_int,
@@ -131,6 +139,11 @@ _SIGS = {
     "pq3d_batch_iterate": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
     "pq3d_batch_iterate_begin": (c_int, [ctypes.POINTER(BatchSim), c_void_p, c_size, c_void_p]),
     "pq3d_batch_iterate_end": (c_int, [ctypes.POINTER(BatchSim), c_void_p]),
+    "pq3d_hmat_cluster_order": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p]),
+    "pq3d_hmat_partition": (c_int, [c_void_p, c_i64, c_int, c_int, c_dbl, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_i64, c_void_p, c_void_p, c_void_p]),
+    "pq3d_selftest_barrier_timeout": (c_int, [c_int, c_int, ctypes.c_uint, c_void_p]),
+    "pq3d_selftest_mbar_timeout": (c_int, [ctypes.c_uint, c_void_p]),
 }
 
 _lib = None

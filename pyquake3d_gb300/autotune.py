@@ -1,4 +1,4 @@
-"""Autotuner of the launch shape of the tensor-core traction product.
+"""Autotuner of the launch shape of the tensor-core traction products.
 
 ``pq3d_batch_gemm_bf16x6`` streams the packed operator through one CTA per
 (128-row tile, K slice).  Two launch parameters are free:
@@ -37,6 +37,7 @@ from . import _lib
 
 TUNE_RUNS = 64        # width at which nsplit is tuned
 MAX_NSPLIT = 16
+MAX_NSPLIT_FIX = 24
 CTAS_ORDER = (2, 1, 3)
 TIE = 0.02
 INNER = 2
@@ -208,3 +209,56 @@ def tune_bf16x6(op, B: int) -> dict:
         store(k_ct, ctas)
         tuned = True
     return {"nsplit": int(nsplit), "ctas_per_sm": int(ctas), "tuned": tuned}
+
+
+class _BenchFix:
+    """Scratch buffers and the timed launch of the fixed-point product."""
+
+    def __init__(self, op, B: int, max_nsplit: int):
+        L = _lib.load()
+        self.L, self.op, self.B, self.N = L, op, B, op.N
+        dev = op.device
+        g = torch.Generator(device="cpu").manual_seed(1234)
+        v = torch.randn(B, 2 * self.N, generator=g, dtype=torch.float64).to(dev)
+        self.vop = torch.zeros(L.pq3d_batch_rhs_fix_bytes(self.N, B), dtype=torch.uint8, device=dev)
+        self.stream = torch.cuda.current_stream(dev)
+        _lib.check(L.pq3d_batch_pack_rhs_fix(v.data_ptr(), self.N, B, None, self.vop.data_ptr(),
+                                             self.stream.cuda_stream))
+        self.out = torch.empty(max_nsplit * padded_runs(B) * 3 * self.N * 2, dtype=torch.float32, device=dev)
+        self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
+
+    def launch(self, nsplit: int):
+        _lib.check(self.L.pq3d_batch_gemm_bf16x14(self.op.data.data_ptr(), self.vop.data_ptr(), self.N, self.B,
+                                                  nsplit, self.out.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
+                                                  self.stream.cuda_stream))
+
+    def time(self, nsplit: int) -> float:
+        self.launch(nsplit)
+        best = float("inf")
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(REPEATS):
+            s.record(self.stream)
+            for _ in range(INNER):
+                self.launch(nsplit)
+            e.record(self.stream)
+            e.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3 / INNER)
+        w = self.ws[:4].view(torch.int32).item()
+        if w != 0:
+            raise RuntimeError(f"fixed-point tensor-core product reported error word {w} while tuning")
+        return best
+
+
+def tune_bf16x14(op, B: int) -> dict:
+    """K slices of the fixed-point product on the packed operator ``op``:
+    {"nsplit", "tuned"}, tuned at TUNE_RUNS runs and cached per mesh size."""
+    N, dev = op.N, op.device
+    key = _key(dev, f"N={N}", "nsplit_fix")
+    nsplit = lookup(key)
+    if nsplit is not None:
+        return {"nsplit": int(nsplit), "tuned": False}
+    bench = _BenchFix(op, TUNE_RUNS, MAX_NSPLIT_FIX)
+    nsplit, _ = tune(nsplit_candidates(N, MAX_NSPLIT_FIX), bench.time)
+    del bench
+    store(key, nsplit)
+    return {"nsplit": int(nsplit), "tuned": True}

@@ -16,6 +16,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "gemm_fix.cuh"
 #include "gemm_tc.cuh"
 #include "rk_device.cuh"
 
@@ -69,6 +70,7 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &p0, __nv_bfloat16
 template <bool kExactV>
 __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_t i, double v1, double v2)
 {
+    if (S.precision == PQ3D_BATCH_BF16X14) return;   // packed per chunk after the update (fx::pack_rhs_from_state)
     const int Bp = padded_runs(S.B);
     const int64_t o = (int64_t)r * 2 * total_cells(S) + 2 * (S.cell0 + i);
     if (S.precision == PQ3D_BATCH_FP64 || S.precision == PQ3D_BATCH_HMAT) {
@@ -286,7 +288,19 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             // slice (added here in float-float, slice order), the other mixed
             // products one FP64 value
             FF q[3];
-            if (S.precision == PQ3D_BATCH_BF16X6) {
+            if (S.precision == PQ3D_BATCH_BF16X14) {   // float-float partials per K slice
+                const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
+                const float2 *pr = (const float2 *)S.rates + (int64_t)r * 3 * N + 3 * pos;
+                const int64_t sstride = (int64_t)Bp * 3 * N;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = ff_norm(pr[c].x, pr[c].y);
+                for (int sl = 1; sl < S.nsplit; ++sl)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float2 t = pr[sl * sstride + c];
+                        q[c] = ff_add2(q[c], FF{t.x, t.y});
+                    }
+            } else if (S.precision == PQ3D_BATCH_BF16X6) {
                 const float *pr = (const float *)S.rates + (int64_t)r * 3 * N + 3 * i;
                 const int64_t sstride = (int64_t)Bp * 3 * N;
 #pragma unroll
@@ -315,7 +329,15 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
         } else {
             double q0 = 0.0, q1 = 0.0, q2 = 0.0;
-            if (S.precision == PQ3D_BATCH_BF16X6) {   // FP32 K-slice partials, added in FP64
+            if (S.precision == PQ3D_BATCH_BF16X14) {   // float-float K-slice partials, added in FP64
+                const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
+                for (int s = 0; s < S.nsplit; ++s) {
+                    const float2 *p = (const float2 *)S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * pos;
+                    q0 += (double)p[0].x + (double)p[0].y;
+                    q1 += (double)p[1].x + (double)p[1].y;
+                    q2 += (double)p[2].x + (double)p[2].y;
+                }
+            } else if (S.precision == PQ3D_BATCH_BF16X6) {   // FP32 K-slice partials, added in FP64
                 for (int s = 0; s < S.nsplit; ++s) {
                     const float *p = (const float *)S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * i;
                     q0 += (double)p[0]; q1 += (double)p[1]; q2 += (double)p[2];
@@ -456,7 +478,12 @@ static int check_sim(const pq3d_batch_sim *S)
 {
     PQ3D_REQUIRE(S && S->N > 0 && S->B > 0 && S->B <= 1024 && S->ctrl && S->K && S->vop && S->rates && S->cand,
                  "pq3d_batch: bad simulation structure");
-    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_HMAT, "pq3d_batch: bad precision");
+    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_BF16X14, "pq3d_batch: bad precision");
+    if (S->precision == PQ3D_BATCH_BF16X14) {
+        PQ3D_REQUIRE(S->B <= fx::kMaxRuns, "pq3d_batch: the BF16X14 product takes at most %d runs", fx::kMaxRuns);
+        PQ3D_REQUIRE((S->fix_order == nullptr) == (S->fix_pos == nullptr),
+                     "pq3d_batch: fix_order and fix_pos are given together");
+    }
     if (S->precision == PQ3D_BATCH_HMAT)
         PQ3D_REQUIRE(((const pq3d_hmat *)S->K)->N == S->N, "pq3d_batch: H-matrix size differs from N");
     PQ3D_REQUIRE(S->nsplit >= 1, "pq3d_batch: nsplit must be >= 1");
@@ -489,6 +516,7 @@ extern "C" size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim)
 {
     if (sim && sim->precision == PQ3D_BATCH_HMAT)
         return pq3d_hmat_workspace_bytes((const pq3d_hmat *)sim->K, padded_runs(sim->B));
+    if (sim && sim->precision == PQ3D_BATCH_BF16X14) return 256;
     if (!sim || sim->precision != PQ3D_BATCH_BF16X6) return 0;
     return pq3d::tc::gemm_bf16x6_workspace_bytes(sim->N, padded_runs(sim->B), sim->nsplit);
 }
@@ -502,6 +530,9 @@ extern "C" int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream)
     dim3 grid((unsigned)((sim->N + 255) / 256), (unsigned)Bp);
     prepare_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*sim);   // the shard's own slice of v'
     PQ3D_CUDA_TRY(cudaGetLastError());
+    if (sim->precision == PQ3D_BATCH_BF16X14)
+        return fx::pack_rhs_from_state(sim->slipv1, sim->slipv2, sim->cos_rake0, sim->sin_rake0, sim->Vpl,
+                                       sim->fix_order, sim->N, sim->B, sim->vop, (cudaStream_t)stream);
     return PQ3D_OK;
 }
 
@@ -531,6 +562,9 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
             smem_dev = dev;
         }
         gemm_f32_kernel<<<grid, 256, kF32Smem, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
+    } else if (S.precision == PQ3D_BATCH_BF16X14) {
+        rc = fx::gemm_bf16x14(S.K, S.vop, S.N, Bp, S.nsplit, (float2 *)S.rates, workspace, workspace_bytes, st);
+        if (rc) return rc;
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
         rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.tc_ctas, (float *)S.rates,
                                    workspace, workspace_bytes, st);
@@ -565,6 +599,9 @@ extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
     if (mixed_attempt(S)) update_kernel<true><<<grid, 256, 0, st>>>(S);
     else update_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
+    if (S.precision == PQ3D_BATCH_BF16X14)   // v' of every run from its slip rates (unchanged for the others)
+        return fx::pack_rhs_from_state(S.slipv1, S.slipv2, S.cos_rake0, S.sin_rake0, S.Vpl, S.fix_order, S.N, S.B,
+                                       S.vop, st);
     return PQ3D_OK;
 }
 

@@ -35,9 +35,10 @@ constexpr unsigned kSpinLimit = 1u << 21;
 
 // Grid-wide barrier for a cooperative launch.  Every block calls it with the
 // same sequence; `count` and `gen` live in device memory and start at 0.
-// Returns false when the wait hit kSpinLimit (the caller then records
-// PQ3D_ERR_TIMEOUT and leaves).
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nblocks)
+// Returns false when the wait hit `limit` iterations (kSpinLimit unless a
+// self-test lowers it; the caller then records PQ3D_ERR_TIMEOUT and leaves).
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nblocks,
+                                             unsigned limit = kSpinLimit)
 {
     __shared__ bool ok;
     __syncthreads();
@@ -53,7 +54,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, uns
         } else {
             unsigned it = 0;
             while (*((volatile unsigned *)gen) == my_gen) {
-                if (++it > kSpinLimit) { ok = false; break; }
+                if (++it > limit) { ok = false; break; }
                 __nanosleep(1000);
             }
         }

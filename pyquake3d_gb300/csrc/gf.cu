@@ -393,26 +393,17 @@ static int assemble_rows(const double *nodes, const int64_t *tris, int64_t N, in
 constexpr int64_t kNoAllocMaxN = 32768;
 static __device__ __align__(256) double g_noalloc_scratch[(size_t)(kSrcStride + kRecvStride) * kNoAllocMaxN];
 
-static std::mutex g_noalloc_mu;
-static double *g_noalloc_ptr[256];   // device address of g_noalloc_scratch, per device ordinal
-
-// Device address of the fixed scratch on the current device, looked up once
-// per device (with that device current) and cached.
+// Device address of the fixed scratch on the current device, looked up with
+// that device current on every call (cheap): a cached address would go stale
+// if the device were reset or its primary context recreated between calls.
 static int noalloc_scratch(double **out)
 {
-    int dev = 0;
-    PQ3D_CUDA_TRY(cudaGetDevice(&dev));
-    PQ3D_REQUIRE(dev >= 0 && dev < 256, "pq3d_assemble_dense_noalloc: device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return set_error(PQ3D_ERR_CUDA, "pq3d_assemble_dense_noalloc: cudaGetSymbolAddress failed: %s",
-                             cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = (double *)p;
-    }
-    *out = g_noalloc_ptr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return set_error(PQ3D_ERR_CUDA, "pq3d_assemble_dense_noalloc: cudaGetSymbolAddress failed: %s",
+                         cudaGetErrorString(e));
+    *out = (double *)p;
     return PQ3D_OK;
 }
 

@@ -182,15 +182,24 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         for (int col = t; col < Nc; col += kThreads) nv2 += v[col] * v[col];
         nu2 = block_sum(nu2, sv);
         nv2 = block_sum(nv2, sv);
-        double cross = 0.0;
-        for (int l = 0; l < k; ++l) {
-            double du = 0.0, dv = 0.0;
-            for (int row = t; row < M; row += kThreads) du += u[row] * U[(int64_t)l * M + row];
-            for (int col = t; col < Nc; col += kThreads) dv += v[col] * V[(int64_t)l * Nc + col];
-            du = block_sum(du, sv);
-            dv = block_sum(dv, sv);
-            cross += du * dv;
+        // the k cross products (u.u_l)(v.v_l): one warp per term l (warp
+        // shuffles, no block barrier), then one block sum of the warps' parts
+        double cross_w = 0.0;
+        {
+            const int w = t >> 5, lane = t & 31;
+            for (int l = w; l < k; l += kThreads / 32) {
+                double du = 0.0, dv = 0.0;
+                for (int row = lane; row < M; row += 32) du += u[row] * U[(int64_t)l * M + row];
+                for (int col = lane; col < Nc; col += 32) dv += v[col] * V[(int64_t)l * Nc + col];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    du += __shfl_xor_sync(0xffffffffu, du, o);
+                    dv += __shfl_xor_sync(0xffffffffu, dv, o);
+                }
+                cross_w += du * dv;
+            }
         }
+        const double cross = block_sum((t & 31) == 0 ? cross_w : 0.0, sv);
         frob2 += 2.0 * cross + nu2 * nv2;
         ++k;
         if (sqrt(nu2 * nv2) <= tol * sqrt(fmax(frob2, 0.0))) { status = 0; break; }

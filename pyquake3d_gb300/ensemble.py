@@ -14,6 +14,12 @@ Precisions of the traction product (``precision=``):
            leading cross products on the tcgen05 tensor cores with FP32
            accumulation in tensor memory; K slices added in float-float;
            launch shape (K slices, CTAs per SM) from :mod:`.autotune`
+  "bf16x14" the operator (32 bits) and v' (40 bits) as exact fixed-point BF16
+           slices with one exponent per 1024-column chunk, 14 slice products
+           on the tensor cores with exact accumulation per chunk, chunks and
+           K slices added in float-float: the FP64 product to ~1e-10 of its
+           scale, for runs that must track the FP64 trajectory (with
+           attempt="fp64"); at most 64 runs
   "hmat"   an :class:`~pyquake3d_gb300.hmatrix.HMatrix` (large meshes)
 Time, slip, the state and the RK error norm stay FP64 in every mode.
 
@@ -37,7 +43,7 @@ from . import _lib, autotune
 from .QDsim_gpu import initial_state
 
 PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6,
-              "hmat": _lib.PQ3D_BATCH_HMAT}
+              "hmat": _lib.PQ3D_BATCH_HMAT, "bf16x14": _lib.PQ3D_BATCH_BF16X14}
 STATE = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2")
 PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0")
 
@@ -66,11 +72,44 @@ class PackedOperator:
                                               torch.cuda.current_stream(self.device).cuda_stream))
 
 
+class PackedFixOperator:
+    """The operand of the fixed-point tensor-core product ("bf16x14"): the FP64
+    operator as four BF16 slices per row and 1024-column chunk (built once per
+    mesh).
+
+    xg: the (N, 3) element centroids.  With them the cells are taken in the
+    depth-first order of the bisection cluster tree (``order``, ``pos``), so
+    that every 1024-column chunk -- whose largest |v'| sets the fixed-point
+    grid of its 512 cells -- covers one compact region of the fault.  In the
+    mesh order a chunk of a long fault spans its whole length, and a receiver
+    far from a nucleating patch that shares its chunk with the patch keeps
+    only ~24 of the 40 bits of its traction rate."""
+
+    def __init__(self, K64: torch.Tensor, xg=None):
+        L = _lib.load()
+        assert K64.dtype == torch.float64 and K64.is_contiguous()
+        self.N = K64.shape[1] // 2
+        self.device = K64.device
+        if xg is not None:
+            from .hmatrix import cluster_order
+            self.order = cluster_order(xg, 1, self.device)
+            self.pos = torch.empty_like(self.order)
+            self.pos[self.order] = torch.arange(self.N, dtype=torch.int64, device=self.device)
+        else:
+            self.order = self.pos = None
+        self.data = torch.empty(L.pq3d_batch_operator_fix_bytes(self.N), dtype=torch.uint8, device=self.device)
+        _lib.check(L.pq3d_batch_pack_operator_fix(K64.data_ptr(), self.N,
+                                                  self.order.data_ptr() if self.order is not None else None,
+                                                  self.data.data_ptr(),
+                                                  torch.cuda.current_stream(self.device).cuda_stream))
+
+
 class Ensemble:
     """Device state and launch structure of B runs on one mesh.
 
     K: the (3N, 2N) operator -- FP64 for "fp64", FP32 for "fp32", a
-    :class:`PackedOperator` for "bf16x6".  tables: (B, N, 10) per-cell tables
+    :class:`PackedOperator` for "bf16x6", a :class:`PackedFixOperator` for
+    "bf16x14".  tables: (B, N, 10) per-cell tables
     (``read_parameter`` layout).
 
     shard=(cell0, N_total): this object steps cells [cell0, cell0 + N) of an
@@ -99,6 +138,15 @@ class Ensemble:
             kop = None
             nsplit = 1
             self.hmat = K
+        elif precision == "bf16x14":
+            assert isinstance(K, PackedFixOperator) and K.N == N
+            if B > 64:
+                raise ValueError("the bf16x14 product takes at most 64 runs")
+            kop = K.data
+            self.fix_op = K
+            if nsplit is None:
+                nsplit = autotune.tune_bf16x14(K, B)["nsplit"]
+            tc_ctas = 1
         elif precision == "bf16x6":
             assert isinstance(K, PackedOperator) and K.N == N
             kop = K.data
@@ -129,6 +177,8 @@ class Ensemble:
             self.vop = torch.zeros(self.Bp * 2 * Nt, **f64)
         elif precision == "fp32":
             self.vop = torch.zeros(self.Bp * 2 * Nt, dtype=torch.float32, device=dev)
+        elif precision == "bf16x14":
+            self.vop = torch.zeros(L.pq3d_batch_rhs_fix_bytes(N, B), dtype=torch.uint8, device=dev)
         else:
             self.vop = torch.zeros(L.pq3d_batch_rhs_bytes(N, B), dtype=torch.uint8, device=dev)
         self.ctrl_t = torch.zeros(B * ctypes.sizeof(_lib.RunCtrl), dtype=torch.uint8, device=dev)
@@ -138,6 +188,8 @@ class Ensemble:
             setattr(S, k, self.t[k].data_ptr())
         S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
         S.base = self.t["base"].data_ptr() if "base" in self.t else None
+        if precision == "bf16x14" and K.order is not None:
+            S.fix_order, S.fix_pos = K.order.data_ptr(), K.pos.data_ptr()
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
         S.attempt64 = int(self.attempt == "fp64" and precision != "fp64")
@@ -191,7 +243,12 @@ class Ensemble:
         K-slice partials of the tensor-core product added, or the one FP64
         partial of the other products."""
         n = self.nsplit * self.Bp * 3 * self.N
-        if self.precision == "bf16x6":
+        if self.precision == "bf16x14":
+            f = self.t["rates"].view(torch.float32)[:2 * n].view(self.nsplit, self.Bp, 3 * self.N, 2).double()
+            r = f.sum(3).sum(0)
+            if self.fix_op.order is not None:   # rows come in the operator's cell order
+                r = r.view(self.Bp, self.N, 3)[:, self.fix_op.pos].reshape(self.Bp, 3 * self.N)
+        elif self.precision == "bf16x6":
             r = self.t["rates"].view(torch.float32)[:n].view(self.nsplit, self.Bp, 3 * self.N).double().sum(0)
         else:
             r = self.t["rates"][:n].view(self.nsplit, self.Bp, 3 * self.N).sum(0)
@@ -262,3 +319,74 @@ class Ensemble:
     def stages(self):
         """Right-hand-side evaluations so far: 7 per attempted step, all runs."""
         return 7 * sum(c.attempts for c in self.read_ctrl())
+
+
+def lockstep(ref: Ensemble, others: dict, max_steps: int, every: int = 5, bar: float = 1e-5,
+             marks=(10, 25, 50, 100, 150, 200, 300, 400)) -> dict:
+    """Step ``ref`` and the ensembles of ``others`` ({name: Ensemble}, the same
+    runs in other arithmetics) in lockstep and measure how far each departs
+    from ``ref`` in slip.
+
+    Every iteration runs as its two halves (pq3d_batch_iterate_begin / _end);
+    between them each other ensemble takes ``ref``'s error norms -- the hand-
+    over that row shards use for their reduced norms -- so all take the same
+    accept/reject decisions and step sizes and reach the same times, and the
+    differences are the arithmetic's alone (left to their own step control,
+    two arithmetics take different step sequences, and the Dormand-Prince
+    tolerance of 1e-4 per step separates them far more than the arithmetic
+    does).  Every ``every`` iterations the normwise relative slip error of
+    each run, ||s - s_ref|| / ||s_ref|| over its (slip1, slip2), is taken;
+    per name the result holds the accepted steps up to which the maximum over
+    runs stays within ``bar`` ("steps_within"), the largest such error and
+    slip-rate error within that window, the error at the ``marks`` step
+    counts (None once a run forced to accept a step its own arithmetic would
+    reject has gone non-finite) and the failed runs."""
+    names = list(others)
+    out = {k: {"steps_within": 0, "max_slip_err_within": 0.0, "max_slip_rate_err_within": 0.0,
+               "slip_rel_err_at_steps": {}} for k in names}
+    ok = {k: True for k in names}
+    marks = [m for m in marks if m <= max_steps]
+    done = False
+    cr = ref.read_ctrl()
+    for _ in range(40 * max_steps // every + 1):
+        for _ in range(every):
+            ref.begin()
+            for k in names:
+                others[k].begin()
+            wr = ref.error_words()
+            for k in names:
+                others[k].set_error_words(wr)
+            ref.end()
+            for k in names:
+                others[k].end()
+        cr = ref.read_ctrl()
+        steps = min(c.steps for c in cr)
+        s_ref = torch.cat([ref.t["slip1"], ref.t["slip2"]], 1)
+        v_ref = torch.cat([ref.t["slipv1"], ref.t["slipv2"]], 1)
+        for k in names:
+            e = others[k]
+            s = torch.cat([e.t["slip1"], e.t["slip2"]], 1)
+            v = torch.cat([e.t["slipv1"], e.t["slipv2"]], 1)
+            es = ((s - s_ref).norm(dim=1) / s_ref.norm(dim=1)).max().item()
+            ev = ((v - v_ref).norm(dim=1) / v_ref.norm(dim=1)).max().item()
+            O = out[k]
+            if ok[k] and es <= bar:
+                O["steps_within"] = steps
+                O["max_slip_err_within"] = max(O["max_slip_err_within"], es)
+                O["max_slip_rate_err_within"] = max(O["max_slip_rate_err_within"], ev)
+            else:
+                ok[k] = False
+            for m in marks:
+                if steps >= m and str(m) not in O["slip_rel_err_at_steps"]:
+                    O["slip_rel_err_at_steps"][str(m)] = es if es == es and es < float("inf") else None
+        if done:
+            break
+        done = not any(c.active for c in cr)
+    for k in names:
+        out[k]["failed_runs"] = int(sum(c.status != 0 for c in others[k].read_ctrl()))
+        if ok[k]:
+            out[k]["steps_within"] = min(c.steps for c in cr)
+    out["_ref"] = {"runs": ref.B, "accepted_steps": int(min(c.steps for c in cr)),
+                   "rk_stages_per_run": int(7 * max(c.attempts for c in cr)),
+                   "simulated_time_s": float(max(c.time for c in cr))}
+    return out

@@ -1,12 +1,13 @@
 """H-matrix of the traction operator on the GPU.
 
-Partition (host, set-up): the reference's geometric rules
+Partition (device, set-up; csrc/htree.cu): the reference's geometric rules
 (src/Hmatrix.py:68-192, 2077-2142): binary cluster tree over the element
 centroids by bisecting the longest bounding-box axis at its midpoint (points
 <= midpoint go left, order kept, a leaf at <= min_size points or when a side
-would be empty); block tree by recursive quad-splitting of (row, column)
-cluster pairs, a leaf block when admissible (min(diam) <= eta * dist, eta = 2)
-or when either side has <= mini_leaf points or no children.  Low-rank blocks:
+would be empty), built level by level; block tree by quad-splitting of (row,
+column) cluster pairs, level by level, a leaf block when admissible
+(min(diam) <= eta * dist, eta = 2) or when either side has <= mini_leaf points
+or no children.  Low-rank blocks:
 both sides > mini_leaf (src/Hmatrix.py:1292-1344); the rest are dense.
 Elements are renumbered in depth-first leaf order, so every cluster is a
 contiguous range and a block is a pair of ranges.
@@ -24,9 +25,7 @@ from __future__ import annotations
 
 import ctypes
 import json
-import math
 import os
-import sys
 
 import numpy as np
 import torch
@@ -34,79 +33,56 @@ import torch
 from . import _lib
 from .mesh import element_frames
 
-sys.setrecursionlimit(max(10000, sys.getrecursionlimit()))
 
 
-class _Node:
-    __slots__ = ("start", "end", "left", "right", "lo", "hi", "box", "diam")
+def build_partition(xg, min_size=16, mini_leaf=32, eta=2.0, device="cuda"):
+    """The partition on the device (pq3d_hmat_partition, csrc/htree.cu):
+    returns (perm, blocks, leaves) as host arrays -- perm[p] = element at
+    position p; blocks = int64 (nb, 5): r0, r1, c0, c1, lowrank (0/1) in
+    depth-first order; leaves = int64 (nl, 2) leaf cluster ranges -- and
+    records the device time and tree depth in ``build_partition.last``."""
+    import time
+    L = _lib.load()
+    dev = torch.device(device)
+    xg_t = torch.as_tensor(np.ascontiguousarray(xg, dtype=np.float64), device=dev).contiguous()
+    N = xg_t.shape[0]
+    perm = torch.empty(N, dtype=torch.int64, device=dev)
+    leaves = torch.empty((N, 2), dtype=torch.int64, device=dev)
+    nl, nb, depth = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int32(0)
+    cap = max(1024, 4 * N)
+    st = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    while True:
+        blocks = torch.empty((cap, 5), dtype=torch.int64, device=dev)
+        rc = L.pq3d_hmat_partition(xg_t.data_ptr(), N, int(min_size), int(mini_leaf), float(eta), perm.data_ptr(),
+                                   leaves.data_ptr(), ctypes.byref(nl), blocks.data_ptr(), cap, ctypes.byref(nb),
+                                   ctypes.byref(depth), st.cuda_stream)
+        if rc == _lib.PQ3D_ERR_ARG and nb.value > cap:
+            cap = int(nb.value)
+            continue
+        _lib.check(rc)
+        break
+    build_partition.last = {"seconds": time.perf_counter() - t0, "depth": int(depth.value),
+                            "blocks": int(nb.value), "leaves": int(nl.value)}
+    return (perm.cpu().numpy(), blocks[:nb.value].cpu().numpy(), leaves[:nl.value].cpu().numpy())
 
 
-def build_partition(xg, min_size=16, mini_leaf=32, eta=2.0):
-    """Returns (perm, blocks, leaves): perm[p] = element at position p;
-    blocks = int64 array (nb, 5): r0, r1, c0, c1, lowrank (0/1) in depth-first
-    order; leaves = int64 array (nl, 2) of leaf cluster ranges."""
-    xg = np.asarray(xg, dtype=np.float64)
-    perm = []
-    leaves = []
+build_partition.last = {}
 
-    def tree(idx, pts):
-        node = _Node()
-        node.start = len(perm)
-        node.lo = pts.min(axis=0)
-        node.hi = pts.max(axis=0)
-        node.left = node.right = None
-        split = None
-        if len(idx) > min_size:
-            j = int(np.argmax(node.hi - node.lo))
-            g = (node.lo[j] + node.hi[j]) / 2
-            m1 = pts[:, j] <= g
-            m2 = pts[:, j] > g
-            if m1.any() and m2.any():
-                split = (m1, m2)
-        if split is None:
-            perm.extend(idx.tolist())
-            leaves.append((node.start, len(perm)))
-        else:
-            m1, m2 = split
-            node.left = tree(idx[m1], pts[m1])
-            node.right = tree(idx[m2], pts[m2])
-        node.end = len(perm)
-        return node
 
-    root = tree(np.arange(len(xg)), xg)
-    blocks = []
-
-    # bounding boxes as Python floats: the block recursion visits every block
-    # (50,000 at N = 100,000) and NumPy calls on 3-vectors dominated it
-    def boxes(nd):
-        if nd is None:
-            return
-        nd.box = (tuple(float(v) for v in nd.lo), tuple(float(v) for v in nd.hi))
-        nd.diam = math.sqrt(sum((h - l) ** 2 for l, h in zip(*nd.box)))
-        boxes(nd.left)
-        boxes(nd.right)
-
-    boxes(root)
-
-    def admissible(a, b):
-        (alo, ahi), (blo, bhi) = a.box, b.box
-        dist = math.sqrt(sum(max(0.0, bl - ah) ** 2 + max(0.0, al - bh) ** 2
-                             for al, ah, bl, bh in zip(alo, ahi, blo, bhi)))
-        return min(a.diam, b.diam) <= eta * dist
-
-    def rec(r, c):
-        nr, nc = r.end - r.start, c.end - c.start
-        if admissible(r, c) or nr <= mini_leaf or nc <= mini_leaf or \
-                r.left is None or r.right is None or c.left is None or c.right is None:
-            blocks.append((r.start, r.end, c.start, c.end, int(nr > mini_leaf and nc > mini_leaf)))
-            return
-        rec(r.left, c.left)
-        rec(r.left, c.right)
-        rec(r.right, c.left)
-        rec(r.right, c.right)
-
-    rec(root, root)
-    return np.asarray(perm, dtype=np.int64), np.asarray(blocks, dtype=np.int64), np.asarray(leaves, dtype=np.int64)
+def cluster_order(xg, min_size=1, device="cuda") -> torch.Tensor:
+    """Depth-first leaf order of the bisection cluster tree on the device
+    (pq3d_hmat_cluster_order): order[p] = element at position p, a spatially
+    compact order (every run of consecutive positions lies in a small region
+    of the fault).  Device int64 tensor."""
+    L = _lib.load()
+    dev = torch.device(device)
+    xg_t = torch.as_tensor(np.ascontiguousarray(xg, dtype=np.float64), device=dev).contiguous()
+    order = torch.empty(xg_t.shape[0], dtype=torch.int64, device=dev)
+    _lib.check(L.pq3d_hmat_cluster_order(xg_t.data_ptr(), xg_t.shape[0], int(min_size), order.data_ptr(), None,
+                                         torch.cuda.current_stream(dev).cuda_stream))
+    return order
 
 
 class HMatrix:
@@ -121,8 +97,21 @@ class HMatrix:
         tris = np.ascontiguousarray(tris, dtype=np.int64)
         N = tris.shape[0]
         self.N = N
+        import time as _time
+        phases = {}
+        tp = [_time.perf_counter()]
+
+        def phase(name):   # wall time of the phase just finished (device synchronised)
+            torch.cuda.synchronize(dev)
+            t = _time.perf_counter()
+            phases[name] = t - tp[0]
+            tp[0] = t
+
         _, xg = element_frames(nodes, tris)
-        perm, blocks, leaves = build_partition(xg, min_size, mini_leaf, eta)
+        phase("frames_host")
+        perm, blocks, leaves = build_partition(xg, min_size, mini_leaf, eta, device=dev)
+        self.partition_info = dict(build_partition.last)
+        phase("partition_device")
         self.perm_host, self.blocks_host, self.leaves_host = perm, blocks, leaves
         st = torch.cuda.current_stream(dev).cuda_stream
         self.nodes_t = torch.as_tensor(nodes, device=dev)
@@ -132,6 +121,7 @@ class HMatrix:
         self.halfspace = bool(halfspace)
         _lib.check(L.pq3d_gf_setup(self.nodes_t.data_ptr(), self.tris_t.data_ptr(), N, hs, self.tables.data_ptr(),
                                    self.tables.numel(), st))
+        phase("gf_tables")
         self.perm = torch.as_tensor(perm, device=dev)
         nb = blocks.shape[0]
         blk = np.ascontiguousarray(blocks[:, :4])
@@ -184,6 +174,7 @@ class HMatrix:
             factors[(i, j)] = (ids, UV, uvo_c, blk_c, kcap_c, rk_c)
             self.aca_chunks += 1
             i = j
+        phase("aca")
         ok = lowrank & (status == 0)
         rank[~ok] = -1
         self.aca_status = status
@@ -197,12 +188,14 @@ class HMatrix:
         self.data = torch.empty(int(size.sum()), dtype=torch.float32, device=dev)
         self.off = torch.as_tensor(off, device=dev)
         self.rank = torch.as_tensor(rank, device=dev)
+        phase("storage_alloc")
         dense_ids = np.nonzero(rank < 0)[0].astype(np.int32)
         if len(dense_ids):
             ids_t = torch.as_tensor(dense_ids, device=dev)
             _lib.check(L.pq3d_hmat_dense_blocks(self.tables.data_ptr(), N, self.perm.data_ptr(), self.blk.data_ptr(),
                                                 ids_t.data_ptr(), len(dense_ids), float(mu), float(lam), hs,
                                                 self.data.data_ptr(), self.off.data_ptr(), st))
+        phase("dense_blocks")
         for (ids, UV, uvo_c, blk_c, kcap_c, rk_c) in factors.values():
             good = np.nonzero(rank[ids] >= 0)[0].astype(np.int32)   # positions inside the chunk
             if len(good) == 0:
@@ -214,6 +207,7 @@ class HMatrix:
                                                 out_off.data_ptr(), st))
         torch.cuda.synchronize(dev)
         del factors
+        phase("pack_factors")
         # low-rank bookkeeping and leaf lists
         lr_ids = np.nonzero(rank >= 0)[0].astype(np.int32)
         ranks = rank[lr_ids].astype(np.int64)
@@ -235,18 +229,20 @@ class HMatrix:
             info = np.zeros((1, 2), dtype=np.int64)
         self.t_info = torch.as_tensor(info, device=dev)
         self._make_sched(info)
+        # per leaf row cluster, the blocks whose row range covers it, in block order
         nl = leaves.shape[0]
         leaf_start = leaves[:, 0]
-        lists = [[] for _ in range(nl)]
-        for b in range(nb):
-            a = np.searchsorted(leaf_start, blocks[b, 0], side="left")
-            z = np.searchsorted(leaf_start, blocks[b, 1], side="left")
-            for q in range(a, z):
-                lists[q].append(b)
-        leaf_ptr = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.int64)
+        a = np.searchsorted(leaf_start, blocks[:, 0], side="left")
+        z = np.searchsorted(leaf_start, blocks[:, 1], side="left")
+        cnt = z - a
+        bl = np.repeat(np.arange(nb, dtype=np.int64), cnt)
+        q = np.repeat(a, cnt) + (np.arange(int(cnt.sum()), dtype=np.int64) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+        srt = np.argsort(q, kind="stable")
+        leaf_ptr = np.concatenate([[0], np.cumsum(np.bincount(q, minlength=nl))]).astype(np.int64)
         self.leaf = torch.as_tensor(np.ascontiguousarray(leaves), device=dev)
         self.leaf_ptr = torch.as_tensor(leaf_ptr, device=dev)
-        self.leaf_blocks = torch.as_tensor(np.concatenate([np.asarray(x, np.int32) for x in lists]), device=dev)
+        self.leaf_blocks = torch.as_tensor(bl[srt].astype(np.int32), device=dev)
+        phase("host_lists")
         self._make_struct()
         self.stats = {"N": N, "blocks": int(nb), "lowrank_blocks": int(len(lr_ids)),
                       "dense_blocks": int(len(dense_ids)), "aca_not_converged": int(np.sum(lowrank & (status != 0))),
@@ -254,6 +250,7 @@ class HMatrix:
                       "mean_rank": float(ranks.mean()) if len(ranks) else 0.0,
                       "bytes": int(self.data.numel() * 4), "dense_fp32_bytes": int(6 * N * N * 4),
                       "leaves": int(nl)}
+        self.build_phases = phases
 
     _ARRAYS = ("perm", "blk", "rank", "off", "data", "lr_ids", "t_info", "t_off", "leaf", "leaf_ptr", "leaf_blocks")
 
@@ -357,7 +354,7 @@ class BlockTree:
         self.nodelst, self.elelst = nodelst, elelst
         self.mu_, self.lambda_, self.mini_leaf, self.eta, self.tol, self.device = mu, lam, mini_leaf, eta, tol, device
         _, xg = element_frames(np.asarray(nodelst, dtype=np.float64), np.asarray(elelst, dtype=np.int64))
-        self.perm, self.blocks, self.leaves = build_partition(xg, 16, mini_leaf, eta)
+        self.perm, self.blocks, self.leaves = build_partition(xg, 16, mini_leaf, eta, device=device)
         self.H = None
         self.blocks_to_process = [tuple(b) for b in self.blocks]
 

@@ -35,7 +35,8 @@ def test_struct_layouts_match_header(tmp_path):
     import subprocess
     src = tmp_path / "probe.c"
     fields = {"pq3d_batch_sim": ("BatchSim", ["N", "B", "precision", "Tno", "rates", "nsplit", "tc_ctas", "cand", "vop", "K",
-                                              "ctrl", "V0", "eta", "fix_Tn", "attempt64", "N_total", "cell0", "base"]),
+                                              "ctrl", "V0", "eta", "fix_Tn", "attempt64", "N_total", "cell0", "base",
+                                              "fix_order", "fix_pos"]),
               "pq3d_dense_sim": ("DenseSim", ["N", "Tno", "fric", "a", "rake0", "rates", "cand", "K64", "K32", "ctrl",
                                               "V0", "eta", "fix_Tn", "ndepth", "P", "Parr", "dila"]),
               "pq3d_run_ctrl": ("RunCtrl", ["h", "time", "attempts", "max_steps", "err2_bits", "status", "accepted"]),

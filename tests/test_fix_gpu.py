@@ -1,0 +1,199 @@
+"""The fixed-point BF16x14 tensor-core product (pq3d_batch_gemm_bf16x14) and
+the batched stepper built on it: exact accumulation on the integer grid, the
+product against the NumPy model of its slices and against FP64, K-slice
+invariance, and slip tracking of the FP64 stepper in lockstep through a
+nucleation."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pyquake3d_gb300 import _lib, gf, mesh
+from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator, lockstep
+from tests import fixemul
+from tests.util import normwise_rel
+
+pytestmark = pytest.mark.gpu
+MU = 32038120320.0
+CS = 3464.0
+
+
+def _run_product(cuda, K, V, nsplit, xg=None):
+    """(nsplit, Bp, 3N, 2) float32 (hi, lo) partials (rows in the operator's
+    cell order: mesh order, or the compact order of xg), the error word and
+    the packed operator."""
+    L = _lib.load()
+    N, B = K.shape[1] // 2, V.shape[0]
+    Kt = torch.as_tensor(K, device=cuda).contiguous()
+    Vt = torch.as_tensor(V, device=cuda).contiguous()
+    P = PackedFixOperator(Kt, xg)
+    vop = torch.zeros(L.pq3d_batch_rhs_fix_bytes(N, B), dtype=torch.uint8, device=cuda)
+    st = torch.cuda.current_stream().cuda_stream
+    order = P.order.data_ptr() if P.order is not None else None
+    _lib.check(L.pq3d_batch_pack_rhs_fix(Vt.data_ptr(), N, B, order, vop.data_ptr(), st))
+    Bp = (B + 15) // 16 * 16
+    out = torch.full((nsplit, Bp, 3 * N, 2), float("nan"), dtype=torch.float32, device=cuda)
+    ws = torch.zeros(256, dtype=torch.uint8, device=cuda)
+    _lib.check(L.pq3d_batch_gemm_bf16x14(P.data.data_ptr(), vop.data_ptr(), N, B, nsplit, out.data_ptr(),
+                                         ws.data_ptr(), ws.numel(), st))
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), int(ws[:4].view(torch.int32).item()), P
+
+
+def _from_digits(rng, rows, cols, ndig, sign):
+    """Values whose fixed-point digits per (row, 1024-column chunk) are known:
+    leading digit +-126/127 (so the chunk exponent is e), the next two random
+    in [-127, 127], the rest zero.  Returns (X, digits, e)."""
+    nch = (cols + fixemul.CHUNK - 1) // fixemul.CHUNK
+    e = rng.integers(-4, 31, size=(rows, nch))
+    eb = np.repeat(e, fixemul.CHUNK, axis=1)[:, :cols]
+    d = [np.zeros((rows, cols), dtype=np.int64) for _ in range(ndig)]
+    d[0] = sign[:, None] * rng.integers(126, 128, size=(rows, cols))
+    d[1] = rng.integers(-127, 128, size=(rows, cols))
+    d[2] = rng.integers(-127, 128, size=(rows, cols))
+    X = sum(np.ldexp(d[p].astype(np.float64), eb - 7 - 8 * p) for p in range(ndig))
+    return X, d, e
+
+
+@pytest.mark.parametrize("nsplit", [1, 3])
+def test_fix_product_accumulates_exactly(cuda, nsplit):
+    """Digits chosen so that every level-0 sum of a chunk is near the 2^24 limit
+    of exact FP32 integers (1024 products of 126..127 x 126..127, one sign):
+    the tensor-core result must equal the exact sum of the slice products
+    (math.fsum of the exact integer chunk sums) to float-float precision.  An
+    accumulation that rounded at FP32 level would be off by ~1e-7."""
+    rng = np.random.default_rng(11)
+    N, B = 1024, 64                      # 2N = 2048 columns: two chunks
+    K, dK, eK = _from_digits(rng, 3 * N, 2 * N, fixemul.K_SLICES, rng.choice([-1, 1], size=3 * N))
+    V, dV, eV = _from_digits(rng, B, 2 * N, fixemul.V_SLICES, rng.choice([-1, 1], size=B))
+    out, err, _ = _run_product(cuda, K, V, nsplit)
+    assert err == 0
+    got = out[..., 0].astype(np.float64).sum(0)[:B] + out[..., 1].astype(np.float64).sum(0)[:B]
+    # exact: per chunk and slice pair an integer sum, scaled by a power of two
+    terms = []
+    for c in range(2):
+        sl = slice(c * 1024, (c + 1) * 1024)
+        for p in range(3):
+            for q in range(3):
+                S = dV[q][:, sl].astype(np.float64) @ dK[p][:, sl].T.astype(np.float64)   # exact: |S| < 2^24
+                assert np.abs(S).max() < 2 ** 24
+                terms.append(np.ldexp(S.astype(np.float64), eV[:, c][:, None] + eK[:, c][None, :] - 14 - 8 * (p + q)))
+    T = np.stack(terms, -1)
+    exact = np.array([[math.fsum(T[n, m]) for m in range(3 * N)] for n in range(B)])
+    scale = np.abs(T).sum(-1)
+    rel = np.abs(got - exact) / scale
+    assert rel.max() < 1e-12, rel.max()
+
+
+def _physical(cuda, N_side=(40, 20), B=8, seed=0):
+    nx, nz = N_side
+    nodes, tris = mesh.planar_fault(float(nx), float(nz), nx, nz)
+    K64, _ = gf.assemble_dense(nodes, tris, MU, MU, device=cuda)
+    N = tris.shape[0]
+    _, xg = mesh.element_frames(nodes, tris)
+    tabs = mesh.ensemble_tables(xg, nx * 1e3, nz * 1e3, B=B, seed=seed, v_nuc=1e-3)
+    return K64, tabs, N, xg
+
+
+@pytest.mark.parametrize("ordered", [False, True])
+def test_fix_product_matches_model_and_fp64(cuda, ordered):
+    """The physical operator (planar N=1,600, four chunks) against a slip-rate
+    deficit with a nucleation patch and magnitudes over 10 decades, in the
+    mesh order and in the compact cluster-tree order: equal to the NumPy model
+    of the slices to 1e-11 (the seventh accumulator, levels 3 and 4 at 2^-24
+    of the result, rounds in tensor memory: up to 512 additions per chunk at
+    2^-24 each), and to the FP64 product to 5e-9 normwise per run (the
+    operator's 32 bits per chunk; the FP32 operator is ~1e-8, BF16x6 ~1e-6)."""
+    K64, tabs, N, xg = _physical(cuda)
+    B = tabs.shape[0]
+    rng = np.random.default_rng(3)
+    V = np.zeros((B, 2 * N))
+    V[:, 0::2] = (tabs[:, :, 7] - 1e-9) * 10 ** rng.uniform(-3, 0, size=(B, N))
+    V[:, 1::2] = 1e-9 * rng.standard_normal((B, N))
+    K = K64.cpu().numpy()
+    out, err, P = _run_product(cuda, K, V, 4, xg if ordered else None)
+    assert err == 0
+    got = (out[..., 0].astype(np.float64) + out[..., 1]).sum(0)[:B]
+    if ordered:
+        order = P.order.cpu().numpy()
+        assert sorted(order.tolist()) == list(range(N))
+        rows = (3 * order[:, None] + np.arange(3)).ravel()
+        cols = (2 * order[:, None] + np.arange(2)).ravel()
+        model = np.empty((B, 3 * N))
+        model[:, rows] = fixemul.product(K[np.ix_(rows, cols)], V[:, cols])
+        g = np.empty_like(got)
+        g[:, rows] = got
+        got = g
+    else:
+        model = fixemul.product(K, V)
+    ref = V @ K.T
+    for r in range(B):
+        assert normwise_rel(model[r], got[r]) < 1e-11, r
+        assert normwise_rel(ref[r], got[r]) < 5e-9, r
+
+
+def test_fix_product_k_slices_and_padding(cuda):
+    """nsplit 1, 5 and 19 (slices that cut chunks) agree to the rounding of
+    the levels-3-4 accumulator; padded runs and padded rows come out zero."""
+    rng = np.random.default_rng(4)
+    N, B = 700, 5
+    K = rng.standard_normal((3 * N, 2 * N)) * 1e8
+    V = rng.standard_normal((B, 2 * N)) * 10 ** rng.uniform(-9, 0, size=(B, 2 * N))
+    res = {}
+    for ns in (1, 5, 19):
+        out, err, _ = _run_product(cuda, K, V, ns)
+        assert err == 0
+        assert np.all(out[:, B:] == 0.0)
+        res[ns] = (out[..., 0].astype(np.float64) + out[..., 1]).sum(0)[:B]
+    ref = V @ K.T
+    for r in range(B):
+        # the seventh accumulator (levels 3-4) rounds in tensor memory, in a
+        # sequence that the K slices change: ~2^-39 of the result
+        assert normwise_rel(res[1][r], res[5][r]) < 5e-11
+        assert normwise_rel(res[1][r], res[19][r]) < 5e-11
+        assert normwise_rel(ref[r], res[1][r]) < 1e-8
+
+
+def test_fix_rejects_bad_arguments(cuda):
+    L = _lib.load()
+    buf = torch.zeros(1 << 16, dtype=torch.uint8, device=cuda)
+    p = buf.data_ptr()
+    assert L.pq3d_batch_gemm_bf16x14(p, p, 16, 65, 1, p, p, 256, None) == _lib.PQ3D_ERR_ARG   # B > 64
+    assert L.pq3d_batch_gemm_bf16x14(p, p, 16, 16, 0, p, p, 256, None) == _lib.PQ3D_ERR_ARG   # nsplit 0
+    assert L.pq3d_batch_gemm_bf16x14(p, p, 16, 16, 2, p, p, 16, None) == _lib.PQ3D_ERR_ARG    # workspace
+    assert L.pq3d_batch_pack_rhs_fix(p, 16, 65, None, p, None) == _lib.PQ3D_ERR_ARG
+
+
+def _rates64(K64, ens):
+    """K.v' in FP64 for the ensemble's current slip rates (cell order)."""
+    v = torch.empty((ens.B, 2 * ens.N), dtype=torch.float64, device=K64.device)
+    v[:, 0::2] = ens.t["slipv1"] - 1e-9 * ens.t["cos_rake0"]
+    v[:, 1::2] = ens.t["slipv2"] - 1e-9 * ens.t["sin_rake0"]
+    return (K64 @ v.T).T.cpu().numpy()
+
+
+def test_batched_fix_tracks_fp64_through_nucleation(cuda):
+    """Lockstep with the FP64 batched stepper (same step sizes and decisions)
+    on planar N=1,600, 8 runs with nucleation patches, 120 accepted steps:
+    the BF16x14 product with the FP64 attempt stays within 2e-6 in slip of the
+    FP64 stepper (NumPy model of the same arithmetic: 2.3e-7 at step 80; the
+    BF16x6 product leaves 1e-5 within ~45 steps here)."""
+    K64, tabs, N, xg = _physical(cuda)
+    kw = dict(mu=MU, Cs=CS, max_steps=120)
+    ref = Ensemble(K64, tabs, precision="fp64", **kw)
+    fix = Ensemble(PackedFixOperator(K64, xg), tabs, precision="bf16x14", attempt="fp64", **kw)
+    # the ensemble's own product (packed v' in the compact order), read back in
+    # the cell order, against FP64 on the same state
+    L = _lib.load()
+    _lib.check(L.pq3d_batch_gemm_bf16x14(fix.K.data_ptr(), fix.vop.data_ptr(), N, fix.B, fix.nsplit,
+                                         fix.t["rates"].data_ptr(), fix.ws.data_ptr(), fix.ws.numel(),
+                                         torch.cuda.current_stream().cuda_stream))
+    got = fix.traction_rates().cpu().numpy()
+    for ref_r, got_r in zip(_rates64(K64, ref), got):
+        assert normwise_rel(ref_r, got_r) < 5e-9
+    res = lockstep(ref, {"bf16x14": fix}, 120, bar=2e-6)
+    r = res["bf16x14"]
+    assert r["failed_runs"] == 0 and fix.error_word() == 0
+    assert r["steps_within"] >= 120, r

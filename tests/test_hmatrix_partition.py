@@ -1,6 +1,6 @@
-"""The H-matrix partition (cluster tree + block tree) against the oracle's
-restatement of the reference rules and against the reference's own
-partition recorded in tests/golden/hmatrix_small.npz."""
+"""The H-matrix partition (cluster tree + block tree, built on the device)
+against the oracle's restatement of the reference rules and against the
+reference's own partition recorded in tests/golden/hmatrix_small.npz."""
 import os
 
 import numpy as np
@@ -19,15 +19,16 @@ def _as_sets(perm, blocks):
     return [(tuple(sorted(perm[b[0]:b[1]])), tuple(sorted(perm[b[2]:b[3]])), bool(b[4])) for b in blocks]
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("which,params", [("planar", (16, 32)), ("rough", (16, 32)), ("rough", (64, 64)),
-                                          ("planar", (8, 16))])
-def test_partition_matches_oracle(which, params):
+                                          ("planar", (8, 16)), ("rough", (1, 1))])
+def test_partition_matches_oracle(cuda, which, params):
     if which == "planar":
         nodes, tris = mesh.planar_fault(30.0, 15.0, 30, 15)
     else:
         nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
     _, xg = mesh.element_frames(nodes, tris)
-    perm, blocks, leaves = build_partition(xg, params[0], params[1])
+    perm, blocks, leaves = build_partition(xg, params[0], params[1], device=cuda)
     got = _as_sets(perm, blocks)
     ref = [(tuple(sorted(r)), tuple(sorted(c)), lr) for r, c, lr in ohm.leaf_blocks(xg, params[0], params[1])]
     assert got == ref
@@ -84,3 +85,19 @@ def test_low_rank_row_schedule_and_groups():
     for a, n in zip(q0, g):
         rows = sched[a:a + n]
         assert np.all(np.diff(rows) == 1) and len(set(block_of[rows])) == 1
+
+
+@pytest.mark.gpu
+def test_partition_reproduces_reference_golden(cuda):
+    """The device partition on the mesh of the reference's own H-matrix
+    (hmatrix_small.npz, min_size 16, mini_leaf 32): the same leaf blocks, in
+    the same depth-first order, with the same ACA/dense split."""
+    g = np.load(GOLDEN)
+    _, xg = mesh.element_frames(g["nodes"], g["tris"])
+    perm, blocks, _ = build_partition(xg, 16, int(g["mini_leaf"]), device=cuda)
+    assert len(blocks) == len(g["row_ptr"]) - 1
+    for b in range(len(blocks)):
+        r0, r1, c0, c1, lr = blocks[b]
+        assert sorted(perm[r0:r1]) == list(g["rows"][g["row_ptr"][b]:g["row_ptr"][b + 1]])
+        assert sorted(perm[c0:c1]) == list(g["cols"][g["col_ptr"][b]:g["col_ptr"][b + 1]])
+        assert bool(lr) == bool(g["aca"][b])

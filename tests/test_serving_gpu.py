@@ -54,3 +54,27 @@ def test_serving_completes_and_result_alone_equals_mix(cuda):
     alone.iterate(r.attempts + 5)
     c = alone.read_ctrl()[0]
     assert c.steps == r.steps and c.attempts == r.attempts and c.time == r.sim_time
+
+
+def test_serving_hmatrix_mesh_result_alone_equals_mix(cuda):
+    """The same with the second mesh (N = 384) served through an H-matrix
+    (dense_max_n below its size): its runs step through the masked H-matrix
+    product (pq3d_hmat_apply_masked, free slots and finished runs skipped) in
+    the mix, and a request replayed alone on the same H-matrix takes the same
+    steps and attempts and reaches the same simulated time, bit for bit."""
+    meshes = _meshes()
+    srv = Server(meshes, mu=MU, lam=MU, cs=3464.0, slots=4, budget_bytes=50e9, graph_iters=8, max_steps=400,
+                 device=cuda, dense_max_n=300, hmat_kw=dict(min_size=32, mini_leaf=32, eta=2.0, tol=1e-6))
+    assert srv.kind[0] == "dense_bf16x6" and srv.kind[1] == "hmatrix"
+    reqs = _requests(meshes, 10, seed=3)
+    res = srv.run(reqs, time_limit_s=120)
+    assert res["completed"] == 10 and res["failed"] == 0
+    hreqs = [r for r in reqs if r.mesh == 1]
+    assert len(hreqs) >= 3
+    H = srv.ens[1].hmat
+    for r in hreqs[:3]:
+        alone = Ensemble(H, r.table[None], mu=MU, Cs=3464.0, precision="hmat", t_end=r.span_s, max_steps=400)
+        alone.iterate(r.attempts + 5)
+        c = alone.read_ctrl()[0]
+        assert c.status == 0 and c.active == 0
+        assert c.steps == r.steps and c.attempts == r.attempts and c.time == r.sim_time, r.rid

@@ -51,3 +51,32 @@ def test_noalloc_rejects_n_beyond_its_fixed_scratch(cuda):
                                        dummy.data_ptr(), None, torch.cuda.current_stream().cuda_stream)
     assert rc == _lib.PQ3D_ERR_ARG
     assert b"32768" in L.pq3d_last_error()
+
+
+def test_noalloc_row_range_empty_range_and_halfspace(cuda):
+    """A receiver-row range [row0, row1) inside the mesh (a caller's K64 then
+    holds those rows only) equals the same rows of the workspace variant;
+    row0 == row1 writes nothing; the half space is refused with
+    PQ3D_ERR_UNSUPPORTED (the fixed array holds the full-space tables only)."""
+    L = _lib.load()
+    nodes, tris = mesh.rough_fault(16.0, 8.0, 16, 16, seed=5, ratio=5e-3)
+    N = tris.shape[0]
+    nodes_t, tris_t = gf.mesh_to_device(nodes, tris, cuda)
+    ref64, _ = gf.assemble_dense(nodes, tris, MU, MU, device=cuda)
+    st = torch.cuda.current_stream().cuda_stream
+    r0, r1 = 37, 301
+    K64 = torch.full((3 * (r1 - r0), 2 * N), float("nan"), dtype=torch.float64, device=cuda)
+    rc = L.pq3d_assemble_dense_noalloc(nodes_t.data_ptr(), tris_t.data_ptr(), N, r0, r1, MU, MU, 0, K64.data_ptr(),
+                                       None, st)
+    assert rc == _lib.PQ3D_OK, L.pq3d_last_error()
+    torch.cuda.synchronize()
+    assert normwise_rel(ref64[3 * r0:3 * r1].cpu().numpy(), K64.cpu().numpy(), axis=1) < 1e-10
+    sentinel = torch.full((6,), 7.0, dtype=torch.float64, device=cuda)
+    rc = L.pq3d_assemble_dense_noalloc(nodes_t.data_ptr(), tris_t.data_ptr(), N, 5, 5, MU, MU, 0,
+                                       sentinel.data_ptr(), None, st)
+    assert rc == _lib.PQ3D_OK
+    torch.cuda.synchronize()
+    assert torch.all(sentinel == 7.0)
+    rc = L.pq3d_assemble_dense_noalloc(nodes_t.data_ptr(), tris_t.data_ptr(), N, 0, N, MU, MU, 1, K64.data_ptr(),
+                                       None, st)
+    assert rc == _lib.PQ3D_ERR_UNSUPPORTED
