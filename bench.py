@@ -345,7 +345,9 @@ def bench_ours(args):
         out["e2e"] = {"value": 6.0 * N * N * e2e_steps / t_e, "unit": "GF entries/s",
                       "h2d_bytes_per_step": int(nodes.nbytes + tris.astype(np.int64).nbytes),
                       "d2h_bytes_per_step": int(host64.numel() * 8), "steps": e2e_steps,
-                      "path": "pq3d_assemble_dense_host (C-ABI): mesh copied in, the kernel stores the FP64 operator straight into the pinned host buffer (mapped)"}
+                      "path": "pq3d_assemble_dense_host (C-ABI): mesh copied in, the kernel stores the FP64 operator straight into the pinned host buffer (mapped)",
+                      "outputs": "the FP64 operator only (the reference's dense path produces FP64 only); the "
+                                 "device-timed value also writes the FP32 copy"}
         del host64
         # -- stepping on the assembled operator
         out["stepping"] = bench_stepping(torch, dev, K64, K32, nodes, tris, Lkm, Wkm, args, dict(peaks, fp64_tflops=fp64))

@@ -313,3 +313,24 @@ def test_mixed_attempt_in_range_through_stage_overshoot(cuda, rows, h):
     assert np.all(np.abs(c32 - c64) <= 1e-6 * inc + 1e-13 * np.abs(y0))
     assert k32.accepted == k64.accepted
     assert abs(k32.h - k64.h) <= 1e-4 * k64.h
+
+
+def test_batched_fp64_matches_single_simulation_n10000(cuda):
+    """The batched workload's mesh and runs (planar 100 x 50 km, N = 10,000,
+    per-run friction draws with nucleation patches): the FP64 batched stepper
+    against the single-simulation FP64 stepper run by run over 40 accepted
+    steps, state and slip to 1e-9."""
+    nodes, tris = mesh.planar_fault(100.0, 50.0, 100, 50)
+    _, xg = mesh.element_frames(nodes, tris)
+    tabs = mesh.ensemble_tables(xg, 100e3, 50e3, B=4, seed=0, v_nuc=1e-3)
+    K64, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
+    ens = Ensemble(K64, tabs, mu=MU, Cs=CS, precision="fp64", max_steps=40)
+    ens.iterate(400)
+    ctrl = ens.read_ctrl()
+    for r in (0, 3):
+        assert ctrl[r].steps == 40 and ctrl[r].status == 0
+        one = DenseDeviceSim(K64, initial_state(tabs[r], 1e-6, 1e-9), mu=MU, Cs=CS, V0=1e-6, Vpl=1e-9)
+        one.step(40)
+        for k in ("slip1", "state", "Tt1o", "Tno"):
+            assert normwise_rel(one.t[k].cpu().numpy(), ens.t[k][r].cpu().numpy()) < 1e-9, (r, k)
+        assert np.isclose(ctrl[r].time, one.read_ctrl().time, rtol=1e-9)
