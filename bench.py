@@ -385,7 +385,7 @@ def batched_summary(bt):
     acc = bt.get("accuracy_vs_fp64", {})
     plain = bt["plain_fp64_single"]["rk_stages_per_s"]
     arms = {}
-    for key, prec, acc_key in (("bf16x14_fp64_attempt", "bf16x14", "bf16x14_fp64_attempt"),
+    for key, prec, acc_key in (("bf16x18_fp64_attempt", "bf16x18", "bf16x18_fp64_attempt"),
                                ("bf16x6_mixed_attempt", "bf16x6", "bf16x6"),
                                ("fp32_mixed_attempt", "fp32", "fp32")):
         if prec not in bt:
@@ -514,7 +514,7 @@ def bench_batched(torch, dev, args, peaks):
     1 km squares), per-run friction draws (seed 0).  Arms, each against the
     plain FP64 single-simulation stepper on the same mesh:
       bf16x6   three-piece BF16 product on tcgen05, FP32 mixed attempt (fast);
-      bf16x14  exact fixed-point slices on tcgen05 (the FP64 product to ~1e-9
+      bf16x18  exact fixed-point slices on tcgen05 (the FP64 product to ~1e-9
                normwise), FP64 attempt: the arm that tracks the FP64
                trajectory;
       fp32     FP32 operator on CUDA cores, FP32 mixed attempt."""
@@ -536,16 +536,16 @@ def bench_batched(torch, dev, args, peaks):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     shape = autotune.tune_bf16x6(P, B)
-    shape_fix = autotune.tune_bf16x14(PF, min(B, 64))
+    shape_fix = autotune.tune_bf16x18(PF, min(B, 64))
     tune_s = time.perf_counter() - t0
     res = {"workload": "batched ensemble: planar %dx%d km, N=%d, B=%d runs, per-run a-b, Dc, sigma_n, nucleation "
                        "patch from seed 0; RK stages = 7 x attempted steps, all runs" % (Lkm, Wkm, N, B),
            "N": N, "B": B}
     out = {}
     st = torch.cuda.current_stream(dev).cuda_stream
-    arms = [("bf16x6", P, "mixed"), ("bf16x14", PF, "fp64"), ("fp32", K32, "mixed")]
+    arms = [("bf16x6", P, "mixed"), ("bf16x18", PF, "fp64"), ("fp32", K32, "mixed")]
     for prec, K, attempt in arms:
-        if prec == "bf16x14" and B > 64:
+        if prec == "bf16x18" and B > 64:
             continue
         ens = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, attempt=attempt,
                        nsplit=args.nsplit if prec == "bf16x6" else None)
@@ -569,7 +569,7 @@ def bench_batched(torch, dev, args, peaks):
                      "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
                      "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
                      "clocks": clk.summary(), "error_word": ens.error_word() if prec != "fp32" else 0}
-        if prec in ("bf16x6", "bf16x14"):
+        if prec in ("bf16x6", "bf16x18"):
             # the tensor-core product alone, CUDA events over repeated launches
             if prec == "bf16x6":
                 launch = lambda: L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
@@ -580,13 +580,13 @@ def bench_batched(torch, dev, args, peaks):
                 note = "packed BF16 3-piece operator streamed once per product"
                 fnote = "6 BF16 products x 2 x 3N x 2N x Bp"
             else:
-                launch = lambda: L_.pq3d_batch_gemm_bf16x14(PF.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
+                launch = lambda: L_.pq3d_batch_gemm_bf16x18(PF.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
                                                             ens.t["rates"].data_ptr(), ens.ws.data_ptr(),
                                                             ens.ws.numel(), st)
                 op_bytes = PF.data.numel()
-                flops = 14 * 2.0 * (3 * N) * (2 * N) * ens.Bp
+                flops = 18 * 2.0 * (3 * N) * (2 * N) * ((B + 31) // 32 * 32)
                 note = "packed fixed-point operator (4 BF16 slices, 8 B per entry) streamed once per product"
-                fnote = "14 BF16 slice products x 2 x 3N x 2N x Bp"
+                fnote = "18 BF16 slice products x 2 x 3N x 2N x runs (rounded up to 32)"
             for _ in range(3):
                 launch()
             nl = 20
@@ -651,8 +651,8 @@ def batched_accuracy(torch, K64, K32, P, PF, tabs, max_steps, every=5):
     pert[:, :, 7] *= 1.0 + 1e-12 * np.random.default_rng(7).choice([-1.0, 1.0], size=pert[:, :, 7].shape)
     kw = dict(mu=MU, Cs=3464.0, max_steps=max_steps)
     ref = Ensemble(K64, tabs, precision="fp64", **kw)
-    others = {"bf16x14_fp64_attempt": Ensemble(PF, tabs, precision="bf16x14", attempt="fp64", **kw),
-              "bf16x14_mixed_attempt": Ensemble(PF, tabs, precision="bf16x14", attempt="mixed", **kw),
+    others = {"bf16x18_fp64_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="fp64", **kw),
+              "bf16x18_mixed_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="mixed", **kw),
               "bf16x6": Ensemble(P, tabs, precision="bf16x6", **kw),
               "fp32": Ensemble(K32, tabs, precision="fp32", **kw),
               "fp64_perturbed_1e-12": Ensemble(K64, pert, precision="fp64", **kw)}
@@ -899,7 +899,7 @@ def profile_case(case):
                  planar 60x50 km, N=6,000, B=64 (12 iterations)
     f32_gemm     batched iterations with the plain FP32 product on CUDA cores, same
                  mesh and runs (6 iterations)
-    fix_gemm     batched iterations with the fixed-point BF16x14 product and the FP64
+    fix_gemm     batched iterations with the fixed-point BF16x18 product and the FP64
                  attempt, same mesh and runs (6 iterations)
     aca          H-matrix build (partition, ACA, dense blocks), rough 100x25 km, N=20,000,
                  leaf 64, eta 2, tol 1e-4 (one ACA launch over all low-rank blocks)"""
@@ -947,12 +947,20 @@ def profile_case(case):
         torch.cuda.empty_cache()
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
-        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x14", attempt="fp64", nsplit=6).iterate(6)
+        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x18", attempt="fp64", nsplit=6).iterate(6)
     elif case == "aca":
         from pyquake3d_gb300.hmatrix import HMatrix
         nodes, tris = mesh.rough_fault(100.0, 25.0, 200, 50, seed=0)
         H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4)
-        print(json.dumps({"stats": H.stats, "phases": H.build_phases}))
+        # GF pair evaluations of the ACA: per iteration one residual row (n
+        # sources) and one column (m receivers); rank + 1 iterations per block
+        b = H.blocks_host
+        rk = H.rank.cpu().numpy()
+        lr = np.nonzero(b[:, 4] == 1)[0]
+        m, n = b[lr, 1] - b[lr, 0], b[lr, 3] - b[lr, 2]
+        pairs = int(np.sum((np.maximum(rk[lr], 0) + 1) * (m + n)))
+        print(json.dumps({"stats": H.stats, "phases": H.build_phases, "aca_pair_evaluations": pairs,
+                          "aca_pairs_per_s": pairs / H.build_phases["aca"]}))
     else:
         raise SystemExit("unknown --case " + case)
     torch.cuda.synchronize()

@@ -232,12 +232,13 @@ typedef struct pq3d_run_ctrl {
                                   FP32 accumulation in tensor memory, K slices added in
                                   float-float */
 #define PQ3D_BATCH_HMAT 3      /* H-matrix product (pq3d_hmat_apply); K points to a host pq3d_hmat */
-#define PQ3D_BATCH_BF16X14 4   /* operator (32 bits) and v' (40 bits) as exact fixed-point BF16 slices,
-                                  one exponent per 1024-column chunk; 14 slice products on tcgen05
-                                  tensor cores with exact accumulation per chunk, chunks added in
-                                  float-float: the FP64 product to ~2^-32 of each chunk's largest
-                                  operator entry (static) and ~2^-40 of its largest v' (dynamic).
-                                  B <= 64, no row shards */
+#define PQ3D_BATCH_BF16X18 4   /* operator (32 bits per row and 1024-column chunk) and v' (48 bits per
+                                  run and 256-column span) as exact fixed-point BF16 slices; the 18
+                                  slice products down to 2^-40 of the leading one on tcgen05 tensor
+                                  cores, exact accumulation per span, spans added in float-float:
+                                  the FP64 product to ~2^-32 of each chunk's largest operator entry
+                                  (static) and ~2^-40 of each span's largest v' (dynamic).  B <= 64,
+                                  no row shards */
 
 /* Device state of B simulations sharing one mesh.  Arrays are run-major
  * [B][N] FP64 unless stated.  Same fields and units as pq3d_dense_sim. */
@@ -251,9 +252,9 @@ typedef struct pq3d_batch_sim {
                               (nsplit = 1) for FP64 and HMAT; FP64 [nsplit][Bp][3N] for FP32 (the K
                               slices' sums, added in slice order by the stepper); for BF16X6 FP32
                               [nsplit][Bp][3N], the K slices' tensor-memory sums, added in
-                              float-float by the stepper; for BF16X14 float2 (hi, lo)
+                              float-float by the stepper; for BF16X18 float2 (hi, lo)
                               [nsplit][Bp][3N], float-float K-slice sums */
-    int32_t nsplit;        /* K-slices of the operator product: >= 1 for BF16X6 and BF16X14, 1..64 for
+    int32_t nsplit;        /* K-slices of the operator product: >= 1 for BF16X6 and BF16X18, 1..64 for
                               FP32, 1 for FP64 and HMAT */
     int32_t tc_ctas;       /* BF16X6: CTAs per SM of the tensor-core product, 0 (= 2) or 1..3; the launch
                               shape only, results do not depend on it */
@@ -261,10 +262,10 @@ typedef struct pq3d_batch_sim {
     void *vop;             /* operator-product right-hand side of all runs, padded to Bp = B rounded up
                               to 16 runs (extra runs zero): FP64 [Bp][2N], FP32 [Bp][2N], for
                               BF16X6 the packed pieces (pq3d_batch_rhs_bytes, zero-initialised),
-                              for BF16X14 the packed fixed-point slices (pq3d_batch_rhs_fix_bytes) */
+                              for BF16X18 the packed fixed-point slices (pq3d_batch_rhs_fix_bytes) */
     const void *K;         /* operator: FP64 (3N)x(2N) for FP64, FP32 (3N)x(2N) for FP32, the
                               packed BF16 pieces (pq3d_batch_pack_operator) for BF16X6, the packed
-                              fixed-point slices (pq3d_batch_pack_operator_fix) for BF16X14, a host
+                              fixed-point slices (pq3d_batch_pack_operator_fix) for BF16X18, a host
                               pointer to a pq3d_hmat for HMAT (v' then FP64 [Bp][2N]) */
     pq3d_run_ctrl *ctrl;   /* [B] */
     double V0, Vpl, eta;
@@ -285,7 +286,7 @@ typedef struct pq3d_batch_sim {
      * FP32 [PQ3D_BATCH_BASE_FIELDS][B][N], written by pq3d_batch_prepare and
      * by the update of every accepted step.  NULL (unused) otherwise. */
     float *base;
-    /* BF16X14: the cell order of the fixed-point product (device int64, NULL =
+    /* BF16X18: the cell order of the fixed-point product (device int64, NULL =
      * identity): fix_order[p] = cell at position p of the packed operator's
      * rows and columns, fix_pos[cell] = its position.  A spatially compact
      * order (pq3d_hmat_cluster_order) keeps each 1024-column chunk, whose
@@ -318,7 +319,7 @@ int pq3d_batch_gemm_bf16x6(const void *Kpacked, const void *Vpacked, int64_t N, 
  * or tensor memory does not fit them), plan[1] = pipeline stages per CTA. */
 int pq3d_batch_gemm_bf16x6_plan(int B, int ctas_per_sm, int32_t *plan);
 
-/* Packed operator of the fixed-point tensor-core product (BF16X14): per operator
+/* Packed operator of the fixed-point tensor-core product (BF16X18): per operator
  * row and 1024-column chunk one exponent e (|K| < 2^e over the chunk) and four
  * BF16 slices d_p 2^(e-7-8p), |d_p| <= 128, stored as [3N/128 tiles][2N/32
  * blocks][4][128 x 32] shared-memory images.  Bytes, and the packing kernel
@@ -329,17 +330,20 @@ size_t pq3d_batch_operator_fix_bytes(int64_t N);
  * positions 3p + c and 2q + s, and the product's outputs come in that row
  * order. */
 int pq3d_batch_pack_operator_fix(const double *K64, int64_t N, const int64_t *order, void *Kpacked, void *stream);
-/* Bytes of the packed fixed-point right-hand side for B <= 64 runs, and its
- * packing from v ([B][2N] FP64 device array, v[r][2j + s]): per run and chunk
- * five slices (40 bits of the chunk's largest |v|).  The batched stepper packs
- * v' itself; this entry serves the product alone. */
+/* Bytes of the packed fixed-point right-hand side for B <= 64 runs (padded to
+ * 32 or 64 runs), and its packing from v ([B][2N] FP64 device array,
+ * v[r][2j + s]): per run and 256-column span six slices (48 bits of the span's
+ * largest |v|).  The batched stepper packs v' itself; this entry serves the
+ * product alone. */
 size_t pq3d_batch_rhs_fix_bytes(int64_t N, int B);
 int pq3d_batch_pack_rhs_fix(const double *v, int64_t N, int B, const int64_t *order, void *Vpacked, void *stream);
 /* The fixed-point tensor-core product alone: out[((s*Bp + n)*3N + m)*2 + {0,1}]
  * = (hi, lo) FP32 with hi + lo = K slice s of sum_k K[m][k] v[n][k] (s < nsplit,
  * Bp = B rounded up to 16, B <= 64), the exact product of the slices up to
- * ~2^-44 relative.  One CTA per SM; nsplit sets the order of the slice sums. */
-int pq3d_batch_gemm_bf16x14(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
+ * ~2^-44 relative.  One CTA per SM, six wide tcgen05.mma per 16-column step
+ * (one per operator slice and run of right-hand-side slices, accumulating in
+ * tensor-memory slots by level); nsplit sets the order of the slice sums. */
+int pq3d_batch_gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
                             void *workspace, size_t workspace_bytes, void *stream);
 /* Device workspace bytes of one batched iteration (GEMM split-K partials live in
  * sim->rates; this is what the tensor-core product needs besides). */
@@ -416,7 +420,7 @@ typedef struct pq3d_hmat {
  * one count per level back to the host (synchronises `stream`). */
 /* The cluster tree alone: perm[N] (device) = the depth-first leaf order of
  * the bisection tree with leaves of <= min_size points -- a spatially compact
- * order of the elements (the BF16X14 product's fix_order). */
+ * order of the elements (the BF16X18 product's fix_order). */
 int pq3d_hmat_cluster_order(const double *xg, int64_t N, int min_size, int64_t *perm, int32_t *depth, void *stream);
 int pq3d_hmat_partition(const double *xg, int64_t N, int min_size, int mini_leaf, double eta, int64_t *perm,
                         int64_t *leaves, int64_t *n_leaves, int64_t *blocks, int64_t cap_blocks, int64_t *n_blocks,

@@ -80,7 +80,7 @@ PQ3D_BATCH_FP64 = 0
 PQ3D_BATCH_FP32 = 1
 PQ3D_BATCH_BF16X6 = 2
 PQ3D_BATCH_HMAT = 3
-PQ3D_BATCH_BF16X14 = 4
+PQ3D_BATCH_BF16X18 = 4
 PQ3D_BATCH_BASE_FIELDS = 24   # floats per cell and run of pq3d_batch_sim.base
 
 
@@ -121,7 +121,7 @@ _SIGS = {
     "pq3d_batch_pack_operator_fix": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
     "pq3d_batch_rhs_fix_bytes": (c_size, [c_i64, c_int]),
     "pq3d_batch_pack_rhs_fix": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p]),
-    "pq3d_batch_gemm_bf16x14": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size,
+    "pq3d_batch_gemm_bf16x18": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_size,
                                         c_void_p]),
     "pq3d_batch_workspace_bytes": (c_size, [ctypes.POINTER(BatchSim)]),
     "pq3d_gf_setup": (c_int, [c_void_p, c_void_p, c_i64, c_int, c_void_p, c_size, c_void_p]),

@@ -228,7 +228,7 @@ class _BenchFix:
         self.ws = torch.zeros(256, dtype=torch.uint8, device=dev)
 
     def launch(self, nsplit: int):
-        _lib.check(self.L.pq3d_batch_gemm_bf16x14(self.op.data.data_ptr(), self.vop.data_ptr(), self.N, self.B,
+        _lib.check(self.L.pq3d_batch_gemm_bf16x18(self.op.data.data_ptr(), self.vop.data_ptr(), self.N, self.B,
                                                   nsplit, self.out.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
                                                   self.stream.cuda_stream))
 
@@ -249,7 +249,7 @@ class _BenchFix:
         return best
 
 
-def tune_bf16x14(op, B: int) -> dict:
+def tune_bf16x18(op, B: int) -> dict:
     """K slices of the fixed-point product on the packed operator ``op``:
     {"nsplit", "tuned"}, tuned at TUNE_RUNS runs and cached per mesh size."""
     N, dev = op.N, op.device

@@ -70,7 +70,7 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &p0, __nv_bfloat16
 template <bool kExactV>
 __device__ __forceinline__ void write_vop(const pq3d_batch_sim &S, int r, int64_t i, double v1, double v2)
 {
-    if (S.precision == PQ3D_BATCH_BF16X14) return;   // packed per chunk after the update (fx::pack_rhs_from_state)
+    if (S.precision == PQ3D_BATCH_BF16X18) return;   // packed per chunk after the update (fx::pack_rhs_from_state)
     const int Bp = padded_runs(S.B);
     const int64_t o = (int64_t)r * 2 * total_cells(S) + 2 * (S.cell0 + i);
     if (S.precision == PQ3D_BATCH_FP64 || S.precision == PQ3D_BATCH_HMAT) {
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             // slice (added here in float-float, slice order), the other mixed
             // products one FP64 value
             FF q[3];
-            if (S.precision == PQ3D_BATCH_BF16X14) {   // float-float partials per K slice
+            if (S.precision == PQ3D_BATCH_BF16X18) {   // float-float partials per K slice
                 const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
                 const float2 *pr = (const float2 *)S.rates + (int64_t)r * 3 * N + 3 * pos;
                 const int64_t sstride = (int64_t)Bp * 3 * N;
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
         } else {
             double q0 = 0.0, q1 = 0.0, q2 = 0.0;
-            if (S.precision == PQ3D_BATCH_BF16X14) {   // float-float K-slice partials, added in FP64
+            if (S.precision == PQ3D_BATCH_BF16X18) {   // float-float K-slice partials, added in FP64
                 const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
                 for (int s = 0; s < S.nsplit; ++s) {
                     const float2 *p = (const float2 *)S.rates + ((int64_t)s * Bp + r) * 3 * N + 3 * pos;
@@ -351,7 +351,11 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             const double dsig = S.fix_Tn ? S.normal_loading[idx] : q2 + S.normal_loading[idx];
             const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], q0, q1, dsig,
                          0.0, 0.0};
-            dp_attempt(c, S.V0, S.eta, hs, y, yo, m1, m2);
+            // the FP64 precision keeps the reference formula (it is the arm the
+            // others are compared with); the FP64 attempt of the mixed
+            // products (attempt64) takes the reciprocal form
+            if (S.precision == PQ3D_BATCH_FP64) dp_attempt<false>(c, S.V0, S.eta, hs, y, yo, m1, m2);
+            else dp_attempt<true>(c, S.V0, S.eta, hs, y, yo, m1, m2);
         }
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
     }
@@ -478,9 +482,9 @@ static int check_sim(const pq3d_batch_sim *S)
 {
     PQ3D_REQUIRE(S && S->N > 0 && S->B > 0 && S->B <= 1024 && S->ctrl && S->K && S->vop && S->rates && S->cand,
                  "pq3d_batch: bad simulation structure");
-    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_BF16X14, "pq3d_batch: bad precision");
-    if (S->precision == PQ3D_BATCH_BF16X14) {
-        PQ3D_REQUIRE(S->B <= fx::kMaxRuns, "pq3d_batch: the BF16X14 product takes at most %d runs", fx::kMaxRuns);
+    PQ3D_REQUIRE(S->precision >= PQ3D_BATCH_FP64 && S->precision <= PQ3D_BATCH_BF16X18, "pq3d_batch: bad precision");
+    if (S->precision == PQ3D_BATCH_BF16X18) {
+        PQ3D_REQUIRE(S->B <= fx::kMaxRuns, "pq3d_batch: the BF16X18 product takes at most %d runs", fx::kMaxRuns);
         PQ3D_REQUIRE((S->fix_order == nullptr) == (S->fix_pos == nullptr),
                      "pq3d_batch: fix_order and fix_pos are given together");
     }
@@ -516,7 +520,7 @@ extern "C" size_t pq3d_batch_workspace_bytes(const pq3d_batch_sim *sim)
 {
     if (sim && sim->precision == PQ3D_BATCH_HMAT)
         return pq3d_hmat_workspace_bytes((const pq3d_hmat *)sim->K, padded_runs(sim->B));
-    if (sim && sim->precision == PQ3D_BATCH_BF16X14) return 256;
+    if (sim && sim->precision == PQ3D_BATCH_BF16X18) return 256;
     if (!sim || sim->precision != PQ3D_BATCH_BF16X6) return 0;
     return pq3d::tc::gemm_bf16x6_workspace_bytes(sim->N, padded_runs(sim->B), sim->nsplit);
 }
@@ -530,7 +534,7 @@ extern "C" int pq3d_batch_prepare(const pq3d_batch_sim *sim, void *stream)
     dim3 grid((unsigned)((sim->N + 255) / 256), (unsigned)Bp);
     prepare_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*sim);   // the shard's own slice of v'
     PQ3D_CUDA_TRY(cudaGetLastError());
-    if (sim->precision == PQ3D_BATCH_BF16X14)
+    if (sim->precision == PQ3D_BATCH_BF16X18)
         return fx::pack_rhs_from_state(sim->slipv1, sim->slipv2, sim->cos_rake0, sim->sin_rake0, sim->Vpl,
                                        sim->fix_order, sim->N, sim->B, sim->vop, (cudaStream_t)stream);
     return PQ3D_OK;
@@ -562,8 +566,8 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
             smem_dev = dev;
         }
         gemm_f32_kernel<<<grid, 256, kF32Smem, st>>>((const float *)S.K, (const float *)S.vop, S.N, Nt, Bp, S.rates);
-    } else if (S.precision == PQ3D_BATCH_BF16X14) {
-        rc = fx::gemm_bf16x14(S.K, S.vop, S.N, Bp, S.nsplit, (float2 *)S.rates, workspace, workspace_bytes, st);
+    } else if (S.precision == PQ3D_BATCH_BF16X18) {
+        rc = fx::gemm_bf16x18(S.K, S.vop, S.N, S.B, S.nsplit, (float2 *)S.rates, workspace, workspace_bytes, st);
         if (rc) return rc;
     } else if (S.precision == PQ3D_BATCH_BF16X6) {
         rc = pq3d::tc::gemm_bf16x6((const float *)S.K, (const void *)S.vop, S.N, Bp, S.nsplit, S.tc_ctas, (float *)S.rates,
@@ -599,7 +603,7 @@ extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
     if (mixed_attempt(S)) update_kernel<true><<<grid, 256, 0, st>>>(S);
     else update_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
-    if (S.precision == PQ3D_BATCH_BF16X14)   // v' of every run from its slip rates (unchanged for the others)
+    if (S.precision == PQ3D_BATCH_BF16X18)   // v' of every run from its slip rates (unchanged for the others)
         return fx::pack_rhs_from_state(S.slipv1, S.slipv2, S.cos_rake0, S.sin_rake0, S.Vpl, S.fix_order, S.N, S.B,
                                        S.vop, st);
     return PQ3D_OK;

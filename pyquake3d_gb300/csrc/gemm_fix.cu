@@ -1,51 +1,55 @@
 // Batched traction product on the 5th-generation tensor cores (tcgen05) with
-// exact fixed-point slices ("BF16x14"):
+// exact fixed-point slices ("BF16x18"):
 //
 //   out[s][n][m] = sum_{k in slice s} K[m][k] * V[n][k]   (hi + lo, ~2^-44 relative)
 //   K: (3N) x (2N) traction operator, V: B slip-rate deficits v' = V - Vpl.
 //
 // Why: the reference evaluates K.(V - Vpl) in FP64 (src/QDsim_gpu.py:948-957).
-// A product that rounds v' or its own running sums to FP32 level (~2^-24) each
+// A product that rounds v' or its own running sums at FP32 level (~2^-24) each
 // step -- BF16x3, TF32 or the three-piece BF16x6 product -- perturbs the
 // traction rate by a fresh ~1e-7 every step, and a nucleating rupture
 // amplifies that past 1e-5 in slip within ~25 accepted steps.  A static
-// rounding of the operator is amplified far less (the operator rounded once
-// to FP32 stays within 1e-5 for ~130 steps).  So this product carries v' to 40
-// bits, the operator to 32 bits, and accumulates without rounding.
+// rounding of the operator is amplified far less (rounded once to FP32 it
+// stays within 1e-5 for ~130 steps).  So this product carries the operator to
+// 32 bits (static) and v' to 48 bits (dynamic), keeps every slice product down
+// to 2^-40 of the leading one, and accumulates without rounding.
 //
-// Representation (Ozaki-style fixed point, one exponent per chunk of 1024
-// columns):
-//   * operator row m, chunk c:  e = exponent of max |K[m][c*1024 ..]|, and
+// Representation (Ozaki-style fixed point):
+//   * operator row m, 1024-column chunk c: e = exponent of max |K[m][c..]|,
 //     K[m][k] ~= sum_{p<4} d_p 2^(e - 7 - 8p), integer digits |d_p| <= 128
-//     (balanced base 256 of round(K 2^(31-e))): 32 bits relative to the
-//     chunk's largest entry.
-//   * run n, chunk c: the same with 5 digits of v'_n (40 bits).
-//   Each digit times its power of two is exact in BF16 (8 significant bits),
-//   and the slices are stored with that scale, so the products are plain BF16
-//   tensor-core products.
-//   * A product of digits d_p e_q is an integer of at most 2^14 units of
-//     2^(eK + eV - 14 - 8(p+q)).  Within one chunk (1024 columns) every
-//     product of one level l = p + q lies on that grid, and the sum of one
-//     (p, q) pair over the chunk is at most 1024 * 2^14 = 2^24 units: exact in
-//     the FP32 tensor-memory accumulator.  Pairs of levels 0, 1 and 2 (6
-//     pairs) therefore get one accumulator each and are exact; the pairs of
-//     levels 3 and 4 (8 pairs, 2^-24 and 2^-32 of the leading term) share a
-//     seventh accumulator, whose rounding is ~2^-48 of the result.  Levels
-//     >= 5 are dropped (~2^-40).
-//   * After each chunk the 7 accumulators are drained (tcgen05.ld) and added,
-//     exactly up to the final rounding, into a float-float running sum held
-//     in registers: 5 TwoSums, then one float-float addition.
+//     (balanced base 256 of round(K 2^(31-e))): 32 bits of the chunk's largest
+//     entry;
+//   * run n, 256-column span: the same with 6 digits of v'_n (48 bits of the
+//     span's largest |v'|).
+//   Each digit times its power of two is exact in BF16, and the slices are
+//   stored with that scale, so the products are plain BF16 tensor-core
+//   products.
+//   * A digit product d_p e_q is an integer of at most 2^14 units of
+//     2^(eK + eV - 14 - 8(p+q)): within one span every product of one level
+//     l = p + q lies on that grid.  Level l collects min(l+1, 4) slice pairs
+//     over 256 columns: at most 4 * 256 * 2^14 = 2^24 units, exact in the FP32
+//     tensor-memory accumulator.  The 18 pairs with p + q <= 5 are kept (the
+//     dropped ones are below 2^-40 of the leading product).
+//   * Tensor-memory slot l (Bq columns, Bq = runs rounded up to 32) holds level
+//     l.  With the right-hand-side slices stored one after another, the
+//     products of operator slice p with slices q..q+w-1 are ONE tcgen05.mma of
+//     N = w Bq whose accumulator starts at slot p + q: 6 instructions per
+//     16-column step cover the 18 pairs (an instruction costs about the same
+//     for N = 64 and 128, so wide instructions halve the time of 14 narrow
+//     ones).
+//   * After each span the 6 slots are drained (tcgen05.ld) and added into a
+//     float-float running sum in registers: 3 TwoSums and one float-float
+//     addition.
 //
-// Data path (one CTA = one 128-row tile of K x one K slice, all runs; 1 CTA
-// per SM since the 7 accumulators of 64 runs take the 512 tensor-memory
-// columns):
+// Data path (one CTA = one 128-row tile of K x one K slice, all runs, 1 CTA
+// per SM):
 //   * warp 0 lane 0: producer, two 1-D bulk copies per 32-column stage (the
-//     four operator slice images, 32 KB, and the five right-hand-side slice
+//     four operator slice images, 32 KB, and the six right-hand-side slice
 //     images), completion on the stage's mbarrier;
-//   * warp 1 lane 0: 2 K-steps x 14 tcgen05.mma (M=128, N=Bp, K=16) per
-//     stage, the stage freed by tcgen05.commit; at the end of a chunk a
-//     commit tells the epilogue that the accumulators are complete, and before
-//     the next chunk it waits until they are drained;
+//   * warp 1 lane 0: 2 K-steps x 6 tcgen05.mma per stage (descriptors
+//     precomputed per stage), the stage freed by tcgen05.commit; at the end of
+//     a span a commit hands the slots to the epilogue, and before the next
+//     span it waits until they are drained;
 //   * warps 2-9: epilogue, two warps per 32-lane quarter of tensor memory
 //     (the rows), each taking half of the runs.
 //   Every mbarrier wait is bounded; a wait that gives up records an error word
@@ -76,8 +80,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// descriptor of the operand `bytes` further on in shared memory (the start
+// address field, bits 0-13 in 16-byte units, does not overflow below 256 KB)
+__device__ __forceinline__ uint64_t desc_at(uint64_t d, uint32_t bytes) { return d + (bytes >> 4); }
+
+// Bq: runs of the product (32 or 64); Bo: runs written (<= Bq, multiple of 16)
 __global__ void __launch_bounds__(kThreads, 1)
-gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bp, int nsplit,
+gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bq, int Bo, int nsplit,
                 float2 *__restrict__ out, int *__restrict__ err, int stages)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -87,17 +96,16 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
     const int64_t KB = (2 * N + kBlockK - 1) / kBlockK;
     const int64_t kb0 = KB * slice / nsplit, kb1 = KB * (slice + 1) / nsplit;
     const int nkb = (int)(kb1 - kb0);
-    const int nch = nkb > 0 ? (int)((kb1 - 1) / kBlocksPerChunk - kb0 / kBlocksPerChunk + 1) : 0;
+    const int nspan = nkb > 0 ? (int)((kb1 - 1) / kBlocksPerSpan - kb0 / kBlocksPerSpan + 1) : 0;
     const uint32_t a_bytes = kKPieces * kImageA;
-    const uint32_t b_img = (uint32_t)Bp * kBlockK * 2;
+    const uint32_t b_img = (uint32_t)Bq * kBlockK * 2;
     const uint32_t b_bytes = kVPieces * b_img;
     const uint32_t stage_bytes = a_bytes + b_bytes;
     uint8_t *bars = smem + (size_t)stages * stage_bytes;
     const uint32_t full0 = tc::smem_u32(bars), empty0 = full0 + 8 * stages;
     const uint32_t acc_full = full0 + 16 * stages, acc_empty = acc_full + 8, done = acc_full + 16;
     uint32_t *tmem_slot = (uint32_t *)(bars + 16 * stages + 24);
-    const int astride = (Bp + 31) / 32 * 32;   // tensor-memory columns per accumulator
-    const uint32_t ncols = tc::tmem_cols(kAcc * astride);
+    const uint32_t ncols = tc::tmem_cols(kLevels * Bq);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < stages; ++s) {
@@ -136,43 +144,37 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
         __syncwarp();
     } else if (warp == 1) {
         if (lane == 0) {
-            // tensor-core issuer
-            const uint32_t idesc = tc::idesc_bf16(kTileM, Bp);
-            int j = 0;   // local chunk
+            // tensor-core issuer: instruction descriptors for N = Bq, 2Bq, 3Bq,
+            // 4Bq and the slot addresses, computed once
+            const uint32_t id1 = tc::idesc_bf16(kTileM, Bq), id2 = tc::idesc_bf16(kTileM, 2 * Bq);
+            const uint32_t id3 = tc::idesc_bf16(kTileM, 3 * Bq), id4 = tc::idesc_bf16(kTileM, 4 * Bq);
+            const uint32_t slot1 = tmem + (uint32_t)Bq, slot2 = tmem + 2u * Bq, slot3 = tmem + 3u * Bq;
+            const uint32_t slot4 = tmem + 4u * Bq, slot5 = tmem + 5u * Bq;
+            const uint32_t bq4 = 4u * b_img;
+            int j = 0;   // local span
             for (int it = 0; it < nkb; ++it) {
                 const int64_t kb = kb0 + it;
-                const bool first = it == 0 || kb % kBlocksPerChunk == 0;
-                const bool last = it == nkb - 1 || (kb + 1) % kBlocksPerChunk == 0;
+                const bool first = it == 0 || kb % kBlocksPerSpan == 0;
+                const bool last = it == nkb - 1 || (kb + 1) % kBlocksPerSpan == 0;
                 if (first && j > 0 && !tc::mbar_wait(acc_empty, (j - 1) & 1)) { atomicExch(err, 4); break; }
                 const int st = it % stages, use = it / stages;
                 if (!tc::mbar_wait(full0 + 8 * st, use & 1)) { atomicExch(err, 2); break; }
                 tc::tc_fence_after();
                 const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
-                const uint32_t sb = sa + a_bytes;
+                const uint64_t ad = tc::smem_desc(sa, 128, 512), bd = tc::smem_desc(sa + a_bytes, 128, 512);
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks) {
-                    const uint32_t acc_on = (first && ks == 0) ? 0u : 1u;
-                    auto mma = [&](int p, int q, int acc, uint32_t accumulate) {
-                        const uint64_t ad = tc::smem_desc(sa + p * kImageA + ks * 256, 128, 512);
-                        const uint64_t bd = tc::smem_desc(sb + q * b_img + ks * 256, 128, 512);
-                        tc::mma_bf16(tmem + (uint32_t)(acc * astride), ad, bd, idesc, accumulate);
-                    };
-                    // levels 0-2: one exact accumulator per (operator slice, rhs slice)
-                    mma(0, 0, 0, acc_on);
-                    mma(0, 1, 1, acc_on);
-                    mma(1, 0, 2, acc_on);
-                    mma(0, 2, 3, acc_on);
-                    mma(1, 1, 4, acc_on);
-                    mma(2, 0, 5, acc_on);
-                    // levels 3 and 4 share accumulator 6
-                    mma(0, 3, 6, acc_on);
-                    mma(1, 2, 6, 1u);
-                    mma(2, 1, 6, 1u);
-                    mma(3, 0, 6, 1u);
-                    mma(0, 4, 6, 1u);
-                    mma(1, 3, 6, 1u);
-                    mma(2, 2, 6, 1u);
-                    mma(3, 1, 6, 1u);
+                    const uint32_t f = (first && ks == 0) ? 0u : 1u;   // the first instruction of a slot overwrites it
+                    const uint32_t k0 = ks * 256;
+                    // operator slice 0 x rhs slices 0-3 -> slots 0-3, x slices 4-5 -> slots 4-5
+                    tc::mma_bf16(tmem, desc_at(ad, k0), desc_at(bd, k0), id4, f);
+                    tc::mma_bf16(slot4, desc_at(ad, k0), desc_at(bd, bq4 + k0), id2, f);
+                    // slice 1 x 0-3 -> slots 1-4, x 4 -> slot 5
+                    tc::mma_bf16(slot1, desc_at(ad, kImageA + k0), desc_at(bd, k0), id4, 1u);
+                    tc::mma_bf16(slot5, desc_at(ad, kImageA + k0), desc_at(bd, bq4 + k0), id1, 1u);
+                    // slice 2 x 0-3 -> slots 2-5; slice 3 x 0-2 -> slots 3-5
+                    tc::mma_bf16(slot2, desc_at(ad, 2 * kImageA + k0), desc_at(bd, k0), id4, 1u);
+                    tc::mma_bf16(slot3, desc_at(ad, 3 * kImageA + k0), desc_at(bd, k0), id3, 1u);
                 }
                 tc::mma_commit(empty0 + 8 * st);
                 if (last) {
@@ -187,14 +189,14 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
         // epilogue: TMEM lane = tile row; this warp's runs [c0, c0 + half)
         const int e = warp - 2;
         const int quarter = warp & 3;
-        const int half = Bp / 2;
+        const int half = Bq / 2;
         const int c0 = (e >> 2) * half;
         const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
         float H[32], L[32];
 #pragma unroll
         for (int c = 0; c < 32; ++c) H[c] = L[c] = 0.f;
         bool ok = true;
-        for (int j = 0; j < nch; ++j) {
+        for (int j = 0; j < nspan; ++j) {
             ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, j & 1) ? 1 : 0);
             if (!ok) {
                 if (lane == 0) atomicExch(err, 3);
@@ -204,20 +206,19 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 if (g * 8 < half) {
-                    uint32_t r[kAcc][8];
+                    uint32_t r[kLevels][8];
 #pragma unroll
-                    for (int a = 0; a < kAcc; ++a) tc::tmem_ld8_nowait(tbase + (uint32_t)(a * astride + g * 8), r[a]);
+                    for (int l = 0; l < kLevels; ++l) tc::tmem_ld8_nowait(tbase + (uint32_t)(l * Bq + g * 8), r[l]);
                     tc::tmem_wait_ld();
 #pragma unroll
                     for (int x = 0; x < 8; ++x) {
-                        float s, e0, e1, e2, e3, e4;
+                        // levels 0-3 exactly (TwoSum), 4 and 5 (2^-32, 2^-40) into the low part
+                        float s, e0, e1, e2;
                         two_sum(__uint_as_float(r[0][x]), __uint_as_float(r[1][x]), s, e0);
                         two_sum(s, __uint_as_float(r[2][x]), s, e1);
                         two_sum(s, __uint_as_float(r[3][x]), s, e2);
-                        two_sum(s, __uint_as_float(r[4][x]), s, e3);
-                        two_sum(s, __uint_as_float(r[5][x]), s, e4);
-                        const float t = __fadd_rn(
-                            __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2), e3), e4), __uint_as_float(r[6][x]));
+                        const float t = __fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2),
+                                                  __fadd_rn(__uint_as_float(r[4][x]), __uint_as_float(r[5][x])));
                         // (H, L) += (s, t)
                         float S, E;
                         two_sum(H[g * 8 + x], s, S, E);
@@ -237,7 +238,7 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
         if (ok && m < M) {
 #pragma unroll
             for (int c = 0; c < 32; ++c)
-                if (c < half) out[((int64_t)slice * Bp + c0 + c) * M + m] = make_float2(H[c], L[c]);
+                if (c < half && c0 + c < Bo) out[((int64_t)slice * Bo + c0 + c) * M + m] = make_float2(H[c], L[c]);
         }
     }
     // free tensor memory once the tensor-core work of this CTA has completed
@@ -309,9 +310,8 @@ __global__ void __launch_bounds__(256) pack_operator_fix_kernel(const double *__
     }
 }
 
-// right-hand side: one block of 512 threads per (chunk, run), one cell per
-// thread (a chunk is 512 cells = 1024 columns); v' from `v` ([B][2N] FP64) or
-// from the stepper's slip rates
+// right-hand side: one block of 128 threads per (256-column span, run), one
+// cell per thread; v' from `v` ([B][2N] FP64) or from the stepper's slip rates
 struct RhsSrc {
     const double *v;   // [B][2N] or null
     const double *slipv1, *slipv2, *cos_rake0, *sin_rake0;   // [B][N]
@@ -319,14 +319,14 @@ struct RhsSrc {
     const int64_t *order;   // position -> cell, or null (identity)
 };
 
-__global__ void __launch_bounds__(512) pack_rhs_fix_kernel(RhsSrc src, int64_t N, int B, int Bp,
-                                                            __nv_bfloat16 *__restrict__ out)
+__global__ void __launch_bounds__(kSpan / 2) pack_rhs_fix_kernel(RhsSrc src, int64_t N, int B, int Bq,
+                                                                  __nv_bfloat16 *__restrict__ out)
 {
-    __shared__ double red[16];
-    const int64_t ch = blockIdx.x;
+    __shared__ double red[kSpan / 64];
+    const int64_t sp = blockIdx.x;
     const int r = blockIdx.y;
     const int i = threadIdx.x;
-    const int64_t pos = ch * (kChunk / 2) + i;
+    const int64_t pos = sp * (kSpan / 2) + i;
     const int64_t KB = k_blocks(N);
     double v1 = 0.0, v2 = 0.0;
     if (r < B && pos < N) {
@@ -344,19 +344,16 @@ __global__ void __launch_bounds__(512) pack_rhs_fix_kernel(RhsSrc src, int64_t N
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((i & 31) == 0) red[i >> 5] = mx;
     __syncthreads();
-    if (i < 32) {
-        double t = i < 16 ? red[i] : 0.0;
-        for (int o = 8; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
-        if (i == 0) red[0] = t;
-    }
-    __syncthreads();
-    const int e = chunk_exponent(red[0]);
-    const int64_t kb = ch * kBlocksPerChunk + i / 16;
+    double m = red[0];
+#pragma unroll
+    for (int w = 1; w < kSpan / 64; ++w) m = fmax(m, red[w]);
+    const int e = chunk_exponent(m);
+    const int64_t kb = sp * kBlocksPerSpan + i / 16;
     if (kb >= KB) return;
     int d1[kVPieces], d2[kVPieces];
     digits<kVPieces>(__double2ll_rn(ldexp(v1, 8 * kVPieces - 1 - e)), d1);
     digits<kVPieces>(__double2ll_rn(ldexp(v2, 8 * kVPieces - 1 - e)), d2);
-    const int64_t img = (int64_t)Bp * kBlockK;
+    const int64_t img = (int64_t)Bq * kBlockK;
     __nv_bfloat16 *P = out + kb * kVPieces * img + image_offset(r, (2 * i) % kBlockK);
 #pragma unroll
     for (int q = 0; q < kVPieces; ++q) {
@@ -367,10 +364,11 @@ __global__ void __launch_bounds__(512) pack_rhs_fix_kernel(RhsSrc src, int64_t N
     }
 }
 
-static int launch_pack_rhs(const RhsSrc &src, int64_t N, int B, int Bp, void *Vpacked, cudaStream_t stream)
+static int launch_pack_rhs(const RhsSrc &src, int64_t N, int B, void *Vpacked, cudaStream_t stream)
 {
-    dim3 grid((unsigned)k_chunks(N), (unsigned)Bp);
-    pack_rhs_fix_kernel<<<grid, kChunk / 2, 0, stream>>>(src, N, B, Bp, (__nv_bfloat16 *)Vpacked);
+    const int Bq = fix_runs(B);
+    dim3 grid((unsigned)k_spans(N), (unsigned)Bq);
+    pack_rhs_fix_kernel<<<grid, kSpan / 2, 0, stream>>>(src, N, B, Bq, (__nv_bfloat16 *)Vpacked);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }
@@ -379,21 +377,22 @@ int pack_rhs_from_state(const double *slipv1, const double *slipv2, const double
                         double Vpl, const int64_t *order, int64_t N, int B, void *Vpacked, cudaStream_t stream)
 {
     const RhsSrc src{nullptr, slipv1, slipv2, cos_rake0, sin_rake0, Vpl, order};
-    return launch_pack_rhs(src, N, B, (B + 15) / 16 * 16, Vpacked, stream);
+    return launch_pack_rhs(src, N, B, Vpacked, stream);
 }
 
 // ---------------------------------------------------------------------------
 // launch
 
-static int stages_for(int Bp, int *stages)
+static size_t stage_bytes_for(int Bq) { return (size_t)kKPieces * kImageA + (size_t)kVPieces * Bq * kBlockK * 2; }
+
+static int stages_for(int Bq, int *stages)
 {
     int dev, maxs = 0;
     PQ3D_CUDA_TRY(cudaGetDevice(&dev));
     PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t stage_bytes = (size_t)kKPieces * kImageA + (size_t)kVPieces * Bp * kBlockK * 2;
-    int s = (int)((maxs - 1024 - 64) / (stage_bytes + 16));
+    int s = (int)((maxs - 1024 - 64) / (stage_bytes_for(Bq) + 16));
     if (s > 6) s = 6;
-    PQ3D_REQUIRE(s >= 2, "gemm_bf16x14: not enough shared memory for B=%d", Bp);
+    PQ3D_REQUIRE(s >= 2, "gemm_bf16x18: not enough shared memory for %d runs", Bq);
     static thread_local int cfg_dev = -1;
     if (cfg_dev != dev) {
         PQ3D_CUDA_TRY(cudaFuncSetAttribute(gemm_fix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs));
@@ -403,25 +402,24 @@ static int stages_for(int Bp, int *stages)
     return PQ3D_OK;
 }
 
-int gemm_bf16x14(const void *Kpacked, const void *Vpacked, int64_t N, int Bp, int nsplit, float2 *out,
+int gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float2 *out,
                  void *workspace, size_t workspace_bytes, cudaStream_t stream)
 {
-    PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x14: null pointer");
-    PQ3D_REQUIRE(N > 0, "gemm_bf16x14: N must be positive");
-    PQ3D_REQUIRE(workspace_bytes >= 256 && aligned16(workspace), "gemm_bf16x14: workspace must be >= 256 bytes");
-    PQ3D_REQUIRE(Bp >= 16 && Bp <= kMaxRuns && Bp % 16 == 0,
-                 "gemm_bf16x14: padded run count must be 16..%d, multiple of 16", kMaxRuns);
+    PQ3D_REQUIRE(Kpacked && Vpacked && out && workspace, "gemm_bf16x18: null pointer");
+    PQ3D_REQUIRE(N > 0, "gemm_bf16x18: N must be positive");
+    PQ3D_REQUIRE(workspace_bytes >= 256 && aligned16(workspace), "gemm_bf16x18: workspace must be >= 256 bytes");
+    PQ3D_REQUIRE(B >= 1 && B <= kMaxRuns, "gemm_bf16x18: B must be 1..%d", kMaxRuns);
     PQ3D_REQUIRE(aligned16(Kpacked) && aligned16(Vpacked) && aligned16(out),
-                 "gemm_bf16x14: operands must be 16-byte aligned");
+                 "gemm_bf16x18: operands must be 16-byte aligned");
     const int64_t KB = k_blocks(N);
-    PQ3D_REQUIRE(nsplit >= 1 && nsplit <= KB, "gemm_bf16x14: nsplit must be in [1, %lld]", (long long)KB);
+    PQ3D_REQUIRE(nsplit >= 1 && nsplit <= KB, "gemm_bf16x18: nsplit must be in [1, %lld]", (long long)KB);
+    const int Bq = fix_runs(B), Bo = (B + 15) / 16 * 16;
     int stages;
-    int rc = stages_for(Bp, &stages);
+    int rc = stages_for(Bq, &stages);
     if (rc) return rc;
-    const size_t stage_bytes = (size_t)kKPieces * kImageA + (size_t)kVPieces * Bp * kBlockK * 2;
-    const size_t smem = (size_t)stages * stage_bytes + 16 * (size_t)stages + 48;
+    const size_t smem = (size_t)stages * stage_bytes_for(Bq) + 16 * (size_t)stages + 48;
     dim3 grid((unsigned)m_tiles(N), (unsigned)nsplit);
-    gemm_fix_kernel<<<grid, kThreads, smem, stream>>>((const uint8_t *)Kpacked, (const uint8_t *)Vpacked, N, Bp,
+    gemm_fix_kernel<<<grid, kThreads, smem, stream>>>((const uint8_t *)Kpacked, (const uint8_t *)Vpacked, N, Bq, Bo,
                                                       nsplit, out, (int *)workspace, stages);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
@@ -436,8 +434,7 @@ extern "C" size_t pq3d_batch_operator_fix_bytes(int64_t N) { return N > 0 ? fx::
 
 extern "C" size_t pq3d_batch_rhs_fix_bytes(int64_t N, int B)
 {
-    const int Bp = (B + 15) / 16 * 16;
-    return N > 0 && B > 0 ? fx::packed_rhs_bytes(N, Bp) : 0;
+    return N > 0 && B > 0 ? fx::packed_rhs_bytes(N, B) : 0;
 }
 
 extern "C" int pq3d_batch_pack_operator_fix(const double *K64, int64_t N, const int64_t *order, void *Kpacked,
@@ -459,14 +456,13 @@ extern "C" int pq3d_batch_pack_rhs_fix(const double *v, int64_t N, int B, const 
     PQ3D_REQUIRE(v && Vpacked && N > 0 && B >= 1 && B <= fx::kMaxRuns, "pq3d_batch_pack_rhs_fix: bad arguments");
     PQ3D_REQUIRE(aligned16(Vpacked), "pq3d_batch_pack_rhs_fix: output must be 16-byte aligned");
     const fx::RhsSrc src{v, nullptr, nullptr, nullptr, nullptr, 0.0, order};
-    return fx::launch_pack_rhs(src, N, B, (B + 15) / 16 * 16, Vpacked, (cudaStream_t)stream);
+    return fx::launch_pack_rhs(src, N, B, Vpacked, (cudaStream_t)stream);
 }
 
-extern "C" int pq3d_batch_gemm_bf16x14(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit,
+extern "C" int pq3d_batch_gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit,
                                        float *out, void *workspace, size_t workspace_bytes, void *stream)
 {
     clear_error();
-    PQ3D_REQUIRE(B >= 1 && B <= fx::kMaxRuns, "pq3d_batch_gemm_bf16x14: B must be 1..%d", fx::kMaxRuns);
-    return fx::gemm_bf16x14(Kpacked, Vpacked, N, (B + 15) / 16 * 16, nsplit, (float2 *)out, workspace,
-                            workspace_bytes, (cudaStream_t)stream);
+    return fx::gemm_bf16x18(Kpacked, Vpacked, N, B, nsplit, (float2 *)out, workspace, workspace_bytes,
+                            (cudaStream_t)stream);
 }

@@ -59,6 +59,48 @@ __device__ __forceinline__ void rhs(const Cell &c, double V0, double eta, double
     dtau2 = t2 / 1e6;
 }
 
+// The same right-hand side in reciprocal form: the per-cell quotients 1/a,
+// 1/b, b/dc and 2 V0/a once per attempt (`CellRecip`), one division 1/Tn per
+// evaluation, e^{-x} as 1/e^{x}, the MPa scaling as a product: 5 divisions
+// and 4 exponentials per evaluation against the reference formula's 15 and
+// 6, with the same values to ~1e-15 relative.  GB300's FP64 pipe runs at
+// 1/64 of the FP32 rate and a division or an exponential is a sequence of
+// ~10-25 FP64 instructions, so this halves the FP64 attempt.
+struct CellRecip {
+    double ia, ib, bdc, v0ia2;   // 1/a, 1/b, b/dc, 2 V0 / a
+};
+
+__device__ __forceinline__ CellRecip cell_recip(const Cell &c, double V0)
+{
+    const double ia = 1.0 / c.a;
+    return CellRecip{ia, 1.0 / c.b, c.b / c.dc, 2.0 * V0 * ia};
+}
+
+__device__ __forceinline__ void rhs_recip(const Cell &c, const CellRecip &k, double V0, double eta, double Tno,
+                                          double Tt1o, double Tt2o, double state, double &dstate, double &dsig,
+                                          double &dtau1, double &dtau2)
+{
+    const double Tn = Tno * 1e6 - c.P, T1 = Tt1o * 1e6, T2 = Tt2o * 1e6;
+    const double iTn = 1.0 / Tn, iaTn = k.ia * iTn;
+    const double es = exp(clip700(-state * k.ia));
+    const double x1 = clip700(T1 * iaTn), x2 = clip700(T2 * iaTn);
+    const double ep1 = exp(x1), em1 = 1.0 / ep1, ep2 = exp(x2), em2 = 1.0 / ep2;
+    const double ch1 = (ep1 + em1) * 0.5, sh1 = (ep1 - em1) * 0.5;
+    const double ch2 = (ep2 + em2) * 0.5, sh2 = (ep2 - em2) * 0.5;
+    const double ct = 2.0 * V0 * iaTn * es;    // 2 V0 / (a Tn) e^{-psi/a}
+    const double cs = k.v0ia2 * es;            // 2 V0 / a e^{-psi/a}
+    const double dV1dtau = ct * ch1, dV2dtau = ct * ch2;
+    const double dV1dsigma = -ct * (T1 * iTn) * ch1, dV2dsigma = -ct * (T2 * iTn) * ch2;
+    const double dV1dstate = -cs * sh1, dV2dstate = -cs * sh2;
+    dstate = k.bdc * (V0 * exp(clip700((c.f0 - state) * k.ib)) - c.slipv);
+    const double ds = c.dsig - c.dPdt;
+    const double t1 = (-c.AdotV1 + c.shear - eta * (dV1dsigma * ds + dV1dstate * dstate)) / (1.0 + eta * dV1dtau);
+    const double t2 = (-c.AdotV2 + c.shear - eta * (dV2dsigma * ds + dV2dstate * dstate)) / (1.0 + eta * dV2dtau);
+    dsig = c.dsig * 1e-6;
+    dtau1 = t1 * 1e-6;
+    dtau2 = t2 * 1e-6;
+}
+
 
 // ---------------------------------------------------------------------------
 // Mixed-precision attempt (batched mixed modes).
@@ -357,15 +399,23 @@ __device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, float dsig,
     }
 }
 
-// One Dormand-Prince attempt of one cell in FP64, the reference arithmetic
-// (src/QDsim_gpu.py:1266-1397).  Writes the 5th-order solution to yo and
-// returns the two relative errors.
+// One Dormand-Prince attempt of one cell in FP64 (src/QDsim_gpu.py:1266-1397):
+// kRecip = false evaluates the reference formula, true the reciprocal form
+// (rhs_recip).  Writes the 5th-order solution to yo and returns the two
+// relative errors.
+template <bool kRecip = false>
 __device__ __forceinline__ void dp_attempt(const Cell &c, double V0, double eta, double h, const double y[4],
                                            double yo[4], double &e1, double &e2)
 {
     double s1, n1, t1, u1, s2, n2, t2, u2, s3, n3, t3, u3, s4, n4, t4, u4, s5, n5, t5, u5, s6, n6, t6, u6, s7, n7, t7,
         u7;
     const double Tno = y[0], Tt1o = y[1], Tt2o = y[2], st = y[3];
+    const CellRecip kr = kRecip ? cell_recip(c, V0) : CellRecip{0.0, 0.0, 0.0, 0.0};
+    auto rhs = [&](const Cell &cc, double V0_, double eta_, double a0, double a1, double a2, double a3, double &o0,
+                   double &o1, double &o2, double &o3) {
+        if (kRecip) rhs_recip(cc, kr, V0_, eta_, a0, a1, a2, a3, o0, o1, o2, o3);
+        else ::pq3d::rk::rhs(cc, V0_, eta_, a0, a1, a2, a3, o0, o1, o2, o3);
+    };
     rhs(c, V0, eta, Tno, Tt1o, Tt2o, st, s1, n1, t1, u1);
     rhs(c, V0, eta, Tno + h * B21 * n1, Tt1o + h * B21 * t1, Tt2o + h * B21 * u1, st + h * B21 * s1, s2, n2, t2, u2);
     rhs(c, V0, eta, Tno + h * (B31 * n1 + B32 * n2), Tt1o + h * (B31 * t1 + B32 * t2), Tt2o + h * (B31 * u1 + B32 * u2),

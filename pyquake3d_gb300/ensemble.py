@@ -14,12 +14,13 @@ Precisions of the traction product (``precision=``):
            leading cross products on the tcgen05 tensor cores with FP32
            accumulation in tensor memory; K slices added in float-float;
            launch shape (K slices, CTAs per SM) from :mod:`.autotune`
-  "bf16x14" the operator (32 bits) and v' (40 bits) as exact fixed-point BF16
-           slices with one exponent per 1024-column chunk, 14 slice products
-           on the tensor cores with exact accumulation per chunk, chunks and
-           K slices added in float-float: the FP64 product to ~1e-10 of its
-           scale, for runs that must track the FP64 trajectory (with
-           attempt="fp64"); at most 64 runs
+  "bf16x18" the operator (32 bits) and v' (48 bits) as exact fixed-point BF16
+           slices (one exponent per 1024-column chunk of an operator row, per
+           256-column span of a run), the 18 slice products down to 2^-40 of
+           the leading one on the tensor cores with exact accumulation per
+           span, spans and K slices added in float-float: the FP64 product to
+           ~1e-9 of its scale, for runs that must track the FP64 trajectory
+           (with attempt="fp64"); at most 64 runs
   "hmat"   an :class:`~pyquake3d_gb300.hmatrix.HMatrix` (large meshes)
 Time, slip, the state and the RK error norm stay FP64 in every mode.
 
@@ -43,7 +44,7 @@ from . import _lib, autotune
 from .QDsim_gpu import initial_state
 
 PRECISIONS = {"fp64": _lib.PQ3D_BATCH_FP64, "fp32": _lib.PQ3D_BATCH_FP32, "bf16x6": _lib.PQ3D_BATCH_BF16X6,
-              "hmat": _lib.PQ3D_BATCH_HMAT, "bf16x14": _lib.PQ3D_BATCH_BF16X14}
+              "hmat": _lib.PQ3D_BATCH_HMAT, "bf16x18": _lib.PQ3D_BATCH_BF16X18}
 STATE = ("Tno", "Tt1o", "Tt2o", "state", "slipv1", "slipv2", "slipv", "slip1", "slip2")
 PARAMS = ("a", "b", "dc", "f0", "shear_loading", "normal_loading", "cos_rake0", "sin_rake0")
 
@@ -73,7 +74,7 @@ class PackedOperator:
 
 
 class PackedFixOperator:
-    """The operand of the fixed-point tensor-core product ("bf16x14"): the FP64
+    """The operand of the fixed-point tensor-core product ("bf16x18"): the FP64
     operator as four BF16 slices per row and 1024-column chunk (built once per
     mesh).
 
@@ -109,7 +110,7 @@ class Ensemble:
 
     K: the (3N, 2N) operator -- FP64 for "fp64", FP32 for "fp32", a
     :class:`PackedOperator` for "bf16x6", a :class:`PackedFixOperator` for
-    "bf16x14".  tables: (B, N, 10) per-cell tables
+    "bf16x18".  tables: (B, N, 10) per-cell tables
     (``read_parameter`` layout).
 
     shard=(cell0, N_total): this object steps cells [cell0, cell0 + N) of an
@@ -138,14 +139,14 @@ class Ensemble:
             kop = None
             nsplit = 1
             self.hmat = K
-        elif precision == "bf16x14":
+        elif precision == "bf16x18":
             assert isinstance(K, PackedFixOperator) and K.N == N
             if B > 64:
-                raise ValueError("the bf16x14 product takes at most 64 runs")
+                raise ValueError("the bf16x18 product takes at most 64 runs")
             kop = K.data
             self.fix_op = K
             if nsplit is None:
-                nsplit = autotune.tune_bf16x14(K, B)["nsplit"]
+                nsplit = autotune.tune_bf16x18(K, B)["nsplit"]
             tc_ctas = 1
         elif precision == "bf16x6":
             assert isinstance(K, PackedOperator) and K.N == N
@@ -177,7 +178,7 @@ class Ensemble:
             self.vop = torch.zeros(self.Bp * 2 * Nt, **f64)
         elif precision == "fp32":
             self.vop = torch.zeros(self.Bp * 2 * Nt, dtype=torch.float32, device=dev)
-        elif precision == "bf16x14":
+        elif precision == "bf16x18":
             self.vop = torch.zeros(L.pq3d_batch_rhs_fix_bytes(N, B), dtype=torch.uint8, device=dev)
         else:
             self.vop = torch.zeros(L.pq3d_batch_rhs_bytes(N, B), dtype=torch.uint8, device=dev)
@@ -188,7 +189,7 @@ class Ensemble:
             setattr(S, k, self.t[k].data_ptr())
         S.vop, S.ctrl = self.vop.data_ptr(), self.ctrl_t.data_ptr()
         S.base = self.t["base"].data_ptr() if "base" in self.t else None
-        if precision == "bf16x14" and K.order is not None:
+        if precision == "bf16x18" and K.order is not None:
             S.fix_order, S.fix_pos = K.order.data_ptr(), K.pos.data_ptr()
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
@@ -243,7 +244,7 @@ class Ensemble:
         K-slice partials of the tensor-core product added, or the one FP64
         partial of the other products."""
         n = self.nsplit * self.Bp * 3 * self.N
-        if self.precision == "bf16x14":
+        if self.precision == "bf16x18":
             f = self.t["rates"].view(torch.float32)[:2 * n].view(self.nsplit, self.Bp, 3 * self.N, 2).double()
             r = f.sum(3).sum(0)
             if self.fix_op.order is not None:   # rows come in the operator's cell order
