@@ -132,9 +132,16 @@ def fp64_peak_tflops(torch, dev):
 
 
 # FP64 operations of one (receiver, source) pair of the assembly kernel
-# (both unit slips, 6 entries): 357 add + 645 mul + 11 div + 3 sqrt, counted by
+# (both unit slips, 6 entries): 324 add + 516 mul + 5 div + 3 sqrt, counted by
 # oracle/count_gf_flops.cpp on the kernel's own device math.
 GF_FLOP_PER_PAIR = 848
+# The same for the half-space kernel (main + image dislocation, the
+# free-surface correction of the three sides in dual numbers): 5,426.7 add +
+# 9,009.4 mul + 72.9 div + 18.0 sqrt per pair (and 18.0 transcendental calls),
+# counted by oracle/count_hs_flops.cpp over every pair of the 40 x 20 km,
+# N = 2,500 mesh of bench_halfspace (the count depends weakly on the mesh
+# through the branches of the angular dislocations).
+HS_FLOP_PER_PAIR = 14527
 # Stores per pair: 6 FP64 + 6 FP32 entries.
 GF_BYTES_PER_PAIR = 72
 
@@ -355,7 +362,7 @@ def bench_ours(args):
             out["batched"] = bench_batched(torch, dev, args, peaks)
         if not args.no_hmat:
             out["hmatrix"] = bench_hmatrix(torch, dev, args, peaks)
-        out["halfspace"] = bench_halfspace(torch, dev, args)
+        out["halfspace"] = bench_halfspace(torch, dev, args, fp64)
         if not args.no_serve:
             out["serving"] = bench_serving(torch, dev, args)
         if not args.no_cpu:
@@ -739,7 +746,7 @@ def bench_hmatrix(torch, dev, args, peaks):
     return res
 
 
-def bench_halfspace(torch, dev, args):
+def bench_halfspace(torch, dev, args, fp64_tflops=None):
     """Half-space GF assembly (image dislocation + free-surface correction):
     rough fault 40 x 20 km reaching the free surface, 50 x 25 cells ->
     N = 2,500 (1 km cells), FP64 operator + FP32 copy, against the full-space
@@ -765,6 +772,13 @@ def bench_halfspace(torch, dev, args):
         t = s.elapsed_time(e) / reps / 1e3
         res["halfspace" if half else "fullspace"] = {"s": t, "pairs_per_s": N * N / t, "entries_per_s": 6 * N * N / t}
     res["cost_ratio"] = res["halfspace"]["s"] / res["fullspace"]["s"]
+    if fp64_tflops:
+        hs = res["halfspace"]
+        ach = HS_FLOP_PER_PAIR * N * N / hs["s"] / 1e12
+        hs["roofline"] = {"bound": "fp64", "unit": "TFLOP/s", "flops_per_pair": HS_FLOP_PER_PAIR,
+                          "achieved": ach, "peak": fp64_tflops, "frac": ach / fp64_tflops,
+                          "peak_source": "cuBLAS DGEMM measured in this run",
+                          "flop_ratio_vs_fullspace": HS_FLOP_PER_PAIR / GF_FLOP_PER_PAIR}
     del K64, K32
     torch.cuda.empty_cache()
     return res

@@ -144,7 +144,9 @@ __device__ __forceinline__ int tri_mode(T x, T y, T z, T p1y, T p1z, T p3y, T p3
 __device__ __forceinline__ bool isfinite_t(double v) { return isfinite(v); }
 #else
 inline bool isfinite_t(double v) { return std::isfinite(v); }
+#ifndef PQ3D_OPCOUNT
 inline bool isfinite_t(long double v) { return std::isfinite(v); }
+#endif
 #endif
 
 // Shared geometric terms of one angular dislocation at (x, y, z) of its own
