@@ -327,18 +327,20 @@ def bench_ours(args):
             roof.update({"achieved": ach, "frac": ach / fp64, "flops_per_pair": fpp})
         else:
             roof.update({"achieved": None, "frac": None})
-        # DRAM bytes of one launch: ncu on the N=2,000 case measured 56.9 B/pair
-        # (226.3 MB written + 1.4 MB read for 4e6 pairs, part of the 288 MB of
-        # stores still dirty in L2 at kernel end); scaled to this launch.
+        # DRAM bytes of one launch: ncu on the N=6,000 case (2.6 GB of stores,
+        # 20x the L2) measured 70.8 B/pair (2.532 GB written + 16 MB read for
+        # 3.6e7 pairs; ~60 MB of the 2.592 GB of stores still dirty in L2 at
+        # kernel end); scaled to this launch by pairs.
         # the FP64 pipe is the bound: DGEMM issues only 2-flop DFMAs, this
         # kernel averages ~1.3 flops per FP64-pipe instruction; ncu on the
         # N = 2,000 case: FP64 pipe 88 % busy (active cycles)
         roof["fp64_pipe_active_pct"] = 88.3
         roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, N=2000 case "
                              "(profiles/gf_assembly_rough_N2000.md)")
-        roof["traffic"] = 56.9 * N * N
-        roof["traffic_note"] = ("ncu dram__bytes_read+write at N=2000 (56.9 B/pair) scaled by pairs; "
-                                "algorithmic stores are %d B/pair" % GF_BYTES_PER_PAIR)
+        roof["traffic"] = 70.8 * N * N
+        roof["traffic_note"] = ("ncu dram__bytes_read+write at N=6000 (70.8 B/pair, 2.6 GB of stores, 20x the L2) "
+                                "scaled by pairs; algorithmic stores are %d B/pair (profiles/gf_traffic_N6000.md)"
+                                % GF_BYTES_PER_PAIR)
         out["roofline"] = roof
         out["clocks"] = clk.summary()
         # -- end to end: host mesh in, FP64 operator out to pinned host memory
@@ -392,17 +394,18 @@ def batched_summary(bt):
     acc = bt.get("accuracy_vs_fp64", {})
     plain = bt["plain_fp64_single"]["rk_stages_per_s"]
     arms = {}
-    for key, prec, acc_key in (("bf16x18_fp64_attempt", "bf16x18", "bf16x18_fp64_attempt"),
-                               ("bf16x6_mixed_attempt", "bf16x6", "bf16x6"),
-                               ("fp32_mixed_attempt", "fp32", "fp32")):
-        if prec not in bt:
+    for key, arm, acc_key, gemm in (("bf16x18_ff_attempt", "bf16x18", "bf16x18_ff_attempt", "bf16x18"),
+                                    ("bf16x18_fp64_attempt", "bf16x18_fp64", "bf16x18_fp64_attempt", "bf16x18"),
+                                    ("bf16x6_mixed_attempt", "bf16x6", "bf16x6", "bf16x6"),
+                                    ("fp32_mixed_attempt", "fp32", "fp32", None)):
+        if arm not in bt:
             continue
-        a = {"rk_stages_per_s": round(bt[prec]["rk_stages_per_s"]),
-             "ratio_vs_plain_fp64": round(bt[prec]["rk_stages_per_s"] / plain, 2)}
+        a = {"rk_stages_per_s": round(bt[arm]["rk_stages_per_s"]),
+             "ratio_vs_plain_fp64": round(bt[arm]["rk_stages_per_s"] / plain, 2)}
         if acc_key in acc:
             a["steps_within_1e-5"] = acc[acc_key]["steps_within_1e-5"]
-        if "gemm" in bt[prec]:
-            a["product_hbm_frac"] = round(bt[prec]["gemm"]["roofline"]["frac"], 3)
+        if gemm and "gemm" in bt.get(gemm, {}):
+            a["product_hbm_frac"] = round(bt[gemm]["gemm"]["roofline"]["frac"], 3)
         arms[key] = a
     out = {"N": bt.get("N"), "B": bt.get("B"), "plain_fp64_rk_stages_per_s": round(plain), "arms": arms}
     if acc:
@@ -522,8 +525,10 @@ def bench_batched(torch, dev, args, peaks):
     plain FP64 single-simulation stepper on the same mesh:
       bf16x6   three-piece BF16 product on tcgen05, FP32 mixed attempt (fast);
       bf16x18  exact fixed-point slices on tcgen05 (the FP64 product to ~1e-9
-               normwise), FP64 attempt: the arm that tracks the FP64
+               normwise), float-float attempt: the arm that tracks the FP64
                trajectory;
+      bf16x18_fp64  the same product with the reference-arithmetic FP64
+               attempt;
       fp32     FP32 operator on CUDA cores, FP32 mixed attempt."""
     from pyquake3d_gb300 import _lib, autotune, gf, mesh
     from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator, PackedOperator
@@ -537,7 +542,7 @@ def bench_batched(torch, dev, args, peaks):
     tabs = mesh.ensemble_tables(xg, Lkm * 1e3, Wkm * 1e3, B=B, seed=0, v_nuc=1e-3)
     K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
     P = PackedOperator(K64)
-    PF = PackedFixOperator(K64)
+    PF = PackedFixOperator(K64, xg)   # cells in the cluster tree's depth-first order
     # launch shapes of the tensor-core products from the project's autotuner,
     # before anything is timed
     torch.cuda.synchronize()
@@ -550,8 +555,11 @@ def bench_batched(torch, dev, args, peaks):
            "N": N, "B": B}
     out = {}
     st = torch.cuda.current_stream(dev).cuda_stream
-    arms = [("bf16x6", P, "mixed"), ("bf16x18", PF, "fp64"), ("fp32", K32, "mixed")]
-    for prec, K, attempt in arms:
+    # (key, product, operator, attempt); the product alone is timed with the
+    # first arm of each tensor-core product
+    arms = [("bf16x6", "bf16x6", P, "mixed"), ("bf16x18", "bf16x18", PF, "ff"),
+            ("bf16x18_fp64", "bf16x18", PF, "fp64"), ("fp32", "fp32", K32, "mixed")]
+    for key, prec, K, attempt in arms:
         if prec == "bf16x18" and B > 64:
             continue
         ens = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, attempt=attempt,
@@ -572,11 +580,11 @@ def bench_batched(torch, dev, args, peaks):
         dt = s.elapsed_time(e) / 1e3
         st1 = ens.stages()
         c = ens.read_ctrl()
-        out[prec] = {"attempt": attempt, "rk_stages_per_s": (st1 - st0) / dt, "iterations": reps * args.graph_iters,
-                     "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
-                     "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
-                     "clocks": clk.summary(), "error_word": ens.error_word() if prec != "fp32" else 0}
-        if prec in ("bf16x6", "bf16x18"):
+        out[key] = {"product": prec, "attempt": attempt, "rk_stages_per_s": (st1 - st0) / dt,
+                    "iterations": reps * args.graph_iters, "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
+                    "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
+                    "clocks": clk.summary(), "error_word": ens.error_word() if prec != "fp32" else 0}
+        if key in ("bf16x6", "bf16x18"):
             # the tensor-core product alone, CUDA events over repeated launches
             if prec == "bf16x6":
                 launch = lambda: L_.pq3d_batch_gemm_bf16x6(P.data.data_ptr(), ens.vop.data_ptr(), N, B, ens.nsplit,
@@ -604,7 +612,7 @@ def bench_batched(torch, dev, args, peaks):
             e.synchronize()
             tg = s.elapsed_time(e) / 1e3 / nl
             sh = shape if prec == "bf16x6" else shape_fix
-            out[prec]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit, "ctas_per_sm": ens.tc_ctas,
+            out[key]["gemm"] = {"launch_s": tg, "nsplit": ens.nsplit, "ctas_per_sm": ens.tc_ctas,
                                  "autotune": dict(sh, tune_s=tune_s),
                                  "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": op_bytes / tg / 1e9,
                                               "peak": peaks["hbm_gbs"], "frac": op_bytes / tg / 1e9 / peaks["hbm_gbs"],
@@ -613,7 +621,7 @@ def bench_batched(torch, dev, args, peaks):
                                             "frac": flops / tg / 1e12 / peaks["bf16_tflops"], "flops": flops,
                                             "note": fnote}}
             if ens.error_word() != 0:
-                out[prec]["error_word"] = ens.error_word()
+                out[key]["error_word"] = ens.error_word()
         del ens
         torch.cuda.empty_cache()
     # plain FP64 single simulation on the same mesh (run 0's parameters)
@@ -630,9 +638,9 @@ def bench_batched(torch, dev, args, peaks):
     plain = 7.0 * (c1.attempts - c0.attempts) / dt
     out["plain_fp64_single"] = {"rk_stages_per_s": plain, "accepted_steps": int(c1.steps_done - c0.steps_done),
                                 "ms_per_step": dt / max(1, c1.steps_done - c0.steps_done) * 1e3}
-    for prec, _, _ in arms:
-        if prec in out:
-            out["ratio_%s_vs_plain_fp64" % prec] = out[prec]["rk_stages_per_s"] / plain
+    for key, _, _, _ in arms:
+        if key in out:
+            out["ratio_%s_vs_plain_fp64" % key] = out[key]["rk_stages_per_s"] / plain
     if args.acc_runs > 0:
         out["accuracy_vs_fp64"] = batched_accuracy(torch, K64, K32, P, PF, tabs[:args.acc_runs], args.acc_steps)
     res.update(out)
@@ -658,7 +666,8 @@ def batched_accuracy(torch, K64, K32, P, PF, tabs, max_steps, every=5):
     pert[:, :, 7] *= 1.0 + 1e-12 * np.random.default_rng(7).choice([-1.0, 1.0], size=pert[:, :, 7].shape)
     kw = dict(mu=MU, Cs=3464.0, max_steps=max_steps)
     ref = Ensemble(K64, tabs, precision="fp64", **kw)
-    others = {"bf16x18_fp64_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="fp64", **kw),
+    others = {"bf16x18_ff_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="ff", **kw),
+              "bf16x18_fp64_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="fp64", **kw),
               "bf16x18_mixed_attempt": Ensemble(PF, tabs, precision="bf16x18", attempt="mixed", **kw),
               "bf16x6": Ensemble(P, tabs, precision="bf16x6", **kw),
               "fp32": Ensemble(K32, tabs, precision="fp32", **kw),
@@ -805,7 +814,7 @@ def bench_serving(torch, dev, args):
         nodes, tris = f(L, W, nx, nz)
         meshes.append({"nodes": nodes, "tris": tris, "L": L * 1e3, "W": W * 1e3})
     srv = Server(meshes, mu=MU, lam=LAM, cs=3464.0, slots=16, budget_bytes=150e9, graph_iters=8,
-                 max_steps=args.serve_max_steps, device=dev)
+                 max_steps=args.serve_max_steps, device=dev, dense_precision=args.serve_precision)
     nreq = args.serve_requests
     arr = poisson_arrivals(nreq, 4.0, seed=0)
     rng = np.random.default_rng(0)
@@ -837,7 +846,7 @@ def bench_serving(torch, dev, args):
         if not mine:
             continue
         N = int(sp["tris"].shape[0])
-        if res["meshes"][m]["kind"] == "dense_bf16x6":
+        if res["meshes"][m]["kind"].startswith("dense"):
             K64, _ = gf.assemble_dense(sp["nodes"], sp["tris"], MU, LAM, fp32_copy=False, device=dev)
             H = None
         else:
@@ -897,6 +906,14 @@ def bench_serving(torch, dev, args):
                                          "attempt count; FIFO one at a time from arrival" % args.serve_plain_seconds}
     res["workload"] = ("serving: %d requests, Poisson 4/s seed 0, 8 meshes N=%s, 16 slots/mesh, 150 GB budget, "
                        "span U(1,20) yr, max %d steps/run" % (nreq, [m[0] for m in sizes], args.serve_max_steps))
+    res["arithmetic"] = {
+        "dense_bf16x18": "exact fixed-point BF16x18 product + float-float Dormand-Prince attempt: slip within 1e-5 "
+                         "of the FP64 stepper for ~100 accepted steps (lockstep, N=10,000; the batched section's "
+                         "bf16x18_ff_attempt), the FP64 stepper's own 1e-12-perturbation floor is 135",
+        "dense_bf16x6": "BF16x6 product + mixed attempt: within 1e-5 for ~25 accepted steps",
+        "hmatrix": "FP32 ACA factors (tol 1e-4) + mixed attempt: the H-matrix approximation of the operator",
+        "runs_beyond_the_horizon": "past its horizon a run follows another trajectory of the same chaotic "
+                                   "system, as the FP64 stepper does past 135 steps under a 1e-12 perturbation"}
     return res
 
 
@@ -907,26 +924,39 @@ def L_ws_bytes(N):
 
 def profile_case(case):
     """Small single-kernel cases for ncu captures (no timing, no JSON):
+    gf_assembly  full-space assembly, rough 60x25 km, N=6,000, FP64 + FP32 copy
+                 (2.6 GB of stores, 20x the L2; 2 launches)
     hs_assembly  half-space assembly, rough 20x10 km to the surface, N=1,600 (2 launches)
     hmat_product H-matrix product, rough 200x40 km, N=100,000, B=1 (13 products)
+    hmat_product_40k  the same, rough 100x40 km, N=40,000 (build scratch released
+                 before the products; ~2 GB resident)
     tc_gemm      batched iterations (tcgen05 BF16x6 product, attempt, decision, update),
                  planar 60x50 km, N=6,000, B=64 (12 iterations)
     f32_gemm     batched iterations with the plain FP32 product on CUDA cores, same
                  mesh and runs (6 iterations)
     fix_gemm     batched iterations with the fixed-point BF16x18 product and the FP64
                  attempt, same mesh and runs (6 iterations)
+    ff_attempt   the same with the float-float attempt (6 iterations)
     aca          H-matrix build (partition, ACA, dense blocks), rough 100x25 km, N=20,000,
                  leaf 64, eta 2, tol 1e-4 (one ACA launch over all low-rank blocks)"""
     import torch
     from pyquake3d_gb300 import gf, mesh
-    if case == "hs_assembly":
+    if case == "gf_assembly":
+        nodes, tris = mesh.rough_fault(60.0, 25.0, 100, 30, hurst=0.8, ratio=1e-3, seed=0)
+        K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM)
+        gf.assemble_dense(nodes, tris, MU, LAM, out64=K64, out32=K32)
+    elif case == "hs_assembly":
         nodes, tris = mesh.rough_fault(20.0, 10.0, 40, 20, seed=0)
         K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, halfspace=True)
         gf.assemble_dense(nodes, tris, MU, LAM, halfspace=True, out64=K64, out32=K32)
-    elif case == "hmat_product":
+    elif case in ("hmat_product", "hmat_product_40k"):
         from pyquake3d_gb300.hmatrix import HMatrix
-        nodes, tris = mesh.rough_fault(200.0, 40.0, 500, 100, seed=0)
+        if case == "hmat_product":
+            nodes, tris = mesh.rough_fault(200.0, 40.0, 500, 100, seed=0)
+        else:
+            nodes, tris = mesh.rough_fault(100.0, 40.0, 250, 80, seed=0)
         H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4)
+        torch.cuda.empty_cache()
         v = torch.randn(1, 2 * H.N, dtype=torch.float64, device="cuda")
         ws = torch.empty(H.workspace_bytes(1), dtype=torch.uint8, device="cuda")
         out = torch.empty(1, 3 * H.N, dtype=torch.float64, device="cuda")
@@ -952,7 +982,7 @@ def profile_case(case):
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
         Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(6)
-    elif case == "fix_gemm":
+    elif case in ("fix_gemm", "ff_attempt"):
         from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator
         nodes, tris = mesh.planar_fault(60.0, 50.0, 60, 50)
         K64, _ = gf.assemble_dense(nodes, tris, MU, LAM, fp32_copy=False)
@@ -961,10 +991,13 @@ def profile_case(case):
         torch.cuda.empty_cache()
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
-        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x18", attempt="fp64", nsplit=6).iterate(6)
+        Ensemble(P, tabs, mu=MU, Cs=3464.0, precision="bf16x18", attempt="fp64" if case == "fix_gemm" else "ff",
+                 nsplit=6).iterate(6)
     elif case == "aca":
         from pyquake3d_gb300.hmatrix import HMatrix
         nodes, tris = mesh.rough_fault(100.0, 25.0, 200, 50, seed=0)
+        # built twice: the first build in a process pays the device warm-up
+        first = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4).build_phases
         H = HMatrix(nodes, tris, MU, LAM, min_size=64, mini_leaf=64, tol=1e-4)
         # GF pair evaluations of the ACA: per iteration one residual row (n
         # sources) and one column (m receivers); rank + 1 iterations per block
@@ -973,8 +1006,9 @@ def profile_case(case):
         lr = np.nonzero(b[:, 4] == 1)[0]
         m, n = b[lr, 1] - b[lr, 0], b[lr, 3] - b[lr, 2]
         pairs = int(np.sum((np.maximum(rk[lr], 0) + 1) * (m + n)))
-        print(json.dumps({"stats": H.stats, "phases": H.build_phases, "aca_pair_evaluations": pairs,
-                          "aca_pairs_per_s": pairs / H.build_phases["aca"]}))
+        print(json.dumps({"stats": H.stats, "phases_first_build": first, "phases": H.build_phases,
+                          "aca_pair_evaluations": pairs,
+                          "aca_kernel_pairs_per_s": pairs / H.build_phases["aca_kernels"]}))
     else:
         raise SystemExit("unknown --case " + case)
     torch.cuda.synchronize()
@@ -997,6 +1031,8 @@ def main():
     ap.add_argument("--no-hmat", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-precision", default="bf16x18", choices=["bf16x18", "bf16x6"],
+                    help="product of the dense serving meshes (bf16x18: float-float attempt, the accurate arm)")
     ap.add_argument("--serve-max-steps", type=int, default=3000)
     ap.add_argument("--serve-time-limit", type=float, default=90.0)
     ap.add_argument("--serve-plain-seconds", type=float, default=60.0,
@@ -1009,7 +1045,7 @@ def main():
     ap.add_argument("--acc-runs", type=int, default=16, help="runs of the slip-accuracy check (0: skip)")
     ap.add_argument("--acc-steps", type=int, default=200)
     ap.add_argument("--case", default=None,
-                    help="profiling case only (hs_assembly, hmat_product, tc_gemm, f32_gemm)")
+                    help="profiling case only (gf_assembly, hs_assembly, hmat_product, tc_gemm, f32_gemm, fix_gemm, aca)")
     args = ap.parse_args()
     if args.case:
         profile_case(args.case)

@@ -270,8 +270,10 @@ typedef struct pq3d_batch_sim {
     pq3d_run_ctrl *ctrl;   /* [B] */
     double V0, Vpl, eta;
     int32_t fix_Tn;
-    int32_t attempt64;     /* FP32, BF16X6, HMAT: 1 = Dormand-Prince stages in the reference FP64
-                              arithmetic (base unused, may be NULL), 0 = mixed precision */
+    int32_t attempt64;     /* FP32, BF16X6, BF16X18, HMAT: 1 = Dormand-Prince stages in the reference
+                              FP64 arithmetic, 2 = in float-float on the FP32 pipes (the FP64
+                              attempt's accuracy: exponent arguments reduced in FP64 once per
+                              attempt), base unused (may be NULL) for both; 0 = mixed precision */
     /* Receiver-row shard (FP64 and FP32 only): this process steps cells
      * [cell0, cell0 + N) of an N_total-cell mesh.  The per-cell arrays, cand
      * and rates hold the shard's N cells; K holds the shard's 3N rows of the
@@ -401,8 +403,10 @@ typedef struct pq3d_hmat {
     const int32_t *leaf_blocks;   /* blocks whose row range covers each leaf row cluster, fixed order */
     const int32_t *t_sched;       /* [t_rows] rank rows: those of at most 8192 columns, then the longer ones */
     int64_t t_nlong;              /* number of the longer rows (the tail of t_sched) */
-    const int32_t *t_grp;         /* [t_ngrp] groups of up to 4 consecutive shorter rank rows of one block
-                                     (they share their x values): first position in t_sched | size << 28 */
+    const int64_t *t_grp;         /* [t_ngrp][2] groups of up to 4 consecutive shorter rank rows of one block
+                                     (they share their x values), 16-byte aligned: V offset of the first row
+                                     (< 2^40) | row length << 40 | group size << 56, then first column
+                                     2 c0 | first rank row << 32 */
     int64_t t_ngrp;
 } pq3d_hmat;
 

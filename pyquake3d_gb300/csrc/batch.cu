@@ -262,6 +262,7 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
     __shared__ int act;
     __shared__ double hs;
     __shared__ float hsf, V0f;
+    __shared__ double lnev;   // ln(eta V0 1e-6) of the float-float attempt
     const int r = blockIdx.y;
     pq3d_run_ctrl *C = S.ctrl + r;
     if (threadIdx.x == 0) {
@@ -270,6 +271,8 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
         if (kMixed) {
             hsf = (float)hs;
             V0f = (float)S.V0;
+        } else if (S.attempt64 == 2) {
+            lnev = log(S.eta * S.V0 * 1e-6);
         }
     }
     __syncthreads();
@@ -353,8 +356,10 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
                          0.0, 0.0};
             // the FP64 precision keeps the reference formula (it is the arm the
             // others are compared with); the FP64 attempt of the mixed
-            // products (attempt64) takes the reciprocal form
+            // products (attempt64 = 1) takes the reciprocal form, the
+            // float-float attempt (attempt64 = 2) the w-form on the FP32 pipes
             if (S.precision == PQ3D_BATCH_FP64) dp_attempt<false>(c, S.V0, S.eta, hs, y, yo, m1, m2);
+            else if (S.attempt64 == 2) dp_attempt_ff(c, S.V0, lnev, hs, y, yo, m1, m2);
             else dp_attempt<true>(c, S.V0, S.eta, hs, y, yo, m1, m2);
         }
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);
@@ -497,7 +502,7 @@ static int check_sim(const pq3d_batch_sim *S)
         PQ3D_REQUIRE(S->nsplit == 1, "pq3d_batch: the FP64 and H-matrix products use nsplit = 1");
     if (S->precision == PQ3D_BATCH_FP32)
         PQ3D_REQUIRE(S->nsplit <= 64, "pq3d_batch: the FP32 product takes at most 64 K slices");
-    PQ3D_REQUIRE(S->attempt64 == 0 || S->attempt64 == 1, "pq3d_batch: attempt64 must be 0 or 1");
+    PQ3D_REQUIRE(S->attempt64 >= 0 && S->attempt64 <= 2, "pq3d_batch: attempt64 must be 0, 1 or 2");
     if (mixed_attempt(*S))
         PQ3D_REQUIRE(S->base != nullptr && aligned16(S->base), "pq3d_batch: mixed precisions need the base array");
     PQ3D_REQUIRE(S->N_total >= 0 && S->cell0 >= 0, "pq3d_batch: bad shard");

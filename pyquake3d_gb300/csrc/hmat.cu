@@ -346,16 +346,22 @@ __global__ void permute_split_kernel(const double *__restrict__ X, const int64_t
 }
 
 // T[w * B + r] = V_b[l] . x_r[cols of b] as an FP32 (hi, lo) pair for rank
-// row w (row l of low-rank block b).  The row's storage offset, first x
-// column and length come in one 16-byte record (t_info), so a warp starts
-// streaming after a single dependent load.  Work list t_sched (built by the
-// host; the split is at 8,192 columns): the shorter rows first, one warp each
-// (8 per CTA), then the longer
-// rows, one CTA each with the columns cut into 8 contiguous pieces (a warp
-// streams only a few KB in flight, so a long row on one warp would be the
-// tail) and the 8 partial sums added in warp order.  Runs are the
-// fastest-varying part of the block index, so the B CTAs that read the same
-// factor rows run together and share them in L2.
+// row w (row l of low-rank block b).  Two work lists, built by the host with
+// the split at 8,192 columns.  The shorter rows come in groups of up to 4
+// consecutive rows of one block (t_grp: one 16-byte record per group holding
+// the first row's storage offset, first x column and length, the first rank
+// row and the group size), kTGroupsPerWarp consecutive groups per warp: the
+// warp loads the next group's record while it streams the current group, so
+// no dependent descriptor load sits between two groups, and consecutive
+// groups of one block find their x values in L1.  The longer rows (t_sched
+// tail, t_info records) take one CTA each with the columns cut into kTWarps
+// contiguous pieces (a warp streams only a few KB in flight, so a long row on
+// one warp would be the tail) and the partial sums added in warp order.
+// Runs are the fastest-varying part of the block index, so the B CTAs that
+// read the same factor rows run together and share them in L2.
+constexpr int kTWarps = 4;
+constexpr int kTGroupsPerWarp = 2;
+
 __device__ __forceinline__ FF t_row_part(const float *__restrict__ v, const float2 *__restrict__ x, int c_begin,
                                          int c_end, int lane)
 {
@@ -416,9 +422,9 @@ __device__ __forceinline__ void t_row_group(const float *__restrict__ v, int nc,
 #pragma unroll
     for (int j = 0; j < 4; ++j) sum[j] = FF{0.f, 0.f};
     for (int c0k = 0; c0k < nc; c0k += 1024) {
-        Acc2 a0[4], a1[4];
+        Acc2 a[4];   // one FMA chain pair per row: the 4 rows give the pipeline its independent chains
 #pragma unroll
-        for (int j = 0; j < 4; ++j) { a0[j] = Acc2{0.f, 0.f}; a1[j] = Acc2{0.f, 0.f}; }
+        for (int j = 0; j < 4; ++j) a[j] = Acc2{0.f, 0.f};
         const int cend = min(nc, c0k + 1024);
         for (int col = c0k + lane; col - lane < cend; col += 256) {
             float2 xv[8];
@@ -432,49 +438,51 @@ __device__ __forceinline__ void t_row_group(const float *__restrict__ v, int nc,
                 for (int j = 0; j < 4; ++j) k[j][u] = (ok && j < g) ? __ldg(v + (int64_t)j * nc + c) : 0.f;
             }
 #pragma unroll
-            for (int u = 0; u < 8; u += 2)
+            for (int u = 0; u < 8; ++u)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    acc2_add(a0[j], k[j][u], xv[u]);
-                    acc2_add(a1[j], k[j][u + 1], xv[u + 1]);
-                }
+                for (int j = 0; j < 4; ++j) acc2_add(a[j], k[j][u], xv[u]);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            sum[j] = ff_add(sum[j], FF{a0[j].s, 0.f});
-            sum[j] = ff_add(sum[j], FF{a1[j].s, 0.f});
-            sum[j] = ff_add(sum[j], FF{__fadd_rn(a0[j].c, a1[j].c), 0.f});
+            sum[j] = ff_add(sum[j], FF{a[j].s, 0.f});
+            sum[j] = ff_add(sum[j], FF{a[j].c, 0.f});
         }
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) out[j] = warp_sum_ff(sum[j]);
 }
 
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(kTWarps * 32, 6)
 lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t_info,
-                 const int32_t *__restrict__ t_sched, const int32_t *__restrict__ t_grp, int64_t ngrp,
+                 const int32_t *__restrict__ t_sched, const longlong2 *__restrict__ t_grp, int64_t ngrp,
                  int64_t nshort, int64_t nlong, int64_t short_ctas,
                  const float2 *__restrict__ Xs, int64_t N, int B, float2 *__restrict__ T, const int32_t *act,
                  int act_stride)
 {
-    __shared__ FF part[8];
+    __shared__ FF part[kTWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int r = (int)(blockIdx.x % (unsigned)B);
     const int64_t cta = blockIdx.x / (unsigned)B;
     if (!run_on(act, act_stride, r)) return;   // uniform per CTA
     const float2 *xr = Xs + (int64_t)r * 2 * N;
     if (cta < short_ctas) {
-        // 8 groups of short rows per CTA, one per warp
-        const int64_t gi = cta * 8 + wid;
-        if (gi >= ngrp) return;
-        const int e = t_grp[gi];
-        const int q0 = e & 0x0FFFFFFF, g = e >> 28;
-        const int w0 = t_sched[q0];
-        const longlong2 info = t_info[w0];
-        FF sg[4];
-        t_row_group(data + info.x, (int)(info.y >> 32), g, xr + (int32_t)(info.y & 0xffffffffll), lane, sg);
-        if (lane == 0)
-            for (int j = 0; j < g; ++j) T[(w0 + j) * (int64_t)B + r] = make_float2(sg[j].hi, sg[j].lo);
+        const int64_t g0 = (cta * kTWarps + wid) * kTGroupsPerWarp;
+        if (g0 >= ngrp) return;
+        const int64_t g1 = min(ngrp, g0 + kTGroupsPerWarp);
+        // record of group gi: .x = V offset | row length << 40 | size << 56,
+        // .y = first x column | first rank row << 32
+        longlong2 nrec = t_grp[g0];
+        for (int64_t gi = g0; gi < g1; ++gi) {
+            const longlong2 rec = nrec;
+            if (gi + 1 < g1) nrec = t_grp[gi + 1];
+            const int64_t off = rec.x & ((1ll << 40) - 1);
+            const int nc = (int)((rec.x >> 40) & 0xffff), g = (int)(rec.x >> 56);
+            const int64_t w0 = (int64_t)((uint64_t)rec.y >> 32);
+            FF sg[4];
+            t_row_group(data + off, nc, g, xr + (int32_t)(rec.y & 0xffffffffll), lane, sg);
+            if (lane == 0)
+                for (int j = 0; j < g; ++j) T[(w0 + j) * (int64_t)B + r] = make_float2(sg[j].hi, sg[j].lo);
+        }
         return;
     }
     const int64_t q = cta - short_ctas;
@@ -482,14 +490,14 @@ lowrank_T_kernel(const float *__restrict__ data, const longlong2 *__restrict__ t
     const int w = t_sched[nshort + q];
     const longlong2 info = t_info[w];
     const int Nc = (int)(info.y >> 32);
-    const int piece = (Nc / 8 + 31) / 32 * 32;
+    const int piece = (Nc / kTWarps + 31) / 32 * 32;
     const int c_begin = min(Nc, wid * piece), c_end = min(Nc, (wid + 1) * piece);
     const FF s = t_row_part(data + info.x, xr + (int32_t)(info.y & 0xffffffffll), c_begin, c_end, lane);
     if (lane == 0) part[wid] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         FF t = part[0];
-        for (int k = 1; k < 8; ++k) t = ff_add(t, part[k]);
+        for (int k = 1; k < kTWarps; ++k) t = ff_add(t, part[k]);
         T[w * (int64_t)B + r] = make_float2(t.hi, t.lo);
     }
 }
@@ -744,10 +752,11 @@ extern "C" int pq3d_hmat_apply_masked(const pq3d_hmat *H, const double *X, int B
     // does not depend on B
     if (H->t_rows > 0) {
         const int64_t nshort = H->t_rows - H->t_nlong;
-        const int64_t short_ctas = (H->t_ngrp + 7) / 8;
+        const int64_t short_ctas = (H->t_ngrp + kTWarps * kTGroupsPerWarp - 1) / (kTWarps * kTGroupsPerWarp);
         const int64_t nT = (short_ctas + H->t_nlong) * B;
         PQ3D_REQUIRE(nT < (int64_t)INT32_MAX, "pq3d_hmat_apply: too many rank rows x runs");
-        lowrank_T_kernel<<<(unsigned)nT, 256, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_sched, H->t_grp,
+        lowrank_T_kernel<<<(unsigned)nT, kTWarps * 32, 0, st>>>(H->data, (const longlong2 *)H->t_info, H->t_sched,
+                                                               (const longlong2 *)H->t_grp,
                                                        H->t_ngrp, nshort,
                                                        H->t_nlong, short_ctas, Xs, N, B, T, run_active,
                                                        active_stride);

@@ -399,6 +399,261 @@ __device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, float dsig,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Float-float attempt (batched products with attempt64 = 2).
+//
+// The right-hand sides of the mixed attempt above, in float-float (hi + lo,
+// ~2^-46 relative) instead of FP32, so that the attempt carries the FP64
+// attempt's accuracy on the FP32 pipes.  What FP64 keeps is the work whose
+// absolute accuracy matters: the large exponent arguments at the start
+// state, ln(eta V0) - psi0/a +- tau_k/(a sigma) and (f0 - psi0)/b (each ~1e2
+// and nearly cancelling), formed in FP64 once per attempt and carried as
+// K ln 2 + r with an integer K and a float-float |r| <= ln 2 / 2 (Cody and
+// Waite's reduction), so that their absolute error stays at the FP64 level
+// (~1e-14) where a float-float value of ~1e2 would keep only ~1e-12.  At a
+// stage only the change of each argument is added to r.  The exponentials
+// are float-float: reduction by a multiple of ln 2 and by 2^-5, the Taylor
+// sum of e^s - 1 to s^7 (terms beyond s^3 in FP32, below 2^-48 of the sum),
+// then five doublings p <- p (p + 2), which keep the relative accuracy of
+// e^s - 1 (so that 1 -+ e^{-2|x|} near x = 0 stays accurate as well).
+// Units: stresses in MPa, so the right-hand side yields dtau/dt in MPa/s
+// directly (the factors 1e-6 sit in the FP64 constants).  The float range
+// bounds it like the mixed attempt: a stage with e^{(f0-psi)/b} > 1e38 gives
+// an infinite error (a rejection, as FP64 decides for such a stage).
+
+struct FFc {   // compile-time float-float constant
+    float hi, lo;
+};
+__host__ __device__ constexpr FFc ffc(double x) { return FFc{(float)x, (float)(x - (double)(float)x)}; }
+__device__ __forceinline__ FF ffv(FFc c) { return FF{c.hi, c.lo}; }
+
+constexpr double kLn2 = 0.69314718055994530941723212145818;
+constexpr double kLn2Hi = kLn2;                                   // ln 2 rounded to FP64
+constexpr double kLn2Lo = 2.3190468138462996154e-17;              // ln 2 - kLn2Hi
+constexpr FFc kFFLn2 = ffc(kLn2);
+
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add2(a, ff_neg(b)); }
+
+__device__ __forceinline__ FF ff_mulf(FF a, float b)
+{
+    const float p = __fmul_rn(a.hi, b);
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return ff_norm(p, e);
+}
+
+// a / b: q1 = a.hi / b.hi, the remainder a - q1 b in float-float, one
+// correction quotient
+__device__ __forceinline__ FF ff_div(FF a, FF b)
+{
+    const float rb = __frcp_rn(b.hi);
+    const float q1 = __fmul_rn(a.hi, rb);
+    const FF rem = ff_sub(a, ff_mulf(b, q1));
+    return ff_norm(q1, __fmul_rn(rem.hi, rb));
+}
+
+__device__ __forceinline__ FF ff_ldexp(FF a, int k) { return FF{ldexpf(a.hi, k), ldexpf(a.lo, k)}; }
+
+// e^t = 2^k (1 + p) with |p| < 0.42, p returned
+__device__ __forceinline__ FF ff_expm1_red(FF t, int &k)
+{
+    const float kf = rintf(t.hi * 1.44269504f);
+    k = (int)kf;
+    FF s = ff_add2(t, ff_mulf(ffv(kFFLn2), -kf));   // |s| <= ln 2 / 2 (+ rounding)
+    s.hi *= 0.03125f;
+    s.lo *= 0.03125f;
+    const float x = s.hi;
+    constexpr FFc c3 = ffc(1.0 / 6.0);
+    const float T = fmaf(x, fmaf(x, fmaf(x, (float)(1.0 / 5040.0), (float)(1.0 / 720.0)), (float)(1.0 / 120.0)),
+                         (float)(1.0 / 24.0));
+    const FF u = ff_add2(ffv(c3), FF{__fmul_rn(x, T), 0.f});    // 1/6 + s/24 + ...
+    const FF v = ff_add2(FF{0.5f, 0.f}, ff_mul(s, u));            // 1/2 + s u
+    FF p = ff_add2(s, ff_mul(ff_mul(s, s), v));                    // s + s^2 v = e^s - 1
+#pragma unroll
+    for (int d = 0; d < 5; ++d) p = ff_mul(p, ff_add2(p, FF{2.f, 0.f}));
+    return p;
+}
+
+// e^{K ln 2 + t} (K from the FP64 reduction)
+__device__ __forceinline__ FF ff_exp2k(int K, FF t)
+{
+    int k;
+    const FF p = ff_expm1_red(t, k);
+    return ff_ldexp(ff_add2(FF{1.f, 0.f}, p), k + K);
+}
+
+// e^t - 1
+__device__ __forceinline__ FF ff_expm1(FF t)
+{
+    int k;
+    const FF p = ff_expm1_red(t, k);
+    return k == 0 ? p : ff_add2(ff_ldexp(ff_add2(FF{1.f, 0.f}, p), k), FF{-1.f, 0.f});
+}
+
+// u = K ln 2 + r: K = rint(u / ln 2), r in FP64 to ~1e-16 absolute, then split
+__device__ __forceinline__ void reduce_ln2(double u, int &K, FF &r)
+{
+    u = fmin(fmax(u, -1.0e4), 1.0e4);
+    const double kd = rint(u * 1.4426950408889634);
+    K = (int)kd;
+    r = ff_split(fma(-kd, kLn2Lo, fma(-kd, kLn2Hi, u)));
+}
+
+// One cell at the attempt's start state y0 (float-float unless noted).
+struct FFCell {
+    FF sig0;          // effective normal stress (MPa)
+    FF q0[2];         // tau_k / sigma
+    FF x0[2];         // tau_k / (a sigma)
+    int Ku[2][2];     // ln(eta V0 1e-6) - psi0/a + (x0_k, -x0_k) = Ku ln 2 + ru   ([k][0: +x, 1: -x])
+    FF ru[2][2];
+    int Kg;           // (f0 - psi0) / b = Kg ln 2 + rg
+    FF rg;
+    FF a, ia, ib, bdc, V0, slipv;
+    FF dsf;           // dsigma/dt - dP/dt (MPa/s)
+    FF L[2];          // -K.v'_k + shear loading (MPa/s)
+};
+
+// dpsi/dt (1/s) and dtau_k/dt (MPa/s) at y0 + (dTn, dT1, dT2, dpsi): the
+// w-form of the mixed right-hand side, (L + w M)/(1 + w D) for W < 1 and
+// (L w + M)/(w + D) for W >= 1, w = e^{-|ln W|} (W = eta V0 e^u in MPa).
+__device__ __forceinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF dT2, FF dpsi, FF &dstate, FF &dtau1,
+                                       FF &dtau2)
+{
+    const FF rs = ff_rcp(ff_add2(m.sig0, dTn));                   // 1 / sigma
+    const FF iaS = ff_mul(m.ia, rs);                               // 1 / (a sigma)
+    const FF ed = ff_exp2k(m.Kg, ff_sub(m.rg, ff_mul(dpsi, m.ib)));   // e^{(f0 - psi)/b}
+    const FF ds_dt = ff_mul(m.bdc, ff_sub(ff_mul(m.V0, ed), m.slipv));
+    const FF dpa = ff_mul(dpsi, m.ia);
+    FF out[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const FF dx = ff_mul(ff_sub(k ? dT2 : dT1, ff_mul(m.q0[k], dTn)), iaS);   // change of tau/(a sigma)
+        const FF xs = ff_add2(m.x0[k], dx);
+        const bool pos = xs.hi >= 0.f;
+        const FF ax = pos ? xs : ff_neg(xs);
+        const FF em = ff_expm1(FF{-2.f * ax.hi, -2.f * ax.lo});   // r - 1, r = e^{-2|x|}
+        const int K = m.Ku[k][pos ? 0 : 1];
+        const FF res = ff_sub(ff_add2(m.ru[k][pos ? 0 : 1], pos ? dx : ff_neg(dx)), dpa);   // ln W - K ln 2
+        const bool big = fmaf((float)K, 0.693147182f, res.hi) >= 0.f;                    // W >= 1
+        const FF w = big ? ff_exp2k(-K, ff_neg(res)) : ff_exp2k(K, res);                  // e^{-|ln W|}
+        const FF q = ff_add2(m.q0[k], ff_mul(m.a, dx));                                    // tau / sigma
+        const FF D = ff_mul(ff_add2(FF{2.f, 0.f}, em), iaS);                               // (1 + r)/(a sigma)
+        const FF M = ff_add2(ff_mul(ff_mul(D, q), m.dsf), ff_mul(m.ia, ff_mul(pos ? ff_neg(em) : em, ds_dt)));
+        out[k] = big ? ff_div(ff_add2(ff_mul(m.L[k], w), M), ff_add2(w, D))
+                     : ff_div(ff_add2(m.L[k], ff_mul(w, M)), ff_add2(FF{1.f, 0.f}, ff_mul(w, D)));
+    }
+    dstate = ds_dt;
+    dtau1 = out[0];
+    dtau2 = out[1];
+}
+
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ bool ff_finite(FF a) { return isfinite(a.hi) && isfinite(a.lo); }
+
+// |num| / |y8| (the reference's relative error of one component) in float-float
+__device__ __forceinline__ double ff_rel_err(FF num, double y8)
+{
+    const FF q = ff_div(num, ff_split(y8));
+    return fabs(ff_to_double(q));
+}
+
+// One Dormand-Prince attempt of one cell in the float-float arithmetic above
+// (the stage sums h sum_l A_jl k_l in float-float, the start state and the
+// 5th-order solution in FP64).  lnEV = ln(eta V0 1e-6).  Writes the
+// 5th-order solution to yo and returns the two relative errors.
+__device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double lnEV, double h, const double y[4],
+                                              double yo[4], double &e1, double &e2)
+{
+    FFCell m;
+    {   // FP64 once per attempt
+        const double Tn0 = y[0] - c.P * 1e-6;                    // MPa
+        const double ia = 1.0 / c.a, iaT = 1.0 / (c.a * Tn0);
+        const double base = lnEV - y[3] * ia;                    // ln(eta V0 1e-6) - psi0/a
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const double x = y[1 + k] * iaT;
+            m.x0[k] = ff_split(x);
+            m.q0[k] = ff_split(x * c.a);
+            reduce_ln2(base + x, m.Ku[k][0], m.ru[k][0]);
+            reduce_ln2(base - x, m.Ku[k][1], m.ru[k][1]);
+        }
+        reduce_ln2((c.f0 - y[3]) / c.b, m.Kg, m.rg);
+        m.sig0 = ff_split(Tn0);
+        m.ia = ff_split(ia);
+        m.a = ff_split(c.a);
+        const FF b = ff_split(c.b);
+        m.ib = ff_rcp(b);
+        m.bdc = ff_mul(b, ff_rcp(ff_split(c.dc)));
+        m.V0 = ff_split(V0);
+        m.slipv = ff_split(c.slipv);
+        m.dsf = ff_split((c.dsig - c.dPdt) * 1e-6);
+        m.L[0] = ff_split((c.shear - c.AdotV1) * 1e-6);
+        m.L[1] = ff_split((c.shear - c.AdotV2) * 1e-6);
+    }
+    constexpr FFc A[6][6] = {{ffc(B21), {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}},
+                             {ffc(B31), ffc(B32), {0, 0}, {0, 0}, {0, 0}, {0, 0}},
+                             {ffc(B41), ffc(B42), ffc(B43), {0, 0}, {0, 0}, {0, 0}},
+                             {ffc(B51), ffc(B52), ffc(B53), ffc(B54), {0, 0}, {0, 0}},
+                             {ffc(B61), ffc(B62), ffc(B63), ffc(B64), ffc(B65), {0, 0}},
+                             {ffc(B71), {0, 0}, ffc(B73), ffc(B74), ffc(B75), ffc(B76)}};
+    constexpr FFc wsum[6] = {ffc(B21), ffc(B31 + B32), ffc(B41 + B42 + B43), ffc(B51 + B52 + B53 + B54),
+                             ffc(B61 + B62 + B63 + B64 + B65), ffc(B71 + B73 + B74 + B75 + B76)};
+    constexpr FFc Dw[7] = {ffc(B81 - B71), {0, 0}, ffc(B83 - B73), ffc(B84 - B74), ffc(B85 - B75), ffc(B86 - B76),
+                           ffc(B87)};
+    const FF hf = ff_split(h);
+    const FF dn = ff_split(c.dsig * 1e-6);   // d(Tno)/dt (MPa/s), constant over the step
+    FF s[7], t[7], u[7];
+    FF inc[4];
+    const FF z{0.f, 0.f};
+    ff_rhs(m, z, z, z, z, s[0], t[0], u[0]);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        FF ds = z, dt1 = z, dt2 = z;
+#pragma unroll
+        for (int l = 0; l <= j; ++l) {
+            if (A[j][l].hi == 0.f) continue;
+            ds = ff_add2(ds, ff_mul(ffv(A[j][l]), s[l]));
+            dt1 = ff_add2(dt1, ff_mul(ffv(A[j][l]), t[l]));
+            dt2 = ff_add2(dt2, ff_mul(ffv(A[j][l]), u[l]));
+        }
+        const FF dTn = ff_mul(hf, ff_mul(ffv(wsum[j]), dn)), dT1 = ff_mul(hf, dt1), dT2 = ff_mul(hf, dt2),
+                 dps = ff_mul(hf, ds);
+        if (j == 5) { inc[0] = dTn; inc[1] = dT1; inc[2] = dT2; inc[3] = dps; }
+        ff_rhs(m, dTn, dT1, dT2, dps, s[j + 1], t[j + 1], u[j + 1]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) yo[q] = y[q] + ff_to_double(inc[q]);
+    // 4th-order minus 5th-order solution: h sum (B8l - B7l) k_l
+    FF es = z, e1t = z, e2t = z;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) {
+        if (Dw[l].hi == 0.f) continue;
+        es = ff_add2(es, ff_mul(ffv(Dw[l]), s[l]));
+        e1t = ff_add2(e1t, ff_mul(ffv(Dw[l]), t[l]));
+        e2t = ff_add2(e2t, ff_mul(ffv(Dw[l]), u[l]));
+    }
+    es = ff_mul(hf, es);
+    e1t = ff_mul(hf, e1t);
+    e2t = ff_mul(hf, e2t);
+    // the normal stress: its rate is constant, the two orders differ by the
+    // rounding of the weight sums
+    constexpr double wn = (B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76);
+    const FF en = ff_mul(hf, ff_mulf(dn, (float)wn));
+    e1 = ff_rel_err(es, yo[3] + ff_to_double(es));
+    const double ea = ff_rel_err(e1t, yo[1] + ff_to_double(e1t)), eb = ff_rel_err(e2t, yo[2] + ff_to_double(e2t)),
+                 ec = ff_rel_err(en, yo[0] + ff_to_double(en));
+    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
+    if (!(isfinite(e1) && isfinite(e2))) {
+        const bool fin = isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) &&
+                         isfinite(c.AdotV1) && isfinite(c.AdotV2) && isfinite(c.dsig) && isfinite(c.slipv);
+        if (fin) {
+            if (!isfinite(e1)) e1 = INFINITY;
+            if (!isfinite(e2)) e2 = INFINITY;
+        }
+    }
+}
+
 // One Dormand-Prince attempt of one cell in FP64 (src/QDsim_gpu.py:1266-1397):
 // kRecip = false evaluates the reference formula, true the reciprocal form
 // (rhs_recip).  Writes the 5th-order solution to yo and returns the two

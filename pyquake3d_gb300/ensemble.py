@@ -20,18 +20,20 @@ Precisions of the traction product (``precision=``):
            the leading one on the tensor cores with exact accumulation per
            span, spans and K slices added in float-float: the FP64 product to
            ~1e-9 of its scale, for runs that must track the FP64 trajectory
-           (with attempt="fp64"); at most 64 runs
+           (with attempt="ff" or "fp64"); at most 64 runs
   "hmat"   an :class:`~pyquake3d_gb300.hmatrix.HMatrix` (large meshes)
 Time, slip, the state and the RK error norm stay FP64 in every mode.
 
 The Dormand-Prince attempt (``attempt=``): "mixed" (default for the mixed
 products) runs the seven right-hand sides in FP32 on the FP64 start state
 with float-float exponent arguments; "fp64" runs them in the reference FP64
-arithmetic (always for precision "fp64").  The FP32 stages add ~1e-7 of each
-step's increment; during nucleation the slip rate's exponential dependence
-on the traction amplifies that, so runs that must track the FP64 trajectory
-closely over many steps take attempt="fp64" (the product keeps its
-precision).
+arithmetic (always for precision "fp64"); "ff" runs them in float-float on
+the FP32 pipes, with the large exponent arguments reduced in FP64 once per
+attempt: the FP64 attempt's accuracy at a fraction of its FP64 work.  The
+FP32 stages add ~1e-7 of each step's increment; during nucleation the slip
+rate's exponential dependence on the traction amplifies that, so runs that
+must track the FP64 trajectory closely over many steps take attempt="ff" or
+"fp64" (the product keeps its precision).
 """
 from __future__ import annotations
 
@@ -80,11 +82,11 @@ class PackedFixOperator:
 
     xg: the (N, 3) element centroids.  With them the cells are taken in the
     depth-first order of the bisection cluster tree (``order``, ``pos``), so
-    that every 1024-column chunk -- whose largest |v'| sets the fixed-point
-    grid of its 512 cells -- covers one compact region of the fault.  In the
-    mesh order a chunk of a long fault spans its whole length, and a receiver
-    far from a nucleating patch that shares its chunk with the patch keeps
-    only ~24 of the 40 bits of its traction rate."""
+    that every 256-column span -- whose largest |v'| sets the fixed-point grid
+    of the 128 cells' v' slices -- and every 1024-column operator chunk cover
+    one compact region of the fault.  In the mesh order a span of a long fault
+    runs along its length, and the slow cells that share a span with a
+    nucleating patch keep only the bits of their v' below the patch's."""
 
     def __init__(self, K64: torch.Tensor, xg=None):
         L = _lib.load()
@@ -122,8 +124,8 @@ class Ensemble:
         L = _lib.load()
         self.precision = precision
         prec = PRECISIONS[precision]
-        if attempt not in ("mixed", "fp64"):
-            raise ValueError("attempt must be 'mixed' or 'fp64'")
+        if attempt not in ("mixed", "fp64", "ff"):
+            raise ValueError("attempt must be 'mixed', 'fp64' or 'ff'")
         self.attempt = "fp64" if precision == "fp64" else attempt
         tables = np.asarray(tables, dtype=np.float64)
         B, N = tables.shape[0], tables.shape[1]
@@ -193,7 +195,7 @@ class Ensemble:
             S.fix_order, S.fix_pos = K.order.data_ptr(), K.pos.data_ptr()
         S.K = ctypes.addressof(self.hmat.H) if precision == "hmat" else self.K.data_ptr()
         S.V0, S.Vpl, S.eta, S.fix_Tn = float(V0), float(Vpl), float(mu) / (2.0 * float(Cs)), int(bool(fix_Tn))
-        S.attempt64 = int(self.attempt == "fp64" and precision != "fp64")
+        S.attempt64 = 0 if precision == "fp64" else {"mixed": 0, "fp64": 1, "ff": 2}[self.attempt]
         if shard is not None:
             S.N_total, S.cell0 = Nt, self.cell0
         self.S = S

@@ -142,6 +142,7 @@ class HMatrix:
         factors = {}
         i = 0
         self.aca_chunks = 0
+        aca_events = []   # (start, end) CUDA events around each ACA launch
         while i < len(lr):
             j = i
             tot = 0
@@ -165,16 +166,23 @@ class HMatrix:
             uso_c = used_off_t[sub].contiguous()
             rk_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             stt_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record()
             _lib.check(L.pq3d_hmat_aca(self.tables.data_ptr(), N, self.perm.data_ptr(), len(ids), blk_c.data_ptr(),
                                        kcap_c.data_ptr(), float(tol), float(mu), float(lam), hs, UV.data_ptr(),
                                        uvo_c.data_ptr(), used.data_ptr(), uso_c.data_ptr(), rk_c.data_ptr(),
                                        stt_c.data_ptr(), st))
+            ev[1].record()
+            aca_events.append(ev)
             rank[ids] = rk_c.cpu().numpy()
             status[ids] = stt_c.cpu().numpy()
             factors[(i, j)] = (ids, UV, uvo_c, blk_c, kcap_c, rk_c)
             self.aca_chunks += 1
             i = j
         phase("aca")
+        # device time of the ACA launches alone (the rest of the phase is the
+        # factor allocations and the rank/status copies back)
+        phases["aca_kernels"] = sum(a.elapsed_time(b) for a, b in aca_events) / 1e3
         ok = lowrank & (status == 0)
         rank[~ok] = -1
         self.aca_status = status
@@ -259,27 +267,33 @@ class HMatrix:
     T_GROUP = 4       # short rank rows of one block handled together (they share the x values)
 
     def _make_sched(self, info):
-        Nc = (np.asarray(info)[:, 1] >> 32) if self.t_rows else np.zeros(0, np.int64)
+        info = np.asarray(info, dtype=np.int64).reshape(-1, 2)
+        Nc = (info[:, 1] >> 32) if self.t_rows else np.zeros(0, np.int64)
         rows = np.arange(len(Nc), dtype=np.int32)
         longm = Nc > self.LONG_ROW
         sched = np.concatenate([rows[~longm], rows[longm]]) if len(Nc) else np.zeros(1, np.int32)
         self.t_sched = torch.as_tensor(np.ascontiguousarray(sched, dtype=np.int32), device=self.device)
         self.t_nlong = int(longm.sum())
         # groups of up to T_GROUP consecutive short rows of one low-rank block
-        # (all rows of a block have the same length): first position in
-        # t_sched | group size << 28
-        grp = []
+        # (all rows of a block have the same length), in block order; one
+        # 16-byte record each: V offset of the first row | row length << 40 |
+        # size << 56, then first column | first row << 32
+        rec = np.zeros((0, 2), dtype=np.int64)
         if self.t_rows:
-            ranks = self.rank.cpu().numpy()[self.lr_ids.cpu().numpy()].astype(np.int64) if len(Nc) else []
-            pos = np.cumsum(~longm) - 1
-            first = 0
-            for k in ranks:
-                if k > 0 and not longm[first]:
-                    for j in range(0, int(k), self.T_GROUP):
-                        grp.append(int(pos[first + j]) | (min(self.T_GROUP, int(k) - j) << 28))
-                first += int(k)
-        self.t_grp = torch.as_tensor(np.asarray(grp if grp else [0], dtype=np.int32), device=self.device)
-        self.t_ngrp = len(grp)
+            ranks = self.rank.cpu().numpy()[self.lr_ids.cpu().numpy()].astype(np.int64)
+            first = np.concatenate([[0], np.cumsum(ranks)[:-1]]).astype(np.int64)
+            keep = ranks > 0
+            keep[keep] = ~longm[first[keep]]
+            k, f = ranks[keep], first[keep]
+            ng = (k + self.T_GROUP - 1) // self.T_GROUP
+            j = np.arange(int(ng.sum()), dtype=np.int64) - np.repeat(np.cumsum(ng) - ng, ng)
+            w0 = np.repeat(f, ng) + self.T_GROUP * j
+            size = np.minimum(self.T_GROUP, np.repeat(k, ng) - self.T_GROUP * j)
+            off, col, nc = info[w0, 0], info[w0, 1] & 0xffffffff, info[w0, 1] >> 32
+            assert np.all(off < 2 ** 40) and np.all(nc <= self.LONG_ROW) and self.t_rows < 2 ** 31
+            rec = np.stack([off | (nc << 40) | (size << 56), col | (w0 << 32)], axis=1)
+        self.t_grp = torch.as_tensor(rec if len(rec) else np.zeros((1, 2), np.int64), device=self.device)
+        self.t_ngrp = len(rec)
 
     def _make_struct(self):
         H = _lib.HMat()

@@ -3,8 +3,10 @@ continuously batched on one GPU.
 
 * Requests arrive by a seeded Poisson process; each names a mesh, carries its
   own friction/stress draw (a per-cell table) and a simulated span.
-* Every mesh keeps its traction operator resident (dense BF16x6-packed
-  operator for N <= dense_max_n, an H-matrix above) and an
+* Every mesh keeps its traction operator resident (a dense packed operator
+  for N <= dense_max_n -- the exact fixed-point BF16x18 product with the
+  float-float Dormand-Prince attempt, or the faster BF16x6 product with the mixed
+  attempt, ``dense_precision`` -- an H-matrix above) and an
   :class:`~pyquake3d_gb300.ensemble.Ensemble` with a fixed number of slots.
 * Admission: a request enters a free slot of its mesh when the HBM budget
   (operators + the run state of occupied slots) allows; otherwise it waits
@@ -90,15 +92,24 @@ class Server:
     """GPU runtime of the serving loop.
 
     meshes: list of dicts with keys nodes, tris, L (m), W (m); the operator
-    kind follows N (dense BF16x6 for N <= dense_max_n, H-matrix above)."""
+    kind follows N (dense for N <= dense_max_n, H-matrix above).
+    dense_precision: "bf16x18" (fixed-point slices, float-float attempt: slip within
+    1e-5 of the FP64 stepper for ~100 accepted steps at N = 10,000) or
+    "bf16x6" (BF16 pieces, mixed attempt: ~25 steps, 4x the product rate)."""
 
     def __init__(self, meshes, *, mu, lam, cs, slots=16, budget_bytes=150e9, dense_max_n=20000, graph_iters=16,
-                 max_steps=4000, device="cuda", hmat_kw=None):
+                 max_steps=4000, device="cuda", hmat_kw=None, dense_precision="bf16x6"):
         import torch
 
         from . import gf
-        from .ensemble import Ensemble, PackedOperator
+        from .ensemble import Ensemble, PackedFixOperator, PackedOperator
         from .hmatrix import HMatrix
+        from .mesh import element_frames
+        if dense_precision not in ("bf16x6", "bf16x18"):
+            raise ValueError("dense_precision must be 'bf16x6' or 'bf16x18'")
+        if dense_precision == "bf16x18" and slots > 64:
+            raise ValueError("the bf16x18 product takes at most 64 slots")
+        self.dense_precision = dense_precision
         self.torch = torch
         self.device = torch.device(device)
         self.meshes = meshes
@@ -117,12 +128,18 @@ class Server:
             dummy[:, :, 6] = 30.0; dummy[:, :, 7] = 1e-9
             if N <= dense_max_n:
                 K64, _ = gf.assemble_dense(nodes, tris, mu, lam, fp32_copy=False, device=self.device)
-                op = PackedOperator(K64)
-                del K64
-                torch.cuda.empty_cache()
-                ens = Ensemble(op, dummy, mu=mu, Cs=cs, precision="bf16x6")
-                op_bytes[m] = op.data.numel()
-                self.kind[m] = "dense_bf16x6"
+                if dense_precision == "bf16x18":
+                    op = PackedFixOperator(K64, element_frames(nodes, tris)[1])
+                    del K64
+                    torch.cuda.empty_cache()
+                    ens = Ensemble(op, dummy, mu=mu, Cs=cs, precision="bf16x18", attempt="ff")
+                else:
+                    op = PackedOperator(K64)
+                    del K64
+                    torch.cuda.empty_cache()
+                    ens = Ensemble(op, dummy, mu=mu, Cs=cs, precision="bf16x6")
+                op_bytes[m] = op.data.numel() * op.data.element_size()
+                self.kind[m] = "dense_" + dense_precision
             else:
                 op = HMatrix(nodes, tris, mu, lam, device=self.device, **hmat_kw)
                 ens = Ensemble(op, dummy, mu=mu, Cs=cs, precision="hmat")

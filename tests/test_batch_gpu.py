@@ -171,6 +171,31 @@ def test_fp32_batched_product_close_to_fp64(cuda, golden):
         assert normwise_rel(ra[r], rb[r]) < 1e-5, r
 
 
+@pytest.mark.parametrize("nsplit", [1, 4, 9])
+def test_fp32_product_k_slices(cuda, golden, nsplit):
+    """The split-K FP32 product with 1, 4 and 9 K slices.  The golden mesh
+    has 2N = 128 columns = 4 chunks of 32, so with 9 slices five get an empty
+    K range and must write zeros.  The partials are NaN before the product,
+    so a slice that writes nothing shows.  Each result is within 1e-5 of the
+    FP64 product and within 1e-6 of the one-slice result (only the order of
+    the FP32 chunk sums differs)."""
+    g, K = _golden(golden, cuda)
+    tabs = _tables(g, 3, seed=2)
+    a = Ensemble(K, tabs, mu=float(g["mu"]), Cs=CS, precision="fp64")
+    K32 = K.float().contiguous()
+    one = Ensemble(K32, tabs, mu=float(g["mu"]), Cs=CS, precision="fp32", nsplit=1)
+    b = Ensemble(K32, tabs, mu=float(g["mu"]), Cs=CS, precision="fp32", nsplit=nsplit)
+    assert b.nsplit == nsplit
+    b.t["rates"].fill_(float("nan"))
+    for e in (a, one, b):
+        e.iterate(1)
+    ra, r1, rb = _rates(a), _rates(one), _rates(b)
+    assert np.all(np.isfinite(rb))
+    for r in range(3):
+        assert normwise_rel(ra[r], rb[r]) < 1e-5, r
+        assert normwise_rel(r1[r], rb[r]) < 1e-6, r
+
+
 def test_run_alone_equals_run_in_mix_bitwise(cuda, golden):
     """Serving determinism: a run's trajectory does not depend on which other
     runs share the batch (per-element accumulation order is fixed)."""

@@ -84,7 +84,7 @@ def test_batch_structure_checks_need_no_gpu():
     cases = [(dict(nsplit=2), "nsplit"),
              (dict(precision=_lib.PQ3D_BATCH_FP32, nsplit=65), "64 K slices"),
              (dict(precision=_lib.PQ3D_BATCH_BF16X6, tc_ctas=4), "tc_ctas"),
-             (dict(precision=_lib.PQ3D_BATCH_FP32, attempt64=2), "attempt64"),
+             (dict(precision=_lib.PQ3D_BATCH_FP32, attempt64=3), "attempt64"),
              (dict(precision=_lib.PQ3D_BATCH_FP32, base=None), "base array")]
     for kw, text in cases:
         S = sim(**kw)

@@ -57,7 +57,7 @@ def test_oracle_partition_matches_reference_golden():
 def test_low_rank_row_schedule_and_groups():
     """Host-side work lists of the low-rank product: short rows first (row
     order), long rows after; groups of up to 4 consecutive short rows of one
-    block, each group's rows contiguous in the schedule."""
+    block, each group one record (the first row's t_info, first row, size)."""
     import torch
     from pyquake3d_gb300.hmatrix import HMatrix
     H = HMatrix.__new__(HMatrix)
@@ -75,16 +75,18 @@ def test_low_rank_row_schedule_and_groups():
     short = np.nonzero(Nc <= H.LONG_ROW)[0]
     assert np.array_equal(sched[:len(short)], short) and H.t_nlong == 9
     assert np.array_equal(np.sort(sched[len(short):]), np.nonzero(Nc > H.LONG_ROW)[0])
-    grp = H.t_grp.numpy()
-    q0, g = grp & 0x0FFFFFFF, grp >> 28
+    rec = H.t_grp.numpy()
+    w0, g = rec[:, 1] >> 32, rec[:, 0] >> 56
     assert list(g) == [4, 1, 3, 1] and H.t_ngrp == 4
-    covered = np.concatenate([sched[a:a + n] for a, n in zip(q0, g)])
+    assert np.array_equal(rec[:, 0] & (2 ** 40 - 1), info[w0, 0])
+    assert np.array_equal((rec[:, 0] >> 40) & 0xffff, info[w0, 1] >> 32)
+    assert np.array_equal(rec[:, 1] & 0xffffffff, info[w0, 1] & 0xffffffff)
+    covered = np.concatenate([np.arange(a, a + n) for a, n in zip(w0, g)])
     assert np.array_equal(np.sort(covered), short)
     # rows of a group are consecutive rows of one block
     block_of = np.repeat(np.arange(len(lr)), ranks)
-    for a, n in zip(q0, g):
-        rows = sched[a:a + n]
-        assert np.all(np.diff(rows) == 1) and len(set(block_of[rows])) == 1
+    for a, n in zip(w0, g):
+        assert len(set(block_of[a:a + n])) == 1
 
 
 @pytest.mark.gpu

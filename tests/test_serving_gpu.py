@@ -78,3 +78,30 @@ def test_serving_hmatrix_mesh_result_alone_equals_mix(cuda):
         c = alone.read_ctrl()[0]
         assert c.status == 0 and c.active == 0
         assert c.steps == r.steps and c.attempts == r.attempts and c.time == r.sim_time, r.rid
+
+
+def test_serving_bf16x18_result_alone_equals_mix(cuda):
+    """Dense meshes on the fixed-point BF16x18 product with the float-float attempt
+    (dense_precision="bf16x18"): a request replayed alone on a one-run
+    ensemble of the same packed operator and K slices takes the same steps
+    and attempts and reaches the same simulated time, bit for bit (the v'
+    exponents, slices and float-float sums are per run)."""
+    from pyquake3d_gb300.ensemble import PackedFixOperator
+    meshes = _meshes()
+    srv = Server(meshes, mu=MU, lam=MU, cs=3464.0, slots=4, budget_bytes=50e9, graph_iters=8, max_steps=400,
+                 device=cuda, dense_max_n=10 ** 9, dense_precision="bf16x18")
+    assert all(k == "dense_bf16x18" for k in srv.kind.values())
+    reqs = _requests(meshes, 8, seed=5)
+    res = srv.run(reqs, time_limit_s=120)
+    assert res["completed"] == 8 and res["failed"] == 0
+    for r in reqs[:3]:
+        ens = srv.ens[r.mesh]
+        op = PackedFixOperator(gf.assemble_dense(meshes[r.mesh]["nodes"], meshes[r.mesh]["tris"], MU, MU,
+                                                 fp32_copy=False, device=cuda)[0],
+                               mesh.element_frames(meshes[r.mesh]["nodes"], meshes[r.mesh]["tris"])[1])
+        alone = Ensemble(op, r.table[None], mu=MU, Cs=3464.0, precision="bf16x18", attempt="ff", t_end=r.span_s,
+                         max_steps=400, nsplit=ens.nsplit)
+        alone.iterate(r.attempts + 5)
+        c = alone.read_ctrl()[0]
+        assert c.status == 0 and c.active == 0
+        assert c.steps == r.steps and c.attempts == r.attempts and c.time == r.sim_time, r.rid

@@ -16,10 +16,10 @@ pytestmark = pytest.mark.gpu
 MU = 32038120320.0
 
 
-def _check(K, tabs, precision, world, iters):
-    whole = Ensemble(K, tabs, mu=MU, Cs=CS, precision=precision)
+def _check(K, tabs, precision, world, iters, **kw):
+    whole = Ensemble(K, tabs, mu=MU, Cs=CS, precision=precision, **kw)
     whole.iterate(iters)
-    shards = make_shards(K, tabs, world, mu=MU, Cs=CS, precision=precision)
+    shards = make_shards(K, tabs, world, mu=MU, Cs=CS, precision=precision, **kw)
     iterate_sharded(shards, InProcessExchange(), iters)
     torch.cuda.synchronize()
     cw = whole.read_ctrl()
@@ -42,6 +42,17 @@ def test_shards_bitwise_golden(cuda, golden, precision):
     if precision == "fp32":
         K = K.float().contiguous()
     _check(K, _tables(g, 3), precision, 3, 150)
+
+
+@pytest.mark.parametrize("nsplit", [1, 9])
+def test_shards_fp32_k_slices(cuda, golden, nsplit):
+    """FP32 product on row shards (each shard: N = 21 or 22 of Nt = 64 cells,
+    its K slices over all 2 Nt columns) with one slice and with more slices
+    than the 4 column chunks: the same bits as the unsharded ensemble."""
+    d = golden("dense_small.npz")
+    g = golden("traj_small.npz")
+    K = torch.as_tensor(gf.join_ops({k: d["planar_" + k] for k in oracle.OPS}), device=cuda).float().contiguous()
+    _check(K, _tables(g, 3), "fp32", 3, 150, nsplit=nsplit)
 
 
 def test_shards_bitwise_n2000(cuda):
