@@ -252,6 +252,46 @@ __global__ void __launch_bounds__(256, 2) gemm_f32_kernel(const float *__restric
     }
 }
 
+// Traction rates of cell i of run r as float-float values (FP32 pipes): the
+// BF16X18 product leaves float-float partials per K slice, BF16X6 FP32
+// partials per K slice (added here in float-float, slice order), the other
+// mixed products FP64 sums (FP64 K-slice partials; one for H-matrix products).
+__device__ __forceinline__ void ff_partials(const pq3d_batch_sim &S, int r, int64_t i, FF q[3])
+{
+    const int64_t N = S.N;
+    const int Bp = padded_runs(S.B);
+    if (S.precision == PQ3D_BATCH_BF16X18) {
+        const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
+        const float2 *pr = (const float2 *)S.rates + (int64_t)r * 3 * N + 3 * pos;
+        const int64_t sstride = (int64_t)Bp * 3 * N;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) q[c] = ff_norm(pr[c].x, pr[c].y);
+        for (int sl = 1; sl < S.nsplit; ++sl)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 t = pr[sl * sstride + c];
+                q[c] = ff_add2(q[c], FF{t.x, t.y});
+            }
+    } else if (S.precision == PQ3D_BATCH_BF16X6) {
+        const float *pr = (const float *)S.rates + (int64_t)r * 3 * N + 3 * i;
+        const int64_t sstride = (int64_t)Bp * 3 * N;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) q[c] = FF{pr[c], 0.f};
+        for (int sl = 1; sl < S.nsplit; ++sl)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) q[c] = ff_add(q[c], pr[sl * sstride + c]);
+    } else {
+        const double *pr = S.rates + (int64_t)r * 3 * N + 3 * i;
+        const int64_t sstride = (int64_t)Bp * 3 * N;
+        double t[3] = {pr[0], pr[1], pr[2]};
+        for (int sl = 1; sl < S.nsplit; ++sl)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[c] += pr[sl * sstride + c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) q[c] = ff_split(t[c]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // attempt / decide / update
 
@@ -263,6 +303,7 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
     __shared__ double hs;
     __shared__ float hsf, V0f;
     __shared__ double lnev;   // ln(eta V0 1e-6) of the float-float attempt
+    __shared__ FF etab[64];
     const int r = blockIdx.y;
     pq3d_run_ctrl *C = S.ctrl + r;
     if (threadIdx.x == 0) {
@@ -275,6 +316,7 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             lnev = log(S.eta * S.V0 * 1e-6);
         }
     }
+    if (!kMixed && threadIdx.x < 64) etab[threadIdx.x] = ffv(kExp2Tab.v[threadIdx.x]);
     __syncthreads();
     if (!act) return;
     const int64_t N = S.N;
@@ -287,40 +329,8 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
         const double y[4] = {S.Tno[idx], S.Tt1o[idx], S.Tt2o[idx], S.state[idx]};
         double yo[4];
         if (kMixed) {
-            // traction rates: the BF16X6 product leaves FP32 partials per K
-            // slice (added here in float-float, slice order), the other mixed
-            // products one FP64 value
             FF q[3];
-            if (S.precision == PQ3D_BATCH_BF16X18) {   // float-float partials per K slice
-                const int64_t pos = S.fix_pos ? S.fix_pos[i] : i;
-                const float2 *pr = (const float2 *)S.rates + (int64_t)r * 3 * N + 3 * pos;
-                const int64_t sstride = (int64_t)Bp * 3 * N;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) q[c] = ff_norm(pr[c].x, pr[c].y);
-                for (int sl = 1; sl < S.nsplit; ++sl)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float2 t = pr[sl * sstride + c];
-                        q[c] = ff_add2(q[c], FF{t.x, t.y});
-                    }
-            } else if (S.precision == PQ3D_BATCH_BF16X6) {
-                const float *pr = (const float *)S.rates + (int64_t)r * 3 * N + 3 * i;
-                const int64_t sstride = (int64_t)Bp * 3 * N;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) q[c] = FF{pr[c], 0.f};
-                for (int sl = 1; sl < S.nsplit; ++sl)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) q[c] = ff_add(q[c], pr[sl * sstride + c]);
-            } else {   // FP64 partial sums per K slice (one for H-matrix products)
-                const double *pr = S.rates + (int64_t)r * 3 * N + 3 * i;
-                const int64_t sstride = (int64_t)Bp * 3 * N;
-                double t[3] = {pr[0], pr[1], pr[2]};
-                for (int sl = 1; sl < S.nsplit; ++sl)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) t[c] += pr[sl * sstride + c];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) q[c] = ff_split(t[c]);
-            }
+            ff_partials(S, r, i, q);
             MixedBase m = load_base(S.base + idx, (int64_t)S.B * N);
             const float shear = (float)S.shear_loading[idx];
             const float dsig = S.fix_Tn ? (float)S.normal_loading[idx]
@@ -330,6 +340,15 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             m.L[0] = (shear - q[0].hi) - q[0].lo;
             m.L[1] = (shear - q[1].hi) - q[1].lo;
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
+        } else if (S.attempt64 == 2 && S.precision != PQ3D_BATCH_FP64) {
+            // float-float attempt: the rates stay float-float (no FP64 sums)
+            FF q[3];
+            ff_partials(S, r, i, q);
+            const FF nl = ff_split(S.normal_loading[idx]);
+            const FFRates fr{q[0], q[1], S.fix_Tn ? nl : ff_add2(q[2], nl)};
+            const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], 0.0, 0.0, 0.0,
+                         0.0, 0.0};
+            dp_attempt_ff(c, fr, S.V0, lnev, hs, y, yo, m1, m2, etab);
         } else {
             double q0 = 0.0, q1 = 0.0, q2 = 0.0;
             if (S.precision == PQ3D_BATCH_BF16X18) {   // float-float K-slice partials, added in FP64
@@ -359,7 +378,6 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             // products (attempt64 = 1) takes the reciprocal form, the
             // float-float attempt (attempt64 = 2) the w-form on the FP32 pipes
             if (S.precision == PQ3D_BATCH_FP64) dp_attempt<false>(c, S.V0, S.eta, hs, y, yo, m1, m2);
-            else if (S.attempt64 == 2) dp_attempt_ff(c, S.V0, lnev, hs, y, yo, m1, m2);
             else dp_attempt<true>(c, S.V0, S.eta, hs, y, yo, m1, m2);
         }
         reinterpret_cast<double4_16a *>(S.cand)[idx] = make_double4_16a(yo[0], yo[1], yo[2], yo[3]);

@@ -41,7 +41,7 @@ namespace gf {
 
 constexpr double kPi = 3.141592653589793;
 
-// Per-source record (29 values, stored with stride kSrcStride).
+// Per-source record (35 values, stored with stride kSrcStride).
 enum SrcField {
     F_P2X, F_P2Y, F_P2Z,          // origin (vertex 2)
     F_NX, F_NY, F_NZ,             // triangle normal
@@ -51,9 +51,12 @@ enum SrcField {
     F_DEN,                        // barycentric denominator of the mode test
     F_E13Y, F_E13Z, F_E12Y, F_E12Z, F_E23Y, F_E23Z,   // unit side vectors (y, z)
     F_CA, F_SA, F_CB, F_SB, F_CC, F_SC,               // cos, sin of (angle - pi) per vertex
+    // double angle (sz^2 - sy^2, 2 sy sz) of each vertex's side vector (sy,
+    // sz) for the back-rotation (sign-free, so the same for both modes)
+    F_C2A, F_S2A, F_C2B, F_S2B, F_C2C, F_S2C,
     F_COUNT
 };
-constexpr int kSrcStride = 32;
+constexpr int kSrcStride = 36;
 constexpr int kRecvStride = 12;   // x, y, z, e1[3], e2[3], n[3]
 
 __host__ __device__ inline void unit3(double v[3])
@@ -96,7 +99,10 @@ __host__ __device__ inline void setup_source(const double P1[3], const double P2
         p1[1], p1[2], p3[1], p3[2],
         -p3[2] * (p1[1] - p3[1]) + p3[1] * (p1[2] - p3[2]),
         e13[1], e13[2], e12[1], e12[2], e23[1], e23[2],
-        cos(Am), sin(Am), cos(Bm), sin(Bm), cos(Cm), sin(Cm)};
+        cos(Am), sin(Am), cos(Bm), sin(Bm), cos(Cm), sin(Cm),
+        e13[2] * e13[2] - e13[1] * e13[1], 2.0 * (e13[1] * e13[2]),
+        e12[2] * e12[2] - e12[1] * e12[1], 2.0 * (e12[1] * e12[2]),
+        e23[2] * e23[2] - e23[1] * e23[1], 2.0 * (e23[1] * e23[2])};
     for (int i = 0; i < F_COUNT; ++i) f[i * fstride] = vals[i];
 }
 
@@ -300,13 +306,23 @@ __device__ __forceinline__ bool tdcs_strain_sd(const Src &F, T x, T y, T z, doub
     for (int i = 0; i < 6; ++i) { Es[i] = 0.0; Ed[i] = 0.0; }
     const int m = tri_mode<T>(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
     if (m == 0) return false;
-    const double sg = (m == 1) ? 1.0 : -1.0;
+    const bool pm = (m == 1);   // the side vectors' signs by selection, not products
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-        T vy, vz, sy, sz, ca, sa;
-        if (v == 0) { vy = F(F_P1Y); vz = F(F_P1Z); sy = -sg * F(F_E13Y); sz = -sg * F(F_E13Z); ca = F(F_CA); sa = F(F_SA); }
-        else if (v == 1) { vy = 0.0; vz = 0.0; sy = sg * F(F_E12Y); sz = sg * F(F_E12Z); ca = F(F_CB); sa = F(F_SB); }
-        else { vy = F(F_P3Y); vz = F(F_P3Z); sy = sg * F(F_E23Y); sz = sg * F(F_E23Z); ca = F(F_CC); sa = F(F_SC); }
+        T vy, vz, sy, sz, ca, sa, c2, s2;
+        if (v == 0) {
+            const T ey = F(F_E13Y), ez = F(F_E13Z);
+            vy = F(F_P1Y); vz = F(F_P1Z); sy = pm ? -ey : ey; sz = pm ? -ez : ez; ca = F(F_CA); sa = F(F_SA);
+            c2 = F(F_C2A); s2 = F(F_S2A);
+        } else if (v == 1) {
+            const T ey = F(F_E12Y), ez = F(F_E12Z);
+            vy = 0.0; vz = 0.0; sy = pm ? ey : -ey; sz = pm ? ez : -ez; ca = F(F_CB); sa = F(F_SB);
+            c2 = F(F_C2B); s2 = F(F_S2B);
+        } else {
+            const T ey = F(F_E23Y), ez = F(F_E23Z);
+            vy = F(F_P3Y); vz = F(F_P3Z); sy = pm ? ey : -ey; sz = pm ? ez : -ez; ca = F(F_CC); sa = F(F_SC);
+            c2 = F(F_C2C); s2 = F(F_S2C);
+        }
         const T ty = y - vy, tz = z - vz;
         AdGeom<T> g;
         ad_geom<T>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
@@ -318,7 +334,6 @@ __device__ __forceinline__ bool tdcs_strain_sd(const Src &F, T x, T y, T z, doub
             ts[i] = sz * Ey[i] + sy * Ez[i];    // strike: (by1, bz1) = (sz, sy)
             td[i] = -sy * Ey[i] + sz * Ez[i];   // dip:    (by1, bz1) = (-sy, sz)
         }
-        const T c2 = sz * sz - sy * sy, s2 = 2.0 * (sy * sz);
         add_rot_x(Es, ts, sy, sz, c2, s2);
         add_rot_x(Ed, td, sy, sz, c2, s2);
     }

@@ -412,10 +412,13 @@ __device__ __forceinline__ void dp_attempt_mixed(const MixedBase &m, float dsig,
 // Waite's reduction), so that their absolute error stays at the FP64 level
 // (~1e-14) where a float-float value of ~1e2 would keep only ~1e-12.  At a
 // stage only the change of each argument is added to r.  The exponentials
-// are float-float: reduction by a multiple of ln 2 and by 2^-5, the Taylor
-// sum of e^s - 1 to s^7 (terms beyond s^3 in FP32, below 2^-48 of the sum),
-// then five doublings p <- p (p + 2), which keep the relative accuracy of
-// e^s - 1 (so that 1 -+ e^{-2|x|} near x = 0 stays accurate as well).
+// are float-float; e^t - 1 (for 1 -+ e^{-2|x|} near x = 0) by reduction by a
+// multiple of ln 2 and by 2^-5, the Taylor sum of e^s - 1 to s^7 (terms
+// beyond s^3 in FP32, below 2^-48 of the sum), then five doublings
+// p <- p (p + 2), which keep the relative accuracy of e^s - 1.
+// The exponentials of the arguments carried as K ln 2 + r use a 64-entry
+// table of 2^{j/64} and a Taylor sum to s^6 (|s| <= ln 2 / 128); e^{-2|x|} - 1
+// near x = 0 keeps the doubling form.
 // Units: stresses in MPa, so the right-hand side yields dtau/dt in MPa/s
 // directly (the factors 1e-6 sit in the FP64 constants).  The float range
 // bounds it like the mixed attempt: a stage with e^{(f0-psi)/b} > 1e38 gives
@@ -452,13 +455,26 @@ __device__ __forceinline__ FF ff_div(FF a, FF b)
     return ff_norm(q1, __fmul_rn(rem.hi, rb));
 }
 
-__device__ __forceinline__ FF ff_ldexp(FF a, int k) { return FF{ldexpf(a.hi, k), ldexpf(a.lo, k)}; }
+// a 2^k by two exact power-of-two products (FP32 pipe only; k clamped to
+// +-252, beyond which every float result is 0 or infinite anyway)
+__device__ __forceinline__ FF ff_ldexp(FF a, int k)
+{
+    k = min(252, max(-252, k));
+    const int k1 = k >> 1, k2 = k - k1;
+    const float s1 = __int_as_float((k1 + 127) << 23), s2 = __int_as_float((k2 + 127) << 23);
+    return FF{__fmul_rn(__fmul_rn(a.hi, s1), s2), __fmul_rn(__fmul_rn(a.lo, s1), s2)};
+}
 
-// e^t = 2^k (1 + p) with |p| < 0.42, p returned
+// e^t = 2^k (1 + p) with |p| < 0.42, p returned.  k = rint(t / ln 2) by the
+// 1.5 2^23 addition (the integer lands in the low mantissa bits; no
+// float-to-integer conversion), t clamped to +-200 (e^{+-200} is out of the
+// float-float range: the caller's scaling saturates to 0 or infinity)
 __device__ __forceinline__ FF ff_expm1_red(FF t, int &k)
 {
-    const float kf = rintf(t.hi * 1.44269504f);
-    k = (int)kf;
+    if (!(fabsf(t.hi) <= 200.f)) t = FF{t.hi != t.hi ? t.hi : copysignf(200.f, t.hi), 0.f};
+    const float sum = __fadd_rn(__fmul_rn(t.hi, 1.44269504f), 12582912.f);
+    const float kf = __fsub_rn(sum, 12582912.f);
+    k = __float_as_int(sum) - 0x4B400000;
     FF s = ff_add2(t, ff_mulf(ffv(kFFLn2), -kf));   // |s| <= ln 2 / 2 (+ rounding)
     s.hi *= 0.03125f;
     s.lo *= 0.03125f;
@@ -474,20 +490,53 @@ __device__ __forceinline__ FF ff_expm1_red(FF t, int &k)
     return p;
 }
 
-// e^{K ln 2 + t} (K from the FP64 reduction)
-__device__ __forceinline__ FF ff_exp2k(int K, FF t)
-{
-    int k;
-    const FF p = ff_expm1_red(t, k);
-    return ff_ldexp(ff_add2(FF{1.f, 0.f}, p), k + K);
-}
-
 // e^t - 1
 __device__ __forceinline__ FF ff_expm1(FF t)
 {
     int k;
     const FF p = ff_expm1_red(t, k);
     return k == 0 ? p : ff_add2(ff_ldexp(ff_add2(FF{1.f, 0.f}, p), k), FF{-1.f, 0.f});
+}
+
+
+// e^x by its Taylor series in FP64 (compile time, |x| < 0.7: 30 terms reach
+// the FP64 rounding)
+__host__ __device__ constexpr double exp_series(double x)
+{
+    double term = 1.0, sum = 1.0;
+    for (int n = 1; n < 30; ++n) { term *= x / n; sum += term; }
+    return sum;
+}
+// 2^{j/64}, j = 0..63, as float-float; each attempt block copies it to
+// shared memory (lanes index it independently)
+struct Exp2Table {
+    FFc v[64];
+    __host__ __device__ constexpr Exp2Table() : v()
+    {
+        for (int j = 0; j < 64; ++j) v[j] = ffc(exp_series(j * (kLn2 / 64.0)));
+    }
+};
+__constant__ Exp2Table kExp2Tab{};
+constexpr FFc kFFLn2_64 = ffc(kLn2 / 64.0);
+
+// e^{K ln 2 + t} = 2^{K + n/64} e^s, n = rint(64 t / ln 2), s = t - n ln 2 / 64
+// (|s| <= ln 2 / 128: the Taylor sum to s^6, terms beyond s^3 in FP32), the
+// factor 2^{(n mod 64)/64} from the table tab (shared memory)
+__device__ __forceinline__ FF ff_exp2k_tab(int K, FF t, const FF *tab)
+{
+    if (!(fabsf(t.hi) <= 200.f)) t = FF{t.hi != t.hi ? t.hi : copysignf(200.f, t.hi), 0.f};
+    const float sum = __fadd_rn(__fmul_rn(t.hi, 92.332482616893656f), 12582912.f);
+    const float nf = __fsub_rn(sum, 12582912.f);
+    const int n = __float_as_int(sum) - 0x4B400000;
+    const FF s = ff_add2(t, ff_mulf(ffv(kFFLn2_64), -nf));
+    const float x = s.hi;
+    constexpr FFc c3 = ffc(1.0 / 6.0);
+    const float T = fmaf(x, fmaf(x, (float)(1.0 / 720.0), (float)(1.0 / 120.0)), (float)(1.0 / 24.0));
+    const FF u = ff_add2(ffv(c3), FF{__fmul_rn(x, T), 0.f});
+    const FF v = ff_add2(FF{0.5f, 0.f}, ff_mul(s, u));
+    const FF p = ff_add2(s, ff_mul(ff_mul(s, s), v));
+    const FF tj = tab[n & 63];
+    return ff_ldexp(ff_add2(tj, ff_mul(tj, p)), (n >> 6) + K);
 }
 
 // u = K ln 2 + r: K = rint(u / ln 2), r in FP64 to ~1e-16 absolute, then split
@@ -516,12 +565,14 @@ struct FFCell {
 // dpsi/dt (1/s) and dtau_k/dt (MPa/s) at y0 + (dTn, dT1, dT2, dpsi): the
 // w-form of the mixed right-hand side, (L + w M)/(1 + w D) for W < 1 and
 // (L w + M)/(w + D) for W >= 1, w = e^{-|ln W|} (W = eta V0 e^u in MPa).
-__device__ __forceinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF dT2, FF dpsi, FF &dstate, FF &dtau1,
-                                       FF &dtau2)
+// Not inlined: the seven call sites of an attempt share one copy of its code
+// (inlined seven times the attempt overflowed the instruction cache).
+static __device__ __noinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF dT2, FF dpsi, FF &dstate, FF &dtau1,
+                                    FF &dtau2, const FF *tab)
 {
     const FF rs = ff_rcp(ff_add2(m.sig0, dTn));                   // 1 / sigma
     const FF iaS = ff_mul(m.ia, rs);                               // 1 / (a sigma)
-    const FF ed = ff_exp2k(m.Kg, ff_sub(m.rg, ff_mul(dpsi, m.ib)));   // e^{(f0 - psi)/b}
+    const FF ed = ff_exp2k_tab(m.Kg, ff_sub(m.rg, ff_mul(dpsi, m.ib)), tab);   // e^{(f0 - psi)/b}
     const FF ds_dt = ff_mul(m.bdc, ff_sub(ff_mul(m.V0, ed), m.slipv));
     const FF dpa = ff_mul(dpsi, m.ia);
     FF out[2];
@@ -531,11 +582,12 @@ __device__ __forceinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF dT2, 
         const FF xs = ff_add2(m.x0[k], dx);
         const bool pos = xs.hi >= 0.f;
         const FF ax = pos ? xs : ff_neg(xs);
-        const FF em = ff_expm1(FF{-2.f * ax.hi, -2.f * ax.lo});   // r - 1, r = e^{-2|x|}
+        // r - 1, r = e^{-2|x|}; for |x| > 20, r < 5e-18 needs no float-float
+        const FF em = ax.hi > 20.f ? FF{-1.f, expf(-2.f * ax.hi)} : ff_expm1(FF{-2.f * ax.hi, -2.f * ax.lo});
         const int K = m.Ku[k][pos ? 0 : 1];
         const FF res = ff_sub(ff_add2(m.ru[k][pos ? 0 : 1], pos ? dx : ff_neg(dx)), dpa);   // ln W - K ln 2
         const bool big = fmaf((float)K, 0.693147182f, res.hi) >= 0.f;                    // W >= 1
-        const FF w = big ? ff_exp2k(-K, ff_neg(res)) : ff_exp2k(K, res);                  // e^{-|ln W|}
+        const FF w = big ? ff_exp2k_tab(-K, ff_neg(res), tab) : ff_exp2k_tab(K, res, tab);                  // e^{-|ln W|}
         const FF q = ff_add2(m.q0[k], ff_mul(m.a, dx));                                    // tau / sigma
         const FF D = ff_mul(ff_add2(FF{2.f, 0.f}, em), iaS);                               // (1 + r)/(a sigma)
         const FF M = ff_add2(ff_mul(ff_mul(D, q), m.dsf), ff_mul(m.ia, ff_mul(pos ? ff_neg(em) : em, ds_dt)));
@@ -551,20 +603,23 @@ __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (do
 
 __device__ __forceinline__ bool ff_finite(FF a) { return isfinite(a.hi) && isfinite(a.lo); }
 
-// |num| / |y8| (the reference's relative error of one component) in float-float
-__device__ __forceinline__ double ff_rel_err(FF num, double y8)
-{
-    const FF q = ff_div(num, ff_split(y8));
-    return fabs(ff_to_double(q));
-}
+// Rates of one cell for the float-float attempt, as float-float values from
+// the product's partial sums (no FP64 arithmetic): K.v' strike and dip
+// (Pa/s), the normal-stress rate dsigma/dt (Pa/s, loading included).
+struct FFRates {
+    FF A1, A2, dsig;
+};
 
 // One Dormand-Prince attempt of one cell in the float-float arithmetic above
 // (the stage sums h sum_l A_jl k_l in float-float, the start state and the
-// 5th-order solution in FP64).  lnEV = ln(eta V0 1e-6).  Writes the
-// 5th-order solution to yo and returns the two relative errors.
-__device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double lnEV, double h, const double y[4],
-                                              double yo[4], double &e1, double &e2)
+// 5th-order solution in FP64).  c supplies the cell's friction parameters,
+// shear loading, slip rate and pore pressure (its AdotV and dsig fields are
+// not read: the rates come as float-float in q).  lnEV = ln(eta V0 1e-6).
+// Writes the 5th-order solution to yo and returns the two relative errors.
+__device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, double V0, double lnEV, double h,
+                                              const double y[4], double yo[4], double &e1, double &e2, const FF *tab)
 {
+    constexpr FFc kMicro = ffc(1e-6);
     FFCell m;
     {   // FP64 once per attempt
         const double Tn0 = y[0] - c.P * 1e-6;                    // MPa
@@ -587,9 +642,10 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double l
         m.bdc = ff_mul(b, ff_rcp(ff_split(c.dc)));
         m.V0 = ff_split(V0);
         m.slipv = ff_split(c.slipv);
-        m.dsf = ff_split((c.dsig - c.dPdt) * 1e-6);
-        m.L[0] = ff_split((c.shear - c.AdotV1) * 1e-6);
-        m.L[1] = ff_split((c.shear - c.AdotV2) * 1e-6);
+        m.dsf = ff_mul(ff_sub(q.dsig, ff_split(c.dPdt)), ffv(kMicro));
+        const FF shear = ff_split(c.shear);
+        m.L[0] = ff_mul(ff_sub(shear, q.A1), ffv(kMicro));
+        m.L[1] = ff_mul(ff_sub(shear, q.A2), ffv(kMicro));
     }
     constexpr FFc A[6][6] = {{ffc(B21), {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}},
                              {ffc(B31), ffc(B32), {0, 0}, {0, 0}, {0, 0}, {0, 0}},
@@ -602,11 +658,11 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double l
     constexpr FFc Dw[7] = {ffc(B81 - B71), {0, 0}, ffc(B83 - B73), ffc(B84 - B74), ffc(B85 - B75), ffc(B86 - B76),
                            ffc(B87)};
     const FF hf = ff_split(h);
-    const FF dn = ff_split(c.dsig * 1e-6);   // d(Tno)/dt (MPa/s), constant over the step
+    const FF dn = ff_mul(q.dsig, ffv(kMicro));   // d(Tno)/dt (MPa/s), constant over the step
     FF s[7], t[7], u[7];
     FF inc[4];
     const FF z{0.f, 0.f};
-    ff_rhs(m, z, z, z, z, s[0], t[0], u[0]);
+    ff_rhs(m, z, z, z, z, s[0], t[0], u[0], tab);
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         FF ds = z, dt1 = z, dt2 = z;
@@ -620,7 +676,7 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double l
         const FF dTn = ff_mul(hf, ff_mul(ffv(wsum[j]), dn)), dT1 = ff_mul(hf, dt1), dT2 = ff_mul(hf, dt2),
                  dps = ff_mul(hf, ds);
         if (j == 5) { inc[0] = dTn; inc[1] = dT1; inc[2] = dT2; inc[3] = dps; }
-        ff_rhs(m, dTn, dT1, dT2, dps, s[j + 1], t[j + 1], u[j + 1]);
+        ff_rhs(m, dTn, dT1, dT2, dps, s[j + 1], t[j + 1], u[j + 1], tab);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) yo[q] = y[q] + ff_to_double(inc[q]);
@@ -640,13 +696,23 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, double V0, double l
     // rounding of the weight sums
     constexpr double wn = (B81 + B83 + B84 + B85 + B86 + B87) - (B71 + B73 + B74 + B75 + B76);
     const FF en = ff_mul(hf, ff_mulf(dn, (float)wn));
-    e1 = ff_rel_err(es, yo[3] + ff_to_double(es));
-    const double ea = ff_rel_err(e1t, yo[1] + ff_to_double(e1t)), eb = ff_rel_err(e2t, yo[2] + ff_to_double(e2t)),
-                 ec = ff_rel_err(en, yo[0] + ff_to_double(en));
-    e2 = (isnan(ea) || isnan(eb) || isnan(ec)) ? NAN : fmax(fmax(ea, eb), ec);
+    // |y8 - yo| / |y8| with y8 = y0 + inc + (y8 - yo), in float-float (the
+    // step-size control takes the 5th root of these: FP32 quotients alone
+    // moved the step sizes, and after 40 steps the slips, by ~1e-9)
+    auto rel = [&](FF num, int qi) {
+        const FF y8 = ff_add2(ff_split(y[qi]), ff_add2(inc[qi], num));
+        const FF r = ff_div(num, y8);
+        return r.hi < 0.f ? FF{-r.hi, -r.lo} : r;
+    };
+    const FF f1 = rel(es, 3), fa = rel(e1t, 1), fb = rel(e2t, 2), fc = rel(en, 0);
+    auto ffmax = [](FF a, FF b) { return (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b; };
+    const bool nan2 = isnan(fa.hi) || isnan(fb.hi) || isnan(fc.hi);
+    const FF f2 = ffmax(ffmax(fa, fb), fc);
+    e1 = ff_to_double(f1);
+    e2 = nan2 ? NAN : ff_to_double(f2);
     if (!(isfinite(e1) && isfinite(e2))) {
         const bool fin = isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) &&
-                         isfinite(c.AdotV1) && isfinite(c.AdotV2) && isfinite(c.dsig) && isfinite(c.slipv);
+                         ff_finite(q.A1) && ff_finite(q.A2) && ff_finite(q.dsig) && isfinite(c.slipv);
         if (fin) {
             if (!isfinite(e1)) e1 = INFINITY;
             if (!isfinite(e2)) e2 = INFINITY;
