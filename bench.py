@@ -132,9 +132,9 @@ def fp64_peak_tflops(torch, dev):
 
 
 # FP64 operations of one (receiver, source) pair of the assembly kernel
-# (both unit slips, 6 entries): 324 add + 516 mul + 5 div + 3 sqrt, counted by
+# (both unit slips, 6 entries): 321 add + 498 mul + 5 div + 3 sqrt, counted by
 # oracle/count_gf_flops.cpp on the kernel's own device math.
-GF_FLOP_PER_PAIR = 848
+GF_FLOP_PER_PAIR = 827
 # The same for the half-space kernel (main + image dislocation, the
 # free-surface correction of the three sides in dual numbers): 5,426.7 add +
 # 9,009.4 mul + 72.9 div + 18.0 sqrt per pair (and 18.0 transcendental calls),
