@@ -95,16 +95,21 @@ __device__ __forceinline__ double block_sum(double v, double *sv)
 }
 
 // One CTA per admissible block.  U: kcap x M (row l = u_l), V: kcap x Nc.
+// kAcaThreads per CTA (238 registers: one CTA per SM).  Fewer threads with
+// more CTAs per SM measured slower (N = 100,000: 1.28 s with 256, 1.55 s with
+// 128, 2.69 s with 64): the residual updates, norms and pivot searches of an
+// iteration scale with the CTA's threads.
+constexpr int kAcaThreads = 256;
 template <bool kHalf>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kAcaThreads)
 aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *__restrict__ perm,
            const int64_t *__restrict__ blk, const int32_t *__restrict__ kcap, double tol,
            double *__restrict__ UV, const int64_t *__restrict__ uv_off,
            uint8_t *__restrict__ used_ws, const int64_t *__restrict__ used_off, int32_t *__restrict__ rank_out,
            int32_t *__restrict__ status_out)
 {
-    __shared__ double sv[kThreads / 32];
-    __shared__ int si[kThreads / 32];
+    __shared__ double sv[kAcaThreads / 32];
+    __shared__ int si[kAcaThreads / 32];
     const int b = blockIdx.x;
     const int64_t r0 = blk[4 * b], r1 = blk[4 * b + 1], c0 = blk[4 * b + 2], c1 = blk[4 * b + 3];
     const int m = (int)(r1 - r0), n = (int)(c1 - c0);
@@ -123,7 +128,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         const int pr = istar / 3, cr = istar % 3;
         const double *R = recv + kRecvStride * perm[r0 + pr];
         double *v = V + (int64_t)k * Nc;
-        for (int q = t; q < n; q += kThreads) {
+        for (int q = t; q < n; q += kAcaThreads) {
             double ts[3], td[3];
             gen(perm[c0 + q], R, ts, td);
             v[2 * q] = ts[cr];
@@ -135,7 +140,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         {
             double mv = -1.0;
             int mi = 0x7fffffff;
-            for (int col = t; col < Nc; col += kThreads) {
+            for (int col = t; col < Nc; col += kAcaThreads) {
                 double x = v[col];
                 for (int l = 0; l < k; ++l) x -= U[(int64_t)l * M + istar] * V[(int64_t)l * Nc + col];
                 v[col] = x;
@@ -161,7 +166,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         const int qc = jstar / 2, sc = jstar % 2;
         const int64_t jb = perm[c0 + qc];
         double *u = U + (int64_t)k * M;
-        for (int p = t; p < m; p += kThreads) {
+        for (int p = t; p < m; p += kAcaThreads) {
             double ts[3], td[3];
             gen(jb, recv + kRecvStride * perm[r0 + p], ts, td);
             const double *tt = sc ? td : ts;
@@ -170,7 +175,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
             u[3 * p + 2] = tt[2];
         }
         __syncthreads();
-        for (int row = t; row < M; row += kThreads) {
+        for (int row = t; row < M; row += kAcaThreads) {
             double x = u[row];
             for (int l = 0; l < k; ++l) x -= V[(int64_t)l * Nc + jstar] * U[(int64_t)l * M + row];
             u[row] = x / pivot;
@@ -178,8 +183,8 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         __syncthreads();
         // norms: |S_k|^2 = |S_{k-1}|^2 + 2 sum_l (u.u_l)(v.v_l) + |u|^2 |v|^2
         double nu2 = 0.0, nv2 = 0.0;
-        for (int row = t; row < M; row += kThreads) nu2 += u[row] * u[row];
-        for (int col = t; col < Nc; col += kThreads) nv2 += v[col] * v[col];
+        for (int row = t; row < M; row += kAcaThreads) nu2 += u[row] * u[row];
+        for (int col = t; col < Nc; col += kAcaThreads) nv2 += v[col] * v[col];
         nu2 = block_sum(nu2, sv);
         nv2 = block_sum(nv2, sv);
         // the k cross products (u.u_l)(v.v_l): one warp per term l (warp
@@ -187,7 +192,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         double cross_w = 0.0;
         {
             const int w = t >> 5, lane = t & 31;
-            for (int l = w; l < k; l += kThreads / 32) {
+            for (int l = w; l < k; l += kAcaThreads / 32) {
                 double du = 0.0, dv = 0.0;
                 for (int row = lane; row < M; row += 32) du += u[row] * U[(int64_t)l * M + row];
                 for (int col = lane; col < Nc; col += 32) dv += v[col] * V[(int64_t)l * Nc + col];
@@ -206,7 +211,7 @@ aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *_
         // next pivot row: largest |u| among unused rows
         double mv = -1.0;
         int mi = 0x7fffffff;
-        for (int row = t; row < M; row += kThreads) {
+        for (int row = t; row < M; row += kAcaThreads) {
             const double ax = fabs(u[row]);
             if (!used[row] && ax > mv) { mv = ax; mi = row; }
         }
@@ -693,10 +698,10 @@ extern "C" int pq3d_hmat_aca(const double *tables, int64_t N, const int64_t *per
     const double *recv = tables + (size_t)kSrcStride * N;
     cudaStream_t st = (cudaStream_t)stream;
     if (halfspace)
-        aca_kernel<true><<<nblocks, kThreads, 0, st>>>(make_gen<true>(tables, N, mu, lambda_), recv, perm, blk, kcap,
+        aca_kernel<true><<<nblocks, kAcaThreads, 0, st>>>(make_gen<true>(tables, N, mu, lambda_), recv, perm, blk, kcap,
                                                        tol, UV, uv_off, used, used_off, rank, status);
     else
-        aca_kernel<false><<<nblocks, kThreads, 0, st>>>(make_gen<false>(tables, N, mu, lambda_), recv, perm, blk,
+        aca_kernel<false><<<nblocks, kAcaThreads, 0, st>>>(make_gen<false>(tables, N, mu, lambda_), recv, perm, blk,
                                                         kcap, tol, UV, uv_off, used, used_off, rank, status);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;

@@ -267,7 +267,7 @@ STAGE_OVERSHOOT_CELLS = np.array([
      1.1721852933987974e-09, -803.5071173343583, -67.20042687143759, -1.0927068774489872)])
 
 
-def _recorded_cells_ensemble(cuda, precision, h, rows):
+def _recorded_cells_ensemble(cuda, precision, h, rows, attempt="mixed"):
     """One run over the recorded cells: state written directly, and a
     (3n x 2n) operator with one non-zero column per cell so that K.v'
     reproduces the recorded traction rates."""
@@ -284,7 +284,7 @@ def _recorded_cells_ensemble(cuda, precision, h, rows):
     Kt = torch.as_tensor(K, device=cuda)
     if precision == "fp32":
         Kt = Kt.float().contiguous()
-    ens = Ensemble(Kt, tab, mu=MU, Cs=CS, precision=precision, dttry=h)
+    ens = Ensemble(Kt, tab, mu=MU, Cs=CS, precision=precision, dttry=h, attempt=attempt)
     for k, col in (("Tno", 4), ("Tt1o", 5), ("Tt2o", 6), ("state", 7), ("slipv", 8), ("slipv1", 8)):
         ens.t[k][0].copy_(torch.as_tensor(cells[:, col]))
     ens.t["slipv2"].zero_()
@@ -338,6 +338,36 @@ def test_mixed_attempt_in_range_through_stage_overshoot(cuda, rows, h):
     assert np.all(np.abs(c32 - c64) <= 1e-6 * inc + 1e-13 * np.abs(y0))
     assert k32.accepted == k64.accepted
     assert abs(k32.h - k64.h) <= 1e-4 * k64.h
+
+
+@pytest.mark.parametrize("rows,h", [(slice(0, 4), STAGE_OVERSHOOT_DT), (slice(0, 8), STAGE_OVERSHOOT_DT / 2),
+                                    (slice(4, 8), STAGE_OVERSHOOT_DT), (slice(0, 8), 0.5)])
+def test_ff_attempt_matches_fp64_attempt_through_stage_overshoot(cuda, rows, h):
+    """The float-float attempt against the FP64 attempt on the recorded cells,
+    the same FP32 product under both: error norms within 1e-6 (the first, a
+    difference of two states ~0.8 apart, carries the FP64 attempt's own
+    rounding of ~1e-6 of it) and 1e-9 relative, candidate state within 1e-12
+    of the step's increment, the same decision and next step size to 1e-9 --
+    including the attempt whose stage 5 overshoots (the w-form keeps the
+    float-float range)."""
+    res = {}
+    for att in ("fp64", "ff"):
+        ens, _ = _recorded_cells_ensemble(cuda, "fp32", h, rows, attempt=att)
+        ens.begin()
+        err = ens.error_words()[0].cpu().numpy().view(np.float64)
+        cand = ens.t["cand"].view(-1, 4).cpu().numpy()
+        ens.end()
+        res[att] = (err, cand, ens.read_ctrl()[0])
+    e64, c64, k64 = res["fp64"]
+    eff, cff, kff = res["ff"]
+    assert np.all(np.isfinite(eff)) and np.all(np.isfinite(cff))
+    assert abs(eff[0] - e64[0]) <= 1e-6 * e64[0] + 1e-14
+    assert abs(eff[1] - e64[1]) <= 1e-9 * e64[1] + 1e-15
+    y0 = STAGE_OVERSHOOT_CELLS[rows][:, [4, 5, 6, 7]]
+    inc = np.abs(c64 - y0)
+    assert np.all(np.abs(cff - c64) <= 1e-12 * inc + 1e-15 * np.abs(y0))
+    assert kff.accepted == k64.accepted
+    assert abs(kff.h - k64.h) <= 1e-9 * k64.h
 
 
 def test_batched_fp64_matches_single_simulation_n10000(cuda):
