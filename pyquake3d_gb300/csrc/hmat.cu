@@ -95,13 +95,17 @@ __device__ __forceinline__ double block_sum(double v, double *sv)
 }
 
 // One CTA per admissible block.  U: kcap x M (row l = u_l), V: kcap x Nc.
-// kAcaThreads per CTA (238 registers: one CTA per SM).  Fewer threads with
-// more CTAs per SM measured slower (N = 100,000: 1.28 s with 256, 1.55 s with
-// 128, 2.69 s with 64): the residual updates, norms and pivot searches of an
-// iteration scale with the CTA's threads.
+// kAcaThreads per CTA (246 registers in full space: one CTA per SM).  Other
+// shapes measured no better (N = 100,000, ACA launches: 1.28 s with 256
+// threads; 128 and 64 threads with 2 and 4 CTAs per SM 1.55 s and 2.69 s --
+// the residual updates, norms and pivot searches of an iteration scale with
+// the CTA's threads; 256 threads capped at 128 registers for 2 CTAs per SM
+// 1.34 s; 512 threads at 128 registers 1.26 s): the FP64 pipe, busy with the
+// GF evaluations of the pivot rows and columns, sets the pace.
 constexpr int kAcaThreads = 256;
+constexpr int kAcaMinBlocks = 1;
 template <bool kHalf>
-__global__ void __launch_bounds__(kAcaThreads)
+__global__ void __launch_bounds__(kAcaThreads, kHalf ? 1 : kAcaMinBlocks)
 aca_kernel(PairGen<kHalf> gen, const double *__restrict__ recv, const int64_t *__restrict__ perm,
            const int64_t *__restrict__ blk, const int32_t *__restrict__ kcap, double tol,
            double *__restrict__ UV, const int64_t *__restrict__ uv_off,
