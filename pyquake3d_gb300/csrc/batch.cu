@@ -295,8 +295,10 @@ __device__ __forceinline__ void ff_partials(const pq3d_batch_sim &S, int r, int6
 // ---------------------------------------------------------------------------
 // attempt / decide / update
 
-template <bool kMixed>
-__global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch_sim S)
+// kFF: the float-float attempt (attempt64 = 2), with its own launch bounds
+// (3 CTAs per SM: its float-float chains are latency bound, not register bound)
+template <bool kMixed, bool kFF = false>
+__global__ void __launch_bounds__(256, kMixed ? 4 : (kFF ? 3 : 2)) attempt_kernel(pq3d_batch_sim S)
 {
     __shared__ unsigned long long red[32];
     __shared__ int act;
@@ -312,11 +314,11 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
         if (kMixed) {
             hsf = (float)hs;
             V0f = (float)S.V0;
-        } else if (S.attempt64 == 2) {
+        } else if (kFF) {
             lnev = log(S.eta * S.V0 * 1e-6);
         }
     }
-    if (!kMixed && threadIdx.x < 64) etab[threadIdx.x] = ffv(kExp2Tab.v[threadIdx.x]);
+    if (kFF && threadIdx.x < 64) etab[threadIdx.x] = ffv(kExp2Tab.v[threadIdx.x]);
     __syncthreads();
     if (!act) return;
     const int64_t N = S.N;
@@ -340,11 +342,11 @@ __global__ void __launch_bounds__(256, kMixed ? 4 : 2) attempt_kernel(pq3d_batch
             m.L[0] = (shear - q[0].hi) - q[0].lo;
             m.L[1] = (shear - q[1].hi) - q[1].lo;
             dp_attempt_mixed(m, dsig, hsf, y, yo, f1, f2);
-        } else if (S.attempt64 == 2 && S.precision != PQ3D_BATCH_FP64) {
+        } else if (kFF) {
             // float-float attempt: the rates stay float-float (no FP64 sums)
             FF q[3];
             ff_partials(S, r, i, q);
-            const FF nl = ff_split(S.normal_loading[idx]);
+            const FF nl = ff_split_fast(S.normal_loading[idx]);
             const FFRates fr{q[0], q[1], S.fix_Tn ? nl : ff_add2(q[2], nl)};
             const Cell c{S.a[idx], S.b[idx], S.dc[idx], S.f0[idx], S.shear_loading[idx], S.slipv[idx], 0.0, 0.0, 0.0,
                          0.0, 0.0};
@@ -445,10 +447,12 @@ template <bool kMixed>
 __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
 {
     __shared__ int acc;
-    __shared__ double hs;
+    __shared__ double hs, lnv0;
     __shared__ float inv_eta, c0hi, c0lo;
+    __shared__ FF etab[64];
     const int r = blockIdx.y;
     const pq3d_run_ctrl *C = S.ctrl + r;
+    const bool ffu = !kMixed && S.attempt64 == 2 && S.precision != PQ3D_BATCH_FP64;
     if (threadIdx.x == 0) {
         acc = C->accepted;
         hs = C->h_last;
@@ -457,8 +461,11 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
             c0hi = c0.hi;
             c0lo = c0.lo;
             inv_eta = (float)(1.0 / S.eta);
+        } else if (ffu) {
+            lnv0 = log(S.V0);
         }
     }
+    if (ffu && threadIdx.x < 64) etab[threadIdx.x] = ffv(kExp2Tab.v[threadIdx.x]);
     __syncthreads();
     if (!acc) return;
     const int64_t N = S.N;
@@ -482,6 +489,14 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
         const float vf = fmaxf(p * sqrtf(fmaf(t, t, 1.f)), 1e-30f);
         pb[19 * stride] = vf;
         v1 = f1; v2 = f2; v = vf;
+    } else if (ffu) {
+        // the float-float arm: 2 V0 e^{-psi/a} sinh(x) = sign(x) V0 e^{-psi/a + |x|} (1 - e^{-2|x|}),
+        // x = tau / (a sigma), the exponent argument in FP64 (reduced), the rest float-float
+        const double a = S.a[idx];
+        const double psia = st * rcp_d(a), iaT = rcp_d(a * Tno);
+        v1 = ff_slip_rate(lnv0, psia, T1 * iaT, etab);
+        v2 = ff_slip_rate(lnv0, psia, T2 * iaT, etab);
+        v = sqrt(v1 * v1 + v2 * v2);
     } else {
         const double a = S.a[idx];
         const double e = (2.0 * S.V0) * exp(-st / a);
@@ -608,6 +623,7 @@ extern "C" int pq3d_batch_iterate_begin(const pq3d_batch_sim *sim, void *workspa
     // 2. attempt (FP64 arm: the reference arithmetic; mixed arms: dp_attempt_mixed)
     dim3 grid((unsigned)((S.N + 255) / 256), (unsigned)S.B);
     if (mixed_attempt(S)) attempt_kernel<true><<<grid, 256, 0, st>>>(S);
+    else if (S.attempt64 == 2 && S.precision != PQ3D_BATCH_FP64) attempt_kernel<false, true><<<grid, 256, 0, st>>>(S);
     else attempt_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;

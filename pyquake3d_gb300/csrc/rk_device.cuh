@@ -430,6 +430,42 @@ struct FFc {   // compile-time float-float constant
 __host__ __device__ constexpr FFc ffc(double x) { return FFc{(float)x, (float)(x - (double)(float)x)}; }
 __device__ __forceinline__ FF ffv(FFc c) { return FF{c.hi, c.lo}; }
 
+// FP64 <-> float-float with integer operations: GB300's FP64 pipe, which
+// also executes the FP64 <-> FP32 conversions, runs at 1/64 of the FP32 rate.
+// ff_split_fast: hi = x truncated to 24 significant bits, lo = the next 24
+// (truncated: |x - hi - lo| < 2^-47 |x|), renormalised; |x| outside
+// [2^-60, 2^127) (and infinities, NaN) takes the conversions of ff_split,
+// zero and FP64 subnormals give a signed zero.
+__device__ __forceinline__ FF ff_split_fast(double x)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    if (e == 0) return FF{__uint_as_float(hw & 0x80000000u), 0.f};
+    if (e < 1023 - 60 || e > 1023 + 126) return ff_split(x);
+    const unsigned sign = hw & 0x80000000u;
+    const float hi =
+        __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+    const unsigned rem = lw & 0x1fffffffu;   // the 29 mantissa bits below hi's
+    if (rem == 0) return FF{hi, 0.f};
+    const int p = 31 - __clz((int)rem);       // rem = 2^p (1.m): p in 0..28
+    const unsigned m = p <= 23 ? (rem << (23 - p)) : (rem >> (p - 23));
+    const float lo = __uint_as_float(sign | ((unsigned)(p + e - 1075 + 127) << 23) | (m & 0x7fffffu));
+    return ff_norm(hi, lo);
+}
+
+// float -> FP64 by the bit layout (zero and normal floats; the rest converts)
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ef = (u >> 23) & 0xffu;
+    if ((u & 0x7fffffffu) == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (ef == 0 || ef == 0xffu) return (double)f;
+    return __hiloint2double((int)((u & 0x80000000u) | ((ef - 127 + 1023) << 20) | ((u & 0x7fffffu) >> 3)),
+                            (int)((u & 0x7u) << 29));
+}
+
+__device__ __forceinline__ double ff_to_double_fast(FF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
 constexpr double kLn2 = 0.69314718055994530941723212145818;
 constexpr double kLn2Hi = kLn2;                                   // ln 2 rounded to FP64
 constexpr double kLn2Lo = 2.3190468138462996154e-17;              // ln 2 - kLn2Hi
@@ -539,13 +575,24 @@ __device__ __forceinline__ FF ff_exp2k_tab(int K, FF t, const FF *tab)
     return ff_ldexp(ff_add2(tj, ff_mul(tj, p)), (n >> 6) + K);
 }
 
-// u = K ln 2 + r: K = rint(u / ln 2), r in FP64 to ~1e-16 absolute, then split
+// u = K ln 2 + r: K = rint(u / ln 2) by the 1.5 2^52 addition (the integer
+// lands in the low word: no conversion instruction), r in FP64 to ~1e-16
+// absolute, then split
 __device__ __forceinline__ void reduce_ln2(double u, int &K, FF &r)
 {
     u = fmin(fmax(u, -1.0e4), 1.0e4);
-    const double kd = rint(u * 1.4426950408889634);
-    K = (int)kd;
-    r = ff_split(fma(-kd, kLn2Lo, fma(-kd, kLn2Hi, u)));
+    const double t = fma(u, 1.4426950408889634, 6755399441055744.0);
+    const double kd = t - 6755399441055744.0;
+    K = __double2loint(t);
+    r = ff_split_fast(fma(-kd, kLn2Lo, fma(-kd, kLn2Hi, u)));
+}
+
+// 1/a in FP64 from the float-float reciprocal and one Newton step (three
+// FP64-pipe instructions where an FP64 division is a sequence of many)
+__device__ __forceinline__ double rcp_d(double a)
+{
+    const double r0 = ff_to_double_fast(ff_rcp(ff_split_fast(a)));
+    return fma(r0, fma(-a, r0, 1.0), r0);
 }
 
 // One cell at the attempt's start state y0 (float-float unless noted).
@@ -623,27 +670,27 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
     FFCell m;
     {   // FP64 once per attempt
         const double Tn0 = y[0] - c.P * 1e-6;                    // MPa
-        const double ia = 1.0 / c.a, iaT = 1.0 / (c.a * Tn0);
+        const double ia = rcp_d(c.a), iaT = rcp_d(c.a * Tn0);
         const double base = lnEV - y[3] * ia;                    // ln(eta V0 1e-6) - psi0/a
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const double x = y[1 + k] * iaT;
-            m.x0[k] = ff_split(x);
-            m.q0[k] = ff_split(x * c.a);
+            m.x0[k] = ff_split_fast(x);
+            m.q0[k] = ff_split_fast(x * c.a);
             reduce_ln2(base + x, m.Ku[k][0], m.ru[k][0]);
             reduce_ln2(base - x, m.Ku[k][1], m.ru[k][1]);
         }
-        reduce_ln2((c.f0 - y[3]) / c.b, m.Kg, m.rg);
-        m.sig0 = ff_split(Tn0);
-        m.ia = ff_split(ia);
-        m.a = ff_split(c.a);
-        const FF b = ff_split(c.b);
+        reduce_ln2((c.f0 - y[3]) * rcp_d(c.b), m.Kg, m.rg);
+        m.sig0 = ff_split_fast(Tn0);
+        m.ia = ff_split_fast(ia);
+        m.a = ff_split_fast(c.a);
+        const FF b = ff_split_fast(c.b);
         m.ib = ff_rcp(b);
-        m.bdc = ff_mul(b, ff_rcp(ff_split(c.dc)));
-        m.V0 = ff_split(V0);
-        m.slipv = ff_split(c.slipv);
-        m.dsf = ff_mul(ff_sub(q.dsig, ff_split(c.dPdt)), ffv(kMicro));
-        const FF shear = ff_split(c.shear);
+        m.bdc = ff_mul(b, ff_rcp(ff_split_fast(c.dc)));
+        m.V0 = ff_split_fast(V0);
+        m.slipv = ff_split_fast(c.slipv);
+        m.dsf = ff_mul(ff_sub(q.dsig, ff_split_fast(c.dPdt)), ffv(kMicro));
+        const FF shear = ff_split_fast(c.shear);
         m.L[0] = ff_mul(ff_sub(shear, q.A1), ffv(kMicro));
         m.L[1] = ff_mul(ff_sub(shear, q.A2), ffv(kMicro));
     }
@@ -657,7 +704,7 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
                              ffc(B61 + B62 + B63 + B64 + B65), ffc(B71 + B73 + B74 + B75 + B76)};
     constexpr FFc Dw[7] = {ffc(B81 - B71), {0, 0}, ffc(B83 - B73), ffc(B84 - B74), ffc(B85 - B75), ffc(B86 - B76),
                            ffc(B87)};
-    const FF hf = ff_split(h);
+    const FF hf = ff_split_fast(h);
     const FF dn = ff_mul(q.dsig, ffv(kMicro));   // d(Tno)/dt (MPa/s), constant over the step
     FF s[7], t[7], u[7];
     FF inc[4];
@@ -679,7 +726,7 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
         ff_rhs(m, dTn, dT1, dT2, dps, s[j + 1], t[j + 1], u[j + 1], tab);
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) yo[q] = y[q] + ff_to_double(inc[q]);
+    for (int q = 0; q < 4; ++q) yo[q] = y[q] + ff_to_double_fast(inc[q]);
     // 4th-order minus 5th-order solution: h sum (B8l - B7l) k_l
     FF es = z, e1t = z, e2t = z;
 #pragma unroll
@@ -700,7 +747,7 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
     // step-size control takes the 5th root of these: FP32 quotients alone
     // moved the step sizes, and after 40 steps the slips, by ~1e-9)
     auto rel = [&](FF num, int qi) {
-        const FF y8 = ff_add2(ff_split(y[qi]), ff_add2(inc[qi], num));
+        const FF y8 = ff_add2(ff_split_fast(y[qi]), ff_add2(inc[qi], num));
         const FF r = ff_div(num, y8);
         return r.hi < 0.f ? FF{-r.hi, -r.lo} : r;
     };
@@ -708,8 +755,8 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
     auto ffmax = [](FF a, FF b) { return (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b; };
     const bool nan2 = isnan(fa.hi) || isnan(fb.hi) || isnan(fc.hi);
     const FF f2 = ffmax(ffmax(fa, fb), fc);
-    e1 = ff_to_double(f1);
-    e2 = nan2 ? NAN : ff_to_double(f2);
+    e1 = ff_to_double_fast(f1);
+    e2 = nan2 ? NAN : ff_to_double_fast(f2);
     if (!(isfinite(e1) && isfinite(e2))) {
         const bool fin = isfinite(y[0]) && isfinite(y[1]) && isfinite(y[2]) && isfinite(y[3]) &&
                          ff_finite(q.A1) && ff_finite(q.A2) && ff_finite(q.dsig) && isfinite(c.slipv);
@@ -718,6 +765,23 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
             if (!isfinite(e2)) e2 = INFINITY;
         }
     }
+}
+
+// One slip-rate component of the float-float arm's update: 2 V0 e^{-psi/a}
+// sinh(x) = sign(x) V0 e^{-psi/a + |x|} (1 - e^{-2|x|}), lnV0 = ln V0, psia =
+// psi/a, x = tau/(a sigma) in FP64; the exponent argument reduced in FP64,
+// the exponentials and the product in float-float, the result in FP64.
+__device__ __forceinline__ double ff_slip_rate(double lnV0, double psia, double x, const FF *tab)
+{
+    const double ax = fabs(x);
+    int K;
+    FF r;
+    reduce_ln2(lnV0 - psia + ax, K, r);
+    const FF e = ff_exp2k_tab(K, r, tab);
+    const FF axf = ff_split_fast(ax);
+    const FF em = axf.hi > 20.f ? FF{-1.f, expf(-2.f * axf.hi)} : ff_expm1(FF{-2.f * axf.hi, -2.f * axf.lo});
+    const double v = ff_to_double_fast(ff_mul(e, ff_neg(em)));
+    return x < 0.0 ? -v : v;
 }
 
 // One Dormand-Prince attempt of one cell in FP64 (src/QDsim_gpu.py:1266-1397):
