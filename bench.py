@@ -750,9 +750,68 @@ def bench_hmatrix(torch, dev, args, peaks):
     st1 = ens.stages()
     res["stepping"] = {"rk_stages_per_s": (st1 - st0) / dt, "stages": int(st1 - st0), "seconds": dt,
                        "status": int(ens.read_ctrl()[0].status)}
-    del H, ens
+    del ens
+    if not args.no_cpu:
+        res["cpu_baseline"] = hmat_cpu_baseline(H, nodes, tris, res["apply_ms"] / 1e3, t_build)
+    del H
     torch.cuda.empty_cache()
     return res
+
+
+def hmat_cpu_baseline(H, nodes, tris, gpu_apply_s, gpu_build_s, n_lowrank=96, n_dense=48):
+    """The reference's CPU H-matrix path restated (oracle/hmat_cpu.py), one
+    host core: the product as blocks_process_MVM's per-block loop over this
+    H-matrix's own storage (FP32 factors as stored), timed whole; the build
+    as the reference's generator calls (one receiver x n sources, one source x
+    m receivers) under partial-pivot ACA on a seeded sample of the low-rank
+    blocks and dense evaluation of a sample of the dense blocks, extrapolated
+    to all blocks by pair evaluations (the ACA ones at the device's ranks)."""
+    from oracle import hmat_cpu
+    blocks = H.blocks_host
+    rank = H.rank.cpu().numpy()
+    off = H.off.cpu().numpy()
+    data = H.data.cpu().numpy()
+    x = np.random.default_rng(0).standard_normal(2 * H.N).astype(np.float32)
+    t0 = time.perf_counter()
+    hmat_cpu.matvec(blocks[:, :4], data, off, rank, x)
+    t_mv = time.perf_counter() - t0
+    del data
+    frames, xg = hmat_cpu.element_frames(nodes, tris)
+    perm = H.perm_host
+    m = (blocks[:, 1] - blocks[:, 0]).astype(np.int64)
+    n = (blocks[:, 3] - blocks[:, 2]).astype(np.int64)
+    lr = np.nonzero(blocks[:, 4] == 1)[0]
+    dn = np.nonzero(blocks[:, 4] == 0)[0]
+    rng = np.random.default_rng(0)
+    out = {"unit": "s", "cores": 1, "kind": "port",
+           "product": {"value": t_mv, "gpu_s": gpu_apply_s, "ratio": t_mv / gpu_apply_s,
+                       "sample": "one whole product (all %d blocks), FP32 factors" % len(blocks)}}
+    t_lr = ev_lr = 0.0
+    for b in rng.choice(lr, size=min(len(lr), n_lowrank), replace=False):
+        r0, r1, c0, c1 = (int(v) for v in blocks[b, :4])
+        gen = hmat_cpu.BlockGen(nodes, tris, frames, xg, perm[r0:r1], perm[c0:c1], MU, LAM)
+        t0 = time.perf_counter()
+        hmat_cpu.aca_block(gen, int(min(128, 3 * m[b], 2 * n[b])), 1e-4)
+        t_lr += time.perf_counter() - t0
+        ev_lr += gen.evals
+    t_dn = ev_dn = 0.0
+    for b in rng.choice(dn, size=min(len(dn), n_dense), replace=False):
+        r0, r1, c0, c1 = (int(v) for v in blocks[b, :4])
+        gen = hmat_cpu.BlockGen(nodes, tris, frames, xg, perm[r0:r1], perm[c0:c1], MU, LAM)
+        t0 = time.perf_counter()
+        hmat_cpu.dense_block(gen)
+        t_dn += time.perf_counter() - t0
+        ev_dn += gen.evals
+    rk = np.where(rank[lr] >= 0, rank[lr], np.minimum(128, np.minimum(3 * m[lr], 2 * n[lr])))
+    total_lr = float(np.sum((rk + 1) * (2 * n[lr] + m[lr])))   # a row (2n) and a column (m) per term
+    total_dn = float(np.sum(2 * m[dn] * n[dn]))
+    est = total_lr * t_lr / max(ev_lr, 1.0) + total_dn * t_dn / max(ev_dn, 1.0)
+    out["build"] = {"value": est, "gpu_s": gpu_build_s, "ratio": est / gpu_build_s,
+                    "sample": "%d low-rank blocks (%.3g pair evaluations, %.1f s) and %d dense blocks (%.3g, %.1f s), "
+                              "extrapolated by pair evaluations to %.3g (ACA at the device's ranks) + %.3g (dense)"
+                              % (min(len(lr), n_lowrank), ev_lr, t_lr, min(len(dn), n_dense), ev_dn, t_dn,
+                                 total_lr, total_dn)}
+    return out
 
 
 def bench_halfspace(torch, dev, args, fp64_tflops=None):

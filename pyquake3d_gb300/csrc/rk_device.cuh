@@ -552,7 +552,7 @@ struct Exp2Table {
         for (int j = 0; j < 64; ++j) v[j] = ffc(exp_series(j * (kLn2 / 64.0)));
     }
 };
-__constant__ Exp2Table kExp2Tab{};
+static __constant__ Exp2Table kExp2Tab{};
 constexpr FFc kFFLn2_64 = ffc(kLn2 / 64.0);
 
 // e^{K ln 2 + t} = 2^{K + n/64} e^s, n = rint(64 t / ln 2), s = t - n ln 2 / 64

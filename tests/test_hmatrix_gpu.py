@@ -45,6 +45,27 @@ def test_hmatrix_product_matches_dense(cuda, leaf):
     assert torch.equal(Ym[0], Y[0]) and torch.equal(Ym[2], Y[2]) and bool(torch.all(Ym[1] == 7.0))
 
 
+def test_cpu_restatement_product_equals_device_product(cuda):
+    """The CPU baseline's per-block product (oracle/hmat_cpu.py, the
+    reference's blocks_process_MVM loop) on this H-matrix's own storage gives
+    the device product (both FP32 factors; FP64 sums on the CPU, float-float
+    on the device)."""
+    from oracle import hmat_cpu
+    nodes, tris = mesh.rough_fault(24.0, 12.0, 40, 20, seed=2, ratio=5e-3)
+    N = tris.shape[0]
+    H = HMatrix(nodes, tris, MU, MU, min_size=32, mini_leaf=32, tol=1e-4, device=cuda)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(2 * N)
+    y_dev = H.apply(torch.as_tensor(x[None], device=cuda))[0].cpu().numpy()
+    perm = H.perm_host
+    xp = x.reshape(N, 2)[perm].reshape(-1)            # element order -> positions
+    data = H.data.cpu().numpy().astype(np.float64)
+    yp = hmat_cpu.matvec(H.blocks_host[:, :4], data, H.off.cpu().numpy(), H.rank.cpu().numpy(), xp)
+    y_cpu = np.empty(3 * N)
+    y_cpu.reshape(N, 3)[perm] = yp.reshape(N, 3)       # positions -> element order
+    assert normwise_rel(y_cpu, y_dev) < 1e-6
+
+
 def test_mesh_smaller_than_a_leaf_is_one_dense_block(cuda):
     """N = 18 cells under a 64-cell leaf: the partition is one dense block and
     the product is the FP32-stored dense operator (~1e-7 relative)."""
