@@ -840,6 +840,23 @@ def bench_halfspace(torch, dev, args, fp64_tflops=None):
         t = s.elapsed_time(e) / reps / 1e3
         res["halfspace" if half else "fullspace"] = {"s": t, "pairs_per_s": N * N / t, "entries_per_s": 6 * N * N / t}
     res["cost_ratio"] = res["halfspace"]["s"] / res["fullspace"]["s"]
+    if not args.no_cpu:
+        # the oracle's C restatement of the half-space path on all host cores,
+        # a bounded sample of source columns (calibrated on 16, then ~3 s)
+        import oracle
+        cores = os.cpu_count() or 1
+        ncol = min(N, 16)
+        t0 = time.perf_counter()
+        oracle.assemble_dense(nodes, tris, MU, LAM, halfspace=True, cols=(0, ncol), nthreads=cores)
+        dt = time.perf_counter() - t0
+        ncol = int(min(N, max(ncol, ncol * 3.0 / max(dt, 1e-3))))
+        t0 = time.perf_counter()
+        oracle.assemble_dense(nodes, tris, MU, LAM, halfspace=True, cols=(0, ncol), nthreads=cores)
+        dt = time.perf_counter() - t0
+        res["halfspace"]["cpu_baseline"] = {"value": N * ncol / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                            "sample": "%d of %d source columns x all receivers, %.1f s"
+                                                      % (ncol, N, dt),
+                                            "gpu_ratio": res["halfspace"]["pairs_per_s"] / (N * ncol / dt)}
     if fp64_tflops:
         hs = res["halfspace"]
         ach = HS_FLOP_PER_PAIR * N * N / hs["s"] / 1e12

@@ -291,10 +291,12 @@ typedef struct pq3d_batch_sim {
     /* BF16X18: the cell order of the fixed-point product (device int64, NULL =
      * identity): fix_order[p] = cell at position p of the packed operator's
      * rows and columns, fix_pos[cell] = its position.  A spatially compact
-     * order (pq3d_hmat_cluster_order) keeps each 1024-column chunk, whose
-     * largest |v'| sets the chunk's fixed-point grid, inside one region of
-     * the fault; the mesh order of a long fault puts far-apart cells in one
-     * chunk and costs the far receivers their relative precision. */
+     * order (pq3d_hmat_cluster_order) keeps each 256-column span, whose
+     * largest |v'| sets the span's fixed-point grid, and each 1024-column
+     * operator chunk inside one region of the fault; the mesh order of a long
+     * fault puts far-apart cells in one span, and the slow cells sharing a
+     * span with a nucleating patch keep only the bits of their v' below the
+     * patch's. */
     const int64_t *fix_order;
     const int64_t *fix_pos;
 } pq3d_batch_sim;
