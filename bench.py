@@ -1013,6 +1013,9 @@ def profile_case(case):
     fix_gemm     batched iterations with the fixed-point BF16x18 product and the FP64
                  attempt, same mesh and runs (6 iterations)
     ff_attempt   the same with the float-float attempt (6 iterations)
+    points       the reference-shaped point entry points (TDstressFS_C full and half
+                 space: 200,000 receivers x 1 source; TDstressEachSourceAtReceiver_C:
+                 1 receiver x 20,000 sources, full and half space)
     aca          H-matrix build (partition, ACA, dense blocks), rough 100x25 km, N=20,000,
                  leaf 64, eta 2, tol 1e-4 (one ACA launch over all low-rank blocks)"""
     import torch
@@ -1058,6 +1061,29 @@ def profile_case(case):
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
         Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(6)
+    elif case == "points":
+        import ctypes as _ct
+        from pyquake3d_gb300 import _lib
+        rng = np.random.default_rng(0)
+        n = 200000
+        X, Y = rng.uniform(-20e3, 20e3, n), rng.uniform(-20e3, 20e3, n)
+        Z = rng.uniform(-20e3, -100.0, n)
+        P = [np.array([0.0, 0.0, -1000.0]), np.array([1000.0, 0.0, -1000.0]), np.array([300.0, -577.35, -2000.0])]
+        gf.TDstressFS(X, Y, Z, *P, 1.0, 0.0, 0.0, MU, LAM)
+        gf.TDstressHS(X, Y, Z, *P, 1.0, 0.0, 0.0, MU, LAM)
+        ns = 20000
+        c = rng.uniform(-20e3, 20e3, (ns, 3))
+        c[:, 2] = -np.abs(c[:, 2]) - 1500.0
+        P1 = np.ascontiguousarray(c + [0.0, 0.0, 500.0])
+        P2 = np.ascontiguousarray(c + [800.0, 0.0, 0.0])
+        P3 = np.ascontiguousarray(c + [0.0, 600.0, -400.0])
+        L = _lib.load()
+        s = np.empty((ns, 6))
+        e = np.empty((ns, 6))
+        dp = lambda a: a.ctypes.data_as(_ct.POINTER(_ct.c_double))
+        for hs in (False, True):
+            L.TDstressEachSourceAtReceiver_C(100.0, 200.0, -300.0, dp(P1), dp(P2), dp(P3), ns, 1.0, 0.0, 0.0,
+                                             MU, LAM, hs, dp(s), dp(e))
     elif case in ("fix_gemm", "ff_attempt"):
         from pyquake3d_gb300.ensemble import Ensemble, PackedFixOperator
         nodes, tris = mesh.planar_fault(60.0, 50.0, 60, 50)
