@@ -96,3 +96,27 @@ def test_ff_attempt_rejected_for_bad_value():
     with pytest.raises(ValueError):
         Ensemble(torch.zeros((3, 2), dtype=torch.float64), np.zeros((1, 1, 10)), mu=MU, Cs=CS, precision="fp64",
                  attempt="fp128")
+
+
+@pytest.mark.parametrize("precision", ["hmat", "fp32"])
+def test_ff_attempt_with_other_products(cuda, precision):
+    """The float-float attempt behind the H-matrix and the plain FP32
+    products (FP64 partial sums, split on the device): one iteration equals
+    the FP64 attempt on the same product to 1e-13 in the states."""
+    from pyquake3d_gb300.hmatrix import HMatrix
+    nodes, tris = mesh.planar_fault(40.0, 20.0, 40, 20)
+    _, xg = mesh.element_frames(nodes, tris)
+    tabs = mesh.ensemble_tables(xg, 40e3, 20e3, B=4, seed=2, v_nuc=1e-3)
+    if precision == "hmat":
+        K = HMatrix(nodes, tris, MU, MU, min_size=32, mini_leaf=32, tol=1e-6, device=cuda)
+    else:
+        K = gf.assemble_dense(nodes, tris, MU, MU, device=cuda)[1]
+    a = Ensemble(K, tabs, mu=MU, Cs=CS, precision=precision, attempt="fp64")
+    b = Ensemble(K, tabs, mu=MU, Cs=CS, precision=precision, attempt="ff")
+    assert b.S.attempt64 == 2
+    a.iterate(1)
+    b.iterate(1)
+    for r in range(4):
+        for k in ("Tt1o", "Tt2o", "state", "slip1"):
+            assert normwise_rel(a.t[k][r].cpu().numpy(), b.t[k][r].cpu().numpy()) < 1e-13, (k, r)
+    assert [c.steps for c in a.read_ctrl()] == [c.steps for c in b.read_ctrl()]
