@@ -120,3 +120,23 @@ def test_ff_attempt_with_other_products(cuda, precision):
         for k in ("Tt1o", "Tt2o", "state", "slip1"):
             assert normwise_rel(a.t[k][r].cpu().numpy(), b.t[k][r].cpu().numpy()) < 1e-13, (k, r)
     assert [c.steps for c in a.read_ctrl()] == [c.steps for c in b.read_ctrl()]
+
+
+def test_ff_attempt_small_mesh_and_odd_run_count(cuda, golden):
+    """The golden mesh (N = 64: one 256-column span, padded operator tiles)
+    with 3 runs: 30 free-running accepted steps of the float-float attempt
+    stay within 1e-9 in slip of the FP64 attempt on the same product."""
+    from tests.test_batch_gpu import CS as CS_G, _golden, _tables
+    g, K = _golden(golden, cuda)
+    tabs = _tables(g, 3, seed=6)
+    P = PackedFixOperator(K)
+    kw = dict(mu=float(g["mu"]), Cs=CS_G, max_steps=30, nsplit=1)
+    a = Ensemble(P, tabs, precision="bf16x18", attempt="fp64", **kw)
+    b = Ensemble(P, tabs, precision="bf16x18", attempt="ff", **kw)
+    a.iterate(150)
+    b.iterate(150)
+    assert all(c.steps == 30 and c.status == 0 for c in b.read_ctrl())
+    assert [c.steps for c in a.read_ctrl()] == [c.steps for c in b.read_ctrl()]
+    for r in range(3):
+        assert normwise_rel(a.t["slip1"][r].cpu().numpy(), b.t["slip1"][r].cpu().numpy()) < 1e-9, r
+    assert b.error_word() == 0
