@@ -193,7 +193,7 @@ class HMatrix:
         size = (size + 3) // 4 * 4
         off = np.concatenate([[0], np.cumsum(size)[:-1]]).astype(np.int64)
         assert np.all(off % 4 == 0)
-        self.data = torch.empty(int(size.sum()), dtype=torch.float32, device=dev)
+        self.data = torch.zeros(int(size.sum()), dtype=torch.float32, device=dev)   # padding defined
         self.off = torch.as_tensor(off, device=dev)
         self.rank = torch.as_tensor(rank, device=dev)
         phase("storage_alloc")
