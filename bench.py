@@ -406,6 +406,8 @@ def batched_summary(bt):
             a["steps_within_1e-5"] = acc[acc_key]["steps_within_1e-5"]
         if gemm and "gemm" in bt.get(gemm, {}):
             a["product_hbm_frac"] = round(bt[gemm]["gemm"]["roofline"]["frac"], 3)
+        if "e2e" in bt[arm]:
+            a["e2e_rk_stages_per_s"] = round(bt[arm]["e2e"]["rk_stages_per_s"])
         arms[key] = a
     out = {"N": bt.get("N"), "B": bt.get("B"), "plain_fp64_rk_stages_per_s": round(plain), "arms": arms}
     if acc:
@@ -588,6 +590,24 @@ def bench_batched(torch, dev, args, peaks):
                     "iterations": reps * args.graph_iters, "ms_per_iteration": dt / (reps * args.graph_iters) * 1e3,
                     "accepted_steps": int(sum(x.steps for x in c)), "failed_runs": int(sum(x.status != 0 for x in c)),
                     "clocks": clk.summary(), "error_word": ens.error_word() if prec != "fp32" else 0}
+        if key == "bf16x18":
+            # end to end through the public API: the runs' tables from host
+            # memory into a fresh ensemble (state set-up on the device), the
+            # same number of graph-replayed iterations, the slips read back
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2 = Ensemble(K, tabs, mu=MU, Cs=3464.0, precision=prec, attempt=attempt, nsplit=ens.nsplit)
+            e2.iterate(2)
+            e2.capture(args.graph_iters)
+            e2.replay(reps + 1)
+            slips = (e2.t["slip1"].cpu(), e2.t["slip2"].cpu())
+            t_e2e = time.perf_counter() - t0
+            out[key]["e2e"] = {"rk_stages_per_s": e2.stages() / t_e2e, "seconds": t_e2e,
+                               "iterations": 2 + (reps + 1) * args.graph_iters,
+                               "h2d_bytes": int(tabs.nbytes), "d2h_bytes": int(sum(x.numel() * 8 for x in slips)),
+                               "note": "Ensemble(...) from the host tables, iterate + graph capture + replays, the "
+                                       "slips copied back: wall clock of the public API calls"}
+            del e2, slips
         if key in ("bf16x6", "bf16x18"):
             # the tensor-core product alone, CUDA events over repeated launches
             if prec == "bf16x6":

@@ -389,7 +389,7 @@ static int assemble_rows(const double *nodes, const int64_t *tris, int64_t N, in
 // ---------------------------------------------------------------------------
 // Fixed scratch for pq3d_assemble_dense_noalloc: the source and receiver
 // tables of one call (kSrcStride + kRecvStride doubles per element) for up to
-// kNoAllocMaxN elements, 11.5 MB held by every GPU that loads this library.
+// kNoAllocMaxN elements, 12.6 MB held by every GPU that loads this library.
 constexpr int64_t kNoAllocMaxN = 32768;
 static __device__ __align__(256) double g_noalloc_scratch[(size_t)(kSrcStride + kRecvStride) * kNoAllocMaxN];
 
