@@ -1037,6 +1037,9 @@ def profile_case(case):
     fix_gemm     batched iterations with the fixed-point BF16x18 product and the FP64
                  attempt, same mesh and runs (6 iterations)
     ff_attempt   the same with the float-float attempt (6 iterations)
+    batch_small  the CUDA-core batched products (FP64 and FP32, 16 runs, 3 iterations
+                 each, planar 40 x 25 km, N = 2,000) and the dense matvec entry
+                 points (pq3d_dense_matvec_f64 / _f32)
     points       the reference-shaped point entry points (TDstressFS_C full and half
                  space: 200,000 receivers x 1 source; TDstressEachSourceAtReceiver_C:
                  1 receiver x 20,000 sources, full and half space)
@@ -1085,6 +1088,24 @@ def profile_case(case):
         _, xg = mesh.element_frames(nodes, tris)
         tabs = mesh.ensemble_tables(xg, 60e3, 50e3, B=64, seed=0, v_nuc=1e-3)
         Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(6)
+    elif case == "batch_small":
+        from pyquake3d_gb300 import _lib
+        from pyquake3d_gb300.ensemble import Ensemble
+        nodes, tris = mesh.planar_fault(40.0, 25.0, 40, 25)
+        N = tris.shape[0]
+        K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM)
+        _, xg = mesh.element_frames(nodes, tris)
+        tabs = mesh.ensemble_tables(xg, 40e3, 25e3, B=16, seed=0, v_nuc=1e-3)
+        Ensemble(K64, tabs, mu=MU, Cs=3464.0, precision="fp64").iterate(3)
+        Ensemble(K32, tabs, mu=MU, Cs=3464.0, precision="fp32").iterate(3)
+        L = _lib.load()
+        v = torch.randn(2 * N, dtype=torch.float64, device="cuda")
+        out = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(L.pq3d_dense_matvec_f64(K64.data_ptr(), N, v.data_ptr(), out.data_ptr(), st))
+        hi = v.float()
+        v32 = torch.cat([hi.view(N, 2), (v - hi.double()).float().view(N, 2)], 1).contiguous()   # [N][4]
+        _lib.check(L.pq3d_dense_matvec_f32(K32.data_ptr(), N, v32.data_ptr(), out.data_ptr(), st))
     elif case == "points":
         import ctypes as _ct
         from pyquake3d_gb300 import _lib
