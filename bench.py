@@ -335,11 +335,11 @@ def bench_ours(args):
         # kernel averages ~1.3 flops per FP64-pipe instruction; ncu on the
         # N = 2,000 case: FP64 pipe 88 % busy (active cycles)
         roof["fp64_pipe_active_pct"] = 88.3
-        roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, N=2000 case "
-                             "(profiles/gf_assembly_rough_N2000.md)")
+        roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, --set full capture of "
+                             "the N=2000 case (bench.py --quick)")
         roof["traffic"] = 70.8 * N * N
         roof["traffic_note"] = ("ncu dram__bytes_read+write at N=6000 (70.8 B/pair, 2.6 GB of stores, 20x the L2) "
-                                "scaled by pairs; algorithmic stores are %d B/pair (profiles/gf_traffic_N6000.md)"
+                                "scaled by pairs (bench.py --case gf_assembly); algorithmic stores are %d B/pair"
                                 % GF_BYTES_PER_PAIR)
         out["roofline"] = roof
         out["clocks"] = clk.summary()
