@@ -37,9 +37,12 @@
 //     16-column step cover the 18 pairs (an instruction costs about the same
 //     for N = 64 and 128, so wide instructions halve the time of 14 narrow
 //     ones).
-//   * After each span the 6 slots are drained (tcgen05.ld) and added into a
-//     float-float running sum in registers: 3 TwoSums and one float-float
-//     addition.
+//   * After each span the 6 slots are drained (tcgen05.ld) and combined into
+//     a float-float pair (s, t): levels 0-3 by three exact Fast2Sums, 4 and 5
+//     into t.  The slots are then released, and (s, t) is added into the
+//     running float-float sum in registers while the tensor cores already
+//     fill the slots with the next span.  Packed f32x2 additions, two runs
+//     per instruction.
 //
 // Data path (one CTA = one 128-row tile of K x one K slice, all runs, 1 CTA
 // per SM):
@@ -51,7 +54,8 @@
 //     a span a commit hands the slots to the epilogue, and before the next
 //     span it waits until they are drained;
 //   * warps 2-9: epilogue, two warps per 32-lane quarter of tensor memory
-//     (the rows), each taking half of the runs.
+//     (the rows), each taking half of the runs (16 epilogue warps measured
+//     no faster: the drain is bound by FP32 issue, not by warps).
 //   Every mbarrier wait is bounded; a wait that gives up records an error word
 //   in the workspace, the kernel waits (bounded) for its own tensor-core work,
 //   frees its tensor memory and returns.  No cluster, no multicast.
@@ -69,15 +73,60 @@ namespace fx {
 
 using tc::image_offset;
 
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 8;                         // a multiple of 4 (one group per TMEM lane quarter)
+constexpr int kEpiRuns = kMaxRuns / (kEpiWarps / 4);   // runs per epilogue warp at most
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kImageA = kTileM * kBlockK * 2;   // one operator slice image: 8 KB
 
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+// Two FP32 values in one 64-bit register and the packed (f32x2) additions of
+// sm_100 and later: each lane adds two pairs per instruction, IEEE round to
+// nearest, so the drain below rounds exactly as the scalar __fadd_rn would.
+typedef uint64_t f32x2;
+__device__ __forceinline__ f32x2 pack2(uint32_t a, uint32_t b)
 {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(a), "r"(b));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(f32x2 a)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a));
+    return r;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ void two_sum2(f32x2 a, f32x2 b, f32x2 &s, f32x2 &e)
+{
+    s = add2(a, b);
+    const f32x2 bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+// Fast2Sum (s + e = a + b exactly) for the level combination.  Levels lie on
+// nested grids: level l is an integer I_l, |I_l| <= 2^24, in units u 2^(-8l).
+// With a a multiple of 256 units of b's grid and b such an integer, s - a is
+// representable (for ulp(s) = 2^k, k <= 8: a multiple of 2^k below 2^(24+k);
+// k > 8: |a| >= 2^(22+k), so a and s - a are multiples of 2^(k-1) with a
+// significand below 2^24), and the error a + b - s is an integer of at most
+// 2^(k-1) <= 2^24 units while the running sum stays below 2^49 units of the
+// finest level -- true for the four levels (2^24 * 2^24 + ...).  So the
+// error is exact although |a| >= |b| need not hold, and equals what TwoSum
+// (6 operations instead of 3) would return.
+__device__ __forceinline__ void fast_two_sum2(f32x2 a, f32x2 b, f32x2 &s, f32x2 &e)
+{
+    s = add2(a, b);
+    e = sub2(b, sub2(s, a));
 }
 
 // descriptor of the operand `bytes` further on in shared memory (the start
@@ -186,15 +235,16 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
         }
         __syncwarp();
     } else {
-        // epilogue: TMEM lane = tile row; this warp's runs [c0, c0 + half)
+        // epilogue: TMEM lane = tile row; this warp's runs [c0, c0 + per)
         const int e = warp - 2;
         const int quarter = warp & 3;
-        const int half = Bq / 2;
-        const int c0 = (e >> 2) * half;
+        const int per = Bq / (kEpiWarps / 4);
+        const int c0 = (e >> 2) * per;
         const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
-        float H[32], L[32];
+        f32x2 H[kEpiRuns / 2], L[kEpiRuns / 2];   // (hi, lo) of runs c0 + 2i, c0 + 2i + 1
+        f32x2 Sp[kEpiRuns / 2], Tp[kEpiRuns / 2];  // the span's (s, t), added after the slots are freed
 #pragma unroll
-        for (int c = 0; c < 32; ++c) H[c] = L[c] = 0.f;
+        for (int c = 0; c < kEpiRuns / 2; ++c) H[c] = L[c] = Sp[c] = Tp[c] = 0ull;
         bool ok = true;
         for (int j = 0; j < nspan; ++j) {
             ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, j & 1) ? 1 : 0);
@@ -204,41 +254,51 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
             }
             tc::tc_fence_after();
 #pragma unroll
-            for (int g = 0; g < 4; ++g) {
-                if (g * 8 < half) {
+            for (int g = 0; g < kEpiRuns / 8; ++g) {
+                if (g * 8 < per) {
                     uint32_t r[kLevels][8];
 #pragma unroll
                     for (int l = 0; l < kLevels; ++l) tc::tmem_ld8_nowait(tbase + (uint32_t)(l * Bq + g * 8), r[l]);
                     tc::tmem_wait_ld();
 #pragma unroll
-                    for (int x = 0; x < 8; ++x) {
-                        // levels 0-3 exactly (TwoSum), 4 and 5 (2^-32, 2^-40) into the low part
-                        float s, e0, e1, e2;
-                        two_sum(__uint_as_float(r[0][x]), __uint_as_float(r[1][x]), s, e0);
-                        two_sum(s, __uint_as_float(r[2][x]), s, e1);
-                        two_sum(s, __uint_as_float(r[3][x]), s, e2);
-                        const float t = __fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2),
-                                                  __fadd_rn(__uint_as_float(r[4][x]), __uint_as_float(r[5][x])));
-                        // (H, L) += (s, t)
-                        float S, E;
-                        two_sum(H[g * 8 + x], s, S, E);
-                        E = __fadd_rn(E, __fadd_rn(L[g * 8 + x], t));
-                        const float Hn = __fadd_rn(S, E);
-                        L[g * 8 + x] = __fsub_rn(E, __fsub_rn(Hn, S));
-                        H[g * 8 + x] = Hn;
+                    for (int x = 0; x < 8; x += 2) {
+                        // levels 0-3 exactly (Fast2Sum on the nested grids), 4 and 5
+                        // (2^-32, 2^-40) into the low part; two runs per instruction
+                        f32x2 s, e0, e1, e2;
+                        fast_two_sum2(pack2(r[0][x], r[0][x + 1]), pack2(r[1][x], r[1][x + 1]), s, e0);
+                        fast_two_sum2(s, pack2(r[2][x], r[2][x + 1]), s, e1);
+                        fast_two_sum2(s, pack2(r[3][x], r[3][x + 1]), s, e2);
+                        Tp[(g * 8 + x) / 2] = add2(add2(add2(e0, e1), e2),
+                                                   add2(pack2(r[4][x], r[4][x + 1]), pack2(r[5][x], r[5][x + 1])));
+                        Sp[(g * 8 + x) / 2] = s;
                     }
                 }
             }
             tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(acc_empty);
+            // (H, L) += (s, t) while the tensor cores fill the slots with the next span
+#pragma unroll
+            for (int c = 0; c < kEpiRuns / 2; ++c) {
+                if (2 * c < per) {
+                    f32x2 S, E;
+                    two_sum2(H[c], Sp[c], S, E);
+                    E = add2(E, add2(L[c], Tp[c]));
+                    const f32x2 Hn = add2(S, E);
+                    L[c] = sub2(E, sub2(Hn, S));
+                    H[c] = Hn;
+                }
+            }
         }
         const int64_t M = 3 * N;
         const int64_t m = mt * kTileM + 32 * quarter + lane;
         if (ok && m < M) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-                if (c < half && c0 + c < Bo) out[((int64_t)slice * Bo + c0 + c) * M + m] = make_float2(H[c], L[c]);
+            for (int c = 0; c < kEpiRuns; c += 2) {
+                const float2 h = unpack2(H[c / 2]), l = unpack2(L[c / 2]);
+                if (c < per && c0 + c < Bo) out[((int64_t)slice * Bo + c0 + c) * M + m] = make_float2(h.x, l.x);
+                if (c + 1 < per && c0 + c + 1 < Bo) out[((int64_t)slice * Bo + c0 + c + 1) * M + m] = make_float2(h.y, l.y);
+            }
         }
     }
     // free tensor memory once the tensor-core work of this CTA has completed
