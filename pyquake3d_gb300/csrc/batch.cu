@@ -494,9 +494,10 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
         // x = tau / (a sigma), the exponent argument in FP64 (reduced), the rest float-float
         const double a = S.a[idx];
         const double psia = st * rcp_d(a), iaT = rcp_d(a * Tno);
-        v1 = ff_slip_rate(lnv0, psia, T1 * iaT, etab);
-        v2 = ff_slip_rate(lnv0, psia, T2 * iaT, etab);
-        v = sqrt(v1 * v1 + v2 * v2);
+        const FF f1 = ff_slip_rate(lnv0, psia, T1 * iaT, etab), f2 = ff_slip_rate(lnv0, psia, T2 * iaT, etab);
+        v1 = ff_to_double_fast(f1);
+        v2 = ff_to_double_fast(f2);
+        v = ff_to_double_fast(ff_hypot(f1, f2));   // |V| in float-float, like its components
     } else {
         const double a = S.a[idx];
         const double e = (2.0 * S.V0) * exp(-st / a);

@@ -435,13 +435,15 @@ __device__ __forceinline__ FF ffv(FFc c) { return FF{c.hi, c.lo}; }
 // ff_split_fast: hi = x truncated to 24 significant bits, lo = the next 24
 // (truncated: |x - hi - lo| < 2^-47 |x|), renormalised; |x| outside
 // [2^-60, 2^127) (and infinities, NaN) takes the conversions of ff_split,
+// out of line (a branch, not conversions predicated into every call),
 // zero and FP64 subnormals give a signed zero.
+static __device__ __noinline__ FF ff_split_rare(double x) { return ff_split(x); }
 __device__ __forceinline__ FF ff_split_fast(double x)
 {
     const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
     const int e = (int)((hw >> 20) & 0x7ffu);
     if (e == 0) return FF{__uint_as_float(hw & 0x80000000u), 0.f};
-    if (e < 1023 - 60 || e > 1023 + 126) return ff_split(x);
+    if (e < 1023 - 60 || e > 1023 + 126) return ff_split_rare(x);
     const unsigned sign = hw & 0x80000000u;
     const float hi =
         __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
@@ -453,15 +455,30 @@ __device__ __forceinline__ FF ff_split_fast(double x)
     return ff_norm(hi, lo);
 }
 
-// float -> FP64 by the bit layout (zero and normal floats; the rest converts)
+// float -> FP64 by the bit layout, integer operations only: normal floats
+// re-biased; zero; subnormals normalised by the position of their leading
+// bit (value = m 2^-149); infinities and NaN keep the all-ones exponent
 __device__ __forceinline__ double f2d_bits(float f)
 {
     const unsigned u = __float_as_uint(f);
-    const unsigned ef = (u >> 23) & 0xffu;
-    if ((u & 0x7fffffffu) == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (ef == 0 || ef == 0xffu) return (double)f;
-    return __hiloint2double((int)((u & 0x80000000u) | ((ef - 127 + 1023) << 20) | ((u & 0x7fffffu) >> 3)),
-                            (int)((u & 0x7u) << 29));
+    const unsigned sign = u & 0x80000000u, ef = (u >> 23) & 0xffu, mf = u & 0x7fffffu;
+    unsigned hi, lo;
+    if (ef == 0xffu) {
+        hi = sign | 0x7ff00000u | (mf >> 3);
+        lo = mf << 29;
+    } else if (ef != 0) {
+        hi = sign | ((ef - 127 + 1023) << 20) | (mf >> 3);
+        lo = mf << 29;
+    } else if (mf == 0) {
+        hi = sign;
+        lo = 0;
+    } else {
+        const int p = 31 - __clz((int)mf);   // leading bit: 0..22
+        const unsigned long long m = (unsigned long long)(mf ^ (1u << p)) << (52 - p);
+        hi = sign | ((unsigned)(p - 149 + 1023) << 20) | (unsigned)(m >> 32);
+        lo = (unsigned)m;
+    }
+    return __hiloint2double((int)hi, (int)lo);
 }
 
 __device__ __forceinline__ double ff_to_double_fast(FF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
@@ -580,7 +597,10 @@ __device__ __forceinline__ FF ff_exp2k_tab(int K, FF t, const FF *tab)
 // absolute, then split
 __device__ __forceinline__ void reduce_ln2(double u, int &K, FF &r)
 {
-    u = fmin(fmax(u, -1.0e4), 1.0e4);
+    // u clamped to [-1e4, 1e4] (NaN -> -1e4), tested on the high word:
+    // 0x40C38800 is the high word of 1e4, so |u| >= 1e4, infinities and NaN
+    // take the branch
+    if ((__double2hiint(u) & 0x7fffffff) >= 0x40C38800) u = u != u ? -1.0e4 : copysign(1.0e4, u);
     const double t = fma(u, 1.4426950408889634, 6755399441055744.0);
     const double kd = t - 6755399441055744.0;
     K = __double2loint(t);
@@ -771,7 +791,7 @@ __device__ __forceinline__ void dp_attempt_ff(const Cell &c, const FFRates &q, d
 // sinh(x) = sign(x) V0 e^{-psi/a + |x|} (1 - e^{-2|x|}), lnV0 = ln V0, psia =
 // psi/a, x = tau/(a sigma) in FP64; the exponent argument reduced in FP64,
 // the exponentials and the product in float-float, the result in FP64.
-__device__ __forceinline__ double ff_slip_rate(double lnV0, double psia, double x, const FF *tab)
+__device__ __forceinline__ FF ff_slip_rate(double lnV0, double psia, double x, const FF *tab)
 {
     const double ax = fabs(x);
     int K;
@@ -780,8 +800,29 @@ __device__ __forceinline__ double ff_slip_rate(double lnV0, double psia, double 
     const FF e = ff_exp2k_tab(K, r, tab);
     const FF axf = ff_split_fast(ax);
     const FF em = axf.hi > 20.f ? FF{-1.f, expf(-2.f * axf.hi)} : ff_expm1(FF{-2.f * axf.hi, -2.f * axf.lo});
-    const double v = ff_to_double_fast(ff_mul(e, ff_neg(em)));
-    return x < 0.0 ? -v : v;
+    const FF v = ff_mul(e, ff_neg(em));
+    return __double2hiint(x) < 0 ? ff_neg(v) : v;   // the sign of x (its sign bit)
+}
+
+// sqrt(a) of a float-float a > 0: s = sqrtf(hi), one Newton correction
+// (hi - s^2 by an exact FMA, plus lo) / 2s
+__device__ __forceinline__ FF ff_sqrt(FF a)
+{
+    const float s = sqrtf(a.hi);
+    const float d = __fadd_rn(__fmaf_rn(-s, s, a.hi), a.lo);
+    return ff_norm(s, __fdiv_rn(d, __fadd_rn(s, s)));
+}
+
+// |(a, b)| of two float-float values without squaring them (no under- or
+// overflow of the squares): p sqrt(1 + (q/p)^2), p = max, q = min magnitude
+__device__ __forceinline__ FF ff_hypot(FF a, FF b)
+{
+    const FF x = a.hi < 0.f ? ff_neg(a) : a, y = b.hi < 0.f ? ff_neg(b) : b;
+    const bool xl = x.hi > y.hi || (x.hi == y.hi && x.lo >= y.lo);
+    const FF p = xl ? x : y, q = xl ? y : x;
+    if (!(p.hi > 0.f)) return p;   // both zero (or NaN)
+    const FF t = ff_div(q, p);
+    return ff_mul(p, ff_sqrt(ff_add2(FF{1.f, 0.f}, ff_mul(t, t))));
 }
 
 // One Dormand-Prince attempt of one cell in FP64 (src/QDsim_gpu.py:1266-1397):
