@@ -438,6 +438,15 @@ __global__ void decide_kernel(pq3d_run_ctrl *ctrl, int B)
     }
 }
 
+// The update kernel packs the BF16x18 right-hand side itself when the packed
+// columns follow the cells (no cell order, one shard): its 256-cell blocks are
+// then two whole 256-column spans, and a rejected run keeps its packed v'.
+__host__ __device__ inline bool fused_rhs_pack(const pq3d_batch_sim &S)
+{
+    return S.precision == PQ3D_BATCH_BF16X18 && S.fix_order == nullptr && S.cell0 == 0 &&
+           (S.N_total == 0 || S.N_total == S.N);
+}
+
 // kMixed: the new state's start-of-step constants (in float-float from the
 // FP64 state, once per accepted step for all the attempts of the next step)
 // and from them the slip rate 2 V0 e^{-psi/a} sinh(tau / (sigma a)) (~2e-7
@@ -470,46 +479,68 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
     if (!acc) return;
     const int64_t N = S.N;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const int64_t idx = (int64_t)r * N + i;
-    const double h = hs;
-    const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
-    const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w;
-    S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
-    double v1, v2, v;
-    if (kMixed) {
-        float *pb = S.base + idx;
-        const int64_t stride = (int64_t)S.B * N;
-        MixedBase m;
-        store_base_state(pb, stride, Tno, T1, T2, st, FF{c0hi, c0lo}, m);
-        const float f1 = base_slip_rate(m, 0, inv_eta), f2 = base_slip_rate(m, 1, inv_eta);
-        // |V| without under/overflow of the squares
-        const float p = fmaxf(fabsf(f1), fabsf(f2)), q = fminf(fabsf(f1), fabsf(f2));
-        const float t = p > 0.f ? q / p : 0.f;
-        const float vf = fmaxf(p * sqrtf(fmaf(t, t, 1.f)), 1e-30f);
-        pb[19 * stride] = vf;
-        v1 = f1; v2 = f2; v = vf;
-    } else if (ffu) {
-        // the float-float arm: 2 V0 e^{-psi/a} sinh(x) = sign(x) V0 e^{-psi/a + |x|} (1 - e^{-2|x|}),
-        // x = tau / (a sigma), the exponent argument in FP64 (reduced), the rest float-float
-        const double a = S.a[idx];
-        const double psia = st * rcp_d(a), iaT = rcp_d(a * Tno);
-        const FF f1 = ff_slip_rate(lnv0, psia, T1 * iaT, etab), f2 = ff_slip_rate(lnv0, psia, T2 * iaT, etab);
-        v1 = ff_to_double_fast(f1);
-        v2 = ff_to_double_fast(f2);
-        v = ff_to_double_fast(ff_hypot(f1, f2));   // |V| in float-float, like its components
-    } else {
-        const double a = S.a[idx];
-        const double e = (2.0 * S.V0) * exp(-st / a);
-        v1 = e * sinh(T1 / Tno / a);
-        v2 = e * sinh(T2 / Tno / a);
-        v = sqrt(v1 * v1 + v2 * v2);
+    const bool fuse = fused_rhs_pack(S);
+    if (i >= N && !fuse) return;
+    double p1 = 0.0, p2 = 0.0;   // the cell's v' (fused packing; zero past the last cell)
+    if (i < N) {
+        const int64_t idx = (int64_t)r * N + i;
+        const double h = hs;
+        const double4_16a y = reinterpret_cast<const double4_16a *>(S.cand)[idx];
+        const double Tno = y.x, T1 = y.y, T2 = y.z, st = y.w;
+        S.Tno[idx] = Tno; S.Tt1o[idx] = T1; S.Tt2o[idx] = T2; S.state[idx] = st;
+        double v1, v2, v;
+        if (kMixed) {
+            float *pb = S.base + idx;
+            const int64_t stride = (int64_t)S.B * N;
+            MixedBase m;
+            store_base_state(pb, stride, Tno, T1, T2, st, FF{c0hi, c0lo}, m);
+            const float f1 = base_slip_rate(m, 0, inv_eta), f2 = base_slip_rate(m, 1, inv_eta);
+            // |V| without under/overflow of the squares
+            const float p = fmaxf(fabsf(f1), fabsf(f2)), q = fminf(fabsf(f1), fabsf(f2));
+            const float t = p > 0.f ? q / p : 0.f;
+            const float vf = fmaxf(p * sqrtf(fmaf(t, t, 1.f)), 1e-30f);
+            pb[19 * stride] = vf;
+            v1 = f1; v2 = f2; v = vf;
+        } else if (ffu) {
+            // the float-float arm: 2 V0 e^{-psi/a} sinh(x) = sign(x) V0 e^{-psi/a + |x|} (1 - e^{-2|x|}),
+            // x = tau / (a sigma), the exponent argument in FP64 (reduced), the rest float-float
+            const double a = S.a[idx];
+            const double psia = st * rcp_d(a), iaT = rcp_d(a * Tno);
+            const FF f1 = ff_slip_rate(lnv0, psia, T1 * iaT, etab), f2 = ff_slip_rate(lnv0, psia, T2 * iaT, etab);
+            v1 = ff_to_double_fast(f1);
+            v2 = ff_to_double_fast(f2);
+            v = ff_to_double_fast(ff_hypot(f1, f2));   // |V| in float-float, like its components
+        } else {
+            const double a = S.a[idx];
+            const double e = (2.0 * S.V0) * exp(-st / a);
+            v1 = e * sinh(T1 / Tno / a);
+            v2 = e * sinh(T2 / Tno / a);
+            v = sqrt(v1 * v1 + v2 * v2);
+        }
+        if (v < 1e-30) v = 1e-30;
+        S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
+        S.slip1[idx] += v1 * h;
+        S.slip2[idx] += v2 * h;
+        write_vop<!kMixed>(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
+        if (fuse) {
+            p1 = fma(-S.Vpl, S.cos_rake0[idx], v1);
+            p2 = fma(-S.Vpl, S.sin_rake0[idx], v2);
+        }
     }
-    if (v < 1e-30) v = 1e-30;
-    S.slipv1[idx] = v1; S.slipv2[idx] = v2; S.slipv[idx] = v;
-    S.slip1[idx] += v1 * h;
-    S.slip2[idx] += v2 * h;
-    write_vop<!kMixed>(S, r, i, v1 - S.Vpl * S.cos_rake0[idx], v2 - S.Vpl * S.sin_rake0[idx]);
+    if (fuse) {
+        // the fixed-point slices of v': threads 0-127 and 128-255 are the
+        // cells of two 256-column spans; each span's largest |v'| sets its
+        // exponent (as the pack kernel does)
+        __shared__ double smax[8];
+        double mx = fmax(fabs(p1), fabs(p2));
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        const int w0 = (threadIdx.x >> 7) * 4;
+        const double m = fmax(fmax(smax[w0], smax[w0 + 1]), fmax(smax[w0 + 2], smax[w0 + 3]));
+        fx::write_rhs_cell((__nv_bfloat16 *)S.vop, fx::fix_runs(S.B), fx::k_blocks(N), i, r, fx::chunk_exponent(m),
+                           p1, p2);
+    }
 }
 
 // The Dormand-Prince attempt and update in mixed precision (FP32 stages on the
@@ -643,7 +674,7 @@ extern "C" int pq3d_batch_iterate_end(const pq3d_batch_sim *sim, void *stream)
     if (mixed_attempt(S)) update_kernel<true><<<grid, 256, 0, st>>>(S);
     else update_kernel<false><<<grid, 256, 0, st>>>(S);
     PQ3D_CUDA_TRY(cudaGetLastError());
-    if (S.precision == PQ3D_BATCH_BF16X18)   // v' of every run from its slip rates (unchanged for the others)
+    if (S.precision == PQ3D_BATCH_BF16X18 && !fused_rhs_pack(S))   // v' of every run from its slip rates
         return fx::pack_rhs_from_state(S.slipv1, S.slipv2, S.cos_rake0, S.sin_rake0, S.Vpl, S.fix_order, S.N, S.B,
                                        S.vop, st);
     return PQ3D_OK;

@@ -316,23 +316,6 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
 // ---------------------------------------------------------------------------
 // packing
 
-// balanced base-256 digits of an integer |X| <= 2^(8 n - 1): X = sum d_p 2^(8 (n-1-p)),
-// |d_p| <= 128, the most significant first
-template <int n>
-__device__ __forceinline__ void digits(long long X, int d[n])
-{
-#pragma unroll
-    for (int p = n - 1; p >= 1; --p) {
-        const int t = (int)((X + 128) & 255) - 128;
-        d[p] = t;
-        X = (X - t) >> 8;
-    }
-    d[0] = (int)X;
-}
-
-// exponent e with |x| < 2^e for the largest magnitude m of a chunk (0 for m = 0)
-__device__ __forceinline__ int chunk_exponent(double m) { return m > 0.0 ? ilogb(m) + 1 : 0; }
-
 // operator: one warp per row of the tile, 1024 columns of chunk blockIdx.x
 __global__ void __launch_bounds__(256) pack_operator_fix_kernel(const double *__restrict__ K64, int64_t N,
                                                                  const int64_t *__restrict__ order,
@@ -396,8 +379,8 @@ __global__ void __launch_bounds__(kSpan / 2) pack_rhs_fix_kernel(RhsSrc src, int
             v1 = src.v[(int64_t)r * 2 * N + 2 * cell];
             v2 = src.v[(int64_t)r * 2 * N + 2 * cell + 1];
         } else {
-            v1 = src.slipv1[idx] - src.Vpl * src.cos_rake0[idx];
-            v2 = src.slipv2[idx] - src.Vpl * src.sin_rake0[idx];
+            v1 = fma(-src.Vpl, src.cos_rake0[idx], src.slipv1[idx]);
+            v2 = fma(-src.Vpl, src.sin_rake0[idx], src.slipv2[idx]);
         }
     }
     double mx = fmax(fabs(v1), fabs(v2));
@@ -407,21 +390,7 @@ __global__ void __launch_bounds__(kSpan / 2) pack_rhs_fix_kernel(RhsSrc src, int
     double m = red[0];
 #pragma unroll
     for (int w = 1; w < kSpan / 64; ++w) m = fmax(m, red[w]);
-    const int e = chunk_exponent(m);
-    const int64_t kb = sp * kBlocksPerSpan + i / 16;
-    if (kb >= KB) return;
-    int d1[kVPieces], d2[kVPieces];
-    digits<kVPieces>(__double2ll_rn(ldexp(v1, 8 * kVPieces - 1 - e)), d1);
-    digits<kVPieces>(__double2ll_rn(ldexp(v2, 8 * kVPieces - 1 - e)), d2);
-    const int64_t img = (int64_t)Bq * kBlockK;
-    __nv_bfloat16 *P = out + kb * kVPieces * img + image_offset(r, (2 * i) % kBlockK);
-#pragma unroll
-    for (int q = 0; q < kVPieces; ++q) {
-        __nv_bfloat162 w;
-        w.x = __float2bfloat16_rn(ldexpf((float)d1[q], e - 7 - 8 * q));
-        w.y = __float2bfloat16_rn(ldexpf((float)d2[q], e - 7 - 8 * q));
-        reinterpret_cast<__nv_bfloat162 *>(P + q * img)[0] = w;
-    }
+    write_rhs_cell(out, Bq, KB, pos, r, chunk_exponent(m), v1, v2);
 }
 
 static int launch_pack_rhs(const RhsSrc &src, int64_t N, int B, void *Vpacked, cudaStream_t stream)

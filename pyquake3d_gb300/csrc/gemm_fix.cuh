@@ -2,8 +2,11 @@
 // fixed-point slices ("BF16x18").  See gemm_fix.cu.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "gemm_tc.cuh"
 
 namespace pq3d {
 namespace fx {
@@ -34,6 +37,49 @@ inline size_t packed_operator_bytes(int64_t N)
 }
 // [k_blocks][6 slices][Bq x 32 BF16 image], Bq = fix_runs(B)
 inline size_t packed_rhs_bytes(int64_t N, int B) { return (size_t)k_blocks(N) * kVPieces * fix_runs(B) * kBlockK * 2; }
+
+#ifdef __CUDACC__
+// balanced base-256 digits of an integer |X| <= 2^(8 n - 1): X = sum d_p 2^(8 (n-1-p)),
+// |d_p| <= 128, the most significant first
+template <int n>
+__device__ __forceinline__ void digits(long long X, int d[n])
+{
+#pragma unroll
+    for (int p = n - 1; p >= 1; --p) {
+        const int t = (int)((X + 128) & 255) - 128;
+        d[p] = t;
+        X = (X - t) >> 8;
+    }
+    d[0] = (int)X;
+}
+
+// exponent e with |x| < 2^e for the largest magnitude m of a chunk (0 for m = 0)
+__device__ __forceinline__ int chunk_exponent(double m) { return m > 0.0 ? ilogb(m) + 1 : 0; }
+
+// The six right-hand-side slices of one cell, (v'_1, v'_2) of run r at column
+// positions 2p and 2p + 1, e the exponent of its span's largest |v'|: the one
+// writer of the packed right-hand side (the pack kernel and the batched
+// stepper's update both call it).  Positions past the last 32-column block
+// (KB blocks) write nothing.
+__device__ __forceinline__ void write_rhs_cell(__nv_bfloat16 *out, int Bq, int64_t KB, int64_t p, int r, int e,
+                                               double v1, double v2)
+{
+    const int64_t kb = p / (kBlockK / 2);
+    if (kb >= KB) return;
+    int d1[kVPieces], d2[kVPieces];
+    digits<kVPieces>(__double2ll_rn(ldexp(v1, 8 * kVPieces - 1 - e)), d1);
+    digits<kVPieces>(__double2ll_rn(ldexp(v2, 8 * kVPieces - 1 - e)), d2);
+    const int64_t img = (int64_t)Bq * kBlockK;
+    __nv_bfloat16 *P = out + kb * kVPieces * img + tc::image_offset(r, (int)((2 * p) % kBlockK));
+#pragma unroll
+    for (int q = 0; q < kVPieces; ++q) {
+        __nv_bfloat162 w;
+        w.x = __float2bfloat16_rn(ldexpf((float)d1[q], e - 7 - 8 * q));
+        w.y = __float2bfloat16_rn(ldexpf((float)d2[q], e - 7 - 8 * q));
+        reinterpret_cast<__nv_bfloat162 *>(P + q * img)[0] = w;
+    }
+}
+#endif
 
 // out[(s * Bo + n) * 3N + m] = float2 (hi, lo) for n < Bo = B rounded up to 16:
 // K slice s of sum_k K[m][k] V[n][k] to ~2^-44 relative (hi + lo), from the

@@ -65,28 +65,34 @@ def test_ff_attempt_free_running_close_to_fp64_attempt(cuda):
         assert normwise_rel(a.t["slip1"][r].cpu().numpy(), b.t["slip1"][r].cpu().numpy()) < 1e-9, r
 
 
-def test_ff_attempt_tracks_fp64_through_nucleation(cuda):
+@pytest.mark.parametrize("order", ["compact", "mesh"])
+def test_ff_attempt_tracks_fp64_through_nucleation(cuda, order):
     """Lockstep with the FP64 batched stepper on planar N = 1,600, 8 runs,
     120 accepted steps: within 2e-6 in slip, the bar the FP64 attempt on the
-    same product meets."""
+    same product meets.  In the mesh's own cell order the update kernel packs
+    v' itself; in the compact order the pack kernel does."""
     K64, tabs, xg = _physical(cuda)
     kw = dict(mu=MU, Cs=CS, max_steps=120)
     ref = Ensemble(K64, tabs, precision="fp64", **kw)
-    ff = Ensemble(PackedFixOperator(K64, xg), tabs, precision="bf16x18", attempt="ff", **kw)
+    ff = Ensemble(PackedFixOperator(K64, xg if order == "compact" else None), tabs, precision="bf16x18",
+                  attempt="ff", **kw)
     r = lockstep(ref, {"ff": ff}, 120, bar=2e-6)["ff"]
     assert r["failed_runs"] == 0 and ff.error_word() == 0
     assert r["steps_within"] >= 120, r
 
 
-def test_ff_attempt_horizon_on_the_batched_workload(cuda):
+@pytest.mark.parametrize("order", ["compact", "mesh"])
+def test_ff_attempt_horizon_on_the_batched_workload(cuda, order):
     """The batched workload (planar 100 x 50 km, N = 10,000, nucleation
     patches at 1e-3 m/s), 8 runs in lockstep with the FP64 batched stepper:
     the BF16x18 product with the float-float attempt keeps every run's slip
-    within 1e-5 of FP64 for 80 accepted steps, like the FP64 attempt."""
+    within 1e-5 of FP64 for 80 accepted steps, like the FP64 attempt (the
+    mesh order is the benchmark's)."""
     K64, tabs, xg = _physical(cuda, nx=100, nz=50, B=8)
     kw = dict(mu=MU, Cs=CS, max_steps=80)
     ref = Ensemble(K64, tabs, precision="fp64", **kw)
-    ff = Ensemble(PackedFixOperator(K64, xg), tabs, precision="bf16x18", attempt="ff", nsplit=5, **kw)
+    ff = Ensemble(PackedFixOperator(K64, xg if order == "compact" else None), tabs, precision="bf16x18",
+                  attempt="ff", nsplit=5, **kw)
     r = lockstep(ref, {"ff": ff}, 80, bar=1e-5)["ff"]
     assert r["failed_runs"] == 0 and ff.error_word() == 0
     assert r["steps_within"] >= 80, r
