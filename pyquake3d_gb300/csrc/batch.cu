@@ -531,15 +531,15 @@ __global__ void __launch_bounds__(256) update_kernel(pq3d_batch_sim S)
         // the fixed-point slices of v': threads 0-127 and 128-255 are the
         // cells of two 256-column spans; each span's largest |v'| sets its
         // exponent (as the pack kernel does)
-        __shared__ double smax[8];
-        double mx = fmax(fabs(p1), fabs(p2));
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __shared__ int smax[8];
+        int mx = fx::rhs_word(p1, p2);
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
         __syncthreads();
         const int w0 = (threadIdx.x >> 7) * 4;
-        const double m = fmax(fmax(smax[w0], smax[w0 + 1]), fmax(smax[w0 + 2], smax[w0 + 3]));
-        fx::write_rhs_cell((__nv_bfloat16 *)S.vop, fx::fix_runs(S.B), fx::k_blocks(N), i, r, fx::chunk_exponent(m),
-                           p1, p2);
+        const int m = max(max(smax[w0], smax[w0 + 1]), max(smax[w0 + 2], smax[w0 + 3]));
+        fx::write_rhs_cell((__nv_bfloat16 *)S.vop, fx::fix_runs(S.B), fx::k_blocks(N), i, r,
+                           fx::rhs_span_exponent(m), p1, p2);
     }
 }
 

@@ -365,7 +365,7 @@ struct RhsSrc {
 __global__ void __launch_bounds__(kSpan / 2) pack_rhs_fix_kernel(RhsSrc src, int64_t N, int B, int Bq,
                                                                   __nv_bfloat16 *__restrict__ out)
 {
-    __shared__ double red[kSpan / 64];
+    __shared__ int red[kSpan / 64];
     const int64_t sp = blockIdx.x;
     const int r = blockIdx.y;
     const int i = threadIdx.x;
@@ -383,14 +383,14 @@ __global__ void __launch_bounds__(kSpan / 2) pack_rhs_fix_kernel(RhsSrc src, int
             v2 = fma(-src.Vpl, src.sin_rake0[idx], src.slipv2[idx]);
         }
     }
-    double mx = fmax(fabs(v1), fabs(v2));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int mx = rhs_word(v1, v2);
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((i & 31) == 0) red[i >> 5] = mx;
     __syncthreads();
-    double m = red[0];
+    int m = red[0];
 #pragma unroll
-    for (int w = 1; w < kSpan / 64; ++w) m = fmax(m, red[w]);
-    write_rhs_cell(out, Bq, KB, pos, r, chunk_exponent(m), v1, v2);
+    for (int w = 1; w < kSpan / 64; ++w) m = max(m, red[w]);
+    write_rhs_cell(out, Bq, KB, pos, r, rhs_span_exponent(m), v1, v2);
 }
 
 static int launch_pack_rhs(const RhsSrc &src, int64_t N, int B, void *Vpacked, cudaStream_t stream)

@@ -56,19 +56,40 @@ __device__ __forceinline__ void digits(long long X, int d[n])
 // exponent e with |x| < 2^e for the largest magnitude m of a chunk (0 for m = 0)
 __device__ __forceinline__ int chunk_exponent(double m) { return m > 0.0 ? ilogb(m) + 1 : 0; }
 
+// A right-hand-side span's exponent from its cells' values by integer
+// operations: the high word of |v| (sign cleared) orders the exponents, the
+// span takes the largest word over its cells (rhs_word, then a 32-bit max),
+// and e = exponent + 1 with |v| < 2^e for every cell; a span whose largest
+// exponent field is 0 (all zero, or subnormal: below FP32's range, its slices
+// are zero either way) gets e = 0.
+__device__ __forceinline__ int rhs_word(double a, double b)
+{
+    return max(__double2hiint(a) & 0x7fffffff, __double2hiint(b) & 0x7fffffff);
+}
+__device__ __forceinline__ int rhs_span_exponent(int word)
+{
+    const int f = word >> 20;
+    return f ? f - 1022 : 0;
+}
+
 // The six right-hand-side slices of one cell, (v'_1, v'_2) of run r at column
-// positions 2p and 2p + 1, e the exponent of its span's largest |v'|: the one
-// writer of the packed right-hand side (the pack kernel and the batched
+// positions 2p and 2p + 1, e the exponent of its span (rhs_span_exponent): the
+// one writer of the packed right-hand side (the pack kernel and the batched
 // stepper's update both call it).  Positions past the last 32-column block
-// (KB blocks) write nothing.
+// (KB blocks) write nothing.  The scaling by 2^(47 - e) is one product with a
+// power of two built from its bits; a span below 2^-976 (its slices would be
+// below FP32's range) is written as zeros.
 __device__ __forceinline__ void write_rhs_cell(__nv_bfloat16 *out, int Bq, int64_t KB, int64_t p, int r, int e,
                                                double v1, double v2)
 {
     const int64_t kb = p / (kBlockK / 2);
     if (kb >= KB) return;
-    int d1[kVPieces], d2[kVPieces];
-    digits<kVPieces>(__double2ll_rn(ldexp(v1, 8 * kVPieces - 1 - e)), d1);
-    digits<kVPieces>(__double2ll_rn(ldexp(v2, 8 * kVPieces - 1 - e)), d2);
+    int d1[kVPieces] = {}, d2[kVPieces] = {};
+    if (e >= -976) {
+        const double sc = __hiloint2double((8 * kVPieces - 1 - e + 1023) << 20, 0);   // 2^(47 - e)
+        digits<kVPieces>(__double2ll_rn(v1 * sc), d1);
+        digits<kVPieces>(__double2ll_rn(v2 * sc), d2);
+    }
     const int64_t img = (int64_t)Bq * kBlockK;
     __nv_bfloat16 *P = out + kb * kVPieces * img + tc::image_offset(r, (int)((2 * p) % kBlockK));
 #pragma unroll

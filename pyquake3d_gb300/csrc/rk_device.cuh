@@ -653,7 +653,8 @@ static __device__ __noinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF d
         const FF em = ax.hi > 20.f ? FF{-1.f, expf(-2.f * ax.hi)} : ff_expm1(FF{-2.f * ax.hi, -2.f * ax.lo});
         const int K = m.Ku[k][pos ? 0 : 1];
         const FF res = ff_sub(ff_add2(m.ru[k][pos ? 0 : 1], pos ? dx : ff_neg(dx)), dpa);   // ln W - K ln 2
-        const bool big = fmaf((float)K, 0.693147182f, res.hi) >= 0.f;                    // W >= 1
+        // W >= 1; K as a float by the 1.5 2^23 bias (|K| < 2^22: no conversion instruction)
+        const bool big = fmaf(__fsub_rn(__int_as_float(0x4B400000 + K), 12582912.f), 0.693147182f, res.hi) >= 0.f;
         const FF w = big ? ff_exp2k_tab(-K, ff_neg(res), tab) : ff_exp2k_tab(K, res, tab);                  // e^{-|ln W|}
         const FF q = ff_add2(m.q0[k], ff_mul(m.a, dx));                                    // tau / sigma
         const FF D = ff_mul(ff_add2(FF{2.f, 0.f}, em), iaS);                               // (1 + r)/(a sigma)
