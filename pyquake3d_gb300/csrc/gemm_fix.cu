@@ -133,19 +133,64 @@ __device__ __forceinline__ void fast_two_sum2(f32x2 a, f32x2 b, f32x2 &s, f32x2 
 // address field, bits 0-13 in 16-byte units, does not overflow below 256 KB)
 __device__ __forceinline__ uint64_t desc_at(uint64_t d, uint32_t bytes) { return d + (bytes >> 4); }
 
+// The work of a CTA as segments: blocks [kb0, kb1) of one 128-row tile,
+// summed into output slice `slice`.
+//   * Slice grid (units == 0): CTA (tile blockIdx.x, K slice blockIdx.y), one
+//     segment, the slice's blocks KB s / nsplit .. KB (s + 1) / nsplit.
+//   * Balanced grid (units = tiles x KB): one CTA per SM; CTA c takes the
+//     units [c W / G, (c + 1) W / G) of the tile-major list u = tile KB + kb,
+//     so every CTA streams the same number of blocks and no partial last
+//     wave is left.  Its segment of a tile writes slice c - c0, c0 the CTA
+//     holding the tile's first block (the host launches this grid only when
+//     no tile meets more than nsplit CTAs), and the segment that ends a tile
+//     writes zeros to the slices above its own.
+struct Seg {
+    int64_t tile, kb0, kb1;
+    int slice;
+    bool tail;   // ends the tile in a balanced grid: zero the slices above
+};
+
+struct FixSched {
+    int64_t KB, units;   // blocks per tile; units of the balanced grid (0: slice grid)
+    int nsplit;
+};
+
+// CTA of a balanced grid of G CTAs over W units that holds unit x
+__host__ __device__ inline int64_t bal_owner(int64_t x, int64_t W, int64_t G) { return ((x + 1) * G - 1) / W; }
+
+// segment i of this CTA (false past the last)
+__device__ __forceinline__ bool fix_segment(const FixSched &sc, int i, Seg &sg)
+{
+    if (sc.units == 0) {
+        if (i > 0) return false;
+        sg.tile = blockIdx.x;
+        sg.slice = blockIdx.y;
+        sg.kb0 = sc.KB * sg.slice / sc.nsplit;
+        sg.kb1 = sc.KB * (sg.slice + 1) / sc.nsplit;
+        sg.tail = false;
+        return sg.kb1 > sg.kb0;
+    }
+    const int64_t G = gridDim.x, c = blockIdx.x;
+    const int64_t u0 = c * sc.units / G, u1 = (c + 1) * sc.units / G;
+    const int64_t t = u0 / sc.KB + i;
+    const int64_t ub = i == 0 ? u0 : t * sc.KB;   // first unit of the segment
+    if (ub >= u1) return false;
+    sg.tile = t;
+    sg.kb0 = ub - t * sc.KB;
+    sg.kb1 = min(sc.KB, u1 - t * sc.KB);
+    sg.slice = sg.kb0 == 0 ? 0 : (int)(c - bal_owner(t * sc.KB, sc.units, G));
+    sg.tail = sg.kb1 == sc.KB;
+    return true;
+}
+
 // Bq: runs of the product (32 or 64); Bo: runs written (<= Bq, multiple of 16)
 __global__ void __launch_bounds__(kThreads, 1)
-gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bq, int Bo, int nsplit,
-                float2 *__restrict__ out, int *__restrict__ err, int stages)
+gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, int64_t N, int Bq, int Bo,
+                FixSched sc, float2 *__restrict__ out, int *__restrict__ err, int stages)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t mt = blockIdx.x;
-    const int slice = blockIdx.y;
-    const int64_t KB = (2 * N + kBlockK - 1) / kBlockK;
-    const int64_t kb0 = KB * slice / nsplit, kb1 = KB * (slice + 1) / nsplit;
-    const int nkb = (int)(kb1 - kb0);
-    const int nspan = nkb > 0 ? (int)((kb1 - 1) / kBlocksPerSpan - kb0 / kBlocksPerSpan + 1) : 0;
+    const int64_t KB = sc.KB;
     const uint32_t a_bytes = kKPieces * kImageA;
     const uint32_t b_img = (uint32_t)Bq * kBlockK * 2;
     const uint32_t b_bytes = kVPieces * b_img;
@@ -180,15 +225,18 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
     if (warp == 0) {
         if (lane == 0) {
             // producer
-            for (int it = 0; it < nkb; ++it) {
-                const int st = it % stages, use = it / stages;
-                if (!tc::mbar_wait(empty0 + 8 * st, (use & 1) ^ 1)) { atomicExch(err, 1); break; }
-                const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
-                const int64_t kb = kb0 + it;
-                tc::mbar_expect_tx(full0 + 8 * st, stage_bytes);
-                tc::bulk_g2s(sa, Kp + (size_t)(mt * KB + kb) * a_bytes, a_bytes, full0 + 8 * st);
-                tc::bulk_g2s(sa + a_bytes, Vp + (size_t)kb * b_bytes, b_bytes, full0 + 8 * st);
-            }
+            int it = 0;
+            bool fail = false;
+            Seg sg;
+            for (int si = 0; !fail && fix_segment(sc, si, sg); ++si)
+                for (int64_t kb = sg.kb0; kb < sg.kb1; ++kb, ++it) {
+                    const int st = it % stages, use = it / stages;
+                    if (!tc::mbar_wait(empty0 + 8 * st, (use & 1) ^ 1)) { atomicExch(err, 1); fail = true; break; }
+                    const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
+                    tc::mbar_expect_tx(full0 + 8 * st, stage_bytes);
+                    tc::bulk_g2s(sa, Kp + (size_t)(sg.tile * KB + kb) * a_bytes, a_bytes, full0 + 8 * st);
+                    tc::bulk_g2s(sa + a_bytes, Vp + (size_t)kb * b_bytes, b_bytes, full0 + 8 * st);
+                }
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -200,37 +248,44 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
             const uint32_t slot1 = tmem + (uint32_t)Bq, slot2 = tmem + 2u * Bq, slot3 = tmem + 3u * Bq;
             const uint32_t slot4 = tmem + 4u * Bq, slot5 = tmem + 5u * Bq;
             const uint32_t bq4 = 4u * b_img;
-            int j = 0;   // local span
-            for (int it = 0; it < nkb; ++it) {
-                const int64_t kb = kb0 + it;
-                const bool first = it == 0 || kb % kBlocksPerSpan == 0;
-                const bool last = it == nkb - 1 || (kb + 1) % kBlocksPerSpan == 0;
-                if (first && j > 0 && !tc::mbar_wait(acc_empty, (j - 1) & 1)) { atomicExch(err, 4); break; }
-                const int st = it % stages, use = it / stages;
-                if (!tc::mbar_wait(full0 + 8 * st, use & 1)) { atomicExch(err, 2); break; }
-                tc::tc_fence_after();
-                const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
-                const uint64_t ad = tc::smem_desc(sa, 128, 512), bd = tc::smem_desc(sa + a_bytes, 128, 512);
+            int j = 0;    // span of this CTA
+            int it = 0;   // block of this CTA
+            bool fail = false;
+            Seg sg;
+            for (int si = 0; !fail && fix_segment(sc, si, sg); ++si)
+                for (int64_t kb = sg.kb0; kb < sg.kb1; ++kb, ++it) {
+                    const bool first = kb == sg.kb0 || kb % kBlocksPerSpan == 0;
+                    const bool last = kb == sg.kb1 - 1 || (kb + 1) % kBlocksPerSpan == 0;
+                    if (first && j > 0 && !tc::mbar_wait(acc_empty, (j - 1) & 1)) {
+                        atomicExch(err, 4);
+                        fail = true;
+                        break;
+                    }
+                    const int st = it % stages, use = it / stages;
+                    if (!tc::mbar_wait(full0 + 8 * st, use & 1)) { atomicExch(err, 2); fail = true; break; }
+                    tc::tc_fence_after();
+                    const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
+                    const uint64_t ad = tc::smem_desc(sa, 128, 512), bd = tc::smem_desc(sa + a_bytes, 128, 512);
 #pragma unroll
-                for (int ks = 0; ks < 2; ++ks) {
-                    const uint32_t f = (first && ks == 0) ? 0u : 1u;   // the first instruction of a slot overwrites it
-                    const uint32_t k0 = ks * 256;
-                    // operator slice 0 x rhs slices 0-3 -> slots 0-3, x slices 4-5 -> slots 4-5
-                    tc::mma_bf16(tmem, desc_at(ad, k0), desc_at(bd, k0), id4, f);
-                    tc::mma_bf16(slot4, desc_at(ad, k0), desc_at(bd, bq4 + k0), id2, f);
-                    // slice 1 x 0-3 -> slots 1-4, x 4 -> slot 5
-                    tc::mma_bf16(slot1, desc_at(ad, kImageA + k0), desc_at(bd, k0), id4, 1u);
-                    tc::mma_bf16(slot5, desc_at(ad, kImageA + k0), desc_at(bd, bq4 + k0), id1, 1u);
-                    // slice 2 x 0-3 -> slots 2-5; slice 3 x 0-2 -> slots 3-5
-                    tc::mma_bf16(slot2, desc_at(ad, 2 * kImageA + k0), desc_at(bd, k0), id4, 1u);
-                    tc::mma_bf16(slot3, desc_at(ad, 3 * kImageA + k0), desc_at(bd, k0), id3, 1u);
+                    for (int ks = 0; ks < 2; ++ks) {
+                        const uint32_t f = (first && ks == 0) ? 0u : 1u;   // the first instruction of a slot overwrites it
+                        const uint32_t k0 = ks * 256;
+                        // operator slice 0 x rhs slices 0-3 -> slots 0-3, x slices 4-5 -> slots 4-5
+                        tc::mma_bf16(tmem, desc_at(ad, k0), desc_at(bd, k0), id4, f);
+                        tc::mma_bf16(slot4, desc_at(ad, k0), desc_at(bd, bq4 + k0), id2, f);
+                        // slice 1 x 0-3 -> slots 1-4, x 4 -> slot 5
+                        tc::mma_bf16(slot1, desc_at(ad, kImageA + k0), desc_at(bd, k0), id4, 1u);
+                        tc::mma_bf16(slot5, desc_at(ad, kImageA + k0), desc_at(bd, bq4 + k0), id1, 1u);
+                        // slice 2 x 0-3 -> slots 2-5; slice 3 x 0-2 -> slots 3-5
+                        tc::mma_bf16(slot2, desc_at(ad, 2 * kImageA + k0), desc_at(bd, k0), id4, 1u);
+                        tc::mma_bf16(slot3, desc_at(ad, 3 * kImageA + k0), desc_at(bd, k0), id3, 1u);
+                    }
+                    tc::mma_commit(empty0 + 8 * st);
+                    if (last) {
+                        tc::mma_commit(acc_full);
+                        ++j;
+                    }
                 }
-                tc::mma_commit(empty0 + 8 * st);
-                if (last) {
-                    tc::mma_commit(acc_full);
-                    ++j;
-                }
-            }
             tc::mma_commit(done);
         }
         __syncwarp();
@@ -246,59 +301,73 @@ gemm_fix_kernel(const uint8_t *__restrict__ Kp, const uint8_t *__restrict__ Vp, 
 #pragma unroll
         for (int c = 0; c < kEpiRuns / 2; ++c) H[c] = L[c] = Sp[c] = Tp[c] = 0ull;
         bool ok = true;
-        for (int j = 0; j < nspan; ++j) {
-            ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, j & 1) ? 1 : 0);
-            if (!ok) {
-                if (lane == 0) atomicExch(err, 3);
-                break;
-            }
-            tc::tc_fence_after();
+        const int64_t M = 3 * N;
+        int j = 0;   // span of this CTA
+        Seg sg;
+        for (int si = 0; ok && fix_segment(sc, si, sg); ++si) {
+            const int nspan = (int)((sg.kb1 - 1) / kBlocksPerSpan - sg.kb0 / kBlocksPerSpan + 1);
+            for (int js = 0; js < nspan; ++js, ++j) {
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, j & 1) ? 1 : 0);
+                if (!ok) {
+                    if (lane == 0) atomicExch(err, 3);
+                    break;
+                }
+                tc::tc_fence_after();
 #pragma unroll
-            for (int g = 0; g < kEpiRuns / 8; ++g) {
-                if (g * 8 < per) {
-                    uint32_t r[kLevels][8];
+                for (int g = 0; g < kEpiRuns / 8; ++g) {
+                    if (g * 8 < per) {
+                        uint32_t r[kLevels][8];
 #pragma unroll
-                    for (int l = 0; l < kLevels; ++l) tc::tmem_ld8_nowait(tbase + (uint32_t)(l * Bq + g * 8), r[l]);
-                    tc::tmem_wait_ld();
+                        for (int l = 0; l < kLevels; ++l) tc::tmem_ld8_nowait(tbase + (uint32_t)(l * Bq + g * 8), r[l]);
+                        tc::tmem_wait_ld();
 #pragma unroll
-                    for (int x = 0; x < 8; x += 2) {
-                        // levels 0-3 exactly (Fast2Sum on the nested grids), 4 and 5
-                        // (2^-32, 2^-40) into the low part; two runs per instruction
-                        f32x2 s, e0, e1, e2;
-                        fast_two_sum2(pack2(r[0][x], r[0][x + 1]), pack2(r[1][x], r[1][x + 1]), s, e0);
-                        fast_two_sum2(s, pack2(r[2][x], r[2][x + 1]), s, e1);
-                        fast_two_sum2(s, pack2(r[3][x], r[3][x + 1]), s, e2);
-                        Tp[(g * 8 + x) / 2] = add2(add2(add2(e0, e1), e2),
-                                                   add2(pack2(r[4][x], r[4][x + 1]), pack2(r[5][x], r[5][x + 1])));
-                        Sp[(g * 8 + x) / 2] = s;
+                        for (int x = 0; x < 8; x += 2) {
+                            // levels 0-3 exactly (Fast2Sum on the nested grids), 4 and 5
+                            // (2^-32, 2^-40) into the low part; two runs per instruction
+                            f32x2 s, e0, e1, e2;
+                            fast_two_sum2(pack2(r[0][x], r[0][x + 1]), pack2(r[1][x], r[1][x + 1]), s, e0);
+                            fast_two_sum2(s, pack2(r[2][x], r[2][x + 1]), s, e1);
+                            fast_two_sum2(s, pack2(r[3][x], r[3][x + 1]), s, e2);
+                            Tp[(g * 8 + x) / 2] = add2(add2(add2(e0, e1), e2),
+                                                       add2(pack2(r[4][x], r[4][x + 1]), pack2(r[5][x], r[5][x + 1])));
+                            Sp[(g * 8 + x) / 2] = s;
+                        }
+                    }
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(acc_empty);
+                // (H, L) += (s, t) while the tensor cores fill the slots with the next span
+#pragma unroll
+                for (int c = 0; c < kEpiRuns / 2; ++c) {
+                    if (2 * c < per) {
+                        f32x2 S, E;
+                        two_sum2(H[c], Sp[c], S, E);
+                        E = add2(E, add2(L[c], Tp[c]));
+                        const f32x2 Hn = add2(S, E);
+                        L[c] = sub2(E, sub2(Hn, S));
+                        H[c] = Hn;
                     }
                 }
             }
-            tc::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(acc_empty);
-            // (H, L) += (s, t) while the tensor cores fill the slots with the next span
+            if (!ok) break;
+            // the segment's sums: its slice; a balanced grid's tile end zeroes the slices above
+            const int64_t m = sg.tile * kTileM + 32 * quarter + lane;
+            if (m < M) {
 #pragma unroll
-            for (int c = 0; c < kEpiRuns / 2; ++c) {
-                if (2 * c < per) {
-                    f32x2 S, E;
-                    two_sum2(H[c], Sp[c], S, E);
-                    E = add2(E, add2(L[c], Tp[c]));
-                    const f32x2 Hn = add2(S, E);
-                    L[c] = sub2(E, sub2(Hn, S));
-                    H[c] = Hn;
+                for (int c = 0; c < kEpiRuns; c += 2) {
+                    const float2 h = unpack2(H[c / 2]), l = unpack2(L[c / 2]);
+                    if (c < per && c0 + c < Bo) out[((int64_t)sg.slice * Bo + c0 + c) * M + m] = make_float2(h.x, l.x);
+                    if (c + 1 < per && c0 + c + 1 < Bo)
+                        out[((int64_t)sg.slice * Bo + c0 + c + 1) * M + m] = make_float2(h.y, l.y);
                 }
+                if (sg.tail)
+                    for (int s2 = sg.slice + 1; s2 < sc.nsplit; ++s2)
+                        for (int c = 0; c < per && c0 + c < Bo; ++c)
+                            out[((int64_t)s2 * Bo + c0 + c) * M + m] = make_float2(0.f, 0.f);
             }
-        }
-        const int64_t M = 3 * N;
-        const int64_t m = mt * kTileM + 32 * quarter + lane;
-        if (ok && m < M) {
 #pragma unroll
-            for (int c = 0; c < kEpiRuns; c += 2) {
-                const float2 h = unpack2(H[c / 2]), l = unpack2(L[c / 2]);
-                if (c < per && c0 + c < Bo) out[((int64_t)slice * Bo + c0 + c) * M + m] = make_float2(h.x, l.x);
-                if (c + 1 < per && c0 + c + 1 < Bo) out[((int64_t)slice * Bo + c0 + c + 1) * M + m] = make_float2(h.y, l.y);
-            }
+            for (int c = 0; c < kEpiRuns / 2; ++c) H[c] = L[c] = 0ull;
         }
     }
     // free tensor memory once the tensor-core work of this CTA has completed
@@ -447,9 +516,20 @@ int gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int
     int rc = stages_for(Bq, &stages);
     if (rc) return rc;
     const size_t smem = (size_t)stages * stage_bytes_for(Bq) + 16 * (size_t)stages + 48;
-    dim3 grid((unsigned)m_tiles(N), (unsigned)nsplit);
+    // the balanced grid (one CTA per SM, equal shares of the tile-major
+    // blocks) when no tile meets more than nsplit CTAs' shares; else one CTA
+    // per (tile, K slice)
+    int dev, sms = 0;
+    PQ3D_CUDA_TRY(cudaGetDevice(&dev));
+    PQ3D_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t tiles = m_tiles(N), W = tiles * KB, G = sms;
+    bool balanced = nsplit >= 2 && G >= 1 && W >= G;
+    for (int64_t t = 0; balanced && t < tiles; ++t)
+        balanced = bal_owner((t + 1) * KB - 1, W, G) - bal_owner(t * KB, W, G) + 1 <= nsplit;
+    const FixSched sc{KB, balanced ? W : 0, nsplit};
+    const dim3 grid = balanced ? dim3((unsigned)G) : dim3((unsigned)tiles, (unsigned)nsplit);
     gemm_fix_kernel<<<grid, kThreads, smem, stream>>>((const uint8_t *)Kpacked, (const uint8_t *)Vpacked, N, Bq, Bo,
-                                                      nsplit, out, (int *)workspace, stages);
+                                                      sc, out, (int *)workspace, stages);
     PQ3D_CUDA_TRY(cudaGetLastError());
     return PQ3D_OK;
 }

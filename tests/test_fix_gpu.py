@@ -158,6 +158,31 @@ def test_fix_product_k_slices_and_padding(cuda):
         assert normwise_rel(ref[r], res[1][r]) < 1e-8
 
 
+def test_fix_product_balanced_grid(cuda):
+    """N = 1,600 (38 row tiles x 100 blocks): with 4 or more output slices a
+    GB300's 152 SMs take the balanced grid (one CTA per SM, equal shares of
+    the tile-major blocks, a tile's share per CTA in its own slice, unused
+    slices zeroed); with 1 or 3 the grid of (tile, K slice) CTAs.  Every
+    schedule gives the same sums to float-float precision, and padded runs
+    stay zero in every slice."""
+    rng = np.random.default_rng(5)
+    N, B = 1600, 40
+    K = rng.standard_normal((3 * N, 2 * N)) * 1e8
+    V = rng.standard_normal((B, 2 * N)) * 10 ** rng.uniform(-9, 0, size=(B, 2 * N))
+    res = {}
+    for ns in (1, 3, 4, 8):
+        out, err, _ = _run_product(cuda, K, V, ns)
+        assert err == 0
+        assert np.all(out[:, B:] == 0.0)
+        assert np.all(np.isfinite(out))
+        res[ns] = (out[..., 0].astype(np.float64) + out[..., 1]).sum(0)[:B]
+    ref = V @ K.T
+    for r in range(B):
+        for ns in (3, 4, 8):
+            assert normwise_rel(res[1][r], res[ns][r]) < 1e-12, (ns, r)
+        assert normwise_rel(ref[r], res[1][r]) < 1e-8
+
+
 def test_fix_rejects_bad_arguments(cuda):
     L = _lib.load()
     buf = torch.zeros(1 << 16, dtype=torch.uint8, device=cuda)
