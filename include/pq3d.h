@@ -342,11 +342,16 @@ int pq3d_batch_pack_operator_fix(const double *K64, int64_t N, const int64_t *or
 size_t pq3d_batch_rhs_fix_bytes(int64_t N, int B);
 int pq3d_batch_pack_rhs_fix(const double *v, int64_t N, int B, const int64_t *order, void *Vpacked, void *stream);
 /* The fixed-point tensor-core product alone: out[((s*Bp + n)*3N + m)*2 + {0,1}]
- * = (hi, lo) FP32 with hi + lo = K slice s of sum_k K[m][k] v[n][k] (s < nsplit,
- * Bp = B rounded up to 16, B <= 64), the exact product of the slices up to
- * ~2^-44 relative.  One CTA per SM, six wide tcgen05.mma per 16-column step
- * (one per operator slice and run of right-hand-side slices, accumulating in
- * tensor-memory slots by level); nsplit sets the order of the slice sums. */
+ * = (hi, lo) FP32, s < nsplit, Bp = B rounded up to 16, B <= 64; the nsplit
+ * partial sums add up to sum_k K[m][k] v[n][k], the exact product of the
+ * slices up to ~2^-44 relative.  A partial sum is either K slice s (column
+ * blocks 2N/32 s / nsplit .. 2N/32 (s+1) / nsplit, one CTA per 128-row tile and
+ * slice) or, when no 128-row tile meets more than nsplit shares of the
+ * balanced grid (one CTA per SM, each streaming an equal share of the
+ * tile-major 32-column blocks), the s-th share of the row's tile, zero past
+ * its last share.  Six wide tcgen05.mma per 16-column step (one per operator
+ * slice and run of right-hand-side slices, accumulating in tensor-memory slots
+ * by level); nsplit sets the schedule and the order of the partial sums. */
 int pq3d_batch_gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float *out,
                             void *workspace, size_t workspace_bytes, void *stream);
 /* Device workspace bytes of one batched iteration (GEMM split-K partials live in

@@ -44,8 +44,8 @@
 //     fill the slots with the next span.  Packed f32x2 additions, two runs
 //     per instruction.
 //
-// Data path (one CTA = one 128-row tile of K x one K slice, all runs, 1 CTA
-// per SM):
+// Data path (one CTA per SM: one 128-row tile of K x one K slice, or in the
+// balanced grid an equal share of the tile-major 32-column blocks; all runs):
 //   * warp 0 lane 0: producer, two 1-D bulk copies per 32-column stage (the
 //     four operator slice images, 32 KB, and the six right-hand-side slice
 //     images), completion on the stage's mbarrier;

@@ -103,7 +103,8 @@ __device__ __forceinline__ void write_rhs_cell(__nv_bfloat16 *out, int Bq, int64
 #endif
 
 // out[(s * Bo + n) * 3N + m] = float2 (hi, lo) for n < Bo = B rounded up to 16:
-// K slice s of sum_k K[m][k] V[n][k] to ~2^-44 relative (hi + lo), from the
+// nsplit partial sums of sum_k K[m][k] V[n][k] (K slices, or the balanced
+// grid's tile shares; see gemm_fix.cu) to ~2^-44 relative (hi + lo), from the
 // packed fixed-point operator and right-hand side.  Returns a PQ3D status.
 int gemm_bf16x18(const void *Kpacked, const void *Vpacked, int64_t N, int B, int nsplit, float2 *out,
                  void *workspace, size_t workspace_bytes, cudaStream_t stream);
