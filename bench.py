@@ -545,9 +545,8 @@ def bench_batched(torch, dev, args, peaks):
     K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
     P = PackedOperator(K64)
     # the mesh's own cell order: on this planar workload it holds 1e-5 longer
-    # than the cluster tree's compact order (16 runs in lockstep: 112 against
-    # 94 accepted steps with the float-float attempt, 106 against 94 with the
-    # FP64 attempt)
+    # than the cluster tree's compact order (16 runs in lockstep: 106 against
+    # 94 accepted steps with either attempt)
     PF = PackedFixOperator(K64)
     # launch shapes of the tensor-core products from the project's autotuner,
     # before anything is timed
