@@ -485,6 +485,13 @@ int pq3d_selftest_barrier_timeout(int nblocks, int skip_block, unsigned spin_lim
  * on an mbarrier nobody arrives at: returns PQ3D_ERR_TIMEOUT with the error
  * word set, *gave_up_host = the threads that gave up (128). */
 int pq3d_selftest_mbar_timeout(unsigned wait_limit, int *gave_up_host);
+/* The FP64 <-> float-float conversions of the float-float attempt (integer
+ * bit operations on the device) on n host values (n <= 2^20): ff_host[2i],
+ * ff_host[2i+1] = (hi, lo) of x_host[i]; d_host[i] = f_host[i] widened to
+ * FP64; h_host[i] = |(x_host[i], y_host[i])| by the float-float norm of the
+ * update kernel.  Allocates small buffers. */
+int pq3d_selftest_ff_conversions(const double *x_host, const float *f_host, const double *y_host, int n,
+                                 float *ff_host, double *d_host, double *h_host);
 
 #ifdef __cplusplus
 }

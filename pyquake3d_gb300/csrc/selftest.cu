@@ -3,10 +3,14 @@
 // reads, and let every thread return with the context still usable.  They
 // exercise the same primitives the steppers and the tensor-core products use
 // (grid_barrier, tc::mbar_wait), with a lowered limit so that a test takes
-// milliseconds.  Nothing here faults or waits without a bound.
+// milliseconds.  Nothing here faults or waits without a bound.  Also: the
+// integer FP64 <-> float-float conversions of the float-float attempt on
+// host-chosen values (subnormal, infinite and NaN operands included), which
+// the steppers reach only through rare states.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "rk_device.cuh"
 #include "tc_ptx.cuh"
 
 namespace pq3d {
@@ -42,6 +46,20 @@ __global__ void mbar_kernel(uint32_t limit, int *gave_up, int *err)
         atomicAdd(gave_up, 1);
         if (threadIdx.x == 0) atomicExch(err, 2);
     }
+}
+
+// The conversions of the float-float attempt on n values: ff_split_fast(x),
+// f2d_bits(f), and |(x, y)| by ff_hypot of the two splits, back to FP64.
+__global__ void ffconv_kernel(const double *x, const float *f, const double *y, int n, float *ff, double *d,
+                              double *h)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const rk::FF a = rk::ff_split_fast(x[i]);
+    ff[2 * i] = a.hi;
+    ff[2 * i + 1] = a.lo;
+    d[i] = rk::f2d_bits(f[i]);
+    h[i] = rk::ff_to_double_fast(rk::ff_hypot(a, rk::ff_split_fast(y[i])));
 }
 
 }  // namespace selftest
@@ -101,4 +119,32 @@ extern "C" int pq3d_selftest_mbar_timeout(unsigned wait_limit, int *gave_up_host
     *gave_up_host = h[0];
     return h[1] ? set_error(PQ3D_ERR_TIMEOUT, "mbarrier wait gave up after %u tries (error word %d)", wait_limit, h[1])
                 : PQ3D_OK;
+}
+
+extern "C" int pq3d_selftest_ff_conversions(const double *x_host, const float *f_host, const double *y_host, int n,
+                                            float *ff_host, double *d_host, double *h_host)
+{
+    clear_error();
+    PQ3D_REQUIRE(x_host && f_host && y_host && ff_host && d_host && h_host && n >= 1 && n <= (1 << 20),
+                 "pq3d_selftest_ff_conversions: bad arguments");
+    const size_t nd = (size_t)n * sizeof(double), nf = (size_t)n * sizeof(float);
+    void *mem = nullptr;
+    PQ3D_CUDA_TRY(cudaMalloc(&mem, 4 * nd + 3 * nf + 64));
+    char *p = (char *)mem;
+    double *x = (double *)p, *y = x + n, *d = y + n, *h = d + n;
+    float *f = (float *)(h + n), *ff = f + n;
+    cudaError_t e = cudaMemcpy(x, x_host, nd, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(y, y_host, nd, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f, f_host, nf, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        selftest::ffconv_kernel<<<(n + 127) / 128, 128>>>(x, f, y, n, ff, d, h);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(ff_host, ff, 2 * nf, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(d_host, d, nd, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_host, h, nd, cudaMemcpyDeviceToHost);
+    cudaFree(mem);
+    if (e != cudaSuccess) return set_error(PQ3D_ERR_CUDA, "pq3d_selftest_ff_conversions: %s", cudaGetErrorString(e));
+    return PQ3D_OK;
 }
