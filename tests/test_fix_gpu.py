@@ -246,19 +246,21 @@ def test_bf16x18_horizon_on_the_batched_workload(cuda):
     assert r["steps_within"] >= 80, r
 
 
+@pytest.mark.parametrize("nsplit", [2, 4])
 @pytest.mark.parametrize("attempt", ["ff", "fp64", "mixed"])
-def test_update_packs_rhs_like_the_pack_kernel(cuda, attempt):
+def test_update_packs_rhs_like_the_pack_kernel(cuda, attempt, nsplit):
     """In the mesh's cell order the update kernel writes the fixed-point
     slices of v' itself (accepted runs only; a rejected run's slip rates, and
     so its slices, are unchanged).  After iterations with rejections, packing
     every run afresh from the slip rates (the pack kernel, through prepare)
     leaves the packed right-hand side bit for bit as it was.  N = 1,600 (the
-    last 256-column span is half full), 8 runs (padded to 32)."""
+    last 256-column span is half full), 8 runs (padded to 32); 2 partial sums
+    (the (tile, K slice) grid) and 4 (the balanced grid on 152 SMs)."""
     nodes, tris = mesh.planar_fault(40.0, 20.0, 40, 20)
     K64, _ = gf.assemble_dense(nodes, tris, MU, MU, fp32_copy=False, device=cuda)
     _, xg = mesh.element_frames(nodes, tris)
     tabs = mesh.ensemble_tables(xg, 40e3, 20e3, B=8, seed=3, v_nuc=1e-3)
-    ens = Ensemble(PackedFixOperator(K64), tabs, mu=MU, Cs=CS, precision="bf16x18", attempt=attempt, nsplit=2)
+    ens = Ensemble(PackedFixOperator(K64), tabs, mu=MU, Cs=CS, precision="bf16x18", attempt=attempt, nsplit=nsplit)
     ens.set_ctrl(dttry=10.0)   # a first step far too long: rejections follow
     ens.iterate(30)
     torch.cuda.synchronize()
