@@ -1,7 +1,8 @@
 // Batched traction product on the 5th-generation tensor cores (tcgen05) with
 // exact fixed-point slices ("BF16x18"):
 //
-//   out[s][n][m] = sum_{k in slice s} K[m][k] * V[n][k]   (hi + lo, ~2^-44 relative)
+//   sum_s out[s][n][m] = sum_k K[m][k] * V[n][k]   (hi + lo, ~2^-44 relative;
+//   s: a K slice, or a share of the balanced grid below)
 //   K: (3N) x (2N) traction operator, V: B slip-rate deficits v' = V - Vpl.
 //
 // Why: the reference evaluates K.(V - Vpl) in FP64 (src/QDsim_gpu.py:948-957).
