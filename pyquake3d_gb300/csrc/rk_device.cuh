@@ -551,6 +551,15 @@ __device__ __forceinline__ FF ff_expm1(FF t)
     return k == 0 ? p : ff_add2(ff_ldexp(ff_add2(FF{1.f, 0.f}, p), k), FF{-1.f, 0.f});
 }
 
+// e^{-2x} - 1 for x >= 0 (a float-float |tau / (a sigma)|).  For x >= 8.5,
+// r = e^{-2x} < 2^-24 is only the low part of -1 + r, so FP32 accuracy of r
+// is float-float accuracy of the sum: r = expf(-2 hi) (1 - 2 lo) (the factor
+// takes the low part of x to first order); below, the float-float e^t - 1.
+__device__ __forceinline__ FF ff_em(FF x)
+{
+    return x.hi >= 8.5f ? FF{-1.f, expf(-2.f * x.hi) * (1.f - 2.f * x.lo)} : ff_expm1(FF{-2.f * x.hi, -2.f * x.lo});
+}
+
 
 // e^x by its Taylor series in FP64 (compile time, |x| < 0.7: 30 terms reach
 // the FP64 rounding)
@@ -649,8 +658,8 @@ static __device__ __noinline__ void ff_rhs(const FFCell &m, FF dTn, FF dT1, FF d
         const FF xs = ff_add2(m.x0[k], dx);
         const bool pos = xs.hi >= 0.f;
         const FF ax = pos ? xs : ff_neg(xs);
-        // r - 1, r = e^{-2|x|}; for |x| > 20, r < 5e-18 needs no float-float
-        const FF em = ax.hi > 20.f ? FF{-1.f, expf(-2.f * ax.hi)} : ff_expm1(FF{-2.f * ax.hi, -2.f * ax.lo});
+        // r - 1, r = e^{-2|x|} (ff_em)
+        const FF em = ff_em(ax);
         const int K = m.Ku[k][pos ? 0 : 1];
         const FF res = ff_sub(ff_add2(m.ru[k][pos ? 0 : 1], pos ? dx : ff_neg(dx)), dpa);   // ln W - K ln 2
         // W >= 1; K as a float by the 1.5 2^23 bias (|K| < 2^22: no conversion instruction)
@@ -800,7 +809,7 @@ __device__ __forceinline__ FF ff_slip_rate(double lnV0, double psia, double x, c
     reduce_ln2(lnV0 - psia + ax, K, r);
     const FF e = ff_exp2k_tab(K, r, tab);
     const FF axf = ff_split_fast(ax);
-    const FF em = axf.hi > 20.f ? FF{-1.f, expf(-2.f * axf.hi)} : ff_expm1(FF{-2.f * axf.hi, -2.f * axf.lo});
+    const FF em = ff_em(axf);
     const FF v = ff_mul(e, ff_neg(em));
     return __double2hiint(x) < 0 ? ff_neg(v) : v;   // the sign of x (its sign bit)
 }
