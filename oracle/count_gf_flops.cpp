@@ -63,8 +63,8 @@ int main()
             const double *R = &rcv[kRecvStride * i];
             C x, y, z;
             tdcs_point(F, C(R[0]), C(R[1]), C(R[2]), x, y, z);
-            C Es[6], Ed[6];
-            if (!tdcs_strain_sd(F, x, y, z, nu, k, Es, Ed)) ++mode0;
+            C Es[6], Ed[6];   // 2/k times the strains
+            if (!tdcs_strain_sd2k(F, x, y, z, nu, Es, Ed)) ++mode0;
             C ue1[3], ue2[3], un[3];
             for (int a = 0; a < 3; ++a) {
                 const int fa = F_NX + 3 * a;
@@ -73,8 +73,8 @@ int main()
                 un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
             }
             C ts[3], td[3];
-            tractions_tdcs<C>(Es, ue1, ue2, un, 2.0 * mu, lam, ts);
-            tractions_tdcs<C>(Ed, ue1, ue2, un, 2.0 * mu, lam, td);
+            tractions_tdcs<C>(Es, ue1, ue2, un, k * mu, 0.5 * k * lam, ts);
+            tractions_tdcs<C>(Ed, ue1, ue2, un, k * mu, 0.5 * k * lam, td);
             ++pairs;
         }
     }

@@ -41,7 +41,7 @@ namespace gf {
 
 constexpr double kPi = 3.141592653589793;
 
-// Per-source record (35 values, stored with stride kSrcStride).
+// Per-source record (41 values, stored with stride kSrcStride).
 enum SrcField {
     F_P2X, F_P2Y, F_P2Z,          // origin (vertex 2)
     F_NX, F_NY, F_NZ,             // triangle normal
@@ -54,15 +54,28 @@ enum SrcField {
     // double angle (sz^2 - sy^2, 2 sy sz) of each vertex's side vector (sy,
     // sz) for the back-rotation (sign-free, so the same for both modes)
     F_C2A, F_S2A, F_C2B, F_S2B, F_C2C, F_S2C,
+    // triple angle (Re, Im of (sz + i sy)^3) of each vertex's side vector as
+    // stored (odd in the sign: negated with (sy, sz) for the other mode)
+    F_C3A, F_S3A, F_C3B, F_S3B, F_C3C, F_S3C,
     F_COUNT
 };
-constexpr int kSrcStride = 36;
+constexpr int kSrcStride = 42;
 constexpr int kRecvStride = 12;   // x, y, z, e1[3], e2[3], n[3]
 
 __host__ __device__ inline void unit3(double v[3])
 {
     const double l = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     v[0] /= l; v[1] /= l; v[2] /= l;
+}
+
+// (sz + i sy)^3 of a side vector (sy, sz): the double angle times the angle.
+__host__ __device__ inline double cube_re(double sy, double sz)
+{
+    return (sz * sz - sy * sy) * sz - 2.0 * (sy * sz) * sy;
+}
+__host__ __device__ inline double cube_im(double sy, double sz)
+{
+    return 2.0 * (sy * sz) * sz + (sz * sz - sy * sy) * sy;
 }
 
 // Source setup (src/TDstressFS_C.cpp:291-396).  f[i * fstride] receives field i.
@@ -102,7 +115,10 @@ __host__ __device__ inline void setup_source(const double P1[3], const double P2
         cos(Am), sin(Am), cos(Bm), sin(Bm), cos(Cm), sin(Cm),
         e13[2] * e13[2] - e13[1] * e13[1], 2.0 * (e13[1] * e13[2]),
         e12[2] * e12[2] - e12[1] * e12[1], 2.0 * (e12[1] * e12[2]),
-        e23[2] * e23[2] - e23[1] * e23[1], 2.0 * (e23[1] * e23[2])};
+        e23[2] * e23[2] - e23[1] * e23[1], 2.0 * (e23[1] * e23[2]),
+        cube_re(e13[1], e13[2]), cube_im(e13[1], e13[2]),
+        cube_re(e12[1], e12[2]), cube_im(e12[1], e12[2]),
+        cube_re(e23[1], e23[2]), cube_im(e23[1], e23[2])};
     for (int i = 0; i < F_COUNT; ++i) f[i * fstride] = vals[i];
 }
 
@@ -166,8 +182,11 @@ struct AdGeom {
     T C, S, gx, gy, gz, fx, fy, fz;
 };
 
+// qg scales the g-terms: 1/(4 pi) gives the strain's own terms; 2 (1 - nu)
+// gives them divided by k = 1/(8 pi (1 - nu)), for a strain with k taken out.
 template <class T>
-__device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, AdGeom<T> &g)
+__device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, AdGeom<T> &g,
+                                        double qg = 1.0 / (4.0 * kPi))
 {
     g.x = x; g.y = y; g.z = z; g.ca = ca; g.sa = sa;
     g.eta = y * ca - z * sa;
@@ -180,34 +199,34 @@ __device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, Ad
     // the three reciprocals from one division (a division is ~9 FP64-pipe
     // instructions, a product one); the plain quotients where the product is
     // zero or not finite (singular lines of the dislocation)
-    T ir, irz, iW;
+    // 1/(r (r - z)) = W/p and 1/(W r) = (r - z)/p
+    T ir, iW;
     const T rrz = r * rz, p = rrz * W;
     if (p != 0.0 && isfinite_t(p)) {
         const T ip = 1.0 / p;
-        const T iWp = ip * W;
-        ir = iWp * rz;
-        irz = iWp * r;
+        g.i_rz = ip * W;
+        g.i_Wr = ip * rz;
         iW = ip * rrz;
+        ir = g.i_rz * rz;
     } else {
         ir = 1.0 / r;
-        irz = 1.0 / rz;
         iW = 1.0 / W;
+        g.i_rz = ir * (1.0 / rz);
+        g.i_Wr = iW * ir;
     }
     const T ir2 = ir * ir;
     g.ir = ir;
     g.ir3 = ir2 * ir;
     g.iW2 = iW * iW;
-    g.i_Wr = iW * ir;
     g.i_W2r2 = g.i_Wr * g.i_Wr;
-    g.i_Wr3 = iW * g.ir3;
-    g.i_rz = ir * irz;
+    g.i_Wr3 = g.i_Wr * ir2;
     g.i_r2z2 = g.i_rz * g.i_rz;
-    g.i_r3z = g.ir3 * irz;
-    g.i_W2r = g.iW2 * ir;
+    g.i_r3z = g.i_rz * ir2;
+    g.i_W2r = iW * g.i_Wr;
     g.C = (r * ca - z) * g.i_Wr;
     g.S = (r * sa - y) * g.i_Wr;
     // with 1/(r - zeta) = -1/W:
-    const double q = 1.0 / (4.0 * kPi);
+    const double q = qg;
     g.gx = -q * (g.eta * g.i_Wr + y * g.i_rz);
     g.gy = (q * x) * (g.i_rz + ca * g.i_Wr);
     g.gz = -(q * x) * (sa * g.i_Wr);
@@ -297,46 +316,105 @@ __device__ __forceinline__ void tdcs_point(const Src &F, T X, T Y, T Z, T &x, T 
     z = F(F_DX) * dx + F(F_DY) * dy + F(F_DZ) * dz;
 }
 
-// TDCS strain (triangle system) of unit strike (Es) and unit dip (Ed) slip.
-// Returns false for mode 0 (strain zero).
+// 2/k times the TDCS strain (triangle system) of unit strike (Es) and unit dip
+// (Ed) slip, k = 1/(8 pi (1 - nu)).  Returns false for mode 0 (strain zero).
+//
+// The back-rotation of each angular dislocation (src/TDstressFS_C.cpp:185-256)
+// in harmonic form.  With e^{i th} = sz + i sy the rotation about x from the
+// triangle system to the dislocation's, a yz-vector v maps to e^{i th} v, so
+// the Burgers vector b = by + i bz enters the dislocation as e^{i th} b and the
+// strain returns with E_xx and E_yy + E_zz unchanged, w = E_xy + i E_xz
+// multiplied by e^{-i th} and q = (E_yy - E_zz)/2 + i E_yz by e^{-2i th}.
+// Writing the dislocation's real-linear response to b' as P b' + Q conj(b'):
+//   w = P_w b + Q_w e^{-2i th} conj(b),   q = P_q e^{-i th} b + Q_q e^{-3i th} conj(b),
+// so per dislocation only Q_w, P_q, Q_q are rotated (one complex product
+// each, accumulated by fused multiply-adds), P_w is summed as it is, and
+// strike (b = 1) and dip (b = i) are read from the same sums at the end.
+// The responses are the grouped by- and bz-parts of ad_parts_yz divided by k
+// (the g-terms scaled by 2 (1 - nu) instead of 1/(4 pi)).
 template <class Src, class T>
-__device__ __forceinline__ bool tdcs_strain_sd(const Src &F, T x, T y, T z, double nu, double k, T Es[6], T Ed[6])
+__device__ __forceinline__ bool tdcs_strain_sd2k(const Src &F, T x, T y, T z, double nu, T Es[6], T Ed[6])
 {
 #pragma unroll
     for (int i = 0; i < 6; ++i) { Es[i] = 0.0; Ed[i] = 0.0; }
     const int m = tri_mode<T>(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
     if (m == 0) return false;
     const bool pm = (m == 1);   // the side vectors' signs by selection, not products
+    const double p2 = 2.0 * nu + 1.0, qg = 2.0 * (1.0 - nu);
+    T xs = 0.0, xd = 0.0;       // E_xx, strike and dip
+    T Ss = 0.0, Sd = 0.0;       // E_yy + E_zz
+    T Pr = 0.0, Pi = 0.0;       // 2 sum P_w
+    T Rr = 0.0, Ri = 0.0;       // 2 sum Q_w e^{-2i th}
+    T Ur = 0.0, Ui = 0.0;       // 4 sum P_q e^{-i th}
+    T Vr = 0.0, Vi = 0.0;       // 4 sum Q_q e^{-3i th}
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-        T vy, vz, sy, sz, ca, sa, c2, s2;
+        T vy, vz, sy, sz, ca, sa, c2, s2, c3, s3;
         if (v == 0) {
-            const T ey = F(F_E13Y), ez = F(F_E13Z);
+            const T ey = F(F_E13Y), ez = F(F_E13Z), a3 = F(F_C3A), b3 = F(F_S3A);
             vy = F(F_P1Y); vz = F(F_P1Z); sy = pm ? -ey : ey; sz = pm ? -ez : ez; ca = F(F_CA); sa = F(F_SA);
-            c2 = F(F_C2A); s2 = F(F_S2A);
+            c2 = F(F_C2A); s2 = F(F_S2A); c3 = pm ? -a3 : a3; s3 = pm ? -b3 : b3;
         } else if (v == 1) {
-            const T ey = F(F_E12Y), ez = F(F_E12Z);
+            const T ey = F(F_E12Y), ez = F(F_E12Z), a3 = F(F_C3B), b3 = F(F_S3B);
             vy = 0.0; vz = 0.0; sy = pm ? ey : -ey; sz = pm ? ez : -ez; ca = F(F_CB); sa = F(F_SB);
-            c2 = F(F_C2B); s2 = F(F_S2B);
+            c2 = F(F_C2B); s2 = F(F_S2B); c3 = pm ? a3 : -a3; s3 = pm ? b3 : -b3;
         } else {
-            const T ey = F(F_E23Y), ez = F(F_E23Z);
+            const T ey = F(F_E23Y), ez = F(F_E23Z), a3 = F(F_C3C), b3 = F(F_S3C);
             vy = F(F_P3Y); vz = F(F_P3Z); sy = pm ? ey : -ey; sz = pm ? ez : -ez; ca = F(F_CC); sa = F(F_SC);
-            c2 = F(F_C2C); s2 = F(F_S2C);
+            c2 = F(F_C2C); s2 = F(F_S2C); c3 = pm ? a3 : -a3; s3 = pm ? b3 : -b3;
         }
         const T ty = y - vy, tz = z - vz;
         AdGeom<T> g;
-        ad_geom<T>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g);
-        T Ey[6], Ez[6];
-        ad_parts_yz<T>(g, nu, k, Ey, Ez);
-        T ts[6], td[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            ts[i] = sz * Ey[i] + sy * Ez[i];    // strike: (by1, bz1) = (sz, sy)
-            td[i] = -sy * Ey[i] + sz * Ez[i];   // dip:    (by1, bz1) = (-sy, sz)
-        }
-        add_rot_x(Es, ts, sy, sz, c2, s2);
-        add_rot_x(Ed, td, sy, sz, c2, s2);
+        ad_geom<T>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g, qg);
+        const T ax = g.x, ay = g.y, az = g.z;
+        const T xsa = ax * sa, yz = ay * az;
+        const T A = g.i_r2z2 + g.i_r3z;
+        const T x2i = g.x2 * g.i_Wr, x2w3 = g.x2 * g.i_Wr3;
+        const T nux = nu + x2i;
+        const T Q3 = g.S * nux + ay * x2w3;
+        const T Q4 = g.C * nux + az * x2w3;
+        const T Pq = sa * ca * g.iW2 - g.ycz * g.i_W2r + yz * (g.i_W2r2 - g.i_Wr3);
+        // E_xx of by (ey) and bz (ez)
+        const T e0y = -ax * (g.fx * ca + p2 * g.i_rz - g.x2 * A);
+        const T e0z = xsa * g.fx;
+        // E_yy, E_zz
+        const T e1y = g.gy - ax * (g.i_rz - g.y2 * A + g.fy * ca);
+        const T e2y = -ax * (g.fz * ca + az * g.ir3);
+        const T e1z = xsa * g.fy;
+        const T e2z = g.gz + xsa * g.fz;
+        // 2 E_yz
+        const T e5y = g.gz - (ax + ax) * (ay * g.ir3 + ca * Pq);
+        const T e5z = g.gy + (xsa + xsa) * Pq;
+        // 2 P_w and 2 Q_w from 2 (E_xy + i E_xz) of by and bz
+        const T X3 = g.x2 * ay * A - nu * ay * g.i_rz + ca * Q3;
+        const T X4 = nu * g.ir - g.x2 * g.ir3 + ca * Q4;
+        const T wPr = (X3 + g.gx) - sa * Q4, wPi = X4 + sa * Q3;
+        const T wQr = X3 + sa * Q4, wQi = X4 - sa * Q3;
+        // 4 P_q and 4 Q_q from (E_yy - E_zz) + 2i E_yz of by and bz
+        const T Sy = e1y + e2y, Sz = e1z + e2z;
+        const T Dy = e1y - e2y, Dz = e1z - e2z;
+        const T ar = e5z + Dy, ai = e5y - Dz;
+        const T br = Dy - e5z, bi = e5y + Dz;
+        // invariants: strike b' = (sz, sy), dip b' = (-sy, sz); the rest rotated
+        xs = sz * e0y + (sy * e0z + xs);
+        xd = sz * e0z + (xd - sy * e0y);
+        Ss = sz * Sy + (sy * Sz + Ss);
+        Sd = sz * Sz + (Sd - sy * Sy);
+        Pr = Pr + wPr;
+        Pi = Pi + wPi;
+        Rr = c2 * wQr + (s2 * wQi + Rr);
+        Ri = c2 * wQi + (Ri - s2 * wQr);
+        Ur = sz * ar + (sy * ai + Ur);
+        Ui = sz * ai + (Ui - sy * ar);
+        Vr = c3 * br + (s3 * bi + Vr);
+        Vi = c3 * bi + (Vi - s3 * br);
     }
+    // strike b = 1: 2w = P + R, 4q = U + V; dip b = i: 2w = i (P - R), 4q = i (U - V)
+    const T uvr = Ur + Vr, uvi = Ui + Vi, umr = Ur - Vr, umi = Ui - Vi;
+    Es[0] = 2.0 * xs; Es[1] = 0.5 * uvr + Ss; Es[2] = Ss - 0.5 * uvr;
+    Es[3] = Pr + Rr; Es[4] = Pi + Ri; Es[5] = 0.5 * uvi;
+    Ed[0] = 2.0 * xd; Ed[1] = Sd - 0.5 * umi; Ed[2] = 0.5 * umi + Sd;
+    Ed[3] = Ri - Pi; Ed[4] = Pr - Rr; Ed[5] = 0.5 * umr;
     return true;
 }
 
@@ -424,8 +502,8 @@ __device__ __forceinline__ void pair_tractions(const Src &F, const double *R, do
 {
     double x, y, z;
     tdcs_point(F, R[0], R[1], R[2], x, y, z);
-    double Es[6], Ed[6];
-    tdcs_strain_sd(F, x, y, z, nu, k, Es, Ed);
+    double Es[6], Ed[6];   // 2/k times the strains
+    tdcs_strain_sd2k(F, x, y, z, nu, Es, Ed);
     double ue1[3], ue2[3], un[3];   // receiver axes in the source system
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -434,8 +512,9 @@ __device__ __forceinline__ void pair_tractions(const Src &F, const double *R, do
         ue2[a] = F(fa) * R[6] + F(fa + 1) * R[7] + F(fa + 2) * R[8];
         un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
     }
-    tractions_tdcs(Es, ue1, ue2, un, two_mu, lam, ts);
-    tractions_tdcs(Ed, ue1, ue2, un, two_mu, lam, td);
+    const double hk = 0.5 * k;
+    tractions_tdcs(Es, ue1, ue2, un, hk * two_mu, hk * lam, ts);
+    tractions_tdcs(Ed, ue1, ue2, un, hk * two_mu, hk * lam, td);
 }
 
 }  // namespace gf
