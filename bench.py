@@ -132,16 +132,16 @@ def fp64_peak_tflops(torch, dev):
 
 
 # FP64 operations of one (receiver, source) pair of the assembly kernel
-# (both unit slips, 6 entries): 315 add + 441 mul + 5 div + 3 sqrt, counted by
+# (both unit slips, 6 entries): 318 add + 403 mul + 5 div + 3 sqrt, counted by
 # oracle/count_gf_flops.cpp on the kernel's own device math.
-GF_FLOP_PER_PAIR = 764
+GF_FLOP_PER_PAIR = 729
 # The same for the half-space kernel (main + image dislocation, the
-# free-surface correction of the three sides in dual numbers): 5,408.7 add +
-# 8,873.4 mul + 72.9 div + 18.0 sqrt per pair (and 18.0 transcendental calls),
+# free-surface correction of the three sides in dual numbers): 5,412.7 add +
+# 8,793.4 mul + 66.9 div + 18.0 sqrt per pair (and 18.0 transcendental calls),
 # counted by oracle/count_hs_flops.cpp over every pair of the 40 x 20 km,
 # N = 2,500 mesh of bench_halfspace (the count depends weakly on the mesh
 # through the branches of the angular dislocations).
-HS_FLOP_PER_PAIR = 14373
+HS_FLOP_PER_PAIR = 14291
 # Stores per pair: 6 FP64 + 6 FP32 entries.
 GF_BYTES_PER_PAIR = 72
 

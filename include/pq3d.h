@@ -95,7 +95,7 @@ int pq3d_assemble_dense(const double *nodes, const int64_t *tris, int64_t N,
  * front and forbids side allocations), or a loop that cannot afford the
  * implicit device synchronisation and the failure modes of cudaMalloc/cudaFree
  * between its launches.  The source and receiver tables live in a fixed
- * 12.6 MB __device__ array inside this library, so N is limited to 32768
+ * 14.2 MB __device__ array inside this library, so N is limited to 32768
  * elements (larger N returns PQ3D_ERR_ARG).  Every call looks up the array's
  * device address with the calling device current (cudaGetSymbolAddress; no
  * cached address, so a device reset between calls is harmless); the first

@@ -6,7 +6,7 @@
 // FP64 operations per pair as JSON.  Convention: add, sub, mul, div and sqrt
 // count one each (a fused multiply-add is a mul and an add); comparisons and
 // negations are free.  The kernel body's own lines (receiver axes rotated into
-// the source system, 2 x traction contraction) are restated here verbatim.
+// the source system, 2 x traction contraction with e1, e2 pre-scaled) are restated here.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -65,16 +65,19 @@ int main()
             tdcs_point(F, C(R[0]), C(R[1]), C(R[2]), x, y, z);
             C Es[6], Ed[6];   // 2/k times the strains
             if (!tdcs_strain_sd2k(F, x, y, z, nu, Es, Ed)) ++mode0;
+            // e1, e2 multiplied by the traction scale once per receiver tile
+            // in the kernel (not a per-pair operation)
+            const double cmu = traction_axis_scale(k, 2.0 * mu);
             C ue1[3], ue2[3], un[3];
             for (int a = 0; a < 3; ++a) {
                 const int fa = F_NX + 3 * a;
-                ue1[a] = F(fa) * R[3] + F(fa + 1) * R[4] + F(fa + 2) * R[5];
-                ue2[a] = F(fa) * R[6] + F(fa + 1) * R[7] + F(fa + 2) * R[8];
+                ue1[a] = F(fa) * (cmu * R[3]) + F(fa + 1) * (cmu * R[4]) + F(fa + 2) * (cmu * R[5]);
+                ue2[a] = F(fa) * (cmu * R[6]) + F(fa + 1) * (cmu * R[7]) + F(fa + 2) * (cmu * R[8]);
                 un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
             }
             C ts[3], td[3];
-            tractions_tdcs<C>(Es, ue1, ue2, un, k * mu, 0.5 * k * lam, ts);
-            tractions_tdcs<C>(Ed, ue1, ue2, un, k * mu, 0.5 * k * lam, td);
+            tractions_tdcs_scaled<C>(Es, ue1, ue2, un, cmu, 0.5 * k * lam, ts);
+            tractions_tdcs_scaled<C>(Ed, ue1, ue2, un, cmu, 0.5 * k * lam, td);
             ++pairs;
         }
     }

@@ -99,14 +99,20 @@ assemble_dense_kernel(const double *__restrict__ src, const double *__restrict__
     const int64_t j = j0 + t;
     for (int f = 0; f < F_COUNT; ++f) s_src[f * kTJ + t] = (j < N) ? src[f * N + j] : 0.0;
     const int nrec = (int)((row1 - i0) < kTI ? (row1 - i0) : kTI);
-    for (int q = t; q < nrec * kRecvStride; q += kTJ) s_rcv[q] = recv[i0 * kRecvStride + q];
+    // receiver records with e1 and e2 multiplied by the traction scale
+    const double axis_scale = traction_axis_scale(k, two_mu);
+    for (int q = t; q < nrec * kRecvStride; q += kTJ) {
+        const int fq = q % kRecvStride;
+        const double v = recv[i0 * kRecvStride + q];
+        s_rcv[q] = (fq >= 3 && fq < 9) ? v * axis_scale : v;
+    }
     __syncthreads();
     if (j >= N) return;
     const SoaSrc F{s_src + t, kTJ};
     const int64_t ld = 2 * N;
     for (int ii = 0; ii < nrec; ++ii) {
         double ts[3], td[3];
-        pair_tractions(F, s_rcv + ii * kRecvStride, nu, k, two_mu, lam, ts, td);
+        pair_tractions<SoaSrc, true>(F, s_rcv + ii * kRecvStride, nu, k, two_mu, lam, ts, td);
         const int64_t r = 3 * (i0 + ii - row0);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -389,7 +395,7 @@ static int assemble_rows(const double *nodes, const int64_t *tris, int64_t N, in
 // ---------------------------------------------------------------------------
 // Fixed scratch for pq3d_assemble_dense_noalloc: the source and receiver
 // tables of one call (kSrcStride + kRecvStride doubles per element) for up to
-// kNoAllocMaxN elements, 12.6 MB held by every GPU that loads this library.
+// kNoAllocMaxN elements, 14.2 MB held by every GPU that loads this library.
 constexpr int64_t kNoAllocMaxN = 32768;
 static __device__ __align__(256) double g_noalloc_scratch[(size_t)(kSrcStride + kRecvStride) * kNoAllocMaxN];
 

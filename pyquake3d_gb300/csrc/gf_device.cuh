@@ -368,14 +368,14 @@ __device__ __forceinline__ bool tdcs_strain_sd2k(const Src &F, T x, T y, T z, do
         ad_geom<T>(x, sz * ty - sy * tz, sy * ty + sz * tz, ca, sa, nu, g, qg);
         const T ax = g.x, ay = g.y, az = g.z;
         const T xsa = ax * sa, yz = ay * az;
-        const T A = g.i_r2z2 + g.i_r3z;
+        const T A = g.i_r2z2 + g.i_r3z, x2A = g.x2 * A;
         const T x2i = g.x2 * g.i_Wr, x2w3 = g.x2 * g.i_Wr3;
         const T nux = nu + x2i;
         const T Q3 = g.S * nux + ay * x2w3;
         const T Q4 = g.C * nux + az * x2w3;
         const T Pq = sa * ca * g.iW2 - g.ycz * g.i_W2r + yz * (g.i_W2r2 - g.i_Wr3);
         // E_xx of by (ey) and bz (ez)
-        const T e0y = -ax * (g.fx * ca + p2 * g.i_rz - g.x2 * A);
+        const T e0y = -ax * ((g.fx * ca + p2 * g.i_rz) - x2A);
         const T e0z = xsa * g.fx;
         // E_yy, E_zz
         const T e1y = g.gy - ax * (g.i_rz - g.y2 * A + g.fy * ca);
@@ -386,7 +386,7 @@ __device__ __forceinline__ bool tdcs_strain_sd2k(const Src &F, T x, T y, T z, do
         const T e5y = g.gz - (ax + ax) * (ay * g.ir3 + ca * Pq);
         const T e5z = g.gy + (xsa + xsa) * Pq;
         // 2 P_w and 2 Q_w from 2 (E_xy + i E_xz) of by and bz
-        const T X3 = g.x2 * ay * A - nu * ay * g.i_rz + ca * Q3;
+        const T X3 = ay * (x2A - nu * g.i_rz) + ca * Q3;
         const T X4 = nu * g.ir - g.x2 * g.ir3 + ca * Q4;
         const T wPr = (X3 + g.gx) - sa * Q4, wPi = X4 + sa * Q3;
         const T wQr = X3 + sa * Q4, wQi = X4 - sa * Q3;
@@ -493,10 +493,29 @@ __device__ __forceinline__ void tractions_tdcs(const T E[6], const T ue1[3], con
     out[2] = two_mu * (un[0] * u0 + un[1] * u1 + un[2] * u2) + lam * tr;
 }
 
+// tractions_tdcs with ue1, ue2 already multiplied by cmu (the traction
+// scale): out_c = ue_c . (E un) for c = e1, e2, cmu un . (E un) + clam tr(E).
+template <class T>
+__device__ __forceinline__ void tractions_tdcs_scaled(const T E[6], const T ue1[3], const T ue2[3], const T un[3],
+                                                      double cmu, double clam, T out[3])
+{
+    const T u0 = E[0] * un[0] + E[3] * un[1] + E[4] * un[2];
+    const T u1 = E[3] * un[0] + E[1] * un[1] + E[5] * un[2];
+    const T u2 = E[4] * un[0] + E[5] * un[1] + E[2] * un[2];
+    const T tr = E[0] + E[1] + E[2];
+    out[0] = ue1[0] * u0 + ue1[1] * u1 + ue1[2] * u2;
+    out[1] = ue2[0] * u0 + ue2[1] * u1 + ue2[2] * u2;
+    out[2] = cmu * (un[0] * u0 + un[1] * u1 + un[2] * u2) + clam * tr;
+}
+
 // The six tractions of one (receiver, source) pair: receiver record R
 // (centroid, e1, e2, n), source fields F; ts = unit strike slip, td = unit dip
-// slip, components (e1, e2, n).
-template <class Src>
+// slip, components (e1, e2, n).  kScaledAxes: R's e1 and e2 come multiplied
+// by traction_axis_scale(k, two_mu) (the assembly kernel scales them once per
+// receiver tile).
+__host__ __device__ inline double traction_axis_scale(double k, double two_mu) { return (0.5 * k) * two_mu; }
+
+template <class Src, bool kScaledAxes = false>
 __device__ __forceinline__ void pair_tractions(const Src &F, const double *R, double nu, double k, double two_mu,
                                                double lam, double ts[3], double td[3])
 {
@@ -513,8 +532,13 @@ __device__ __forceinline__ void pair_tractions(const Src &F, const double *R, do
         un[a] = F(fa) * R[9] + F(fa + 1) * R[10] + F(fa + 2) * R[11];
     }
     const double hk = 0.5 * k;
-    tractions_tdcs(Es, ue1, ue2, un, hk * two_mu, hk * lam, ts);
-    tractions_tdcs(Ed, ue1, ue2, un, hk * two_mu, hk * lam, td);
+    if (kScaledAxes) {
+        tractions_tdcs_scaled(Es, ue1, ue2, un, traction_axis_scale(k, two_mu), hk * lam, ts);
+        tractions_tdcs_scaled(Ed, ue1, ue2, un, traction_axis_scale(k, two_mu), hk * lam, td);
+    } else {
+        tractions_tdcs(Es, ue1, ue2, un, hk * two_mu, hk * lam, ts);
+        tractions_tdcs(Ed, ue1, ue2, un, hk * two_mu, hk * lam, td);
+    }
 }
 
 }  // namespace gf
