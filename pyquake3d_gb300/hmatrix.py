@@ -135,35 +135,38 @@ class HMatrix:
         rank = np.full(nb, -1, dtype=np.int32)
         status = np.zeros(nb, dtype=np.int32)
         lr = np.nonzero(lowrank)[0]
-        # ACA in chunks of blocks, bounded scratch
+        # ACA in chunks of blocks (at most chunk_bytes of FP64 factors each).
+        # One FP64 scratch, sized for the largest chunk, serves every chunk:
+        # each chunk's converged factors are packed to FP32 right after its
+        # ACA, so the FP64 factors of all blocks never coexist (N = 100,000:
+        # 22 GB of FP64 factors, 3 GB packed).
         uv_need = kcap.astype(np.int64) * (3 * m + 2 * n)
-        rank_t = torch.full((nb,), -1, dtype=torch.int32, device=dev)
-        status_t = torch.zeros(nb, dtype=torch.int32, device=dev)
-        factors = {}
+        bounds = []
         i = 0
-        self.aca_chunks = 0
-        aca_events = []   # (start, end) CUDA events around each ACA launch
         while i < len(lr):
             j = i
             tot = 0
             while j < len(lr) and (j == i or tot + uv_need[lr[j]] * 8 <= chunk_bytes):
                 tot += uv_need[lr[j]] * 8
                 j += 1
+            bounds.append((i, j))
+            i = j
+        self.aca_chunks = len(bounds)
+        UV = torch.empty(max([int(uv_need[lr[i:j]].sum()) for i, j in bounds] + [1]), dtype=torch.float64,
+                         device=dev)
+        lr_parts = []     # per chunk: block ids, FP32 offsets inside the chunk, packed factors
+        aca_events = []   # (start, end) CUDA events around each ACA launch
+        for (i, j) in bounds:
             ids = lr[i:j]
-            uv_off = np.zeros(nb, dtype=np.int64)
-            used_off = np.zeros(nb, dtype=np.int64)
-            uv_off[ids] = np.concatenate([[0], np.cumsum(uv_need[ids])[:-1]])
-            used_off[ids] = np.concatenate([[0], np.cumsum(3 * m[ids])[:-1]])
-            UV = torch.empty(int(uv_need[ids].sum()), dtype=torch.float64, device=dev)
+            uv_off = np.concatenate([[0], np.cumsum(uv_need[ids])[:-1]]).astype(np.int64)
+            used_off = np.concatenate([[0], np.cumsum(3 * m[ids])[:-1]]).astype(np.int64)
             used = torch.zeros(int((3 * m[ids]).sum()), dtype=torch.uint8, device=dev)
-            uv_off_t = torch.as_tensor(uv_off, device=dev)
-            used_off_t = torch.as_tensor(used_off, device=dev)
             # the kernel indexes blocks by grid position: pass the chunk's sub-arrays
             sub = torch.as_tensor(ids, device=dev)
             blk_c = self.blk[sub].contiguous()
             kcap_c = self.kcap[sub].contiguous()
-            uvo_c = uv_off_t[sub].contiguous()
-            uso_c = used_off_t[sub].contiguous()
+            uvo_c = torch.as_tensor(uv_off, device=dev)
+            uso_c = torch.as_tensor(used_off, device=dev)
             rk_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             stt_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -174,48 +177,63 @@ class HMatrix:
                                        stt_c.data_ptr(), st))
             ev[1].record()
             aca_events.append(ev)
-            rank[ids] = rk_c.cpu().numpy()
-            status[ids] = stt_c.cpu().numpy()
-            factors[(i, j)] = (ids, UV, uvo_c, blk_c, kcap_c, rk_c)
-            self.aca_chunks += 1
-            i = j
+            st_h = stt_c.cpu().numpy()
+            rk_h = np.where(st_h == 0, rk_c.cpu().numpy(), -1).astype(np.int32)   # not converged: dense
+            rank[ids] = rk_h
+            status[ids] = st_h
+            # packed FP32 factors k (3m + 2n), each block padded to a multiple
+            # of 4 floats (16-byte aligned starts), zero padding
+            sz = np.maximum(rk_h, 0).astype(np.int64) * (3 * m[ids] + 2 * n[ids])
+            sz = (sz + 3) // 4 * 4
+            loc = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+            buf = torch.zeros(max(int(sz.sum()), 4), dtype=torch.float32, device=dev)
+            good = np.nonzero(rk_h >= 0)[0].astype(np.int32)   # positions inside the chunk
+            if len(good):
+                pos = torch.as_tensor(good, device=dev)
+                loc_t = torch.as_tensor(loc, device=dev)
+                _lib.check(L.pq3d_hmat_pack_factors(UV.data_ptr(), uvo_c.data_ptr(), blk_c.data_ptr(),
+                                                    kcap_c.data_ptr(), rk_c.data_ptr(), pos.data_ptr(), len(good),
+                                                    buf.data_ptr(), loc_t.data_ptr(), st))
+            lr_parts.append((ids, rk_h, loc, int(sz.sum()), buf))
+        del UV
         phase("aca")
         # device time of the ACA launches alone (the rest of the phase is the
-        # factor allocations and the rank/status copies back)
+        # FP32 packing of each chunk, the small allocations and the rank and
+        # status copies back)
         phases["aca_kernels"] = sum(a.elapsed_time(b) for a, b in aca_events) / 1e3
-        ok = lowrank & (status == 0)
-        rank[~ok] = -1
         self.aca_status = status
-        # storage offsets: dense 3m x 2n (column-major), low rank k (3m + 2n)
-        # floats (U column-major, then V row-major), each block padded to a
-        # multiple of 4 floats so that every block starts 16-byte aligned
-        size = np.where(rank >= 0, rank.astype(np.int64) * (3 * m + 2 * n), 6 * m * n)
-        size = (size + 3) // 4 * 4
-        off = np.concatenate([[0], np.cumsum(size)[:-1]]).astype(np.int64)
+        # storage: the converged low-rank blocks first, in block order (U
+        # column-major 3m x k, then V k x 2n), then the dense blocks in block
+        # order (3m x 2n column-major); every block padded to a multiple of 4
+        # floats so that each starts 16-byte aligned
+        off = np.zeros(nb, dtype=np.int64)
+        base = 0
+        for (ids, rk_h, loc, used_f, _) in lr_parts:
+            ok = rk_h >= 0
+            off[ids[ok]] = base + loc[ok]
+            base += used_f
+        dense_ids = np.nonzero(rank < 0)[0].astype(np.int32)
+        dsz = (6 * m[dense_ids].astype(np.int64) * n[dense_ids] + 3) // 4 * 4
+        off[dense_ids] = base + np.concatenate([[0], np.cumsum(dsz)[:-1]]).astype(np.int64)
+        total = base + int(dsz.sum())
         assert np.all(off % 4 == 0)
-        self.data = torch.zeros(int(size.sum()), dtype=torch.float32, device=dev)   # padding defined
+        self.data = torch.zeros(max(total, 4), dtype=torch.float32, device=dev)   # padding defined
         self.off = torch.as_tensor(off, device=dev)
         self.rank = torch.as_tensor(rank, device=dev)
         phase("storage_alloc")
-        dense_ids = np.nonzero(rank < 0)[0].astype(np.int32)
         if len(dense_ids):
             ids_t = torch.as_tensor(dense_ids, device=dev)
             _lib.check(L.pq3d_hmat_dense_blocks(self.tables.data_ptr(), N, self.perm.data_ptr(), self.blk.data_ptr(),
                                                 ids_t.data_ptr(), len(dense_ids), float(mu), float(lam), hs,
                                                 self.data.data_ptr(), self.off.data_ptr(), st))
         phase("dense_blocks")
-        for (ids, UV, uvo_c, blk_c, kcap_c, rk_c) in factors.values():
-            good = np.nonzero(rank[ids] >= 0)[0].astype(np.int32)   # positions inside the chunk
-            if len(good) == 0:
-                continue
-            pos = torch.as_tensor(good, device=dev)
-            out_off = self.off[torch.as_tensor(ids, device=dev)].contiguous()
-            _lib.check(L.pq3d_hmat_pack_factors(UV.data_ptr(), uvo_c.data_ptr(), blk_c.data_ptr(), kcap_c.data_ptr(),
-                                                rk_c.data_ptr(), pos.data_ptr(), len(good), self.data.data_ptr(),
-                                                out_off.data_ptr(), st))
-        torch.cuda.synchronize(dev)
-        del factors
-        phase("pack_factors")
+        base = 0
+        for (_, _, _, used_f, buf) in lr_parts:
+            if used_f:
+                self.data[base:base + used_f].copy_(buf[:used_f])
+            base += used_f
+        del lr_parts
+        phase("place_factors")
         # low-rank bookkeeping and leaf lists
         lr_ids = np.nonzero(rank >= 0)[0].astype(np.int32)
         ranks = rank[lr_ids].astype(np.int64)
