@@ -555,7 +555,7 @@ def bench_batched(torch, dev, args, peaks):
     tabs = mesh.ensemble_tables(xg, Lkm * 1e3, Wkm * 1e3, B=B, seed=0, v_nuc=1e-3)
     K64, K32 = gf.assemble_dense(nodes, tris, MU, LAM, device=dev)
     P = PackedOperator(K64)
-    # the mesh's own cell order: on this planar workload it holds 1e-5 longer
+    # the mesh's own cell order: on this planar workload it held 1e-5 longer
     # than the cluster tree's compact order (16 runs in lockstep: 106 against
     # 94 accepted steps with either attempt)
     PF = PackedFixOperator(K64)
@@ -1019,11 +1019,11 @@ def bench_serving(torch, dev, args):
     res["arithmetic"] = {
         "dense_bf16x18": "exact fixed-point BF16x18 product + float-float Dormand-Prince attempt: slip within 1e-5 "
                          "of the FP64 stepper for ~100 accepted steps (lockstep, N=10,000; the batched section's "
-                         "bf16x18_ff_attempt), the FP64 stepper's own 1e-12-perturbation floor is 135",
+                         "bf16x18_ff_attempt), the FP64 stepper's own 1e-12-perturbation floor ~120",
         "dense_bf16x6": "BF16x6 product + mixed attempt: within 1e-5 for ~25 accepted steps",
         "hmatrix": "FP32 ACA factors (tol 1e-4) + mixed attempt: the H-matrix approximation of the operator",
         "runs_beyond_the_horizon": "past its horizon a run follows another trajectory of the same chaotic "
-                                   "system, as the FP64 stepper does past 135 steps under a 1e-12 perturbation"}
+                                   "system, as the FP64 stepper does past ~120 steps under a 1e-12 perturbation"}
     return res
 
 
