@@ -34,6 +34,9 @@
 #define __host__
 #define __device__
 #define __forceinline__ inline
+#define PQ3D_NOINLINE __attribute__((noinline))
+#else
+#define PQ3D_NOINLINE __noinline__
 #endif
 
 namespace pq3d {

@@ -226,9 +226,12 @@ __device__ __forceinline__ void fsc_unit_disp(Dv y1, Dv y2, Dv y3, const FscTrig
 // d/dy of the harmonic displacement at one end point for NB Burgers vectors b
 // (side frame), accumulated with weight sgn into J[q][i][j] = d v_i / d y_j.
 // Configuration I evaluates at (-y1, -y2, y3) with (-b1, -b2, b3) and maps
-// the Jacobian back (rows and columns 1, 2 change sign).
+// the Jacobian back (rows and columns 1, 2 change sign).  A called function,
+// not inlined: the dual-number intermediates of one end point then take the
+// register file alone (inlined into the pair evaluation they spilled 1.6 KB
+// per thread).
 template <int NB>
-__device__ __forceinline__ void fsc_endpoint(const double y[3], bool confI, const FscTrig &T, double nu,
+__device__ PQ3D_NOINLINE void fsc_endpoint(const double y[3], bool confI, const FscTrig &T, double nu,
                                                       double a, const double b[NB][3], double sgn,
                                                       double J[NB][3][3])
 {
