@@ -4,7 +4,9 @@
 // (receiver, source) pair.  Test infrastructure only.
 //
 // stdin: "n" then n lines "P1(3) P2(3) P3(3) X Y Z Ss Ds Ts e1(3) e2(3) nv(3)"
-// stdout: per case 12 numbers: strain(6) ts(3) td(3)
+// stdout: per case 18 numbers: half-space strain(6) ts(3) td(3), then the
+// full-space ts(3) td(3) as the dense assembly kernel forms them (receiver
+// axes e1, e2 pre-scaled, pair_tractions<..., true>)
 #include <cmath>
 #include <cstdio>
 
@@ -40,6 +42,12 @@ int main()
         double ts[3], td[3];
         pair_tractions_hs(F, Fi, G, R, nu, k, 2.0 * mu, lam, ts, td);
         for (int i = 0; i < 6; ++i) printf("%.17g ", e[i]);
+        for (int i = 0; i < 3; ++i) printf("%.17g ", ts[i]);
+        for (int i = 0; i < 3; ++i) printf("%.17g ", td[i]);
+        const double cmu = traction_axis_scale(k, 2.0 * mu);
+        double Rs[kRecvStride];
+        for (int i = 0; i < kRecvStride; ++i) Rs[i] = (i >= 3 && i < 9) ? R[i] * cmu : R[i];
+        pair_tractions<Arr, true>(F, Rs, nu, k, 2.0 * mu, lam, ts, td);
         for (int i = 0; i < 3; ++i) printf("%.17g ", ts[i]);
         for (int i = 0; i < 3; ++i) printf("%.17g ", td[i]);
         printf("\n");

@@ -142,7 +142,50 @@ def test_device_math_matches_oracle(host_check):
                 t = S @ n
                 acc.extend([t @ e1, t @ e2, t @ n])
         scale = max(np.linalg.norm(tt), np.linalg.norm(t0))
-        assert np.linalg.norm(res[i, 6:] - np.array(tt)) / scale < 1e-10, i
+        assert np.linalg.norm(res[i, 6:12] - np.array(tt)) / scale < 1e-10, i
+
+
+def _tractions(x, P, n, e1, e2, half):
+    out = []
+    for Ss, Ds in ((1.0, 0.0), (0.0, 1.0)):
+        s, _ = oracle.tdstress(*x, P[0], P[1], P[2], Ss, Ds, 0.0, MU, MU, half)
+        S = np.array([[s[0, 0], s[0, 3], s[0, 4]], [s[0, 3], s[0, 1], s[0, 5]], [s[0, 4], s[0, 5], s[0, 2]]])
+        t = S @ n
+        out.extend([t @ e1, t @ e2, t @ n])
+    return np.array(out)
+
+
+def test_full_space_pair_matches_oracle(host_check):
+    """The dense assembly kernel's own pair evaluation (harmonic
+    back-rotation of the angular dislocations, k taken out, pre-scaled
+    receiver axes), compiled for the host, against the oracle's full-space
+    tractions (the reference's operation order): 600 seeded pairs, a third
+    of them with the receiver in the source's plane (inside, and outside in
+    both configurations of the mode test), each pair within 1e-10 of its
+    largest traction."""
+    rng = np.random.default_rng(7)
+    cases = []
+    for t in range(600):
+        P = rng.normal(size=(3, 3)) * 2000 + np.array([0, 0, -8000.0])
+        if t % 3 == 0:
+            # in the plane: P1 + s (P2 - P1) + u (P3 - P1), s, u off the side lines
+            s_, u_ = rng.uniform(-1.5, 2.5, size=2)
+            X = P[0] + s_ * (P[1] - P[0]) + u_ * (P[2] - P[0])
+        else:
+            X = P.mean(axis=0) + rng.normal(size=3) * rng.choice([300.0, 3000.0, 30000.0])
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        e1 = np.cross([0, 0, 1.0], n)
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(n, e1)
+        cases.append((P, X, np.array([1.0, 0.0, 0.0]), e1, e2, n))
+    inp = "%d\n" % len(cases) + "\n".join(
+        " ".join("%.17g" % v for v in np.concatenate([P.ravel(), X, b, e1, e2, n])) for P, X, b, e1, e2, n in cases)
+    out = subprocess.run([host_check], input=inp, capture_output=True, text=True, check=True).stdout
+    res = np.array([[float(v) for v in line.split()] for line in out.strip().split("\n")])
+    for i, (P, X, b, e1, e2, n) in enumerate(cases):
+        ref = _tractions((X[:1], X[1:2], X[2:3]), P, n, e1, e2, False)
+        assert np.abs(res[i, 12:] - ref).max() <= 1e-10 * np.abs(ref).max(), i
 
 
 def test_rough_fault_oracle_not_less_accurate_than_reference(golden):
