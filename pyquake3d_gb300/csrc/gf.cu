@@ -118,7 +118,7 @@ assemble_dense_kernel(const double *__restrict__ src, const double *__restrict__
         for (int c = 0; c < 3; ++c) {
             *reinterpret_cast<double2 *>(K64 + (r + c) * ld + 2 * j) = make_double2(ts[c], td[c]);
             if (kWrite32)
-                *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2((float)ts[c], (float)td[c]);
+                *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2(d2f_rn_bits(ts[c]), d2f_rn_bits(td[c]));
         }
     }
 }
@@ -155,7 +155,7 @@ assemble_dense_hs_kernel(const double *__restrict__ src, const double *__restric
         for (int c = 0; c < 3; ++c) {
             *reinterpret_cast<double2 *>(K64 + (r + c) * ld + 2 * j) = make_double2(ts[c], td[c]);
             if (kWrite32)
-                *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2((float)ts[c], (float)td[c]);
+                *reinterpret_cast<float2 *>(K32 + (r + c) * ld + 2 * j) = make_float2(d2f_rn_bits(ts[c]), d2f_rn_bits(td[c]));
         }
     }
 }

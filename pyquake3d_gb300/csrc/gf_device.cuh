@@ -167,11 +167,39 @@ __device__ __forceinline__ int tri_mode(T x, T y, T z, T p1y, T p1z, T p3y, T p3
 
 #ifdef __CUDACC__
 __device__ __forceinline__ bool isfinite_t(double v) { return isfinite(v); }
+// v != 0 and finite, by integer tests of the bit pattern (GB300 runs FP64
+// compares on its FP64 pipe, which the pair evaluation keeps busy)
+__device__ __forceinline__ bool nonzero_finite_t(double v)
+{
+    const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
+    return (hw & 0x7ff00000u) != 0x7ff00000u && ((hw & 0x7fffffffu) | lw) != 0u;
+}
 #else
 inline bool isfinite_t(double v) { return std::isfinite(v); }
 #ifndef PQ3D_OPCOUNT
 inline bool isfinite_t(long double v) { return std::isfinite(v); }
 #endif
+#endif
+template <class T>
+__host__ __device__ inline bool nonzero_finite_t(T v) { return v != 0.0 && isfinite_t(v); }
+
+// FP64 -> FP32, round to nearest even, by the bit layout: integer operations
+// only where the result is a normal float; values that round to a subnormal
+// float or to zero, overflow, infinities and NaN take the conversion
+// instruction (a branch that the operator's entries do not take).
+#ifdef __CUDACC__
+__device__ __forceinline__ float d2f_rn_bits(double x)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    if (e < 1023 - 126 || e > 1023 + 127) return (float)x;
+    unsigned f = (hw & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+    const unsigned rem = lw & 0x1fffffffu;   // the 29 bits below the float's last
+    // above half an ulp, or exactly half with an odd last bit: one ulp up (a
+    // carry into the exponent is the next binade; past the largest float, inf)
+    f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f);
+}
 #endif
 
 // Shared geometric terms of one angular dislocation at (x, y, z) of its own
@@ -205,7 +233,7 @@ __device__ __forceinline__ void ad_geom(T x, T y, T z, T ca, T sa, double nu, Ad
     // 1/(r (r - z)) = W/p and 1/(W r) = (r - z)/p
     T ir, iW;
     const T rrz = r * rz, p = rrz * W;
-    if (p != 0.0 && isfinite_t(p)) {
+    if (nonzero_finite_t(p)) {
         const T ip = 1.0 / p;
         g.i_rz = ip * W;
         g.i_Wr = ip * rz;

@@ -126,6 +126,20 @@ def test_dense_assembly_full_size_sampled_columns(cuda):
     torch.cuda.empty_cache()
 
 
+@pytest.mark.parametrize("half", [False, True])
+def test_fp32_copy_is_the_rounded_fp64_operator(cuda, half):
+    """The kernels round the FP32 copy from the FP64 entries by the bit
+    layout (integer operations, round to nearest even): every entry equals
+    PyTorch's conversion of the FP64 operator, bit for bit."""
+    nodes, tris = mesh.rough_fault(12.0, 6.0, 24, 12, seed=4, ratio=5e-3)
+    if half:
+        nodes = nodes.copy()
+        nodes[:, 2] -= nodes[:, 2].max()   # reaches the free surface
+    K64, K32 = gf.assemble_dense(nodes, tris, MU, MU, halfspace=half, device=cuda)
+    assert torch.equal(K32, K64.to(torch.float32))
+    assert bool(torch.isfinite(K64).all())
+
+
 def test_row_blocks_equal_full_assembly_and_are_deterministic(cuda):
     nodes, tris = mesh.rough_fault(10.0, 5.0, 11, 7, seed=2)
     N = tris.shape[0]
