@@ -339,17 +339,17 @@ def bench_ours(args):
         else:
             roof.update({"achieved": None, "frac": None})
         # DRAM bytes of one launch: ncu on the N=6,000 case (2.6 GB of stores,
-        # 20x the L2) measured 70.8 B/pair (2.532 GB written + 16 MB read for
+        # 20x the L2) measured 70.7 B/pair (2.532 GB written + 13 MB read for
         # 3.6e7 pairs; ~60 MB of the 2.592 GB of stores still dirty in L2 at
         # kernel end); scaled to this launch by pairs.
         # the FP64 pipe is the bound: DGEMM issues only 2-flop DFMAs, this
-        # kernel averages ~1.3 flops per FP64-pipe instruction; ncu on the
-        # N = 2,000 case: FP64 pipe 88 % busy (active cycles)
-        roof["fp64_pipe_active_pct"] = 88.3
-        roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, --set full capture of "
-                             "the N=2000 case (bench.py --quick)")
-        roof["traffic"] = 70.8 * N * N
-        roof["traffic_note"] = ("ncu dram__bytes_read+write at N=6000 (70.8 B/pair, 2.6 GB of stores, 20x the L2) "
+        # kernel averages ~1.33 flops per FP64-pipe instruction (550 per
+        # pair); ncu on the N = 6,000 case: FP64 pipe 90 % busy (active cycles)
+        roof["fp64_pipe_active_pct"] = 89.8
+        roof["pipe_note"] = ("ncu sm__inst_executed_pipe_fp64 pct_of_peak_sustained_active, capture of the N=6000 "
+                             "case (bench.py --case gf_assembly)")
+        roof["traffic"] = 70.7 * N * N
+        roof["traffic_note"] = ("ncu dram__bytes_read+write at N=6000 (70.7 B/pair, 2.6 GB of stores, 20x the L2) "
                                 "scaled by pairs (bench.py --case gf_assembly); algorithmic stores are %d B/pair"
                                 % GF_BYTES_PER_PAIR)
         out["roofline"] = roof
