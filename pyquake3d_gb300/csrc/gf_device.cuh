@@ -17,6 +17,11 @@
 //   * the strain is linear in the Burgers vector, so the by- and bz-parts of
 //     each angular dislocation are formed once and combined for unit strike
 //     and unit dip slip (the reference evaluates the whole pair twice);
+//   * the back-rotation of each angular dislocation's strain is done in
+//     harmonic form (tdcs_strain_sd2k): rotation invariants summed, the
+//     other parts turned by e^{-i th}, e^{-2i th}, e^{-3i th} and summed, strike
+//     and dip read from the sums; the factor 1/(8 pi (1 - nu)) common to
+//     every term is applied with the traction constants;
 //   * rotation to the receiver frame, Hooke's law and the traction projection
 //     are one contraction: with the receiver axes rotated into the source
 //     system, t_c = 2 mu e_c^T E n + lambda tr(E) delta_{c,n} (tr and the
