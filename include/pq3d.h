@@ -492,6 +492,13 @@ int pq3d_selftest_mbar_timeout(unsigned wait_limit, int *gave_up_host);
  * update kernel.  Allocates small buffers. */
 int pq3d_selftest_ff_conversions(const double *x_host, const float *f_host, const double *y_host, int n,
                                  float *ff_host, double *d_host, double *h_host);
+/* The configuration test of the dense assembly (coordinates from the
+ * reciprocal of the barycentric denominator, decisions in FP32 where the
+ * coordinates are well separated, else the division-based test) and the
+ * division-based test of src/TDstressFS_C.cpp:125-166 on n host points
+ * (n <= 2^22), pts_host[8i..8i+7] = (x, y, z, p1y, p1z, p3y, p3z, den):
+ * fast_host[i], exact_host[i] in {1, -1, 0}.  Allocates small buffers. */
+int pq3d_selftest_tri_mode(const double *pts_host, int n, int *fast_host, int *exact_host);
 
 #ifdef __cplusplus
 }

@@ -145,6 +145,7 @@ _SIGS = {
     "pq3d_selftest_barrier_timeout": (c_int, [c_int, c_int, ctypes.c_uint, c_void_p]),
     "pq3d_selftest_mbar_timeout": (c_int, [ctypes.c_uint, c_void_p]),
     "pq3d_selftest_ff_conversions": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "pq3d_selftest_tri_mode": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
 }
 
 _lib = None

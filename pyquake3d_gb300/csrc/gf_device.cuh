@@ -49,7 +49,7 @@ namespace gf {
 
 constexpr double kPi = 3.141592653589793;
 
-// Per-source record (41 values, stored with stride kSrcStride).
+// Per-source record (42 values, stored with stride kSrcStride).
 enum SrcField {
     F_P2X, F_P2Y, F_P2Z,          // origin (vertex 2)
     F_NX, F_NY, F_NZ,             // triangle normal
@@ -65,6 +65,7 @@ enum SrcField {
     // triple angle (Re, Im of (sz + i sy)^3) of each vertex's side vector as
     // stored (odd in the sign: negated with (sy, sz) for the other mode)
     F_C3A, F_S3A, F_C3B, F_S3B, F_C3C, F_S3C,
+    F_IDEN,                       // 1 / F_DEN
     F_COUNT
 };
 constexpr int kSrcStride = 42;
@@ -126,7 +127,8 @@ __host__ __device__ inline void setup_source(const double P1[3], const double P2
         e23[2] * e23[2] - e23[1] * e23[1], 2.0 * (e23[1] * e23[2]),
         cube_re(e13[1], e13[2]), cube_im(e13[1], e13[2]),
         cube_re(e12[1], e12[2]), cube_im(e12[1], e12[2]),
-        cube_re(e23[1], e23[2]), cube_im(e23[1], e23[2])};
+        cube_re(e23[1], e23[2]), cube_im(e23[1], e23[2]),
+        1.0 / (-p3[2] * (p1[1] - p3[1]) + p3[1] * (p1[2] - p3[2]))};
     for (int i = 0; i < F_COUNT; ++i) f[i * fstride] = vals[i];
 }
 
@@ -168,6 +170,50 @@ __device__ __forceinline__ int tri_mode(T x, T y, T z, T p1y, T p1z, T p3y, T p3
     else if (a >= 0 && b >= 0 && c == 0) m = 0;
     if (m == 0 && x != 0) m = 1;
     return m;
+}
+
+#ifdef __CUDACC__
+// v truncated to FP32 by the bit layout for the configuration test's guard
+// (relative error < 2^-23): |v| < 2^-126 gives 0, |v| >= 2^128, infinities
+// and NaN give NaN (every comparison with it fails, so the guard falls back).
+__device__ __forceinline__ float guard_f32(double v)
+{
+    const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    if (e < 1023 - 126) return 0.f;
+    if (e > 1023 + 127) return __uint_as_float(0x7fc00000u);
+    return __uint_as_float((hw & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+}
+
+// tri_mode with the barycentric coordinates from the reciprocal of the
+// denominator and the decisions taken in FP32: where every coordinate and
+// every difference of two is larger than 1e-5 of their scale, the FP64
+// coordinates (a few ulps from tri_mode's quotients) and their FP32
+// truncations order exactly as tri_mode's, and no coordinate is zero (so the
+// result is +1 or -1); closer cases -- receivers near a side line or a
+// boundary of the wedges -- are decided by tri_mode itself.  Keeps the two
+// divisions and the FP64 compares off the FP64 pipe for almost every pair.
+__device__ __forceinline__ int tri_mode_fast(double x, double y, double z, double p1y, double p1z, double p3y,
+                                             double p3z, double den, double iden)
+{
+    const double ya = y - p3y, za = z - p3z;
+    const double a = (ya * (0.0 - p3z) - (0.0 - p3y) * za) * iden;
+    const double b = ((p1y - p3y) * za - ya * (p1z - p3z)) * iden;
+    const double c = 1.0 - a - b;
+    const float af = guard_f32(a), bf = guard_f32(b), cf = guard_f32(c);
+    const float t = 1e-5f * fmaxf(1.f, fmaxf(fabsf(af), fabsf(bf)));
+    const bool sep = fabsf(af) > t && fabsf(bf) > t && fabsf(cf) > t && fabsf(af - bf) > t &&
+                     fabsf(bf - cf) > t && fabsf(cf - af) > t;
+    if (!sep) return tri_mode<double>(x, y, z, p1y, p1z, p3y, p3z, den);
+    if ((af < 0.f && bf > cf && cf > af) || (bf < 0.f && cf > af && af > bf) || (cf < 0.f && af > bf && bf > cf))
+        return -1;
+    return 1;
+}
+#endif
+template <class T>
+__host__ __device__ inline int tri_mode_fast(T x, T y, T z, T p1y, T p1z, T p3y, T p3z, T den, T)
+{
+    return tri_mode<T>(x, y, z, p1y, p1z, p3y, p3z, den);
 }
 
 #ifdef __CUDACC__
@@ -373,7 +419,7 @@ __device__ __forceinline__ bool tdcs_strain_sd2k(const Src &F, T x, T y, T z, do
 {
 #pragma unroll
     for (int i = 0; i < 6; ++i) { Es[i] = 0.0; Ed[i] = 0.0; }
-    const int m = tri_mode<T>(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN));
+    const int m = tri_mode_fast(x, y, z, F(F_P1Y), F(F_P1Z), F(F_P3Y), F(F_P3Z), F(F_DEN), F(F_IDEN));
     if (m == 0) return false;
     const bool pm = (m == 1);   // the side vectors' signs by selection, not products
     const double p2 = 2.0 * nu + 1.0, qg = 2.0 * (1.0 - nu);

@@ -6,10 +6,13 @@
 // milliseconds.  Nothing here faults or waits without a bound.  Also: the
 // integer FP64 <-> float-float conversions of the float-float attempt on
 // host-chosen values (subnormal, infinite and NaN operands included), which
-// the steppers reach only through rare states.
+// the steppers reach only through rare states; and the assembly's
+// configuration test (FP32 decisions with a division-based fallback) against
+// the division-based test on host-chosen points.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "gf_device.cuh"
 #include "rk_device.cuh"
 #include "tc_ptx.cuh"
 
@@ -146,5 +149,46 @@ extern "C" int pq3d_selftest_ff_conversions(const double *x_host, const float *f
     if (e == cudaSuccess) e = cudaMemcpy(h_host, h, nd, cudaMemcpyDeviceToHost);
     cudaFree(mem);
     if (e != cudaSuccess) return set_error(PQ3D_ERR_CUDA, "pq3d_selftest_ff_conversions: %s", cudaGetErrorString(e));
+    return PQ3D_OK;
+}
+
+namespace pq3d {
+namespace selftest {
+
+// pts[i] = (x, y, z, p1y, p1z, p3y, p3z, den): the assembly's configuration
+// test (tri_mode_fast, reciprocal of den as the source record holds it) and
+// the division-based one (tri_mode) on the same point.
+__global__ void tri_mode_kernel(const double *pts, int n, int *fast, int *exact)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *q = pts + 8 * (size_t)i;
+    fast[i] = gf::tri_mode_fast(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], 1.0 / q[7]);
+    exact[i] = gf::tri_mode<double>(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
+}
+
+}  // namespace selftest
+}  // namespace pq3d
+
+extern "C" int pq3d_selftest_tri_mode(const double *pts_host, int n, int *fast_host, int *exact_host)
+{
+    clear_error();
+    PQ3D_REQUIRE(pts_host && fast_host && exact_host && n >= 1 && n <= (1 << 22),
+                 "pq3d_selftest_tri_mode: bad arguments");
+    const size_t np = (size_t)n * 8 * sizeof(double), ni = (size_t)n * sizeof(int);
+    void *mem = nullptr;
+    PQ3D_CUDA_TRY(cudaMalloc(&mem, np + 2 * ni));
+    double *pts = (double *)mem;
+    int *fast = (int *)((char *)mem + np), *exact = fast + n;
+    cudaError_t e = cudaMemcpy(pts, pts_host, np, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        selftest::tri_mode_kernel<<<(n + 255) / 256, 256>>>(pts, n, fast, exact);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(fast_host, fast, ni, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(exact_host, exact, ni, cudaMemcpyDeviceToHost);
+    cudaFree(mem);
+    if (e != cudaSuccess) return set_error(PQ3D_ERR_CUDA, "pq3d_selftest_tri_mode: %s", cudaGetErrorString(e));
     return PQ3D_OK;
 }
