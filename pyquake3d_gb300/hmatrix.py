@@ -152,8 +152,21 @@ class HMatrix:
             bounds.append((i, j))
             i = j
         self.aca_chunks = len(bounds)
+        # wall-clock split of the ACA phase (each part device-synchronised):
+        # scratch allocation, per-chunk set-up (allocations, uploads), the
+        # launch up to its results on the host, the FP32 packing
+        aca_split = {"scratch_alloc": 0.0, "chunk_setup": 0.0, "launch_to_host": 0.0, "pack": 0.0}
+
+        def lap(key, t0):
+            torch.cuda.synchronize(dev)
+            t = _time.perf_counter()
+            aca_split[key] += t - t0
+            return t
+
+        t_l = _time.perf_counter()
         UV = torch.empty(max([int(uv_need[lr[i:j]].sum()) for i, j in bounds] + [1]), dtype=torch.float64,
                          device=dev)
+        t_l = lap("scratch_alloc", t_l)
         lr_parts = []     # per chunk: block ids, FP32 offsets inside the chunk, packed factors
         aca_events = []   # (start, end) CUDA events around each ACA launch
         for (i, j) in bounds:
@@ -161,14 +174,15 @@ class HMatrix:
             uv_off = np.concatenate([[0], np.cumsum(uv_need[ids])[:-1]]).astype(np.int64)
             used_off = np.concatenate([[0], np.cumsum(3 * m[ids])[:-1]]).astype(np.int64)
             used = torch.zeros(int((3 * m[ids]).sum()), dtype=torch.uint8, device=dev)
-            # the kernel indexes blocks by grid position: pass the chunk's sub-arrays
-            sub = torch.as_tensor(ids, device=dev)
-            blk_c = self.blk[sub].contiguous()
-            kcap_c = self.kcap[sub].contiguous()
+            # the kernel indexes blocks by grid position: pass the chunk's
+            # sub-arrays, gathered on the host (no device indexing kernel)
+            blk_c = torch.as_tensor(np.ascontiguousarray(blk[ids]), device=dev)
+            kcap_c = torch.as_tensor(np.ascontiguousarray(kcap[ids]), device=dev)
             uvo_c = torch.as_tensor(uv_off, device=dev)
             uso_c = torch.as_tensor(used_off, device=dev)
             rk_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
             stt_c = torch.empty(len(ids), dtype=torch.int32, device=dev)
+            t_l = lap("chunk_setup", t_l)
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record()
             _lib.check(L.pq3d_hmat_aca(self.tables.data_ptr(), N, self.perm.data_ptr(), len(ids), blk_c.data_ptr(),
@@ -179,6 +193,7 @@ class HMatrix:
             aca_events.append(ev)
             st_h = stt_c.cpu().numpy()
             rk_h = np.where(st_h == 0, rk_c.cpu().numpy(), -1).astype(np.int32)   # not converged: dense
+            t_l = lap("launch_to_host", t_l)
             rank[ids] = rk_h
             status[ids] = st_h
             # packed FP32 factors k (3m + 2n), each block padded to a multiple
@@ -195,8 +210,10 @@ class HMatrix:
                                                     kcap_c.data_ptr(), rk_c.data_ptr(), pos.data_ptr(), len(good),
                                                     buf.data_ptr(), loc_t.data_ptr(), st))
             lr_parts.append((ids, rk_h, loc, int(sz.sum()), buf))
+            t_l = lap("pack", t_l)
         del UV
         phase("aca")
+        phases["aca_split"] = aca_split
         # device time of the ACA launches alone (the rest of the phase is the
         # FP32 packing of each chunk, the small allocations and the rank and
         # status copies back)
